@@ -1,0 +1,371 @@
+#!/usr/bin/env python
+"""Headline benchmark: fused FE loss + adjoint, hex8 linear elasticity, 64^3.
+
+Workload (one "step" = one pass of the hot path over one batch):
+  * structured unit-cube hex8 mesh, 64^3 elements (274,625 nodes, 823,875
+    dofs), 2x2x2 Gauss; two-phase voxel Young's modulus (seeded white noise,
+    Gaussian-smoothed sigma = 3 voxels, thresholded at 0 -> E in {1.0, 0.1}),
+    nu = 0.3, one value per element; u = 0 on z = 0, u_z = 0.05 on z = 1;
+  * input dofs: the uniaxial field u_z = 0.05 z plus seeded N(0, 0.01^2) noise
+    (synthetic, seeded);
+  * one step = FE loss (energy u^T(K u - f) summed over elements) plus its
+    adjoint: dLoss/du (823,875 dofs) and dLoss/dE (262,144 elements).
+
+Metric: M elements/s of fused loss + adjoint.  Reported beside it: the plain
+GPU path (element matrices materialised in HBM, separate backward pass), the
+end-to-end number through the public API with host buffers, the dominant
+kernel's roofline, and the FP64 oracle port timed on the host cores.
+
+`--impl reference` times the oracle port (the reference is JAX, absent here)
+with every host core on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+L2_BYTES = 129 * 1024 * 1024
+FLUSH_BYTES = 512 * 1024 * 1024
+# algorithmic work of the fused element kernel per element, 2x2x2 Gauss:
+# per Gauss point J (72 FMA), det + inverse (~30 flops), dN/dx (72 FMA),
+# grad u (72 FMA), stress (~20), B^T sigma (72 FMA), energy and dE (~25):
+# 4 x 72 x 2 + 75 = 651 flops, x 8 points = 5,208 flops; plus gathers ~0.
+FLOPS_PER_ELEMENT = 5208.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--n", type=int, default=64)
+    ap.add_argument("--seed", type=int, default=2024)
+    ap.add_argument("--plain-steps", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload(n, seed):
+    from folax_gb300 import fields
+    from folax_gb300.mesh import create_3D_box_mesh
+    mesh = create_3D_box_mesh(n, n, n)
+    E = fields.two_phase_voxels(n, seed, sigma=3.0, high=1.0, low=0.1)
+    rng = np.random.default_rng(seed + 1)
+    u = np.zeros((mesh.GetNumberOfNodes(), 3))
+    u[:, 2] = 0.05 * mesh.nodes_coordinates[:, 2]
+    u += 0.01 * rng.standard_normal(u.shape)
+    settings = {"dirichlet_bc_dict": {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0},
+                                      "Uz": {"bottom": 0.0, "top": 0.05}},
+                "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
+                "control_layout": "element", "num_gp": 2}
+    return mesh, settings, E.astype(np.float32), u.ravel().astype(np.float32)
+
+
+def workload_config(n, B):
+    E = n ** 3
+    N = (n + 1) ** 3
+    return {"workload": f"hex8 linear-elastic fused loss+adjoint, {n}^3 elements, 2x2x2 Gauss",
+            "elements": E, "nodes": N, "dofs": 3 * N, "instances_per_step": B,
+            "material": "two-phase voxel E in {1.0, 0.1} (sigma 3), nu 0.3, per element",
+            "l2": "flushed before every timed step (512 MB write)"}
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = None
+        self.index = device_index
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_port(n_sample=12, seed=7):
+    """FP64 oracle port (NumPy, one thread) on a bounded sample: a 12^3 hex8
+    mesh with the same physics; returns M elements/s of loss + adjoint."""
+    from oracle import fe_oracle as fo
+    from folax_gb300 import fields
+    from folax_gb300.mesh import create_3D_box_mesh
+    m = create_3D_box_mesh(n_sample, n_sample, n_sample)
+    L = fo.FELossOracle("hex8", "elastic", m.nodes_coordinates, m.elements_nodes["hexahedron"],
+                        dirichlet={"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.05}},
+                        node_sets=m.node_sets, control_layout="element")
+    ctrl = fields.two_phase_voxels(n_sample, seed)
+    u = 0.01 * np.random.default_rng(seed).standard_normal(L.total_dofs)
+    L.batch_loss_and_grads(ctrl[None], u[None])
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        L.batch_loss_and_grads(ctrl[None], u[None])
+        reps += 1
+        if time.perf_counter() - t0 > 10.0:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    E = n_sample ** 3
+    return {"value": E / dt / 1e6, "unit": "M elements/s", "cores": 1, "kind": "port",
+            "sample": f"NumPy FP64 oracle, hex8 elastic loss+adjoint on a {n_sample}^3 mesh ({E} elements), "
+                      f"{reps} repetitions, {dt * 1e3:.1f} ms each"}
+
+
+def _oracle_chunk(args):
+    """Worker of the reference arm: loss + element gradients for a slab of elements."""
+    xyz, conn, ctrl, u = args
+    from oracle import fe_oracle as fo
+    X = xyz[conn]
+    de = np.repeat(ctrl[:, None], 8, axis=1)
+    dofidx = (3 * conn[:, :, None] + np.arange(3)).reshape(len(conn), -1)
+    en, re, _, dE = fo.linear_elastic_element("hex8", X, de, u[dofidx], 2, 1.0, 0.3, None)
+    return float(en.sum()), re, dE.sum(axis=1)
+
+
+def run_reference(args):
+    """Oracle port on every host core (process pool, spawn) over a bounded
+    sample of the 64^3 workload: each step evaluates a fixed slab of elements
+    (loss + per-element gradients + nodal scatter)."""
+    import multiprocessing as mp
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    mesh, settings, E, u = workload(args.n, args.seed)
+    conn = mesh.elements_nodes["hexahedron"]
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    sample = min(len(conn), 2048 * cores)
+    chunks = np.array_split(np.arange(sample), cores)
+    xyz = mesh.nodes_coordinates
+    ud = u.astype(np.float64)
+    work = [(xyz, conn[c], E[c].astype(np.float64), ud) for c in chunks]
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(cores) as pool:
+        def step():
+            res = pool.map(_oracle_chunk, work)
+            g = np.zeros(3 * len(xyz))
+            for c, (_, re, _) in zip(chunks, res):
+                idx = (3 * conn[c][:, :, None] + np.arange(3)).ravel()
+                np.add.at(g, idx, re.ravel())
+            return sum(r[0] for r in res)
+        for _ in range(max(1, args.warmup)):
+            step()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step()
+        dt = (time.perf_counter() - t0) / args.steps
+    value = sample / dt / 1e6
+    line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
+            "impl": "reference", "value": value, "unit": "M elements/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": workload_config(args.n, 1),
+            "cpu_baseline": {"value": value, "unit": "M elements/s", "cores": cores, "kind": "port",
+                             "sample": f"FP64 NumPy oracle port (the reference is JAX, not installed), "
+                                       f"{sample} of {len(conn)} elements per step over {cores} processes"},
+            "e2e": {"value": value, "unit": "M elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+    from folax_gb300 import _capi
+    from folax_gb300.loss import MechanicalLoss3DHexa
+    import ctypes as C
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    mesh, settings, E_h, u_h = workload(args.n, args.seed)
+    loss = MechanicalLoss3DHexa("bench", settings, mesh)
+    loss.Initialize()
+    lib = _capi.load()
+    ctrl = torch.from_numpy(E_h).cuda()[None]
+    u = torch.from_numpy(u_h).cuda()[None]
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    nE = args.n ** 3
+    B = 1
+
+    def timed(fn, steps):
+        total = 0.0
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for k in range(steps):
+            flush.zero_()
+            ev[k][0].record()
+            fn()
+            ev[k][1].record()
+        torch.cuda.synchronize()
+        for a, b in ev:
+            total += a.elapsed_time(b)
+        return total / steps
+
+    fused = lambda: loss.ComputeBatchLossAndGrad(ctrl, u)
+    plain = lambda: loss.ComputeBatchLossAndGrad(ctrl, u, plain=True)
+    for _ in range(args.warmup):
+        fused()
+    torch.cuda.synchronize()
+    barrier()
+    torch.cuda.synchronize()
+    clocks = Clocks(local)
+    clocks.start()
+    ms = timed(fused, args.steps)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    barrier()
+    if world > 1:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * B * nE / (ms * 1e-3) / 1e6
+
+    # dominant kernel: tracing events around the element kernel
+    lib.folgb_trace_enable(1)
+    lib.folgb_trace_reset()
+    timed(fused, max(3, args.steps // 2))
+    n_l, t_ms = C.c_int64(), C.c_double()
+    lib.folgb_trace_read(_capi.KERNEL_IDS["elem_loss"], C.byref(n_l), C.byref(t_ms))
+    elem_ms = t_ms.value / max(1, n_l.value)
+    lib.folgb_trace_read(_capi.KERNEL_IDS["gather"], C.byref(n_l), C.byref(t_ms))
+    gather_ms = t_ms.value / max(1, n_l.value)
+    lib.folgb_trace_enable(0)
+
+    # plain path
+    for _ in range(2):
+        plain()
+    ms_plain = timed(plain, args.plain_steps)
+    value_plain = B * nE / (ms_plain * 1e-3) / 1e6
+
+    # end to end through the public API with host buffers
+    u_pin = torch.from_numpy(u_h).pin_memory()[None]
+    c_pin = torch.from_numpy(E_h).pin_memory()[None]
+    out_du = torch.empty_like(u_pin).pin_memory()
+    out_dc = torch.empty_like(c_pin).pin_memory()
+    out_l = torch.empty(1).pin_memory()
+    u_dev = torch.empty_like(u)
+    c_dev = torch.empty_like(ctrl)
+
+    def e2e_step():
+        u_dev.copy_(u_pin, non_blocking=True)
+        c_dev.copy_(c_pin, non_blocking=True)
+        _, _, losses, du, dc = loss.ComputeBatchLossAndGrad(c_dev, u_dev)
+        out_l.copy_(losses, non_blocking=True)
+        out_du.copy_(du, non_blocking=True)
+        out_dc.copy_(dc, non_blocking=True)
+
+    for _ in range(3):
+        e2e_step()
+    ms_e2e = timed(e2e_step, args.steps)
+    h2d = u_pin.numel() * 4 + c_pin.numel() * 4
+    d2h = out_du.numel() * 4 + out_dc.numel() * 4 + 4
+
+    # roofline of the element kernel (algorithmic bytes per launch):
+    # conn 32 B + control 4 B + dLoss/dE 4 B per element; coordinates 12 B and
+    # dofs 12 B per node (each node read once)
+    N = (args.n + 1) ** 3
+    alg_bytes = nE * (32 + 4 + 4) + N * (12 + 12)
+    achieved = alg_bytes / (elem_ms * 1e-3) / 1e9
+    peaks = measured_peaks()
+    hbm = (peaks or {}).get("hbm_gbs", 6800.0)
+    sm_max = (peaks or {}).get("sm_max_mhz", 2070.0)
+    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
+    fp32_achieved = FLOPS_PER_ELEMENT * nE / (elem_ms * 1e-3) / 1e12
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline_port()
+    if rank == 0:
+        line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
+                "value": value, "unit": "M elements/s", "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded two-phase voxels, noisy uniaxial u)",
+                "config": workload_config(args.n, B),
+                "plain": {"value": value_plain, "unit": "M elements/s", "ms_per_step": ms_plain,
+                          "speedup_fused_vs_plain": value / value_plain},
+                "kernels": {"elem_loss_ms": elem_ms, "gather_ms": gather_ms},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                             "frac": achieved / hbm, "traffic": None,
+                             "kernel": "k_elem_vector<HEX8,ELASTIC,LOSS>",
+                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                             "fp32": {"achieved_tflops": fp32_achieved, "nominal_peak_tflops": fp32_peak,
+                                      "frac": fp32_achieved / fp32_peak,
+                                      "flops_per_element": FLOPS_PER_ELEMENT}},
+                "e2e": {"value": B * nE / (ms_e2e * 1e-3) / 1e6, "unit": "M elements/s", "ms_per_step": ms_e2e,
+                        "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "cpu_baseline": cpu,
+                "clocks": clk,
+                "gpu_launches": 2 * args.steps}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,124 @@
+"""ctypes binding of libfolgb.so (the C ABI declared in include/folgb.h).
+
+The library is loaded from the package's ``lib/`` folder.  There is no CPU
+fallback: if the library is missing or fails to load, every product entry
+point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+OK = 0
+ERR_INVALID_ARGUMENT = 1
+ERR_NONPOSITIVE_DETJ = 2
+ERR_NAN = 3
+ERR_NOT_CONVERGED = 4
+ERR_CUDA = 5
+ERR_WORKSPACE = 6
+ERR_NO_PATTERN = 7
+
+STATUS_NAMES = {
+    OK: "ok", ERR_INVALID_ARGUMENT: "invalid argument", ERR_NONPOSITIVE_DETJ: "non-positive detJ",
+    ERR_NAN: "non-finite value", ERR_NOT_CONVERGED: "not converged", ERR_CUDA: "CUDA error",
+    ERR_WORKSPACE: "workspace too small", ERR_NO_PATTERN: "plan has no CSR pattern",
+}
+
+QUAD4, HEX8, TET4 = 0, 1, 2
+THERMAL, ELASTIC, NEOHOOKE = 0, 1, 2
+CONTROL_NODAL, CONTROL_ELEMENT = 0, 1
+SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
+OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN = 0, 1, 2, 3
+
+
+class FolgbError(RuntimeError):
+    def __init__(self, func, code):
+        super().__init__(f"{func} failed: {STATUS_NAMES.get(code, code)} (status {code})")
+        self.code = code
+
+
+class Physics(C.Structure):
+    _fields_ = [
+        ("element_type", C.c_int32), ("physics", C.c_int32), ("num_gp", C.c_int32),
+        ("control_layout", C.c_int32), ("shear_mode", C.c_int32), ("reserved", C.c_int32),
+        ("young_modulus", C.c_double), ("poisson_ratio", C.c_double),
+        ("body_force", C.c_double * 3), ("beta", C.c_double), ("c", C.c_double),
+        ("loss_exponent", C.c_double),
+    ]
+
+
+vp = C.c_void_p
+i32, i64, f32, f64, sz = C.c_int32, C.c_int64, C.c_float, C.c_double, C.c_size_t
+
+# name -> (restype, argtypes)
+PROTOTYPES = {
+    "folgb_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), vp, i64, vp, i64, vp, vp, i64, i32]),
+    "folgb_plan_destroy": (C.c_int, [vp]),
+    "folgb_plan_info": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+    "folgb_plan_set_dirichlet_values": (C.c_int, [vp, vp, f64]),
+    "folgb_workspace_bytes": (sz, [vp, i32, i32]),
+    "folgb_loss_adjoint": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_loss_adjoint_plain": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_csr_pattern": (C.c_int, [vp, vp, vp, vp]),
+    "folgb_assemble": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_pcg": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
+    "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
+    "folgb_adam_step": (C.c_int, [vp, vp, vp, vp, i64, vp, f32, f32, f32, f32, vp]),
+    "folgb_batch_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), i32, vp, vp, vp, vp, vp, vp, i64, i32]),
+    "folgb_batch_plan_destroy": (C.c_int, [vp]),
+    "folgb_batch_workspace_bytes": (sz, [vp]),
+    "folgb_batch_loss_adjoint": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_trace_enable": (C.c_int, [i32]),
+    "folgb_trace_reset": (C.c_int, []),
+    "folgb_trace_read": (C.c_int, [i32, C.POINTER(i64), C.POINTER(f64)]),
+}
+
+KERNEL_IDS = {"elem_loss": 0, "gather": 1, "elem_matrix": 2, "pair_reduce": 3, "plain_backward": 4,
+              "elem_residual": 5, "pcg_spmv": 6, "pcg_update": 7, "batch_loss": 8, "hex8_fused": 9}
+
+_LIB = None
+
+
+def lib_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load libfolgb.so (building it first when it is missing or stale)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = lib_path()
+    if build_if_missing and (_build.needs_build()):
+        _build.build()
+    if not os.path.exists(path):
+        raise RuntimeError(f"libfolgb.so not found at {path}; run folax_gb300.build.build()")
+    lib = C.CDLL(path)
+    for name, (res, args) in PROTOTYPES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = lib
+    return lib
+
+
+def check(func: str, code: int):
+    if code != OK:
+        raise FolgbError(func, code)
+
+
+def ptr(t) -> int | None:
+    """Device (or host) address of a torch tensor / numpy array, or None."""
+    if t is None:
+        return None
+    if hasattr(t, "data_ptr"):
+        return t.data_ptr()
+    return t.ctypes.data
+
+
+def stream_handle(stream=None) -> int:
+    import torch
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream

@@ -1,0 +1,343 @@
+// Per-element device code shared by the single-mesh and the batched kernels:
+// argument blocks, gathers, the Gauss-point loop of each element physics,
+// and the deterministic loss reduction.
+//
+// Reference behaviour restated here (paths inside the folax project):
+//   gather by connectivity          fol/loss_functions/fe_loss.py:155-164, 232-248
+//   isoparametric map               fol/geometries/geometry.py:87-97
+//   thermal element                 fol/loss_functions/thermal.py:28-49
+//   linear elastic element          fol/loss_functions/mechanical.py:98-117
+//   Neo-Hookean (AD) element        fol/loss_functions/mechanical_neohooke_AD.py:254-293
+//   batch loss                      fol/loss_functions/fe_loss.py:250-262
+#pragma once
+
+#include <cmath>
+
+#include "folgb_internal.cuh"
+
+namespace folgb {
+
+template <int ET_, int PH_>
+struct Tag {
+  static constexpr int ET = ET_, PH = PH_;
+};
+
+template <class F>
+int dispatch(int et, int ph, F&& f) {
+  switch (et * 3 + ph) {
+    case 0: return f(Tag<FOLGB_QUAD4, FOLGB_THERMAL>{});
+    case 1: return f(Tag<FOLGB_QUAD4, FOLGB_ELASTIC>{});
+    case 2: return f(Tag<FOLGB_QUAD4, FOLGB_NEOHOOKE>{});
+    case 3: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
+    case 4: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
+    case 5: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
+    case 6: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
+    case 7: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
+    case 8: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
+  }
+  return FOLGB_ERR_INVALID_ARGUMENT;
+}
+
+enum { MODE_LOSS = 0, MODE_RESIDUAL = 1 };
+
+struct VecArgs {
+  int64_t E, N;
+  const int* conn;
+  const float4* xyz4;
+  const GPTable* gp;
+  const float* ctrl;
+  int64_t ctrl_stride;
+  const float* dofs;
+  int64_t dofs_stride;
+  const unsigned char* dmask;
+  const float* dval;
+  int apply_dirichlet;
+  int ctrl_layout;
+  MatConst mat;
+  float* g;           // [B][E][nen*ndof] element vectors
+  float* gde;         // [B][E][nen] (nodal control) or NULL
+  float* dctrl_elem;  // [B][E] element-layout control gradient or NULL
+  float* partials;    // [B][gridDim.x]
+  unsigned* counters; // [B]
+  float* losses;      // [B]
+  float* scale;       // [B]
+  float exponent, inv_batch;
+  int* status;
+};
+
+__device__ __forceinline__ void load_gp_table(GPTable& dst, const GPTable* src) {
+  const int* s = reinterpret_cast<const int*>(src);
+  int* d = reinterpret_cast<int*>(&dst);
+  // npts first, then only the rows that are used
+  for (int i = threadIdx.x; i < (int)(sizeof(GPTable) / 4); i += blockDim.x) d[i] = __ldg(s + i);
+}
+
+template <int NEN>
+__device__ __forceinline__ void load_nodes(const int* conn, int64_t e, int (&nodes)[NEN]) {
+  if constexpr (NEN == 8) {
+    const int4* c4 = reinterpret_cast<const int4*>(conn + e * 8);
+    int4 p = __ldg(c4), q = __ldg(c4 + 1);
+    nodes[0] = p.x; nodes[1] = p.y; nodes[2] = p.z; nodes[3] = p.w;
+    nodes[4] = q.x; nodes[5] = q.y; nodes[6] = q.z; nodes[7] = q.w;
+  } else {
+    int4 p = __ldg(reinterpret_cast<const int4*>(conn + e * 4));
+    nodes[0] = p.x; nodes[1] = p.y; nodes[2] = p.z; nodes[3] = p.w;
+  }
+}
+
+// Last-block-done reduction of per-block energies into the per-instance loss:
+// the block that finishes last (integer atomic counter) sums the partials in
+// a fixed order, so the result is deterministic.
+__device__ __forceinline__ void finish_loss(float block_energy, const VecArgs& A, int b, float* sh) {
+  __shared__ bool last;
+  const int nblk = gridDim.x;
+  if (threadIdx.x == 0) {
+    A.partials[(int64_t)b * nblk + blockIdx.x] = block_energy;
+    __threadfence();
+    unsigned prev = atomicAdd(A.counters + b, 1u);
+    last = (prev == (unsigned)nblk - 1);
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  float s = 0.f;
+  const volatile float* pv = A.partials + (int64_t)b * nblk;
+  for (int i = threadIdx.x; i < nblk; i += blockDim.x) s += pv[i];
+  float L = block_sum(s, sh);
+  if (threadIdx.x == 0) {
+    float p = A.exponent;
+    float Lp = (p == 1.f) ? L : powf(L, p);
+    float sc = (p == 1.f) ? A.inv_batch : p * powf(L, p - 1.f) * A.inv_batch;
+    A.losses[b] = Lp;
+    A.scale[b] = sc;
+    if (!isfinite(Lp) && A.status) atomicOr(A.status, 1 << FOLGB_ERR_NAN);
+    A.counters[b] = 0u;  // ready for the next launch
+  }
+}
+
+// Per-element body shared by the single-mesh and the batched kernels.
+template <int ET, int PH, int MODE>
+__device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable& gp, const int b, const int64_t e,
+                                                 float& energy, int& bad) {
+  constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM, NDOF = NdofT<PH, DIM>::V;
+  constexpr int ND = NEN * NDOF;
+  {
+    int nodes[NEN];
+    load_nodes<NEN>(A.conn, e, nodes);
+    float X[NEN][3];
+    float ue[ND];
+    float de[NEN];
+    float eval = 0.f;
+    const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+    const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+      float4 x = __ldg(A.xyz4 + nodes[a]);
+      X[a][0] = x.x; X[a][1] = x.y; X[a][2] = x.z;
+      unsigned m = A.apply_dirichlet ? __ldg(A.dmask + nodes[a]) : 0u;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
+        int64_t d = (int64_t)NDOF * nodes[a] + c;
+        ue[a * NDOF + c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+      }
+      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) de[a] = __ldg(ctrl + nodes[a]);
+    }
+    if (A.ctrl_layout != FOLGB_CONTROL_NODAL) eval = __ldg(ctrl + e);
+    float g[ND];
+    float gd[NEN];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) g[i] = 0.f;
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) gd[a] = 0.f;
+    const MatConst& mt = A.mat;
+#pragma unroll 1
+    for (int q = 0; q < gp.npts; ++q) {
+      float J[DIM][DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) {
+          float s = 0.f;
+#pragma unroll
+          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], gp.dN[q][a][k], s);
+          J[i][k] = s;
+        }
+      float Ji[DIM][DIM];
+      float det = det_inv<DIM>(J, Ji);
+      bad |= !(det > 0.f);
+      const float wd = gp.w[q] * det;
+      float dNdx[NEN][DIM];
+#pragma unroll
+      for (int a = 0; a < NEN; ++a)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          float s = 0.f;
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], Ji[k][j], s);
+          dNdx[a][j] = s;
+        }
+      float egp;
+      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) {
+        egp = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) egp = fmaf(gp.N[q][a], de[a], egp);
+      } else {
+        egp = eval;
+      }
+      if constexpr (PH == FOLGB_THERMAL) {
+        float Tg = 0.f, gT[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gT[j] = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          Tg = fmaf(gp.N[q][a], ue[a], Tg);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
+        }
+        float gf = 1.f;
+        if (mt.beta != 0.f) gf = 1.f + mt.beta * powf(Tg, mt.c);
+        float kw = wd * egp * gf;
+        float gg = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gg = fmaf(gT[j], gT[j], gg);
+        energy = fmaf(kw, gg, energy);
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          float s = 0.f;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) s = fmaf(dNdx[a][j], gT[j], s);
+          g[a] = fmaf(kw, s, g[a]);
+          gd[a] = fmaf(wd * gf * gg, gp.N[q][a], gd[a]);
+        }
+      } else if constexpr (PH == FOLGB_ELASTIC) {
+        float H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+            H[i][j] = s;
+          }
+        float tr = 0.f, sq = 0.f, sh2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          tr += H[i][i];
+          sq = fmaf(H[i][i], H[i][i], sq);
+        }
+        float sig[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          sig[i][i] = egp * (mt.lam * tr + 2.f * mt.mu * H[i][i]);
+#pragma unroll
+          for (int j = i + 1; j < DIM; ++j) {
+            float gam = H[i][j] + H[j][i];
+            sh2 = fmaf(gam, gam, sh2);
+            sig[i][j] = sig[j][i] = egp * mt.mu * gam;
+          }
+        }
+        float sed = mt.lam * tr * tr + 2.f * mt.mu * sq + mt.mu * sh2;
+        energy = fmaf(wd * egp, sed, energy);
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+          for (int i = 0; i < DIM; ++i) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) s = fmaf(sig[i][j], dNdx[a][j], s);
+            g[a * DIM + i] = fmaf(wd, s, g[a * DIM + i]);
+          }
+          gd[a] = fmaf(wd * sed, gp.N[q][a], gd[a]);
+        }
+        if (mt.has_bf) {
+#pragma unroll
+          for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) {
+              float f = wd * gp.N[q][a] * mt.bf[i];
+              g[a * DIM + i] -= f;
+              energy = fmaf(-f, ue[a * DIM + i], energy);
+            }
+        }
+      } else {  // neo-Hooke
+        float H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+            H[i][j] = s;
+          }
+        const float mu = mt.mu_f * egp, lam = mt.lam_f * egp;
+        NHState<DIM> st;
+        nh_state<DIM>(H, mu, lam, st);
+        float M[DIM][DIM];
+        const float off = (MODE == MODE_RESIDUAL && mt.shear_ref) ? 2.f : 1.f;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) M[i][j] = st.S[i][j] * (i == j ? 1.f : off);
+        float P[DIM][DIM];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int p = 0; p < DIM; ++p) s = fmaf(st.F[k][p], M[p][j], s);
+            P[k][j] = s;
+          }
+        energy = fmaf(wd, st.psi, energy);
+        const float dpsi_de = st.dpsi_dmu * mt.mu_f + st.dpsi_dlam * mt.lam_f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
+            g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
+          }
+          gd[a] = fmaf(wd * dpsi_de, gp.N[q][a], gd[a]);
+        }
+        if (MODE == MODE_RESIDUAL && mt.has_bf) {
+#pragma unroll
+          for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
+        }
+      }
+    }
+    if (!isfinite(energy)) bad |= 2;
+    // element vector (16-byte stores; ND is a multiple of 4 for every element)
+    float4* gout = reinterpret_cast<float4*>(A.g + ((int64_t)b * A.E + e) * ND);
+#pragma unroll
+    for (int i = 0; i < ND / 4; ++i) gout[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
+    if (MODE == MODE_LOSS) {
+      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) {
+        float4* go = reinterpret_cast<float4*>(A.gde + ((int64_t)b * A.E + e) * NEN);
+#pragma unroll
+        for (int i = 0; i < NEN / 4; ++i) go[i] = make_float4(gd[4 * i], gd[4 * i + 1], gd[4 * i + 2], gd[4 * i + 3]);
+      } else if (A.dctrl_elem) {
+        float s = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) s += gd[a];
+        // scale by 1/B here when the exponent is 1; otherwise the gather pass rescales
+        A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? s * A.inv_batch : s;
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void report_bad(int bad, int* status) {
+  int anybad = __syncthreads_or(bad);
+  if (anybad && threadIdx.x == 0 && status) {
+    if (anybad & 1) atomicOr(status, 1 << FOLGB_ERR_NONPOSITIVE_DETJ);
+    if (anybad & 2) atomicOr(status, 1 << FOLGB_ERR_NAN);
+  }
+}
+
+}  // namespace folgb

@@ -1,0 +1,878 @@
+// Element kernels: fused loss + adjoint, deterministic node gather, element
+// matrices, CSR segmented reduction, and the plain (materialised Se) path.
+//
+// Reference behaviour restated here (paths inside the folax project):
+//   gather by connectivity          fol/loss_functions/fe_loss.py:155-164, 232-248
+//   isoparametric map               fol/geometries/geometry.py:87-97
+//   thermal element                 fol/loss_functions/thermal.py:28-49
+//   linear elastic element          fol/loss_functions/mechanical.py:98-117
+//   Neo-Hookean (AD) element        fol/loss_functions/mechanical_neohooke_AD.py:254-293
+//   batch loss                      fol/loss_functions/fe_loss.py:250-262
+//   residual / Jacobian assembly    fol/loss_functions/fe_loss.py:191-207, 264-318
+#include <cmath>
+#include <type_traits>
+
+#include "element_body.cuh"
+
+using namespace folgb;
+
+namespace folgb {
+
+// One thread per element: gather, Gauss-point loop, element energy, element
+// energy gradient (LOSS) or element residual (RESIDUAL).
+template <int ET, int PH, int MODE>
+__global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
+  __shared__ GPTable gp;
+  __shared__ float red[32];
+  load_gp_table(gp, A.gp);
+  __syncthreads();
+  const int b = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float energy = 0.f;
+  int bad = 0;
+  if (e < A.E) elem_vector_body<ET, PH, MODE>(A, gp, b, e, energy, bad);
+  report_bad(bad, A.status);
+  if (MODE == MODE_LOSS) {
+    float be = block_sum(energy, red);
+    finish_loss(be, A, b, red);
+  }
+}
+
+
+struct GatherArgs {
+  int64_t E, N;
+  int nen;
+  const int* inc_ptr;
+  const int* inc_slot;
+  const unsigned char* dmask;
+  const float* g;      // [B][E*nen][ndof] element vectors
+  const float* gde;    // [B][E*nen] or NULL
+  const float* scale;  // [B] or NULL (scale 1)
+  float* out;          // [B][ndof*N] or NULL
+  int64_t out_stride;
+  float* dctrl;        // [B][N] nodal control gradient or NULL
+  int64_t dctrl_stride;
+  float* dctrl_elem;   // [B][E] rescaled in place when rescale_elem != 0
+  int rescale_elem;
+  const int* node_inst;  // batched meshes: instance of each node (scale index), or NULL
+  const int* elem_inst;  // batched meshes: instance of each element, or NULL
+};
+
+// Deterministic transpose-gather: every node sums its incident element slots
+// in ascending element order (no float atomics).  Dirichlet dofs get 0
+// (fe_loss.py:91-100 overwrites them, so their gradient is zero; the BC
+// residual rows are zeroed by fe_loss.py:191-207).
+template <int NDOF>
+__global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
+  const int b = blockIdx.y;
+  const float scb = A.scale ? A.scale[b] : 1.f;
+  const int64_t sbase = (int64_t)b * A.E * A.nen;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < A.N; n += stride) {
+    const int s0 = __ldg(A.inc_ptr + n), s1 = __ldg(A.inc_ptr + n + 1);
+    float acc[NDOF];
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) acc[c] = 0.f;
+    float accd = 0.f;
+    for (int k = s0; k < s1; ++k) {
+      const int64_t slot = sbase + __ldg(A.inc_slot + k);
+      const float* gv = A.g + slot * NDOF;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) acc[c] += gv[c];
+      if (A.gde) accd += A.gde[slot];
+    }
+    const float sc = A.node_inst ? A.scale[__ldg(A.node_inst + n)] : scb;
+    if (A.out) {
+      const unsigned m = __ldg(A.dmask + n);
+      float* o = A.out + (int64_t)b * A.out_stride + (int64_t)NDOF * n;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) o[c] = ((m >> c) & 1u) ? 0.f : sc * acc[c];
+    }
+    if (A.dctrl) A.dctrl[(int64_t)b * A.dctrl_stride + n] = sc * accd;
+  }
+  if (A.rescale_elem && A.dctrl_elem) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += stride)
+      A.dctrl_elem[(int64_t)b * A.E + e] *= A.elem_inst ? A.scale[__ldg(A.elem_inst + e)] : scb;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Element matrices.  Phase 1: one task per (element, Gauss point) writes the
+// Gauss-point record (dN/dx, weights, and for neo-Hooke F, the used stress M
+// and the Voigt tangent) to shared memory.  Phase 2: one task per
+// (element, a, b) node-pair block sums its ndof x ndof block over the Gauss
+// points, applies the transpose and the row-only Dirichlet rule, and stores it.
+// ---------------------------------------------------------------------------
+enum { MAT_ASSEMBLE = 0, MAT_PLAIN = 1 };
+
+struct MatArgs {
+  int64_t E;
+  const int* conn;
+  const float4* xyz4;
+  const GPTable* gp;
+  const float* ctrl;
+  int64_t ctrl_stride;
+  const float* dofs;
+  int64_t dofs_stride;
+  const unsigned char* dmask;
+  const float* dval;
+  int apply_dirichlet;
+  int ctrl_layout;
+  MatConst mat;
+  int transpose;
+  int epb;         // elements per block
+  float* Ke;       // [B][E][nen][nen][ndof][ndof]
+  float* Fe;       // plain: [B][E][nd] or NULL
+  float* gde;      // plain, nodal control: [B][E][nen]
+  float* dctrl_elem;  // plain, element control: [B][E]
+  float exponent, inv_batch;
+  int* status;
+};
+
+template <int ET, int PH>
+struct MatRec {
+  static constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM;
+  static constexpr int NV = Voigt<DIM>::NV;
+  static constexpr int GEO = NEN * DIM + 3;  // dNdx, wd, coef, sedw
+  static constexpr int EXTRA = (PH == FOLGB_NEOHOOKE) ? (2 * DIM * DIM + NV * NV) : 0;
+  static constexpr int SIZE = GEO + EXTRA;
+  static constexpr int O_WD = NEN * DIM, O_COEF = O_WD + 1, O_SED = O_WD + 2;
+  static constexpr int O_F = GEO, O_M = GEO + DIM * DIM, O_HM = GEO + 2 * DIM * DIM;
+};
+
+template <int ET, int PH, int MMODE>
+__global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
+  constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM, NDOF = NdofT<PH, DIM>::V;
+  constexpr int ND = NEN * NDOF;
+  using R = MatRec<ET, PH>;
+  constexpr int NV = R::NV;
+  extern __shared__ float smem[];
+  __shared__ GPTable gp;
+  load_gp_table(gp, A.gp);
+  __syncthreads();
+  const int npts = gp.npts;
+  const int b = blockIdx.y;
+  const int64_t e0 = (int64_t)blockIdx.x * A.epb;
+  const float* dofs = A.dofs ? A.dofs + (int64_t)b * A.dofs_stride : nullptr;
+  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+  const MatConst& mt = A.mat;
+  int bad = 0;
+  // ---- phase 1
+  for (int t = threadIdx.x; t < A.epb * npts; t += blockDim.x) {
+    const int el = t / npts, q = t % npts;
+    const int64_t e = e0 + el;
+    if (e >= A.E) continue;
+    float* rec = smem + (size_t)t * R::SIZE;
+    int nodes[NEN];
+    load_nodes<NEN>(A.conn, e, nodes);
+    float X[NEN][3];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+      float4 x = __ldg(A.xyz4 + nodes[a]);
+      X[a][0] = x.x; X[a][1] = x.y; X[a][2] = x.z;
+    }
+    float J[DIM][DIM];
+#pragma unroll
+    for (int i = 0; i < DIM; ++i)
+#pragma unroll
+      for (int k = 0; k < DIM; ++k) {
+        float s = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], gp.dN[q][a][k], s);
+        J[i][k] = s;
+      }
+    float Ji[DIM][DIM];
+    const float det = det_inv<DIM>(J, Ji);
+    bad |= !(det > 0.f);
+    const float wd = gp.w[q] * det;
+    float dNdx[NEN][DIM];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a)
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        float s = 0.f;
+#pragma unroll
+        for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], Ji[k][j], s);
+        dNdx[a][j] = s;
+        rec[a * DIM + j] = s;
+      }
+    float egp = 0.f;
+    if (A.ctrl_layout == FOLGB_CONTROL_NODAL) {
+#pragma unroll
+      for (int a = 0; a < NEN; ++a) egp = fmaf(gp.N[q][a], __ldg(ctrl + nodes[a]), egp);
+    } else {
+      egp = __ldg(ctrl + e);
+    }
+    rec[R::O_WD] = wd;
+    const bool need_u = (PH == FOLGB_NEOHOOKE) || (MMODE == MAT_PLAIN) ||
+                        (PH == FOLGB_THERMAL && mt.beta != 0.f);
+    float ue[ND];
+    if (need_u) {
+#pragma unroll
+      for (int a = 0; a < NEN; ++a) {
+        unsigned m = A.apply_dirichlet ? __ldg(A.dmask + nodes[a]) : 0u;
+#pragma unroll
+        for (int c = 0; c < NDOF; ++c) {
+          int64_t d = (int64_t)NDOF * nodes[a] + c;
+          ue[a * NDOF + c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+        }
+      }
+    }
+    if constexpr (PH == FOLGB_THERMAL) {
+      float gf = 1.f, gg = 0.f;
+      if (need_u) {
+        float Tg = 0.f, gT[DIM] = {};
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          Tg = fmaf(gp.N[q][a], ue[a], Tg);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
+        }
+        if (mt.beta != 0.f) gf = 1.f + mt.beta * powf(Tg, mt.c);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gg = fmaf(gT[j], gT[j], gg);
+      }
+      rec[R::O_COEF] = wd * egp * gf;
+      rec[R::O_SED] = wd * gf * gg;
+    } else if constexpr (PH == FOLGB_ELASTIC) {
+      rec[R::O_COEF] = wd * egp;
+      float sed = 0.f;
+      if (MMODE == MAT_PLAIN) {
+        float H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+            H[i][j] = s;
+          }
+        float tr = 0.f, sq = 0.f, sh2 = 0.f;
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) {
+          tr += H[i][i];
+          sq = fmaf(H[i][i], H[i][i], sq);
+#pragma unroll
+          for (int j = i + 1; j < DIM; ++j) sh2 = fmaf(H[i][j] + H[j][i], H[i][j] + H[j][i], sh2);
+        }
+        sed = mt.lam * tr * tr + 2.f * mt.mu * sq + mt.mu * sh2;
+      }
+      rec[R::O_SED] = wd * sed;
+    } else {
+      float H[DIM][DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          float s = 0.f;
+#pragma unroll
+          for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+          H[i][j] = s;
+        }
+      const float mu = mt.mu_f * egp, lam = mt.lam_f * egp;
+      NHState<DIM> st;
+      nh_state<DIM>(H, mu, lam, st);
+      const float off = mt.shear_ref ? 2.f : 1.f;
+      rec[R::O_COEF] = wd;
+      rec[R::O_SED] = 0.f;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          rec[R::O_F + i * DIM + j] = st.F[i][j];
+          rec[R::O_M + i * DIM + j] = st.S[i][j] * (i == j ? 1.f : off);
+        }
+      // Voigt tangent of the used stress wrt the independent Voigt entries of C
+#pragma unroll
+      for (int w = 0; w < NV; ++w) {
+        float dC[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) dC[i][j] = 0.f;
+        const int pw = Voigt<DIM>::p(w), qw = Voigt<DIM>::q(w);
+        dC[pw][qw] = 1.f;
+        dC[qw][pw] = 1.f;
+        float dS[DIM][DIM];
+        nh_dS<DIM>(st, mu, lam, dC, dS);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+          const int pv = Voigt<DIM>::p(v), qv = Voigt<DIM>::q(v);
+          rec[R::O_HM + v * NV + w] = dS[pv][qv] * (pv == qv ? 1.f : off);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // ---- phase 2: node-pair blocks
+  for (int t = threadIdx.x; t < A.epb * NEN * NEN; t += blockDim.x) {
+    const int el = t / (NEN * NEN), ab = t % (NEN * NEN);
+    const int a = ab / NEN, bb = ab % NEN;
+    const int64_t e = e0 + el;
+    if (e >= A.E) continue;
+    // transposed assembly computes block (bb, a) and transposes it
+    const int ra = (MMODE == MAT_ASSEMBLE && A.transpose) ? bb : a;
+    const int rb = (MMODE == MAT_ASSEMBLE && A.transpose) ? a : bb;
+    float K[NDOF][NDOF];
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j) K[i][j] = 0.f;
+    for (int q = 0; q < npts; ++q) {
+      const float* rec = smem + (size_t)(el * npts + q) * R::SIZE;
+      float dNa[DIM], dNb[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) {
+        dNa[j] = rec[ra * DIM + j];
+        dNb[j] = rec[rb * DIM + j];
+      }
+      float dot = 0.f;
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) dot = fmaf(dNa[j], dNb[j], dot);
+      const float coef = rec[R::O_COEF];
+      if constexpr (PH == FOLGB_THERMAL) {
+        K[0][0] = fmaf(coef, dot, K[0][0]);
+      } else if constexpr (PH == FOLGB_ELASTIC) {
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float v = mt.lam * dNa[i] * dNb[j] + mt.mu * dNa[j] * dNb[i] + (i == j ? mt.mu * dot : 0.f);
+            K[i][j] = fmaf(coef, v, K[i][j]);
+          }
+      } else {
+        float F[DIM][DIM], M[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            F[i][j] = rec[R::O_F + i * DIM + j];
+            M[i][j] = rec[R::O_M + i * DIM + j];
+          }
+        // B_v(a,i) and Bc_w(b,l) = d c_w / d u_(b,l)
+        float Ba[DIM][NV], Bc[DIM][NV];
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            const int p = Voigt<DIM>::p(v), qq = Voigt<DIM>::q(v);
+            if (p == qq) {
+              Ba[k][v] = F[k][p] * dNa[p];
+              Bc[k][v] = 2.f * F[k][p] * dNb[p];
+            } else {
+              Ba[k][v] = F[k][p] * dNa[qq] + F[k][qq] * dNa[p];
+              Bc[k][v] = F[k][p] * dNb[qq] + F[k][qq] * dNb[p];
+            }
+          }
+#pragma unroll
+        for (int l = 0; l < DIM; ++l) {
+          float Z[NV];
+#pragma unroll
+          for (int v = 0; v < NV; ++v) {
+            float s = 0.f;
+#pragma unroll
+            for (int w = 0; w < NV; ++w) s = fmaf(rec[R::O_HM + v * NV + w], Bc[l][w], s);
+            Z[v] = s;
+          }
+#pragma unroll
+          for (int i = 0; i < DIM; ++i) {
+            float s = 0.f;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) s = fmaf(Ba[i][v], Z[v], s);
+            K[i][l] = fmaf(coef, s, K[i][l]);
+          }
+        }
+        float geo = 0.f;
+#pragma unroll
+        for (int p = 0; p < DIM; ++p)
+#pragma unroll
+          for (int qq = 0; qq < DIM; ++qq) geo = fmaf(dNa[p] * M[p][qq], dNb[qq], geo);
+#pragma unroll
+        for (int i = 0; i < DIM; ++i) K[i][i] = fmaf(coef, geo, K[i][i]);
+      }
+    }
+    float out[NDOF][NDOF];
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j)
+        out[i][j] = (MMODE == MAT_ASSEMBLE && A.transpose) ? K[j][i] : K[i][j];
+    if (MMODE == MAT_ASSEMBLE) {
+      // row-only Dirichlet (fe_loss.py:191-207): zero row (a,i), keep its diagonal
+      const int na = __ldg(A.conn + e * NEN + a);
+      const unsigned m = __ldg(A.dmask + na);
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i)
+        if ((m >> i) & 1u) {
+#pragma unroll
+          for (int j = 0; j < NDOF; ++j)
+            if (!(a == bb && i == j)) out[i][j] = 0.f;
+        }
+    }
+    float* dst = A.Ke + ((((int64_t)b * A.E + e) * NEN + a) * NEN + bb) * (NDOF * NDOF);
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+      for (int j = 0; j < NDOF; ++j) dst[i * NDOF + j] = out[i][j];
+  }
+  if (MMODE == MAT_PLAIN) {
+    // per (element, node): control sensitivity and body-force vector
+    for (int t = threadIdx.x; t < A.epb * NEN; t += blockDim.x) {
+      const int el = t / NEN, a = t % NEN;
+      const int64_t e = e0 + el;
+      if (e >= A.E) continue;
+      float gd = 0.f, fw = 0.f;
+      for (int q = 0; q < npts; ++q) {
+        const float* rec = smem + (size_t)(el * npts + q) * R::SIZE;
+        gd = fmaf(rec[R::O_SED], gp.N[q][a], gd);
+        fw = fmaf(rec[R::O_WD], gp.N[q][a], fw);
+      }
+      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) A.gde[((int64_t)b * A.E + e) * NEN + a] = gd;
+      if (A.Fe) {
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i)
+          A.Fe[(((int64_t)b * A.E + e) * NEN + a) * NDOF + i] = (PH == FOLGB_THERMAL) ? 0.f : fw * mt.bf[i];
+      }
+    }
+    if (A.ctrl_layout != FOLGB_CONTROL_NODAL && A.dctrl_elem) {
+      for (int el = threadIdx.x; el < A.epb; el += blockDim.x) {
+        const int64_t e = e0 + el;
+        if (e >= A.E) continue;
+        float s = 0.f;
+        for (int q = 0; q < npts; ++q) {
+          const float* rec = smem + (size_t)(el * npts + q) * R::SIZE;
+          float nsum = 0.f;
+          for (int a = 0; a < NEN; ++a) nsum += gp.N[q][a];
+          s = fmaf(rec[R::O_SED], nsum, s);
+        }
+        A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? s * A.inv_batch : s;
+      }
+    }
+  }
+  int anybad = __syncthreads_or(bad);
+  if (anybad && threadIdx.x == 0 && A.status) atomicOr(A.status, 1 << FOLGB_ERR_NONPOSITIVE_DETJ);
+}
+
+// Segmented reduction over the element-to-nonzero map: one thread per node
+// pair sums its contributing element blocks in ascending element order and
+// writes the ndof x ndof block into the canonical CSR rows.
+template <int NDOF>
+__global__ void __launch_bounds__(256) k_pair_reduce(int64_t P, const int* __restrict__ pair_row,
+                                                     const int* __restrict__ adj_ptr, const int* __restrict__ adj,
+                                                     const int* __restrict__ pair_ptr, const int* __restrict__ pair_slot,
+                                                     const int* __restrict__ rowptr, const float* __restrict__ Ke,
+                                                     float* __restrict__ vals, float* __restrict__ inv_diag) {
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t p = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; p < P; p += stride) {
+    const int n = __ldg(pair_row + p);
+    const int j = (int)(p - __ldg(adj_ptr + n));
+    const int m = __ldg(adj + p);
+    float acc[NDOF * NDOF];
+#pragma unroll
+    for (int i = 0; i < NDOF * NDOF; ++i) acc[i] = 0.f;
+    const int k0 = __ldg(pair_ptr + p), k1 = __ldg(pair_ptr + p + 1);
+    for (int k = k0; k < k1; ++k) {
+      const float* blk = Ke + (int64_t)__ldg(pair_slot + k) * (NDOF * NDOF);
+#pragma unroll
+      for (int i = 0; i < NDOF * NDOF; ++i) acc[i] += __ldg(blk + i);
+    }
+    if (vals) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        float* row = vals + __ldg(rowptr + (int64_t)NDOF * n + i) + NDOF * j;
+#pragma unroll
+        for (int l = 0; l < NDOF; ++l) row[l] = acc[i * NDOF + l];
+      }
+    }
+    if (inv_diag && m == n) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) inv_diag[(int64_t)NDOF * n + i] = 1.f / acc[i * NDOF + i];
+    }
+  }
+}
+
+// Plain backward pass: re = Se ue - Fe from the materialised element matrix,
+// energy = ue . re, loss reduction (thermal / linear elastic only).
+template <int ET, int PH>
+__global__ void __launch_bounds__(256) k_plain_backward(const VecArgs A, const float* __restrict__ Ke,
+                                                        const float* __restrict__ Fe) {
+  constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM, NDOF = NdofT<PH, DIM>::V;
+  constexpr int ND = NEN * NDOF;
+  __shared__ float red[32];
+  const int b = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float energy = 0.f;
+  if (e < A.E) {
+    int nodes[NEN];
+    load_nodes<NEN>(A.conn, e, nodes);
+    const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+    float ue[ND];
+#pragma unroll
+    for (int a = 0; a < NEN; ++a) {
+      unsigned m = A.apply_dirichlet ? __ldg(A.dmask + nodes[a]) : 0u;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) {
+        int64_t d = (int64_t)NDOF * nodes[a] + c;
+        ue[a * NDOF + c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+      }
+    }
+    float r[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i) r[i] = 0.f;
+    const float4* K4 = reinterpret_cast<const float4*>(Ke + ((int64_t)b * A.E + e) * ND * ND);
+    // element matrix layout [a][b][i][j]; flat index f -> (a,b,i,j)
+#pragma unroll
+    for (int f4 = 0; f4 < ND * ND / 4; ++f4) {
+      float4 v = __ldg(K4 + f4);
+      float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        const int f = 4 * f4 + s;
+        const int blk = f / (NDOF * NDOF), ij = f % (NDOF * NDOF);
+        const int a = blk / NEN, bb = blk % NEN, i = ij / NDOF, j = ij % NDOF;
+        r[a * NDOF + i] = fmaf(vv[s], ue[bb * NDOF + j], r[a * NDOF + i]);
+      }
+    }
+    if (Fe) {
+#pragma unroll
+      for (int i = 0; i < ND; ++i) r[i] -= __ldg(Fe + ((int64_t)b * A.E + e) * ND + i);
+    }
+#pragma unroll
+    for (int i = 0; i < ND; ++i) energy = fmaf(ue[i], r[i], energy);
+    float4* gout = reinterpret_cast<float4*>(A.g + ((int64_t)b * A.E + e) * ND);
+#pragma unroll
+    for (int i = 0; i < ND / 4; ++i) gout[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
+  }
+  float be = block_sum(energy, red);
+  finish_loss(be, A, b, red);
+}
+
+// ---------------------------------------------------------------------------
+// workspace layouts
+// ---------------------------------------------------------------------------
+struct LossWS {
+  float* g;
+  float* gde;
+  float* partials;
+  unsigned* counters;
+  float* scale;
+  float* Ke;
+  float* Fe;
+};
+
+static int loss_blocks(const folgb_plan* p) { return (int)((p->E + 255) / 256); }
+
+static size_t layout_loss(const folgb_plan* p, int B, bool plain, void* base, size_t cap, LossWS* w) {
+  Bump bp(base, cap);
+  const int64_t ND = (int64_t)p->nen * p->ndof;
+  float* g = bp.take<float>((size_t)B * p->E * ND);
+  float* gde = p->ctrl_layout == FOLGB_CONTROL_NODAL ? bp.take<float>((size_t)B * p->E * p->nen) : nullptr;
+  float* partials = bp.take<float>((size_t)B * loss_blocks(p));
+  unsigned* counters = bp.take<unsigned>((size_t)B);
+  float* scale = bp.take<float>((size_t)B);
+  float* Ke = plain ? bp.take<float>((size_t)B * p->E * ND * ND) : nullptr;
+  float* Fe = (plain && p->mat.has_bf) ? bp.take<float>((size_t)B * p->E * ND) : nullptr;
+  if (w) *w = LossWS{g, gde, partials, counters, scale, Ke, Fe};
+  return align_up(bp.off);
+}
+
+static size_t layout_assemble(const folgb_plan* p, void* base, size_t cap, float** g, float** Ke) {
+  Bump bp(base, cap);
+  const int64_t ND = (int64_t)p->nen * p->ndof;
+  float* gg = bp.take<float>((size_t)p->E * ND);
+  float* kk = bp.take<float>((size_t)p->E * ND * ND);
+  if (g) *g = gg;
+  if (Ke) *Ke = kk;
+  return align_up(bp.off);
+}
+
+size_t pcg_workspace_bytes(const folgb_plan* p);
+
+static int mat_epb(int rec_size, int npts) {
+  const int budget = 96 * 1024;
+  int epb = budget / (rec_size * npts * 4);
+  if (epb > 32) epb = 32;
+  if (epb < 1) epb = 1;
+  return epb;
+}
+
+template <int ET, int PH, int MMODE>
+static int launch_matrix(const MatArgs& A0, int B, int npts, cudaStream_t s) {
+  using R = MatRec<ET, PH>;
+  MatArgs A = A0;
+  A.epb = mat_epb(R::SIZE, npts);
+  const size_t shm = (size_t)A.epb * npts * R::SIZE * sizeof(float);
+  FOLGB_CUDA_TRY(cudaFuncSetAttribute(k_elem_matrix<ET, PH, MMODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)shm));
+  dim3 grid((unsigned)((A.E + A.epb - 1) / A.epb), (unsigned)B);
+  trace_begin(KID_ELEM_MATRIX, s);
+  k_elem_matrix<ET, PH, MMODE><<<grid, 256, shm, s>>>(A);
+  trace_end(KID_ELEM_MATRIX, s);
+  FOLGB_LAUNCH_CHECK();
+  return FOLGB_OK;
+}
+
+int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, const float* scale, float* out,
+                  int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
+                  cudaStream_t s, const int* node_inst, const int* elem_inst) {
+  GatherArgs G;
+  G.node_inst = node_inst;
+  G.elem_inst = elem_inst;
+  G.E = p->E;
+  G.N = p->N;
+  G.nen = p->nen;
+  G.inc_ptr = p->d_inc_ptr;
+  G.inc_slot = p->d_inc_slot;
+  G.dmask = p->d_dmask;
+  G.g = g;
+  G.gde = gde;
+  G.scale = scale;
+  G.out = out;
+  G.out_stride = out_stride;
+  G.dctrl = dctrl;
+  G.dctrl_stride = dctrl_stride;
+  G.dctrl_elem = dctrl_elem;
+  G.rescale_elem = rescale_elem;
+  int64_t work = p->N > p->E ? p->N : p->E;
+  int blocks = (int)((work + 255) / 256);
+  int cap = num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  dim3 grid((unsigned)blocks, (unsigned)B);
+  trace_begin(KID_GATHER, s);
+  switch (p->ndof) {
+    case 1: k_node_gather<1><<<grid, 256, 0, s>>>(G); break;
+    case 2: k_node_gather<2><<<grid, 256, 0, s>>>(G); break;
+    case 3: k_node_gather<3><<<grid, 256, 0, s>>>(G); break;
+    default: return FOLGB_ERR_INVALID_ARGUMENT;
+  }
+  trace_end(KID_GATHER, s);
+  FOLGB_LAUNCH_CHECK();
+  return FOLGB_OK;
+}
+
+static VecArgs make_vec_args(const folgb_plan* p, int B, const float* control, int64_t cstride, const float* dofs,
+                             int64_t dstride, int apply_dirichlet, const LossWS& w, float* losses,
+                             float* dctrl_elem, int* status) {
+  VecArgs A;
+  A.E = p->E;
+  A.N = p->N;
+  A.conn = p->d_conn;
+  A.xyz4 = p->d_xyz4;
+  A.gp = p->d_gp;
+  A.ctrl = control;
+  A.ctrl_stride = cstride;
+  A.dofs = dofs;
+  A.dofs_stride = dstride;
+  A.dmask = p->d_dmask;
+  A.dval = p->d_dval;
+  A.apply_dirichlet = apply_dirichlet;
+  A.ctrl_layout = p->ctrl_layout;
+  A.mat = p->mat;
+  A.g = w.g;
+  A.gde = w.gde;
+  A.dctrl_elem = dctrl_elem;
+  A.partials = w.partials;
+  A.counters = w.counters;
+  A.losses = losses;
+  A.scale = w.scale;
+  A.exponent = (float)p->phys.loss_exponent;
+  A.inv_batch = 1.f / (float)B;
+  A.status = status;
+  return A;
+}
+
+static int check_loss_args(const folgb_plan* p, int B, const float* control, const float* dofs, const float* losses) {
+  if (!p || B <= 0 || !control || !dofs || !losses) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (B > 65535) return FOLGB_ERR_INVALID_ARGUMENT;
+  return FOLGB_OK;
+}
+
+}  // namespace folgb
+
+using namespace folgb;
+
+extern "C" size_t folgb_workspace_bytes(const folgb_plan* p, int32_t op, int32_t batch) {
+  if (!p || batch <= 0) return 0;
+  switch (op) {
+    case FOLGB_OP_LOSS_ADJOINT: return layout_loss(p, batch, false, nullptr, 0, nullptr);
+    case FOLGB_OP_PLAIN: return layout_loss(p, batch, true, nullptr, 0, nullptr);
+    case FOLGB_OP_ASSEMBLE: return layout_assemble(p, nullptr, 0, nullptr, nullptr);
+    case FOLGB_OP_PCG: return pcg_workspace_bytes(p);
+  }
+  return 0;
+}
+
+extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* control, int64_t control_stride,
+                                  const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet, float* losses,
+                                  float* dloss_ddofs, float* dloss_dcontrol, int32_t* device_status, void* workspace,
+                                  size_t workspace_bytes, void* stream) {
+  int rc = check_loss_args(p, B, control, dofs, losses);
+  if (rc) return rc;
+  LossWS w;
+  size_t need = layout_loss(p, B, false, workspace, workspace_bytes, &w);
+  if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * B, s));
+  const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
+  VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
+                            elem_ctrl ? dloss_dcontrol : nullptr, device_status);
+  dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
+  rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
+    constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
+    trace_begin(KID_ELEM_LOSS, s);
+    k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
+    trace_end(KID_ELEM_LOSS, s);
+    FOLGB_LAUNCH_CHECK();
+    return FOLGB_OK;
+  });
+  if (rc) return rc;
+  if (dloss_ddofs || dloss_dcontrol) {
+    rc = launch_gather(p, B, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
+                       elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
+                       (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr);
+  }
+  return rc;
+}
+
+extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const float* control, int64_t control_stride,
+                                        const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
+                                        float* losses, float* dloss_ddofs, float* dloss_dcontrol,
+                                        int32_t* device_status, void* workspace, size_t workspace_bytes,
+                                        void* stream) {
+  int rc = check_loss_args(p, B, control, dofs, losses);
+  if (rc) return rc;
+  if (p->physics == FOLGB_NEOHOOKE) return FOLGB_ERR_INVALID_ARGUMENT;
+  LossWS w;
+  size_t need = layout_loss(p, B, true, workspace, workspace_bytes, &w);
+  if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * B, s));
+  const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
+  MatArgs M;
+  M.E = p->E;
+  M.conn = p->d_conn;
+  M.xyz4 = p->d_xyz4;
+  M.gp = p->d_gp;
+  M.ctrl = control;
+  M.ctrl_stride = control_stride;
+  M.dofs = dofs;
+  M.dofs_stride = dofs_stride;
+  M.dmask = p->d_dmask;
+  M.dval = p->d_dval;
+  M.apply_dirichlet = apply_dirichlet;
+  M.ctrl_layout = p->ctrl_layout;
+  M.mat = p->mat;
+  M.transpose = 0;
+  M.epb = 0;
+  M.Ke = w.Ke;
+  M.Fe = w.Fe;
+  M.gde = w.gde;
+  M.dctrl_elem = elem_ctrl ? dloss_dcontrol : nullptr;
+  M.exponent = (float)p->phys.loss_exponent;
+  M.inv_batch = 1.f / (float)B;
+  M.status = device_status;
+  VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
+                            elem_ctrl ? dloss_dcontrol : nullptr, device_status);
+  const int npts = p->h_gp.npts;
+  dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
+  rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
+    constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
+    if constexpr (PH == FOLGB_NEOHOOKE) {
+      return (int)FOLGB_ERR_INVALID_ARGUMENT;
+    } else {
+      int r = launch_matrix<ET, PH, MAT_PLAIN>(M, B, npts, s);
+      if (r) return r;
+      trace_begin(KID_PLAIN_BACKWARD, s);
+      k_plain_backward<ET, PH><<<grid, 256, 0, s>>>(A, w.Ke, w.Fe);
+      trace_end(KID_PLAIN_BACKWARD, s);
+      FOLGB_LAUNCH_CHECK();
+      return (int)FOLGB_OK;
+    }
+  });
+  if (rc) return rc;
+  if (dloss_ddofs || dloss_dcontrol) {
+    rc = launch_gather(p, B, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
+                       elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
+                       (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr);
+  }
+  return rc;
+}
+
+extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const float* dofs, int32_t transpose,
+                              float* residual, float* csr_values, float* inv_diag, int32_t* device_status,
+                              void* workspace, size_t workspace_bytes, void* stream) {
+  if (!p || !control || !dofs) return FOLGB_ERR_INVALID_ARGUMENT;
+  if ((csr_values || inv_diag) && !p->has_csr) return FOLGB_ERR_NO_PATTERN;
+  float *g, *Ke;
+  size_t need = layout_assemble(p, workspace, workspace_bytes, &g, &Ke);
+  if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  LossWS w{g, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  VecArgs A = make_vec_args(p, 1, control, 0, dofs, 0, 0, w, nullptr, nullptr, device_status);
+  A.gde = nullptr;
+  MatArgs M;
+  M.E = p->E;
+  M.conn = p->d_conn;
+  M.xyz4 = p->d_xyz4;
+  M.gp = p->d_gp;
+  M.ctrl = control;
+  M.ctrl_stride = 0;
+  M.dofs = dofs;
+  M.dofs_stride = 0;
+  M.dmask = p->d_dmask;
+  M.dval = p->d_dval;
+  M.apply_dirichlet = 0;
+  M.ctrl_layout = p->ctrl_layout;
+  M.mat = p->mat;
+  M.transpose = transpose ? 1 : 0;
+  M.epb = 0;
+  M.Ke = Ke;
+  M.Fe = nullptr;
+  M.gde = nullptr;
+  M.dctrl_elem = nullptr;
+  M.exponent = 1.f;
+  M.inv_batch = 1.f;
+  M.status = device_status;
+  const int npts = p->h_gp.npts;
+  dim3 grid((unsigned)loss_blocks(p), 1u);
+  int rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
+    constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
+    if (residual) {
+      trace_begin(KID_ELEM_RESIDUAL, s);
+      k_elem_vector<ET, PH, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
+      trace_end(KID_ELEM_RESIDUAL, s);
+      FOLGB_LAUNCH_CHECK();
+    }
+    if (csr_values || inv_diag) return launch_matrix<ET, PH, MAT_ASSEMBLE>(M, 1, npts, s);
+    return (int)FOLGB_OK;
+  });
+  if (rc) return rc;
+  if (residual) {
+    rc = launch_gather(p, 1, g, nullptr, nullptr, residual, 0, nullptr, 0, nullptr, 0, s, nullptr, nullptr);
+    if (rc) return rc;
+  }
+  if (csr_values || inv_diag) {
+    int blocks = (int)((p->P + 255) / 256);
+    int cap = num_sms() * 16;
+    if (blocks > cap) blocks = cap;
+    trace_begin(KID_PAIR_REDUCE, s);
+    switch (p->ndof) {
+      case 1:
+        k_pair_reduce<1><<<blocks, 256, 0, s>>>(p->P, p->d_pair_row, p->d_adj_ptr, p->d_adj, p->d_pair_ptr,
+                                                 p->d_pair_slot, p->d_rowptr, Ke, csr_values, inv_diag);
+        break;
+      case 2:
+        k_pair_reduce<2><<<blocks, 256, 0, s>>>(p->P, p->d_pair_row, p->d_adj_ptr, p->d_adj, p->d_pair_ptr,
+                                                 p->d_pair_slot, p->d_rowptr, Ke, csr_values, inv_diag);
+        break;
+      case 3:
+        k_pair_reduce<3><<<blocks, 256, 0, s>>>(p->P, p->d_pair_row, p->d_adj_ptr, p->d_adj, p->d_pair_ptr,
+                                                 p->d_pair_slot, p->d_rowptr, Ke, csr_values, inv_diag);
+        break;
+    }
+    trace_end(KID_PAIR_REDUCE, s);
+    FOLGB_LAUNCH_CHECK();
+  }
+  return FOLGB_OK;
+}

@@ -1,0 +1,382 @@
+// Internal declarations shared by the folgb translation units.
+//
+// Data layout in HBM (built once per mesh by folgb_plan_create):
+//   conn      int32 [E][nen]          element -> node ids (16/32-byte rows)
+//   xyz4      float4[N]               node coordinates padded to 16 bytes
+//   inc_ptr   int32 [N+1]             node -> incident element slots (CSR)
+//   inc_slot  int32 [E*nen]           slot = e*nen + a, ascending e per node
+//   dmask     uint8 [N]               bit c set if dof (node, c) is Dirichlet
+//   dval      float [ndof*N]          Dirichlet value (read only where masked)
+//   gp        GPTable                 Gauss points: w, N, dN/dxi (fp32)
+// CSR tables (optional):
+//   adj_ptr/adj   node-pair pattern (sorted neighbours, self included)
+//   rowptr/colind canonical dof-level CSR (row ndof*n+c)
+//   pair_row      row node of each node pair
+//   pair_ptr/pair_slot  pair -> contributing element-matrix blocks,
+//                       slot = (e*nen + a)*nen + b, ascending e (the segments
+//                       of the deterministic reduction)
+#pragma once
+
+#include <cstdint>
+#include <cstdio>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/folgb.h"
+
+namespace folgb {
+
+constexpr int kMaxGP = 27;
+constexpr int kMaxNen = 8;
+
+struct GPTable {
+  int npts;
+  int pad_[3];
+  float w[kMaxGP];
+  float N[kMaxGP][kMaxNen];
+  float dN[kMaxGP][kMaxNen][3];
+};
+
+// Material/physics constants in the precision the kernels use.
+struct MatConst {
+  float lam, mu;        // elastic: D = e_gp * (lam, mu) isotropic (2-D: plane stress pair)
+  float lam_f, mu_f;    // neo-Hooke: lambda = lam_f * e_gp, mu = mu_f * e_gp
+  float beta, c;        // thermal conductivity nonlinearity
+  float bf[3];          // body force
+  int has_bf;
+  int shear_ref;        // 1: reference (doubled) shear for the FE residual/tangent
+};
+
+}  // namespace folgb
+
+struct folgb_plan {
+  folgb_physics phys;
+  int etype, physics, nen, dim, ndof;
+  int64_t E, N;
+  int ctrl_layout;
+  folgb::MatConst mat;
+  folgb::GPTable h_gp;
+  // device tables
+  int* d_conn = nullptr;
+  float4* d_xyz4 = nullptr;
+  int* d_inc_ptr = nullptr;
+  int* d_inc_slot = nullptr;
+  unsigned char* d_dmask = nullptr;
+  float* d_dval = nullptr;
+  folgb::GPTable* d_gp = nullptr;
+  std::vector<int64_t> dir_dofs;
+  std::vector<double> dir_vals;
+  // CSR tables
+  bool has_csr = false;
+  int64_t P = 0, nnz = 0, rows = 0;
+  int maxdeg = 0;
+  int* d_adj_ptr = nullptr;
+  int* d_adj = nullptr;
+  int* d_rowptr = nullptr;
+  int* d_colind = nullptr;
+  int* d_pair_row = nullptr;
+  int* d_pair_ptr = nullptr;
+  int* d_pair_slot = nullptr;
+};
+
+namespace folgb {
+
+// ---------------------------------------------------------------------------
+// error helpers
+// ---------------------------------------------------------------------------
+#define FOLGB_CUDA_TRY(expr)                                                        \
+  do {                                                                              \
+    cudaError_t err__ = (expr);                                                     \
+    if (err__ != cudaSuccess) {                                                     \
+      fprintf(stderr, "folgb: %s failed: %s (%s:%d)\n", #expr,                      \
+              cudaGetErrorString(err__), __FILE__, __LINE__);                       \
+      return (int)FOLGB_ERR_CUDA;                                                      \
+    }                                                                               \
+  } while (0)
+
+#define FOLGB_LAUNCH_CHECK() FOLGB_CUDA_TRY(cudaGetLastError())
+
+inline size_t align_up(size_t x, size_t a = 256) { return (x + a - 1) / a * a; }
+
+// Simple bump allocator over a caller-provided workspace.
+struct Bump {
+  char* base;
+  size_t cap, off = 0;
+  Bump(void* b, size_t c) : base(static_cast<char*>(b)), cap(c) {}
+  template <class T>
+  T* take(size_t count) {
+    size_t o = align_up(off);
+    off = o + count * sizeof(T);
+    return reinterpret_cast<T*>(base + o);
+  }
+  bool ok() const { return base != nullptr && off <= cap; }
+};
+
+int num_sms();
+
+// deterministic node gather of element vectors (elements.cu)
+int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, const float* scale, float* out,
+                  int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
+                  cudaStream_t s, const int* node_inst, const int* elem_inst);
+
+// ---------------------------------------------------------------------------
+// element traits
+// ---------------------------------------------------------------------------
+template <int ET> struct ElemT;
+template <> struct ElemT<FOLGB_QUAD4> { static constexpr int NEN = 4, DIM = 2; };
+template <> struct ElemT<FOLGB_HEX8>  { static constexpr int NEN = 8, DIM = 3; };
+template <> struct ElemT<FOLGB_TET4>  { static constexpr int NEN = 4, DIM = 3; };
+
+template <int PH, int DIM> struct NdofT { static constexpr int V = (PH == FOLGB_THERMAL) ? 1 : DIM; };
+
+// ---------------------------------------------------------------------------
+// small dense helpers (fp32)
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ float det_inv(const float (&J)[D][D], float (&Ji)[D][D]);
+
+template <>
+__device__ __forceinline__ float det_inv<2>(const float (&J)[2][2], float (&Ji)[2][2]) {
+  float det = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  float r = 1.0f / det;
+  Ji[0][0] = J[1][1] * r;
+  Ji[0][1] = -J[0][1] * r;
+  Ji[1][0] = -J[1][0] * r;
+  Ji[1][1] = J[0][0] * r;
+  return det;
+}
+
+template <>
+__device__ __forceinline__ float det_inv<3>(const float (&J)[3][3], float (&Ji)[3][3]) {
+  float c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  float c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  float c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  float det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  float r = 1.0f / det;
+  Ji[0][0] = c00 * r;
+  Ji[1][0] = c01 * r;
+  Ji[2][0] = c02 * r;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * r;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * r;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * r;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * r;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * r;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * r;
+  return det;
+}
+
+// Neo-Hookean kinematics and stress at one Gauss point, written to avoid the
+// fp32 cancellation of det(C) near C = I: J - 1 comes from the invariant
+// expansion of det(I + H) and ln J from log1p.
+//   psi = mu/2 (J^-2/3 I1 - 3) - mu lnJ + lam/2 ln^2 J           (3-D)
+//   psi = mu/2 (I1 - 2)        - mu lnJ + lam/2 ln^2 J           (2-D)
+// (fol/constitutive_material_models/neo_hooke.py:129-135, 178-181)
+template <int D>
+struct NHState {
+  float F[D][D];
+  float Ci[D][D];
+  float S[D][D];   // true second Piola-Kirchhoff stress
+  float lnJ, a, I1, psi, dpsi_dmu, dpsi_dlam;
+};
+
+template <int D>
+__device__ __forceinline__ void nh_state(const float (&H)[D][D], float mu, float lam, NHState<D>& st) {
+  float E[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(H[k][i], H[k][j], s);
+      E[i][j] = 0.5f * (H[i][j] + H[j][i] + s);
+      st.F[i][j] = H[i][j] + (i == j ? 1.f : 0.f);
+    }
+  float trE = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) trE += E[i][i];
+  float Jm1;
+  if constexpr (D == 3) {
+    float m2 = H[0][0] * H[1][1] - H[0][1] * H[1][0] + H[0][0] * H[2][2] - H[0][2] * H[2][0] +
+               H[1][1] * H[2][2] - H[1][2] * H[2][1];
+    float dH = H[0][0] * (H[1][1] * H[2][2] - H[1][2] * H[2][1]) -
+               H[0][1] * (H[1][0] * H[2][2] - H[1][2] * H[2][0]) +
+               H[0][2] * (H[1][0] * H[2][1] - H[1][1] * H[2][0]);
+    Jm1 = (H[0][0] + H[1][1] + H[2][2]) + m2 + dH;
+  } else {
+    Jm1 = (H[0][0] + H[1][1]) + (H[0][0] * H[1][1] - H[0][1] * H[1][0]);
+  }
+  float lnJ = log1pf(Jm1);
+  float J = 1.f + Jm1;
+  float detC = J * J;
+  float C[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) C[i][j] = 2.f * E[i][j] + (i == j ? 1.f : 0.f);
+  float rdet = 1.f / detC;
+  if constexpr (D == 3) {
+    st.Ci[0][0] = (C[1][1] * C[2][2] - C[1][2] * C[2][1]) * rdet;
+    st.Ci[0][1] = (C[0][2] * C[2][1] - C[0][1] * C[2][2]) * rdet;
+    st.Ci[0][2] = (C[0][1] * C[1][2] - C[0][2] * C[1][1]) * rdet;
+    st.Ci[1][1] = (C[0][0] * C[2][2] - C[0][2] * C[2][0]) * rdet;
+    st.Ci[1][2] = (C[0][2] * C[1][0] - C[0][0] * C[1][2]) * rdet;
+    st.Ci[2][2] = (C[0][0] * C[1][1] - C[0][1] * C[1][0]) * rdet;
+    st.Ci[1][0] = st.Ci[0][1];
+    st.Ci[2][0] = st.Ci[0][2];
+    st.Ci[2][1] = st.Ci[1][2];
+    float I1 = 3.f + 2.f * trE;
+    float am1 = expm1f(-2.f / 3.f * lnJ);
+    float a = 1.f + am1;
+    float iso = fmaf(am1, I1, 2.f * trE);  // J^-2/3 I1 - 3
+    st.psi = 0.5f * mu * iso - mu * lnJ + 0.5f * lam * lnJ * lnJ;
+    st.dpsi_dmu = 0.5f * iso - lnJ;
+    st.dpsi_dlam = 0.5f * lnJ * lnJ;
+    st.a = a;
+    st.I1 = I1;
+    float t = I1 * (1.f / 3.f);
+    float cc = lam * lnJ - mu;
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        st.S[i][j] = mu * a * ((i == j ? 1.f : 0.f) - t * st.Ci[i][j]) + cc * st.Ci[i][j];
+  } else {
+    st.Ci[0][0] = C[1][1] * rdet;
+    st.Ci[1][1] = C[0][0] * rdet;
+    st.Ci[0][1] = -C[0][1] * rdet;
+    st.Ci[1][0] = st.Ci[0][1];
+    float I1m2 = 2.f * trE;
+    st.psi = 0.5f * mu * I1m2 - mu * lnJ + 0.5f * lam * lnJ * lnJ;
+    st.dpsi_dmu = 0.5f * I1m2 - lnJ;
+    st.dpsi_dlam = 0.5f * lnJ * lnJ;
+    st.a = 1.f;
+    st.I1 = 2.f + I1m2;
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int j = 0; j < 2; ++j)
+        st.S[i][j] = mu * ((i == j ? 1.f : 0.f) - st.Ci[i][j]) + lam * lnJ * st.Ci[i][j];
+  }
+  st.lnJ = lnJ;
+}
+
+// Directional derivative dS of the true S along a symmetric dC.
+template <int D>
+__device__ __forceinline__ void nh_dS(const NHState<D>& st, float mu, float lam, const float (&dC)[D][D],
+                                      float (&dS)[D][D]) {
+  float CidC[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(st.Ci[i][k], dC[k][j], s);
+      CidC[i][j] = s;
+    }
+  float tr = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) tr += CidC[i][i];
+  float dCi[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(CidC[i][k], st.Ci[k][j], s);
+      dCi[i][j] = -s;
+    }
+  float dlnJ = 0.5f * tr;
+  float cc = lam * st.lnJ - mu;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) dS[i][j] = lam * dlnJ * st.Ci[i][j] + cc * dCi[i][j];
+  if constexpr (D == 3) {
+    float da = -(1.f / 3.f) * st.a * tr;
+    float dI1 = dC[0][0] + dC[1][1] + dC[2][2];
+    float t = st.I1 * (1.f / 3.f);
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+        dS[i][j] += mu * (da * ((i == j ? 1.f : 0.f) - t * st.Ci[i][j]) -
+                          st.a * (dI1 * (1.f / 3.f) * st.Ci[i][j] + t * dCi[i][j]));
+  }
+}
+
+// Voigt index pairs: 3-D [xx,yy,zz,yz,xz,xy], 2-D [xx,yy,xy]
+// (fol/constitutive_material_models/utils.py:13-32).
+template <int D> struct Voigt;
+template <> struct Voigt<3> {
+  static constexpr int NV = 6;
+  __device__ static constexpr int p(int v) { return v == 0 ? 0 : v == 1 ? 1 : v == 2 ? 2 : v == 3 ? 1 : 0; }
+  __device__ static constexpr int q(int v) { return v == 0 ? 0 : v == 1 ? 1 : v == 2 ? 2 : v == 3 ? 2 : v == 4 ? 2 : 1; }
+};
+template <> struct Voigt<2> {
+  static constexpr int NV = 3;
+  __device__ static constexpr int p(int v) { return v == 0 ? 0 : v == 1 ? 1 : 0; }
+  __device__ static constexpr int q(int v) { return v == 0 ? 0 : v == 1 ? 1 : 1; }
+};
+
+// deterministic block reduction of one float (blockDim multiple of 32, <= 1024)
+__device__ __forceinline__ float block_sum(float v, float* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  int nw = blockDim.x >> 5;
+  float r = 0.f;
+  if (threadIdx.x < 32) {
+    r = (l < nw) ? sh[l] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;  // valid in thread 0
+}
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  __syncthreads();
+  if (l == 0) sh[w] = v;
+  __syncthreads();
+  int nw = blockDim.x >> 5;
+  double r = 0.0;
+  if (threadIdx.x < 32) {
+    r = (l < nw) ? sh[l] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_xor_sync(0xffffffffu, r, o);
+  }
+  return r;
+}
+
+}  // namespace folgb
+
+namespace folgb {
+// ---------------------------------------------------------------------------
+// Opt-in kernel tracing: CUDA events recorded on the caller's stream around
+// each kernel launch, summed per kernel id when read (folgb_trace_read).
+// ---------------------------------------------------------------------------
+enum KernelId {
+  KID_ELEM_LOSS = 0,
+  KID_GATHER = 1,
+  KID_ELEM_MATRIX = 2,
+  KID_PAIR_REDUCE = 3,
+  KID_PLAIN_BACKWARD = 4,
+  KID_ELEM_RESIDUAL = 5,
+  KID_PCG_SPMV = 6,
+  KID_PCG_UPDATE = 7,
+  KID_BATCH_LOSS = 8,
+  KID_HEX8_FUSED = 9,
+  KID_COUNT = 16
+};
+void trace_begin(int kid, cudaStream_t s);
+void trace_end(int kid, cudaStream_t s);
+}  // namespace folgb

@@ -1,0 +1,91 @@
+// Opt-in kernel tracing (CUDA events on the launching stream).  The reference
+// has only wall-clock decorators around its Python methods
+// (fol/tools/decoration_functions.py:7-32), which see dispatch time, not
+// device time; these events see the kernels themselves.
+#include <mutex>
+#include <vector>
+
+#include "folgb_internal.cuh"
+
+namespace folgb {
+namespace {
+struct Pending {
+  int kid;
+  cudaEvent_t a, b;
+};
+std::mutex mu;
+bool enabled = false;
+std::vector<Pending> pending;
+std::vector<cudaEvent_t> pool;
+int64_t launches[KID_COUNT];
+double total_ms[KID_COUNT];
+cudaEvent_t open_event[KID_COUNT];
+
+cudaEvent_t get_event() {
+  if (!pool.empty()) {
+    cudaEvent_t e = pool.back();
+    pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  cudaEventCreate(&e);
+  return e;
+}
+}  // namespace
+
+void trace_begin(int kid, cudaStream_t s) {
+  if (!enabled || kid < 0 || kid >= KID_COUNT) return;
+  std::lock_guard<std::mutex> g(mu);
+  cudaEvent_t e = get_event();
+  cudaEventRecord(e, s);
+  open_event[kid] = e;
+}
+
+void trace_end(int kid, cudaStream_t s) {
+  if (!enabled || kid < 0 || kid >= KID_COUNT) return;
+  std::lock_guard<std::mutex> g(mu);
+  cudaEvent_t e = get_event();
+  cudaEventRecord(e, s);
+  pending.push_back({kid, open_event[kid], e});
+}
+}  // namespace folgb
+
+using namespace folgb;
+
+extern "C" int folgb_trace_enable(int32_t on) {
+  std::lock_guard<std::mutex> g(mu);
+  enabled = on != 0;
+  return FOLGB_OK;
+}
+
+extern "C" int folgb_trace_reset(void) {
+  std::lock_guard<std::mutex> g(mu);
+  for (auto& p : pending) {
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  pending.clear();
+  for (int i = 0; i < KID_COUNT; ++i) {
+    launches[i] = 0;
+    total_ms[i] = 0.0;
+  }
+  return FOLGB_OK;
+}
+
+extern "C" int folgb_trace_read(int32_t kernel_id, int64_t* n_launches, double* ms) {
+  if (kernel_id < 0 || kernel_id >= KID_COUNT) return FOLGB_ERR_INVALID_ARGUMENT;
+  std::lock_guard<std::mutex> g(mu);
+  for (auto& p : pending) {
+    FOLGB_CUDA_TRY(cudaEventSynchronize(p.b));
+    float t = 0.f;
+    FOLGB_CUDA_TRY(cudaEventElapsedTime(&t, p.a, p.b));
+    launches[p.kid] += 1;
+    total_ms[p.kid] += t;
+    pool.push_back(p.a);
+    pool.push_back(p.b);
+  }
+  pending.clear();
+  if (n_launches) *n_launches = launches[kernel_id];
+  if (ms) *ms = total_ms[kernel_id];
+  return FOLGB_OK;
+}

@@ -1,0 +1,475 @@
+"""FE loss classes: the reference's FiniteElementLoss API over libfolgb.so.
+
+Mirrors fol/loss_functions/fe_loss.py:19-318 and its subclasses
+(thermal.py, mechanical.py, mechanical_neohooke_AD.py): the same class names,
+constructor arguments (name, loss_settings, fe_mesh), settings keys and
+methods.  Arrays go to the GPU as float32 torch tensors; every numerical step
+runs in the CUDA kernels behind include/folgb.h.  There is no CPU path.
+
+Differences a caller can see:
+* ComputeBatchLossAndGrad returns the gradients jax.grad would give for the
+  dofs, and the true derivative of the loss value for the control (the
+  reference's jax.grad wrt the control is 0 for the stop_gradient losses,
+  mechanical.py:116, thermal.py:45-49).
+* loss_settings["control_layout"] = "element" takes one control value per
+  element (de = value * 1); the default "nodal" gathers nodal controls by
+  connectivity as the reference does.
+* ComputeJacobianMatrixAndResidualVector returns a CSRJacobian (canonical CSR,
+  the pattern scipy.sparse.csr_array builds from the reference's BCOO).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _capi as capi
+from .mesh import Mesh
+
+_ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
+_NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _dev(x, dtype=None):
+    torch = _torch()
+    dtype = dtype or torch.float32
+    if isinstance(x, torch.Tensor):
+        return x.to(device="cuda", dtype=dtype).contiguous()
+    return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda").contiguous()
+
+
+class Plan:
+    """Owns one folgb_plan (mesh tables on the device) and cached workspaces."""
+
+    def __init__(self, phys: capi.Physics, conn: np.ndarray, xyz: np.ndarray, dir_idx: np.ndarray,
+                 dir_val: np.ndarray, build_csr: bool):
+        self.lib = capi.load()
+        conn = np.ascontiguousarray(conn, dtype=np.int64)
+        xyz3 = np.zeros((len(xyz), 3))
+        xyz = np.asarray(xyz, dtype=np.float64)
+        xyz3[:, : xyz.shape[1]] = xyz
+        di = np.ascontiguousarray(dir_idx, dtype=np.int64)
+        dv = np.ascontiguousarray(dir_val, dtype=np.float64)
+        self.phys = phys
+        h = C.c_void_p()
+        _torch().cuda.init()
+        rc = self.lib.folgb_plan_create(C.byref(h), C.byref(phys), conn.ctypes.data, len(conn), xyz3.ctypes.data,
+                                        len(xyz3), di.ctypes.data if len(di) else None,
+                                        dv.ctypes.data if len(dv) else None, len(di), int(build_csr))
+        capi.check("folgb_plan_create", rc)
+        self.handle = h
+        nd, tot, rows, nnz = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int64()
+        capi.check("folgb_plan_info", self.lib.folgb_plan_info(h, C.byref(nd), C.byref(tot), C.byref(rows),
+                                                                C.byref(nnz)))
+        self.ndof, self.total_dofs, self.rows, self.nnz = nd.value, tot.value, rows.value, nnz.value
+        self.num_elements = len(conn)
+        self.num_nodes = len(xyz3)
+        self.has_csr = bool(build_csr)
+        self._ws = {}
+        self._pattern = None
+
+    def workspace(self, op: int, batch: int = 1):
+        torch = _torch()
+        n = int(self.lib.folgb_workspace_bytes(self.handle, op, batch))
+        buf = self._ws.get(op)
+        if buf is None or buf.numel() < n:
+            buf = torch.empty(max(n, 256), dtype=torch.uint8, device="cuda")
+            self._ws[op] = buf
+        return buf
+
+    def set_dirichlet_values(self, values: np.ndarray, load_increment: float = 1.0):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        capi.check("folgb_plan_set_dirichlet_values",
+                   self.lib.folgb_plan_set_dirichlet_values(self.handle, v.ctypes.data if len(v) else None,
+                                                            float(load_increment)))
+
+    def pattern(self):
+        """Canonical CSR pattern (indptr, indices) as int32 device tensors."""
+        torch = _torch()
+        if self._pattern is None:
+            indptr = torch.empty(self.rows + 1, dtype=torch.int32, device="cuda")
+            indices = torch.empty(self.nnz, dtype=torch.int32, device="cuda")
+            capi.check("folgb_csr_pattern", self.lib.folgb_csr_pattern(self.handle, capi.ptr(indptr),
+                                                                        capi.ptr(indices), capi.stream_handle()))
+            self._pattern = (indptr, indices)
+        return self._pattern
+
+    def __del__(self):
+        try:
+            if getattr(self, "handle", None):
+                self.lib.folgb_plan_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+
+@dataclass
+class CSRJacobian:
+    """BC-applied Jacobian in canonical CSR form (device tensors)."""
+    indptr: object
+    indices: object
+    data: object
+    inv_diag: object
+    shape: tuple
+    plan: Plan
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+        return sp.csr_array((self.data.double().cpu().numpy(), self.indices.cpu().numpy(),
+                             self.indptr.cpu().numpy()), shape=self.shape)
+
+    def to_torch(self):
+        torch = _torch()
+        return torch.sparse_csr_tensor(self.indptr, self.indices, self.data, size=self.shape)
+
+    def todense(self):
+        return self.to_scipy().toarray()
+
+    def matvec(self, x):
+        torch = _torch()
+        x = _dev(x)
+        y = torch.empty_like(x)
+        capi.check("folgb_spmv", self.plan.lib.folgb_spmv(self.plan.handle, capi.ptr(self.data), capi.ptr(x),
+                                                          capi.ptr(y), capi.stream_handle()))
+        return y
+
+
+class FiniteElementLoss:
+    """fe_loss.py:19-318 over the GB300 kernels."""
+
+    physics = None  # set by subclasses
+
+    def __init__(self, name: str, loss_settings: dict, fe_mesh: Mesh):
+        self._name = name
+        self.loss_settings = loss_settings
+        self.dofs = loss_settings["ordered_dofs"]
+        self.element_type = loss_settings["element_type"]
+        self.fe_mesh = fe_mesh
+        self.initialized = False
+        if "dirichlet_bc_dict" not in loss_settings:
+            raise ValueError("dirichlet_bc_dict should provided in the loss settings !")
+
+    def GetName(self):
+        return self._name
+
+    # fe_loss.py:34-55
+    def _create_dofs_dict(self):
+        n = len(self.dofs)
+        idx, val = [], []
+        for di, dof in enumerate(self.dofs):
+            for set_name, value in self.loss_settings["dirichlet_bc_dict"].get(dof, {}).items():
+                nodes = np.asarray(self.fe_mesh.GetNodeSet(set_name), dtype=np.int64)
+                idx.append(n * nodes + di)
+                val.append(float(value) * np.ones(len(nodes)))
+        self.dirichlet_indices = np.concatenate(idx) if idx else np.zeros(0, np.int64)
+        self.dirichlet_values = np.concatenate(val) if val else np.zeros(0)
+        all_idx = np.arange(n * self.fe_mesh.GetNumberOfNodes())
+        self.non_dirichlet_indices = np.setdiff1d(all_idx, self.dirichlet_indices)
+
+    def _physics_struct(self) -> capi.Physics:
+        s = self.loss_settings
+        mat = s.get("material_dict", {})
+        p = capi.Physics()
+        p.element_type = _ETYPE[self.element_type]
+        p.physics = self.physics
+        p.num_gp = int(self.num_gp)
+        p.control_layout = capi.CONTROL_ELEMENT if s.get("control_layout", "nodal") == "element" else capi.CONTROL_NODAL
+        p.shear_mode = capi.SHEAR_CONSISTENT if s.get("voigt_shear_mode", "reference") == "consistent" else capi.SHEAR_REFERENCE
+        p.young_modulus = float(mat.get("young_modulus", 1.0))
+        p.poisson_ratio = float(mat.get("poisson_ratio", 0.3))
+        bf = np.zeros(3)
+        if "body_foce" in s and self.physics != capi.THERMAL:
+            b = np.asarray(s["body_foce"], dtype=np.float64).ravel()
+            bf[: len(b)] = b
+        p.body_force[0], p.body_force[1], p.body_force[2] = bf
+        p.beta = float(getattr(self, "_beta", 0.0))
+        p.c = float(getattr(self, "_c", 1.0))
+        p.loss_exponent = float(self.loss_function_exponent)
+        return p
+
+    def Initialize(self, reinitialize=False) -> None:
+        if self.initialized and not reinitialize:
+            return
+        s = self.loss_settings
+        self.number_dofs_per_node = len(self.dofs)
+        self.total_number_of_dofs = len(self.dofs) * self.fe_mesh.GetNumberOfNodes()
+        self._create_dofs_dict()
+        self.number_of_unknown_dofs = self.non_dirichlet_indices.size
+        # fe_loss.py:68-83 (order 1 when unset)
+        self.num_gp = int(s.get("num_gp", 1))
+        s["num_gp"] = self.num_gp
+        if self.num_gp not in (1, 2, 3):
+            raise ValueError(f" number gauss points {self.num_gp} is not supported ! ")
+        if "compute_dims" not in s:
+            raise ValueError(f"compute_dims must be provided in the loss settings of {self.GetName()}! ")
+        self.dim = s["compute_dims"]
+        self.loss_function_exponent = float(s.get("loss_function_exponent", 1.0))
+        self.parametric_boundary_learning = bool(s.get("parametric_boundary_learning", False))
+        conn = np.asarray(self.fe_mesh.GetElementsNodes(self.element_type), dtype=np.int64)
+        xyz = np.asarray(self.fe_mesh.GetNodesCoordinates(), dtype=np.float64)
+        self._conn, self._xyz = conn, xyz
+        self._plan = Plan(self._physics_struct(), conn, xyz, self.dirichlet_indices, self.dirichlet_values, False)
+        self._csr_plan = None
+        self._status = _torch().zeros(1, dtype=_torch().int32, device="cuda")
+        self.initialized = True
+
+    def _get_csr_plan(self) -> Plan:
+        if self._csr_plan is None:
+            self._csr_plan = Plan(self._physics_struct(), self._conn, self._xyz, self.dirichlet_indices,
+                                  self.dirichlet_values, True)
+        return self._csr_plan
+
+    def Finalize(self) -> None:
+        pass
+
+    def GetNumberOfUnknowns(self):
+        return self.number_of_unknown_dofs
+
+    def GetTotalNumberOfDOFs(self):
+        return self.total_number_of_dofs
+
+    def GetDOFs(self):
+        return self.dofs
+
+    def GetNumberOfControls(self):
+        if self.loss_settings.get("control_layout", "nodal") == "element":
+            return self.fe_mesh.GetNumberOfElements(self.element_type)
+        return self.fe_mesh.GetNumberOfNodes()
+
+    def GetDeviceStatus(self) -> int:
+        """Status bits raised by the kernels (1 << FOLGB_ERR_*); reading it synchronises."""
+        return int(self._status.item())
+
+    def CheckDeviceStatus(self):
+        """Raise FolgbError if a kernel flagged a non-positive detJ or a
+        non-finite value, then clear the flags."""
+        st = self.GetDeviceStatus()
+        self._status.zero_()
+        for code in (capi.ERR_NONPOSITIVE_DETJ, capi.ERR_NAN):
+            if (st >> code) & 1:
+                raise capi.FolgbError("FE kernel", code)
+
+    # fe_loss.py:91-100, 124-125
+    def GetFullDofVector(self, known_dofs, unknown_dofs):
+        torch = _torch()
+        full = _dev(unknown_dofs).clone()
+        squeeze = full.dim() == 1
+        if squeeze:
+            full = full[None]
+        idx = torch.as_tensor(self.dirichlet_indices, device="cuda")
+        if self.parametric_boundary_learning:
+            full[:, idx] = _dev(known_dofs).reshape(full.shape[0], -1)
+        else:
+            full[:, idx] = torch.as_tensor(self.dirichlet_values, dtype=torch.float32, device="cuda")
+        return full[0] if squeeze else full
+
+    # fe_loss.py:186-189
+    def ApplyDirichletBCOnDofVector(self, full_dof_vector, load_increment: float = 1.0):
+        torch = _torch()
+        u = _dev(full_dof_vector).clone()
+        idx = torch.as_tensor(self.dirichlet_indices, device="cuda")
+        u[..., idx] = torch.as_tensor(load_increment * self.dirichlet_values, dtype=torch.float32, device="cuda")
+        return u
+
+    def _batched(self, batch_params, batch_dofs):
+        P = _dev(batch_params)
+        U = _dev(batch_dofs)
+        U = U.reshape(-1, self.total_number_of_dofs) if U.dim() != 2 else U
+        if U.shape[1] != self.total_number_of_dofs:
+            raise ValueError(f"dofs must have {self.total_number_of_dofs} entries per instance")
+        ncontrol = self.GetNumberOfControls()
+        P = P.reshape(-1, ncontrol)
+        B = U.shape[0]
+        if P.shape[0] not in (1, B):
+            raise ValueError("batch_params must have 1 or batch rows")
+        return P, U, B
+
+    def ComputeBatchLossAndGrad(self, batch_params, batch_dofs, grads: bool = True, plain: bool = False):
+        """Fused FE loss + adjoint (fe_loss.py:250-262 and its reverse pass).
+
+        Returns (mean, (min, max, mean), per-instance losses, dLoss/d dofs,
+        dLoss/d params); the gradients are None when grads is False."""
+        torch = _torch()
+        P, U, B = self._batched(batch_params, batch_dofs)
+        apply_bc = 1
+        if self.parametric_boundary_learning:
+            U = self.GetFullDofVector(P, U)
+            apply_bc = 0
+        losses = torch.empty(B, dtype=torch.float32, device="cuda")
+        du = torch.empty_like(U) if grads else None
+        dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if grads else None
+        op = capi.OP_PLAIN if plain else capi.OP_LOSS_ADJOINT
+        ws = self._plan.workspace(op, B)
+        fn = self._plan.lib.folgb_loss_adjoint_plain if plain else self._plan.lib.folgb_loss_adjoint
+        rc = fn(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1], capi.ptr(U), U.shape[1],
+                apply_bc, capi.ptr(losses), capi.ptr(du), capi.ptr(dp), capi.ptr(self._status), capi.ptr(ws),
+                ws.numel(), capi.stream_handle())
+        capi.check("folgb_loss_adjoint_plain" if plain else "folgb_loss_adjoint", rc)
+        mean = losses.mean()
+        return mean, (losses.min(), losses.max(), mean), losses, du, dp
+
+    def ComputeBatchLoss(self, batch_params, batch_dofs):
+        mean, stats, _, _, _ = self.ComputeBatchLossAndGrad(batch_params, batch_dofs, grads=False)
+        return mean, stats
+
+    def ComputeTotalEnergy(self, total_control_vars, total_primal_vars):
+        """Sum of element energies for one instance (fe_loss.py:175-176); the
+        dofs are used as given (no Dirichlet overwrite)."""
+        torch = _torch()
+        P, U, B = self._batched(total_control_vars, total_primal_vars)
+        losses = torch.empty(B, dtype=torch.float32, device="cuda")
+        ws = self._plan.workspace(capi.OP_LOSS_ADJOINT, B)
+        # a plan with exponent != 1 would raise the sum to p; the energy is p = 1
+        if self.loss_function_exponent != 1.0:
+            raise NotImplementedError("ComputeTotalEnergy with loss_function_exponent != 1")
+        rc = self._plan.lib.folgb_loss_adjoint(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1],
+                                               capi.ptr(U), U.shape[1], 0, capi.ptr(losses), None, None,
+                                               capi.ptr(self._status), capi.ptr(ws), ws.numel(), capi.stream_handle())
+        capi.check("folgb_loss_adjoint", rc)
+        return losses[0] if B == 1 else losses
+
+    # fe_loss.py:264-318
+    def ComputeJacobianMatrixAndResidualVector(self, total_control_vars, total_primal_vars,
+                                               transpose_jacobian: bool = False, with_matrix: bool = True):
+        torch = _torch()
+        plan = self._get_csr_plan()
+        ctrl = _dev(total_control_vars).reshape(-1)
+        u = _dev(total_primal_vars).reshape(-1)
+        residual = torch.empty(self.total_number_of_dofs, dtype=torch.float32, device="cuda")
+        data = torch.empty(plan.nnz, dtype=torch.float32, device="cuda") if with_matrix else None
+        inv_diag = torch.empty(self.total_number_of_dofs, dtype=torch.float32, device="cuda") if with_matrix else None
+        ws = plan.workspace(capi.OP_ASSEMBLE)
+        rc = plan.lib.folgb_assemble(plan.handle, capi.ptr(ctrl), capi.ptr(u), int(bool(transpose_jacobian)),
+                                     capi.ptr(residual), capi.ptr(data), capi.ptr(inv_diag), capi.ptr(self._status),
+                                     capi.ptr(ws), ws.numel(), capi.stream_handle())
+        capi.check("folgb_assemble", rc)
+        if not with_matrix:
+            return None, residual
+        indptr, indices = plan.pattern()
+        n = self.total_number_of_dofs
+        return CSRJacobian(indptr, indices, data, inv_diag, (n, n), plan), residual
+
+    def ComputeElement(self, xyze, de, uvwe):
+        """One element's (energy, residual, stiffness) through the GPU kernels
+        (the element API of fe_loss.py:143-147), as float64 numpy arrays."""
+        xyze = np.asarray(xyze, dtype=np.float64)
+        nen = _NEN[self.element_type]
+        de = np.asarray(de, dtype=np.float64).reshape(-1)
+        ue = np.asarray(uvwe, dtype=np.float64).reshape(-1)
+        mesh = Mesh("element", "element.mem")
+        mesh.node_ids = np.arange(nen)
+        mesh.nodes_coordinates = xyze
+        mesh.elements_nodes = {self.element_type: np.arange(nen)[None]}
+        settings = dict(self.loss_settings)
+        settings["dirichlet_bc_dict"] = {d: {} for d in self.dofs}
+        settings["loss_function_exponent"] = 1.0
+        settings["control_layout"] = "nodal"
+        one = type(self)(self._name + "_element", settings, mesh)
+        one.Initialize()
+        jac, res = one.ComputeJacobianMatrixAndResidualVector(de, ue)
+        en = one.ComputeTotalEnergy(de, ue)
+        return float(en.item()), res.double().cpu().numpy(), jac.todense()
+
+
+# ---------------------------------------------------------------------------
+# element physics (class names and defaults of the reference)
+# ---------------------------------------------------------------------------
+
+def _with(loss_settings, **kw):
+    return {**loss_settings, **kw}
+
+
+class ThermalLoss(FiniteElementLoss):
+    """thermal.py:14-49: k_gp = (N.de)(1 + beta (N.T)^c); energy T.sg(Se T - Fe)."""
+    physics = capi.THERMAL
+
+    def Initialize(self, reinitialize=False) -> None:
+        self._beta = float(self.loss_settings.get("beta", 0.0))
+        self._c = float(self.loss_settings.get("c", 1.0))
+        super().Initialize(reinitialize)
+
+
+class ThermalLoss2DQuad(ThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["T"], element_type="quad"), fe_mesh)
+
+
+class ThermalLoss3DHexa(ThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["T"], element_type="hexahedron"),
+                         fe_mesh)
+
+
+class ThermalLoss3DTetra(ThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["T"], element_type="tetra"), fe_mesh)
+
+
+class MechanicalLoss(FiniteElementLoss):
+    """mechanical.py:13-117: Se = sum w detJ (N.de) B^T D B; energy u.sg(Se u - Fe)."""
+    physics = capi.ELASTIC
+
+    def Initialize(self, reinitialize=False) -> None:
+        if "material_dict" not in self.loss_settings:
+            raise ValueError("material_dict should provided in the loss settings !")
+        super().Initialize(reinitialize)
+
+
+class MechanicalLoss3DHexa(MechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="hexahedron"), fe_mesh)
+
+
+class MechanicalLoss3DTetra(MechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="tetra"), fe_mesh)
+
+
+class MechanicalLoss2DQuad(MechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["Ux", "Uy"], element_type="quad"),
+                         fe_mesh)
+
+
+class NeoHookeMechanicalLoss(FiniteElementLoss):
+    """mechanical_neohooke_AD.py:18-293: energy sum w detJ psi(C); residual
+    B^T S_voigt - Fe with the reference's doubled-shear S_voigt unless
+    loss_settings["voigt_shear_mode"] = "consistent"."""
+    physics = capi.NEOHOOKE
+
+    def Initialize(self, reinitialize=False) -> None:
+        if "material_dict" not in self.loss_settings:
+            raise ValueError("material_dict should provided in the loss settings !")
+        super().Initialize(reinitialize)
+
+
+class NeoHookeMechanicalLoss3DTetra(NeoHookeMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="tetra"), fe_mesh)
+
+
+class NeoHookeMechanicalLoss3DHexa(NeoHookeMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="hexahedron"), fe_mesh)
+
+
+class NeoHookeMechanicalLoss2DQuad(NeoHookeMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["Ux", "Uy"], element_type="quad"),
+                         fe_mesh)

@@ -1,0 +1,144 @@
+"""FE solvers: the reference's solver API over the GB300 assembly and PCG.
+
+Mirrors fol/solvers/solver.py:11-49, fe_solver.py:21-105,
+fe_linear_residual_based_solver.py:10-22 and
+fe_nonlinear_residual_based_solver.py:15-170.  The linear solve is the
+Jacobi-preconditioned CG of folgb_pcg (fp32 vectors, fp64 inner products and
+norms, x0 = 0) on the assembled CSR; the reference's BiCGSTAB / direct / PETSc
+choices ("JAX-bicgstab", "JAX-direct", "PETSc-*") all map to it.  With the
+row-only Dirichlet rule (fe_loss.py:191-207) the BC rows of the system are
+diag * dx = 0, so CG started from 0 never leaves the free-dof subspace and
+solves K_FF dx_F = -r_F exactly as a symmetric system.
+"""
+from __future__ import annotations
+
+import copy
+import ctypes as C
+
+import numpy as np
+
+from . import _capi as capi
+from .loss import FiniteElementLoss, _dev, _torch
+
+
+def UpdateDefaultDict(default_dict: dict, given_dict: dict):
+    """Only keys already in default_dict are taken (fol/tools/usefull_functions.py:569-573)."""
+    out = copy.deepcopy(default_dict)
+    out.update({k: given_dict[k] for k in default_dict if k in given_dict})
+    return out
+
+
+class Solver:
+    def __init__(self, solver_name: str) -> None:
+        self._name = solver_name
+
+    def GetName(self) -> str:
+        return self._name
+
+    def Initialize(self) -> None:
+        pass
+
+    def Solve(self, control_vars, dofs):
+        raise NotImplementedError
+
+    def BatchSolve(self, batch_control_vars, batch_dofs):
+        """solver.py:47-49 (a vmap there; a loop of device solves here)."""
+        torch = _torch()
+        ctrl = _dev(batch_control_vars)
+        dofs = _dev(batch_dofs)
+        return torch.stack([self.Solve(c, d) for c, d in zip(ctrl, dofs)]).squeeze()
+
+    def Finalize(self) -> None:
+        pass
+
+
+class FiniteElementSolver(Solver):
+    def __init__(self, fe_solver_name: str, fe_loss_function: FiniteElementLoss, fe_solver_settings: dict = {}):
+        super().__init__(fe_solver_name)
+        self.fe_loss_function = fe_loss_function
+        self.fe_solver_settings = fe_solver_settings
+        self.linear_solver_settings = {"solver": "JAX-bicgstab", "tol": 1e-6, "atol": 1e-6, "maxiter": 1000,
+                                       "pre-conditioner": "ilu", "check_every": 32}
+        self.last_linear_info = None
+
+    def Initialize(self) -> None:
+        if "linear_solver_settings" in self.fe_solver_settings:
+            self.linear_solver_settings = UpdateDefaultDict(self.linear_solver_settings,
+                                                            self.fe_solver_settings["linear_solver_settings"])
+        name = self.linear_solver_settings["solver"]
+        known = ["PETSc-bcgsl", "PETSc-tfqmr", "PETSc-minres", "PETSc-gmres", "JAX-direct", "JAX-bicgstab",
+                 "GB300-pcg"]
+        if name not in known:
+            raise ValueError(f"linear solver {name} does exist, available options are {known}")
+        self.LinearSolve = self.PCGLinearSolver
+
+    def PCGLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
+        """Solve tangent_matrix dx = -residual with Jacobi-PCG; returns dx."""
+        torch = _torch()
+        plan = tangent_matrix.plan
+        b = -_dev(residual_vector)
+        x = torch.empty_like(b)
+        ws = plan.workspace(capi.OP_PCG)
+        iters, rel = C.c_int32(), C.c_double()
+        s = self.linear_solver_settings
+        rc = plan.lib.folgb_pcg(plan.handle, capi.ptr(tangent_matrix.data), capi.ptr(tangent_matrix.inv_diag),
+                                capi.ptr(b), capi.ptr(x), float(s["tol"]), int(s["maxiter"]),
+                                int(s.get("check_every", 32)), C.byref(iters), C.byref(rel), capi.ptr(ws), ws.numel(),
+                                capi.stream_handle())
+        self.last_linear_info = {"iterations": iters.value, "relative_residual": rel.value, "status": rc}
+        if rc not in (capi.OK, capi.ERR_NOT_CONVERGED):
+            capi.check("folgb_pcg", rc)
+        return x
+
+
+class FiniteElementLinearResidualBasedSolver(FiniteElementSolver):
+    """fe_linear_residual_based_solver.py:15-22."""
+
+    def Solve(self, current_control_vars, current_dofs):
+        loss = self.fe_loss_function
+        u = loss.ApplyDirichletBCOnDofVector(current_dofs)
+        jac, r = loss.ComputeJacobianMatrixAndResidualVector(current_control_vars, u)
+        du = self.LinearSolve(jac, r, u)
+        return u + du
+
+
+class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBasedSolver):
+    """Newton-Raphson with load stepping (fe_nonlinear_residual_based_solver.py:76-170).
+
+    Convergence: |r|_2 < abs_tol or |dx|_2 < rel_tol or maxiter (the
+    converged step's update is not applied, as in the reference).  Norms are
+    fp64 reductions on the device; one host read per Newton iteration."""
+
+    def __init__(self, fe_solver_name, fe_loss_function, fe_solver_settings: dict = {}, history_plot_settings: dict = {}):
+        super().__init__(fe_solver_name, fe_loss_function, fe_solver_settings)
+        self.nonlinear_solver_settings = {"rel_tol": 1e-8, "abs_tol": 1e-8, "maxiter": 20, "load_incr": 5}
+        self.history = []
+
+    def Initialize(self) -> None:
+        super().Initialize()
+        if "nonlinear_solver_settings" in self.fe_solver_settings:
+            self.nonlinear_solver_settings = UpdateDefaultDict(self.nonlinear_solver_settings,
+                                                               self.fe_solver_settings["nonlinear_solver_settings"])
+
+    def Solve(self, current_control_vars, current_dofs):
+        torch = _torch()
+        loss = self.fe_loss_function
+        s = self.nonlinear_solver_settings
+        u = _dev(current_dofs).clone()
+        n_steps = int(s["load_incr"])
+        self.history = []
+        for step in range(1, n_steps + 1):
+            u = loss.ApplyDirichletBCOnDofVector(u, step / n_steps)
+            for it in range(1, int(s["maxiter"]) + 1):
+                jac, r = loss.ComputeJacobianMatrixAndResidualVector(current_control_vars, u)
+                res_norm = torch.linalg.vector_norm(r.double()).item()
+                if not np.isfinite(res_norm):
+                    raise ValueError("Residual norm contains NaN values.")
+                du = self.LinearSolve(jac, r, u)
+                delta_norm = torch.linalg.vector_norm(du.double()).item()
+                self.history.append({"load_step": step, "iteration": it, "res_norm": res_norm,
+                                     "delta_dofs_norm": delta_norm, "linear": self.last_linear_info})
+                if res_norm < s["abs_tol"] or delta_norm < s["rel_tol"] or it == s["maxiter"]:
+                    break
+                u = u + du
+        return u

@@ -1,0 +1,221 @@
+/*
+ * folgb.h — C ABI of the GB300 finite-element weighted-residual library.
+ *
+ * Drop-in boundary for folax's FE loss / solver hot path.  Every entry point
+ * takes plain pointers and sizes; device arrays are caller-owned, work is
+ * ordered on the caller's CUDA stream, and status is returned as an int
+ * (never thrown).  Per-call entry points allocate nothing: scratch memory is
+ * the caller-provided workspace whose size folgb_workspace_bytes() reports.
+ * Mesh tables are built once per mesh by folgb_plan_create() (the analogue of
+ * the reference's FiniteElementLoss.Initialize and of an XLA FFI "State").
+ *
+ * Reference interfaces replaced (paths inside the folax project):
+ *   fol/loss_functions/fe_loss.py           FiniteElementLoss
+ *   fol/loss_functions/thermal.py, mechanical.py, mechanical_neohooke_AD.py
+ *   fol/solvers/fe_solver.py                FiniteElementSolver.LinearSolve
+ *   fol/loss_functions/ffi_functions/kr_small_displacement_element.cc
+ *                                           (XLA FFI handler precedent)
+ */
+#ifndef FOLGB_H
+#define FOLGB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (kr_small_displacement_element.cc:56,220-222 returns
+ *      ffi::Error::InvalidArgument / Internal; these are the C equivalents) */
+enum {
+  FOLGB_OK = 0,
+  FOLGB_ERR_INVALID_ARGUMENT = 1,
+  FOLGB_ERR_NONPOSITIVE_DETJ = 2, /* an element Jacobian determinant <= 0    */
+  FOLGB_ERR_NAN = 3,              /* a non-finite energy / residual / norm   */
+  FOLGB_ERR_NOT_CONVERGED = 4,    /* PCG hit maxiter above tolerance         */
+  FOLGB_ERR_CUDA = 5,             /* a CUDA runtime call failed              */
+  FOLGB_ERR_WORKSPACE = 6,        /* workspace NULL or smaller than required */
+  FOLGB_ERR_NO_PATTERN = 7        /* plan built without the CSR tables       */
+};
+
+/* element types (fol/geometries/__init__.py:18-21) */
+enum { FOLGB_QUAD4 = 0, FOLGB_HEX8 = 1, FOLGB_TET4 = 2 };
+/* element physics */
+enum {
+  FOLGB_THERMAL = 0,  /* thermal.py:28-49                 */
+  FOLGB_ELASTIC = 1,  /* mechanical.py:98-117             */
+  FOLGB_NEOHOOKE = 2  /* mechanical_neohooke_AD.py:254-293 */
+};
+/* control layout: nodal values gathered by connectivity (fe_loss.py:160), or
+ * one value per element used as de = value * 1 (partition of unity). */
+enum { FOLGB_CONTROL_NODAL = 0, FOLGB_CONTROL_ELEMENT = 1 };
+/* Neo-Hookean shear convention of the FE residual/tangent: REFERENCE doubles
+ * the shear entries of S_voigt as constitutive_material_models/utils.py:45-56
+ * does; CONSISTENT uses the true S (residual = energy gradient). */
+enum { FOLGB_SHEAR_REFERENCE = 0, FOLGB_SHEAR_CONSISTENT = 1 };
+
+typedef struct folgb_physics {
+  int32_t element_type;   /* FOLGB_QUAD4 / HEX8 / TET4                         */
+  int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE                */
+  int32_t num_gp;         /* Gauss order 1..3 ("num_gp", fe_loss.py:68-83)     */
+  int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
+  int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */
+  int32_t reserved;
+  double young_modulus;   /* material_dict young_modulus (elastic D scale)     */
+  double poisson_ratio;   /* material_dict poisson_ratio                       */
+  double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */
+  double beta, c;         /* thermal conductivity nonlinearity (thermal.py:22) */
+  double loss_exponent;   /* loss_function_exponent (fe_loss.py:117-120)       */
+} folgb_physics;
+
+typedef struct folgb_plan folgb_plan;
+
+/* Builds the per-mesh tables on the host and uploads them to the current
+ * device.  conn (num_elements x nodes_per_element, row-major) and xyz
+ * (num_nodes x 3) are HOST arrays in the reference's layout
+ * (Mesh.GetElementsNodes / GetNodesCoordinates, mesh.py:150-169);
+ * dirichlet_dofs/values are the reference's dirichlet_indices/values
+ * (fe_loss.py:34-55, global dof = ndof*node + component).  build_csr != 0 also
+ * builds the fixed CSR pattern and the element-to-nonzero map.
+ * Replaces FiniteElementLoss.Initialize (fe_loss.py:57-122). */
+int folgb_plan_create(folgb_plan** plan, const folgb_physics* phys,
+                      const int64_t* conn, int64_t num_elements,
+                      const double* xyz, int64_t num_nodes,
+                      const int64_t* dirichlet_dofs, const double* dirichlet_values,
+                      int64_t num_dirichlet, int32_t build_csr);
+int folgb_plan_destroy(folgb_plan* plan);
+
+/* Sizes of the plan: dofs per node, total dofs, CSR rows and nonzeros (nnz 0
+ * when the plan has no CSR tables). */
+int folgb_plan_info(const folgb_plan* plan, int64_t* ndof_per_node, int64_t* total_dofs,
+                    int64_t* csr_rows, int64_t* csr_nnz);
+
+/* Sets the Dirichlet values used by the in-kernel GetFullDofVector, scaled by
+ * load_increment (ApplyDirichletBCOnDofVector, fe_loss.py:186-189). values is a
+ * HOST array in the order given to folgb_plan_create. */
+int folgb_plan_set_dirichlet_values(folgb_plan* plan, const double* values, double load_increment);
+
+/* Operation ids for folgb_workspace_bytes. */
+enum { FOLGB_OP_LOSS_ADJOINT = 0, FOLGB_OP_ASSEMBLE = 1, FOLGB_OP_PCG = 2,
+       FOLGB_OP_PLAIN = 3 };
+size_t folgb_workspace_bytes(const folgb_plan* plan, int32_t op, int32_t batch);
+
+/* Fused FE loss + adjoint for a batch of instances on one mesh.
+ * Replaces FiniteElementLoss.ComputeBatchLoss (fe_loss.py:250-262) and the
+ * reverse-mode pass jax.grad takes through it, plus the material sensitivity
+ * (fe_response.py:434-526 semantics for the loss).
+ *   dofs    [batch][total_dofs] full DOF vectors (interleaved, ndof*node+c);
+ *           when apply_dirichlet != 0 the plan's Dirichlet values replace the
+ *           Dirichlet entries first (GetFullDofVector, fe_loss.py:91-100).
+ *   control [batch][N or E] (stride 0 broadcasts one field to every instance)
+ *   losses  [batch] per-instance loss L_b = (sum_e energy_e)^p
+ *   dloss_ddofs    [batch][total_dofs] d(mean_b L_b)/d dofs, 0 at Dirichlet dofs
+ *   dloss_dcontrol [batch][N or E]     d(mean_b L_b)/d control (true
+ *                  derivative of the loss value)
+ * Either gradient pointer may be NULL.  device_status (may be NULL) receives
+ * FOLGB_ERR_NONPOSITIVE_DETJ / FOLGB_ERR_NAN found on the device (it is only
+ * ever raised, never cleared, by the kernels). */
+int folgb_loss_adjoint(const folgb_plan* plan, int32_t batch,
+                       const float* control, int64_t control_stride,
+                       const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
+                       float* losses, float* dloss_ddofs, float* dloss_dcontrol,
+                       int32_t* device_status, void* workspace, size_t workspace_bytes,
+                       void* stream);
+
+/* Same values as folgb_loss_adjoint, computed the plain way: a forward pass
+ * that materialises every element matrix Se in HBM (as the reference's
+ * ComputeElement does, mechanical.py:112-117) and a separate backward pass
+ * re = Se ue - Fe with its deterministic scatter.  Speed-up denominator. */
+int folgb_loss_adjoint_plain(const folgb_plan* plan, int32_t batch,
+                             const float* control, int64_t control_stride,
+                             const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
+                             float* losses, float* dloss_ddofs, float* dloss_dcontrol,
+                             int32_t* device_status, void* workspace, size_t workspace_bytes,
+                             void* stream);
+
+/* Copies the plan's CSR pattern (canonical: sorted column indices, one entry
+ * per connected dof pair, the pattern scipy.sparse.csr_array builds from the
+ * reference's BCOO, fe_solver.py:71-72) into device arrays indptr[rows+1],
+ * indices[nnz]. */
+int folgb_csr_pattern(const folgb_plan* plan, int32_t* indptr, int32_t* indices, void* stream);
+
+/* ComputeJacobianMatrixAndResidualVector (fe_loss.py:264-318): BC-applied
+ * residual [total_dofs] and Jacobian values [nnz] in the plan's CSR pattern,
+ * assembled by a deterministic segmented reduction over the element-to-nonzero
+ * map (no float atomics).  dofs must already hold the Dirichlet values.
+ * transpose != 0 assembles the transposed element matrices (fe_loss.py:222-230).
+ * csr_values or residual may be NULL to skip that output.  inv_diag (may be
+ * NULL) receives 1/diag for the Jacobi preconditioner. */
+int folgb_assemble(const folgb_plan* plan, const float* control, const float* dofs,
+                   int32_t transpose, float* residual, float* csr_values, float* inv_diag,
+                   int32_t* device_status, void* workspace, size_t workspace_bytes,
+                   void* stream);
+
+/* Jacobi-preconditioned CG on the plan's CSR (x0 = 0), replacing
+ * FiniteElementSolver.LinearSolve (fe_solver.py:60-78).  Vectors are FP32,
+ * inner products and norms FP64.  Solves A x = rhs to ||r|| <= rtol ||rhs||.
+ * Runs on the stream; it returns after the solve (it reads the residual norm
+ * every check_every iterations).  iterations / rel_residual may be NULL. */
+int folgb_pcg(const folgb_plan* plan, const float* csr_values, const float* inv_diag,
+              const float* rhs, float* x, double rtol, int32_t maxiter, int32_t check_every,
+              int32_t* iterations, double* rel_residual,
+              void* workspace, size_t workspace_bytes, void* stream);
+
+/* y = A x on the plan's CSR (FP32). */
+int folgb_spmv(const folgb_plan* plan, const float* csr_values, const float* x, float* y,
+               void* stream);
+
+/* Adam update of a parameter array in place (optax.adam as used by the
+ * reference's training loop, deep_network.py:100,141; tests/integration/
+ * test_thermal_2D.py:58-59).  step_counter is a device int incremented by
+ * the kernel, so the launch can be replayed inside a CUDA graph. */
+int folgb_adam_step(float* params, const float* grads, float* m, float* v, int64_t n,
+                    int32_t* step_counter, float lr, float beta1, float beta2, float eps,
+                    void* stream);
+
+/* ---- many instances with uneven meshes in one launch ------------------- */
+typedef struct folgb_batch_plan folgb_batch_plan;
+
+/* Builds one plan over num_instances meshes of one element type and physics,
+ * concatenated (HOST arrays): element_offsets[num_instances+1] into conn
+ * (rows of nodes_per_element LOCAL node ids) and node_offsets[num_instances+1]
+ * into xyz.  Dirichlet dofs are GLOBAL dofs of the concatenated dof vector.
+ * The reference batches only one mesh (fe_loss.py:250-262); this has no
+ * counterpart there. */
+int folgb_batch_plan_create(folgb_batch_plan** plan, const folgb_physics* phys,
+                            int32_t num_instances, const int64_t* element_offsets,
+                            const int64_t* node_offsets, const int64_t* conn, const double* xyz,
+                            const int64_t* dirichlet_dofs, const double* dirichlet_values,
+                            int64_t num_dirichlet, int32_t elements_per_tile);
+int folgb_batch_plan_destroy(folgb_batch_plan* plan);
+size_t folgb_batch_workspace_bytes(const folgb_batch_plan* plan);
+
+/* Fused loss + adjoint over every instance in one persistent launch (plus one
+ * deterministic gather launch).  losses[num_instances]; gradients are of
+ * mean_i L_i.  dofs/control/gradients are concatenated over instances. */
+int folgb_batch_loss_adjoint(const folgb_batch_plan* plan, const float* control,
+                             const float* dofs, int32_t apply_dirichlet, float* losses,
+                             float* dloss_ddofs, float* dloss_dcontrol, int32_t* device_status,
+                             void* workspace, size_t workspace_bytes, void* stream);
+
+/* ---- opt-in kernel tracing ------------------------------------------------
+ * CUDA events recorded on the launching stream around every kernel of the
+ * entry points above, summed per kernel id.  The reference's only tracing is
+ * wall-clock decorators (fol/tools/decoration_functions.py:7-32), which time
+ * dispatch, not the device; this has no other counterpart there.
+ * folgb_trace_read synchronises on the recorded events. */
+enum {
+  FOLGB_KERNEL_ELEM_LOSS = 0, FOLGB_KERNEL_GATHER = 1, FOLGB_KERNEL_ELEM_MATRIX = 2,
+  FOLGB_KERNEL_PAIR_REDUCE = 3, FOLGB_KERNEL_PLAIN_BACKWARD = 4, FOLGB_KERNEL_ELEM_RESIDUAL = 5,
+  FOLGB_KERNEL_PCG_SPMV = 6, FOLGB_KERNEL_PCG_UPDATE = 7, FOLGB_KERNEL_BATCH_LOSS = 8,
+  FOLGB_KERNEL_HEX8_FUSED = 9
+};
+int folgb_trace_enable(int32_t on);
+int folgb_trace_reset(void);
+int folgb_trace_read(int32_t kernel_id, int64_t* launches, double* total_ms);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FOLGB_H */

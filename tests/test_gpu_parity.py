@@ -1,0 +1,214 @@
+"""CUDA path (through the C ABI) against the FP64 oracle and the reference's
+golden vectors.  Tolerance: 1e-5 relative (Frobenius) for fp32 results."""
+import numpy as np
+import pytest
+
+from conftest import arr, golden
+from gpu_cases import bc_dict, gpu_loss, make_mesh, oracle_loss, rel_fro
+from oracle import fe_oracle as fo
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+CASES = [("quad4", "thermal", 8), ("hex8", "elastic", 4), ("tet4", "neohooke", 3), ("quad4", "elastic", 8),
+         ("hex8", "neohooke", 3), ("tet4", "thermal", 3), ("hex8", "thermal", 4), ("tet4", "elastic", 3),
+         ("quad4", "neohooke", 8)]
+
+
+def _settings(etype, physics, layout="nodal", exponent=1.0, bf=None, shear="reference"):
+    s = {"dirichlet_bc_dict": bc_dict(etype, physics), "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
+         "control_layout": layout, "loss_function_exponent": exponent, "voigt_shear_mode": shear}
+    if bf is not None:
+        s["body_foce"] = bf
+    return s
+
+
+@pytest.mark.parametrize("kind,etype", [(k, e) for k in ("mechanical_linear", "neohooke_ad")
+                                        for e in ("tet4", "hex8", "quad4")])
+def test_element_golden_vectors_on_gpu(cuda, kind, etype):
+    """tests/unit/test_mechanical_loss.py / test_neo_hooke_mechanical_loss_AD.py
+    through the CUDA kernels (ComputeElement on a one-element mesh)."""
+    from folax_gb300 import loss as L
+    g = golden(kind + ".json")[etype]
+    X = arr(g["xyz"])
+    nen, dim = fo.ELEMENTS[etype]
+    mesh = make_mesh(etype, 1)
+    bf = arr(g["body_force"]).ravel().tolist()
+    settings = {"dirichlet_bc_dict": {}, "material_dict": {"young_modulus": 1, "poisson_ratio": 0.3}, "body_foce": bf}
+    cls = {("mechanical_linear", "tet4"): L.MechanicalLoss3DTetra, ("mechanical_linear", "hex8"): L.MechanicalLoss3DHexa,
+           ("mechanical_linear", "quad4"): L.MechanicalLoss2DQuad, ("neohooke_ad", "tet4"): L.NeoHookeMechanicalLoss3DTetra,
+           ("neohooke_ad", "hex8"): L.NeoHookeMechanicalLoss3DHexa, ("neohooke_ad", "quad4"): L.NeoHookeMechanicalLoss2DQuad}[(kind, etype)]
+    loss = cls("golden", settings, mesh)
+    loss.Initialize()
+    en, re, K = loss.ComputeElement(X, np.ones(nen), np.ones(nen * dim))
+    np.testing.assert_allclose(K, arr(g["stiffness"]), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(re, arr(g["residual"]), rtol=1e-4 if (etype == "tet4" and kind == "mechanical_linear") else 1e-5,
+                               atol=1e-6)
+
+
+@pytest.mark.parametrize("etype,physics,n", CASES)
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_loss_adjoint_matches_oracle(cuda, etype, physics, n, layout):
+    torch = cuda
+    m = make_mesh(etype, n, seed=1)
+    s = _settings(etype, physics, layout)
+    gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
+    rng = np.random.default_rng(2)
+    B = 2
+    nctrl = gl.GetNumberOfControls()
+    ctrl = 0.5 + rng.random((B, nctrl))
+    u = 0.05 * rng.standard_normal((B, gl.GetTotalNumberOfDOFs()))
+    mean, (mn, mx, _), losses, du, dc = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    omean, _, olosses, odu, odc = ol.batch_loss_and_grads(ctrl, u)
+    assert rel_fro(losses.cpu().numpy(), olosses) < TOL
+    assert rel_fro(du.cpu().numpy(), odu) < TOL
+    assert rel_fro(dc.cpu().numpy(), odc) < TOL
+    assert np.all(du.cpu().numpy()[:, ol.dirichlet_indices] == 0)
+
+
+@pytest.mark.parametrize("exponent,bf", [(1.5, None), (1.0, [0.3, -0.2, 0.1]), (2.0, [0.1, 0.2, 0.3])])
+def test_loss_exponent_body_force_broadcast(cuda, exponent, bf):
+    m = make_mesh("hex8", 3, seed=3)
+    s = _settings("hex8", "elastic", "nodal", exponent, bf)
+    gl, ol = gpu_loss("hex8", "elastic", m, s), oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(4)
+    ctrl = 0.5 + rng.random((1, m.GetNumberOfNodes()))          # one control broadcast to every instance
+    u = 0.05 * rng.standard_normal((3, gl.GetTotalNumberOfDOFs()))
+    _, _, losses, du, dc = gl.ComputeBatchLossAndGrad(ctrl, u)
+    _, _, olosses, odu, odc = ol.batch_loss_and_grads(np.repeat(ctrl, 3, 0), u)
+    assert rel_fro(losses.cpu().numpy(), olosses) < TOL
+    assert rel_fro(du.cpu().numpy(), odu) < TOL
+    assert rel_fro(dc.cpu().numpy(), odc) < TOL
+
+
+@pytest.mark.parametrize("etype,physics", [("hex8", "elastic"), ("quad4", "thermal"), ("tet4", "elastic")])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_plain_path_matches_fused(cuda, etype, physics, layout):
+    m = make_mesh(etype, 4 if etype != "quad4" else 10, seed=5)
+    s = _settings(etype, physics, layout, 1.0, [0.1, 0.0, -0.2] if physics == "elastic" else None)
+    gl = gpu_loss(etype, physics, m, s)
+    rng = np.random.default_rng(6)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = 0.05 * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    f = gl.ComputeBatchLossAndGrad(ctrl, u)
+    p = gl.ComputeBatchLossAndGrad(ctrl, u, plain=True)
+    for a, b in zip(f[2:], p[2:]):
+        assert rel_fro(a.cpu().numpy(), b.cpu().numpy()) < TOL
+
+
+def test_fused_is_deterministic(cuda):
+    m = make_mesh("hex8", 6, seed=7)
+    gl = gpu_loss("hex8", "elastic", m, _settings("hex8", "elastic"))
+    rng = np.random.default_rng(8)
+    ctrl = 0.5 + rng.random((1, m.GetNumberOfNodes()))
+    u = 0.05 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
+    a = [t.clone() for t in gl.ComputeBatchLossAndGrad(ctrl, u)[2:]]
+    b = gl.ComputeBatchLossAndGrad(ctrl, u)[2:]
+    for x, y in zip(a, b):
+        assert cuda.equal(x, y)
+
+
+@pytest.mark.parametrize("etype,physics,n", [("quad4", "thermal", 6), ("hex8", "elastic", 3), ("tet4", "neohooke", 2),
+                                             ("quad4", "elastic", 5), ("hex8", "neohooke", 2), ("tet4", "thermal", 2)])
+@pytest.mark.parametrize("transpose", [False, True])
+def test_csr_pattern_bit_exact_and_values(cuda, etype, physics, n, transpose):
+    """Pattern identical to scipy.sparse.csr_array of the reference COO
+    (fe_solver.py:71-72); values and residual within 1e-5."""
+    m = make_mesh(etype, n, seed=9)
+    s = _settings(etype, physics, "nodal", 1.0, [0.2, 0.1, 0.0] if physics != "thermal" else None)
+    gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
+    rng = np.random.default_rng(10)
+    ctrl = 0.5 + rng.random(m.GetNumberOfNodes())
+    u = ol.full_dof_vector(0.05 * rng.standard_normal(ol.total_dofs))
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, u, transpose_jacobian=transpose)
+    gl.CheckDeviceStatus()
+    A, Ro = ol.csr(ctrl, u, transpose=transpose)
+    np.testing.assert_array_equal(jac.indptr.cpu().numpy(), A.indptr)
+    np.testing.assert_array_equal(jac.indices.cpu().numpy(), A.indices)
+    assert rel_fro(jac.data.cpu().numpy(), A.data) < TOL
+    assert rel_fro(R.cpu().numpy(), Ro) < TOL
+    np.testing.assert_allclose(jac.inv_diag.cpu().numpy(), 1.0 / A.diagonal(), rtol=1e-5)
+
+
+def test_spmv_matches_scipy(cuda):
+    m = make_mesh("hex8", 5, seed=11)
+    s = _settings("hex8", "elastic")
+    gl, ol = gpu_loss("hex8", "elastic", m, s), oracle_loss("hex8", "elastic", m, s)
+    ctrl = 0.5 + np.random.default_rng(12).random(m.GetNumberOfNodes())
+    jac, _ = gl.ComputeJacobianMatrixAndResidualVector(ctrl, np.zeros(ol.total_dofs))
+    x = np.random.default_rng(13).standard_normal(ol.total_dofs)
+    y = jac.matvec(x).cpu().numpy()
+    assert rel_fro(y, jac.to_scipy() @ x) < TOL
+
+
+@pytest.mark.parametrize("etype,physics,n", [("hex8", "elastic", 8), ("quad4", "thermal", 40), ("tet4", "elastic", 5)])
+def test_linear_solve_matches_direct(cuda, etype, physics, n):
+    """FiniteElementLinearResidualBasedSolver.Solve (PCG, rtol 1e-8) against an
+    FP64 direct solve of the oracle system: within 1e-6 relative."""
+    from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
+    m = make_mesh(etype, n, seed=14)
+    s = _settings(etype, physics)
+    gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
+    ctrl = 0.5 + np.random.default_rng(15).random(m.GetNumberOfNodes())
+    solver = FiniteElementLinearResidualBasedSolver("lin", gl, {"linear_solver_settings": {"tol": 1e-8, "maxiter": 5000}})
+    solver.Initialize()
+    x = solver.Solve(ctrl, np.zeros(ol.total_dofs)).cpu().numpy()
+    xo = fo.linear_solve(ol, ctrl, np.zeros(ol.total_dofs))
+    info = solver.last_linear_info
+    assert info["status"] == 0, info
+    assert rel_fro(x, xo) < 1e-6, (rel_fro(x, xo), info)
+
+
+def test_newton_neohooke_matches_oracle(cuda):
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    m = make_mesh("tet4", 3, seed=16)
+    s = _settings("tet4", "neohooke", shear="consistent")
+    gl, ol = gpu_loss("tet4", "neohooke", m, s), oracle_loss("tet4", "neohooke", m, s)
+    ctrl = 0.5 + np.random.default_rng(17).random(m.GetNumberOfNodes())
+    settings = {"linear_solver_settings": {"tol": 1e-10, "maxiter": 5000},
+                "nonlinear_solver_settings": {"load_incr": 2, "maxiter": 10, "abs_tol": 1e-6, "rel_tol": 1e-7}}
+    solver = FiniteElementNonLinearResidualBasedSolver("nl", gl, settings)
+    solver.Initialize()
+    x = solver.Solve(ctrl, np.zeros(ol.total_dofs)).cpu().numpy()
+    xo, _ = fo.newton_solve(ol, ctrl, np.zeros(ol.total_dofs), load_incr=2, maxiter=10, abs_tol=1e-6, rel_tol=1e-7)
+    assert rel_fro(x, xo) < 1e-5
+    # the Newton root of the consistent residual minimises the loss: its gradient vanishes
+    _, _, _, du, _ = gl.ComputeBatchLossAndGrad(ctrl[None], x[None])
+    _, _, _, du0, _ = gl.ComputeBatchLossAndGrad(ctrl[None], np.zeros((1, ol.total_dofs)))
+    assert cuda.linalg.vector_norm(du) < 1e-3 * cuda.linalg.vector_norm(du0)
+
+
+def test_inverted_element_and_nan_are_reported(cuda):
+    """Host-made faults: an inverted element raises the detJ status bit, a NaN
+    in u the NaN bit; the context stays usable."""
+    from folax_gb300 import _capi
+    m = make_mesh("hex8", 2, seed=18, jitter=0.0)
+    conn = m.elements_nodes["hexahedron"].copy()
+    conn[0, [0, 1]] = conn[0, [1, 0]]
+    m.elements_nodes["hexahedron"] = conn
+    gl = gpu_loss("hex8", "elastic", m, _settings("hex8", "elastic"))
+    u = np.zeros((1, gl.GetTotalNumberOfDOFs()))
+    ctrl = np.ones((1, m.GetNumberOfNodes()))
+    gl.ComputeBatchLossAndGrad(ctrl, u)
+    with pytest.raises(_capi.FolgbError) as e:
+        gl.CheckDeviceStatus()
+    assert e.value.code == _capi.ERR_NONPOSITIVE_DETJ
+    m2 = make_mesh("hex8", 2, seed=18)
+    gl2 = gpu_loss("hex8", "elastic", m2, _settings("hex8", "elastic"))
+    u[0, 5] = np.nan
+    gl2.ComputeBatchLossAndGrad(ctrl, u)
+    with pytest.raises(_capi.FolgbError) as e:
+        gl2.CheckDeviceStatus()
+    assert e.value.code == _capi.ERR_NAN
+    gl2.ComputeBatchLossAndGrad(ctrl, np.zeros_like(u))
+    gl2.CheckDeviceStatus()
+
+
+def test_invalid_arguments_raise(cuda):
+    from folax_gb300 import _capi
+    m = make_mesh("quad4", 3)
+    m.elements_nodes["quad"] = m.elements_nodes["quad"].copy()
+    m.elements_nodes["quad"][0, 0] = 10 ** 6          # node id out of range
+    with pytest.raises(_capi.FolgbError):
+        gpu_loss("quad4", "thermal", m, _settings("quad4", "thermal"))
