@@ -42,7 +42,7 @@ class FolgbError(RuntimeError):
 class Physics(C.Structure):
     _fields_ = [
         ("element_type", C.c_int32), ("physics", C.c_int32), ("num_gp", C.c_int32),
-        ("control_layout", C.c_int32), ("shear_mode", C.c_int32), ("reserved", C.c_int32),
+        ("control_layout", C.c_int32), ("shear_mode", C.c_int32), ("kernel_variant", C.c_int32),
         ("young_modulus", C.c_double), ("poisson_ratio", C.c_double),
         ("body_force", C.c_double * 3), ("beta", C.c_double), ("c", C.c_double),
         ("loss_exponent", C.c_double),
@@ -64,6 +64,7 @@ PROTOTYPES = {
     "folgb_csr_pattern": (C.c_int, [vp, vp, vp, vp]),
     "folgb_assemble": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_pcg": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
+    "folgb_bicgstab": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
     "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
     "folgb_adam_step": (C.c_int, [vp, vp, vp, vp, i64, vp, f32, f32, f32, f32, vp]),
     "folgb_batch_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), i32, vp, vp, vp, vp, vp, vp, i64, i32]),

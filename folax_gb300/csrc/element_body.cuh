@@ -332,12 +332,20 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
   }
 }
 
+// __syncthreads_or returns whether any thread's predicate is non-zero (not
+// the bitwise OR), so each flag gets its own reduction.
 __device__ __forceinline__ void report_bad(int bad, int* status) {
-  int anybad = __syncthreads_or(bad);
-  if (anybad && threadIdx.x == 0 && status) {
-    if (anybad & 1) atomicOr(status, 1 << FOLGB_ERR_NONPOSITIVE_DETJ);
-    if (anybad & 2) atomicOr(status, 1 << FOLGB_ERR_NAN);
+  const int detj = __syncthreads_or(bad & 1);
+  const int nan = __syncthreads_or(bad & 2);
+  if (threadIdx.x == 0 && status) {
+    if (detj) atomicOr(status, 1 << FOLGB_ERR_NONPOSITIVE_DETJ);
+    if (nan) atomicOr(status, 1 << FOLGB_ERR_NAN);
   }
 }
 
+}  // namespace folgb
+
+namespace folgb {
+// sum-factorised hex8 2x2x2 elasticity (hex8_fused.cu); returns 1 if launched
+int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s);
 }  // namespace folgb

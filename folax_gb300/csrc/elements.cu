@@ -718,14 +718,18 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
                             elem_ctrl ? dloss_dcontrol : nullptr, device_status);
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
-  rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
-    constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
-    trace_begin(KID_ELEM_LOSS, s);
-    k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
-    trace_end(KID_ELEM_LOSS, s);
+  if (p->phys.kernel_variant == 0 && launch_hex8_fast(p, A, grid, MODE_LOSS, s)) {
     FOLGB_LAUNCH_CHECK();
-    return FOLGB_OK;
-  });
+  } else {
+    rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
+      constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
+      trace_begin(KID_ELEM_LOSS, s);
+      k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
+      trace_end(KID_ELEM_LOSS, s);
+      FOLGB_LAUNCH_CHECK();
+      return FOLGB_OK;
+    });
+  }
   if (rc) return rc;
   if (dloss_ddofs || dloss_dcontrol) {
     rc = launch_gather(p, B, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
@@ -839,9 +843,11 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   int rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
     if (residual) {
-      trace_begin(KID_ELEM_RESIDUAL, s);
-      k_elem_vector<ET, PH, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
-      trace_end(KID_ELEM_RESIDUAL, s);
+      if (!(p->phys.kernel_variant == 0 && launch_hex8_fast(p, A, grid, MODE_RESIDUAL, s))) {
+        trace_begin(KID_ELEM_RESIDUAL, s);
+        k_elem_vector<ET, PH, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
+        trace_end(KID_ELEM_RESIDUAL, s);
+      }
       FOLGB_LAUNCH_CHECK();
     }
     if (csr_values || inv_diag) return launch_matrix<ET, PH, MAT_ASSEMBLE>(M, 1, npts, s);

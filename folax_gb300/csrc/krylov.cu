@@ -1,0 +1,708 @@
+// Krylov solvers on the plan's fixed CSR pattern (Jacobi-preconditioned CG and
+// BiCGSTAB), SpMV, and the Adam update.  Replaces
+// FiniteElementSolver.LinearSolve (fol/solvers/fe_solver.py:60-78; the
+// reference's default is JAX BiCGSTAB, fe_solver.py:60-67).
+//
+// SpMV reads the canonical CSR values but indexes columns through the node
+// adjacency (one column index per ndof x ndof block), so the index stream is
+// 1/ndof^2 of a scalar CSR's.  One group of G lanes handles one node's ndof
+// rows; lane j of the group owns neighbour j.
+//
+// Precision: matrix and Krylov vectors in fp32, every inner product and norm
+// accumulated in fp64, the iterate x kept in fp64.  fp32 SpMV bounds how far
+// the recurrence residual tracks the true one, so the solvers use reliable
+// updates: when the recurrence residual has dropped 1e3 below the last true
+// residual (or reached the tolerance) the host launches one fp64 SpMV that
+// recomputes r = b - A x and restarts the recurrence from it.  Convergence is
+// declared on that true residual only.
+//
+// Every iteration kernel returns at once when the device flags "done" or
+// "replace" are set, so the host enqueues a chunk of iterations and reads
+// the flags once per chunk.
+#include <cmath>
+#include <type_traits>
+
+#include "folgb_internal.cuh"
+
+using namespace folgb;
+
+namespace folgb {
+
+struct KScalars {
+  double rho, bnorm2, rnorm2, rref2, tol2;
+  double alpha, beta, omega;
+  int iters, done, replace, maxiter, restart, breakdowns;
+};
+// done: 1 converged (true residual), 2 maxiter, 3 repeated breakdown / non-finite
+
+struct KWork {
+  float *r, *z, *p0, *p1, *q;   // PCG: r, z, p (two buffers), q = A p
+  float *rhat, *v0, *v1, *y, *t;  // BiCGSTAB extras
+  double* x;                    // fp64 iterate
+  double* part;                 // [2][65536]
+  unsigned* counters;           // [8]
+  KScalars* sc;
+};
+
+constexpr int kVecBlocks = 1024;
+constexpr double kReplaceDrop2 = 1e-6;  // replace when |r|^2 <= 1e-6 |r_true|^2
+
+static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork* w) {
+  Bump bp(base, cap);
+  const size_t n = (size_t)p->ndof * p->N;
+  KWork t;
+  t.r = bp.take<float>(n);
+  t.z = bp.take<float>(n);
+  t.p0 = bp.take<float>(n);
+  t.p1 = bp.take<float>(n);
+  t.q = bp.take<float>(n);
+  t.rhat = bp.take<float>(n);
+  t.v0 = bp.take<float>(n);
+  t.v1 = bp.take<float>(n);
+  t.y = bp.take<float>(n);
+  t.t = bp.take<float>(n);
+  t.x = bp.take<double>(n);
+  t.part = bp.take<double>(2 * 65536);
+  t.counters = bp.take<unsigned>(8);
+  t.sc = bp.take<KScalars>(1);
+  if (w) *w = t;
+  return align_up(bp.off);
+}
+
+size_t pcg_workspace_bytes(const folgb_plan* p) { return layout_krylov(p, nullptr, 0, nullptr); }
+
+__device__ __forceinline__ bool last_block(unsigned* counter) {
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned prev = atomicAdd(counter, 1u);
+    last = (prev == gridDim.x - 1);
+  }
+  __syncthreads();
+  return last;
+}
+
+__device__ __forceinline__ double sum_partials(const double* part, int n, double* sh) {
+  double s = 0.0;
+  const volatile double* pv = part;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) s += pv[i];
+  return block_sum_d(s, sh);
+}
+
+// Per-node row product over the node adjacency: acc[i] = sum_j sum_l
+// A(ndof*n+i, ndof*m_j+l) * col(m_j, l), computed by a group of G lanes and
+// reduced with shuffles.  Called warp-uniformly (inactive lanes pass deg 0).
+template <int NDOF, int G, class T, class Col>
+__device__ __forceinline__ void node_rows(const int* __restrict__ adj, const float* __restrict__ vals, int a0,
+                                          int deg, const int (&rb)[NDOF], int lane, Col col, T (&acc)[NDOF]) {
+#pragma unroll
+  for (int i = 0; i < NDOF; ++i) acc[i] = T(0);
+  for (int j = lane; j < deg; j += G) {
+    const int m = __ldg(adj + a0 + j);
+    T cv[NDOF];
+#pragma unroll
+    for (int l = 0; l < NDOF; ++l) cv[l] = col((int64_t)NDOF * m + l);
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+      for (int l = 0; l < NDOF; ++l) acc[i] += (T)__ldg(vals + rb[i] + NDOF * j + l) * cv[l];
+  }
+#pragma unroll
+  for (int i = 0; i < NDOF; ++i)
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o, G);
+}
+
+// Warp-uniform loop over nodes: every lane runs the same number of rounds so
+// the group shuffles always see the whole warp.
+#define FOLGB_NODE_LOOP(NDOF, G)                                                                 \
+  const int lane = threadIdx.x % G;                                                              \
+  const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;                    \
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;                                 \
+  for (int64_t n = group; __any_sync(0xffffffffu, n < N); n += ngroups)
+
+#define FOLGB_NODE_SETUP(NDOF)                                                    \
+  const bool active = n < N;                                                      \
+  const int a0 = active ? __ldg(adj_ptr + n) : 0;                                 \
+  const int deg = active ? __ldg(adj_ptr + n + 1) - a0 : 0;                       \
+  int rb[NDOF];                                                                   \
+  _Pragma("unroll") for (int i = 0; i < NDOF; ++i) rb[i] = active ? __ldg(rowptr + (int64_t)NDOF * n + i) : 0;
+
+template <int NDOF, int G>
+__global__ void __launch_bounds__(256) k_spmv(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
+                                              const int* __restrict__ rowptr, const float* __restrict__ vals,
+                                              const float* __restrict__ x, float* __restrict__ y) {
+  FOLGB_NODE_LOOP(NDOF, G) {
+    FOLGB_NODE_SETUP(NDOF)
+    float acc[NDOF];
+    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(x + d); }, acc);
+    if (active && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) y[(int64_t)NDOF * n + i] = acc[i];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// shared: fp64 true residual r = b - A x (reliable update / restart)
+// ---------------------------------------------------------------------------
+template <int NDOF, int G, bool BICG>
+__global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __restrict__ adj_ptr,
+                                                       const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                       const float* __restrict__ vals, const float* __restrict__ b,
+                                                       const float* __restrict__ dinv, const double* __restrict__ x,
+                                                       float* __restrict__ r, float* __restrict__ z,
+                                                       float* __restrict__ rhat, double* part, unsigned* counters,
+                                                       KScalars* sc) {
+  __shared__ double sh[32];
+  double rz = 0.0, rr = 0.0;
+  FOLGB_NODE_LOOP(NDOF, G) {
+    FOLGB_NODE_SETUP(NDOF)
+    double acc[NDOF];
+    node_rows<NDOF, G, double>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return x[d]; }, acc);
+    if (active && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        const int64_t d = (int64_t)NDOF * n + i;
+        const double ri = (double)b[d] - acc[i];
+        const float rf = (float)ri;
+        r[d] = rf;
+        const float zf = dinv[d] * rf;
+        if (!BICG) z[d] = zf;
+        else rhat[d] = rf;
+        rz += (double)rf * (double)zf;
+        rr += ri * ri;
+      }
+    }
+  }
+  double s1 = block_sum_d(rz, sh);
+  double s2 = block_sum_d(rr, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s1;
+    part[gridDim.x + blockIdx.x] = s2;
+  }
+  if (!last_block(&counters[3])) return;
+  double RZ = sum_partials(part, gridDim.x, sh);
+  double RR = sum_partials(part + gridDim.x, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->rnorm2 = RR;
+    sc->rref2 = RR;
+    sc->replace = 0;
+    if (BICG) {
+      sc->rho = RR;  // rhat = r
+      sc->restart = 1;
+    } else {
+      sc->rho = RZ;
+      sc->beta = 0.0;  // restart the search direction: p = z
+    }
+    if (!isfinite(RR)) sc->done = 3;
+    else if (RR <= sc->tol2) sc->done = 1;
+    counters[3] = 0u;
+  }
+}
+
+__global__ void k_to_float(int64_t n, const double* __restrict__ x, float* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = (float)x[i];
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi PCG
+// ---------------------------------------------------------------------------
+__global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* __restrict__ dinv,
+                           double* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
+                           float* __restrict__ p0, double* part, unsigned* counters, KScalars* sc, double rtol,
+                           int maxiter) {
+  __shared__ double sh[32];
+  double rz = 0.0, bb = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float bi = b[i];
+    float zi = dinv[i] * bi;
+    x[i] = 0.0;
+    r[i] = bi;
+    z[i] = zi;
+    p0[i] = 0.f;
+    rz += (double)bi * (double)zi;
+    bb += (double)bi * (double)bi;
+  }
+  double s1 = block_sum_d(rz, sh);
+  double s2 = block_sum_d(bb, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s1;
+    part[gridDim.x + blockIdx.x] = s2;
+  }
+  if (!last_block(&counters[0])) return;
+  double RZ = sum_partials(part, gridDim.x, sh);
+  double BB = sum_partials(part + gridDim.x, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->rho = RZ;
+    sc->bnorm2 = BB;
+    sc->rnorm2 = BB;
+    sc->rref2 = BB;
+    sc->tol2 = rtol * rtol * BB;
+    sc->alpha = sc->beta = 0.0;
+    sc->omega = 1.0;
+    sc->iters = 0;
+    sc->maxiter = maxiter;
+    sc->replace = 0;
+    sc->restart = 0;
+    sc->breakdowns = 0;
+    sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
+    counters[0] = 0u;
+  }
+}
+
+template <int NDOF, int G>
+__global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
+                                                  const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                  const float* __restrict__ vals, const float* __restrict__ z,
+                                                  const float* __restrict__ pold, float* __restrict__ pnew,
+                                                  float* __restrict__ q, double* part, unsigned* counters,
+                                                  KScalars* sc) {
+  __shared__ double sh[32];
+  if (sc->done || sc->replace) return;
+  const float beta = (float)sc->beta;
+  double dot = 0.0;
+  FOLGB_NODE_LOOP(NDOF, G) {
+    FOLGB_NODE_SETUP(NDOF)
+    float acc[NDOF];
+    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane,
+                              [&](int64_t d) { return fmaf(beta, __ldg(pold + d), __ldg(z + d)); }, acc);
+    if (active && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        const int64_t d = (int64_t)NDOF * n + i;
+        const float pn = fmaf(beta, pold[d], z[d]);
+        pnew[d] = pn;
+        q[d] = acc[i];
+        dot += (double)pn * (double)acc[i];
+      }
+    }
+  }
+  double s = block_sum_d(dot, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (!last_block(&counters[1])) return;
+  double PQ = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    if (!(PQ > 0.0) || !isfinite(PQ)) {
+      // breakdown: restart from the true residual; give up if it repeats
+      sc->alpha = 0.0;
+      sc->breakdowns += 1;
+      if (sc->breakdowns > 2) sc->done = 3;
+      else sc->replace = 1;
+    } else {
+      sc->alpha = sc->rho / PQ;
+    }
+    counters[1] = 0u;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __restrict__ dinv,
+                                                    double* __restrict__ x, float* __restrict__ r,
+                                                    float* __restrict__ z, const float* __restrict__ p,
+                                                    const float* __restrict__ q, double* part, unsigned* counters,
+                                                    KScalars* sc) {
+  __shared__ double sh[32];
+  if (sc->done || sc->replace) return;
+  const double alpha = sc->alpha;
+  const float af = (float)alpha;
+  double rz = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] = fma(alpha, (double)p[i], x[i]);
+    const float ri = fmaf(-af, q[i], r[i]);
+    r[i] = ri;
+    const float zi = dinv[i] * ri;
+    z[i] = zi;
+    rz += (double)ri * (double)zi;
+    rr += (double)ri * (double)ri;
+  }
+  double s1 = block_sum_d(rz, sh);
+  double s2 = block_sum_d(rr, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s1;
+    part[gridDim.x + blockIdx.x] = s2;
+  }
+  if (!last_block(&counters[2])) return;
+  double RZ = sum_partials(part, gridDim.x, sh);
+  double RR = sum_partials(part + gridDim.x, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->beta = RZ / sc->rho;
+    sc->rho = RZ;
+    sc->rnorm2 = RR;
+    sc->iters += 1;
+    sc->breakdowns = 0;
+    if (!isfinite(RR)) sc->done = 3;
+    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2) sc->replace = 1;
+    if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
+    counters[2] = 0u;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Jacobi BiCGSTAB (right preconditioned): y = D^-1 p, z = D^-1 s,
+// x += alpha y + omega z.  Three kernels per iteration.
+// ---------------------------------------------------------------------------
+__global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
+                            float* __restrict__ rhat, double* part, unsigned* counters, KScalars* sc, double rtol,
+                            int maxiter) {
+  __shared__ double sh[32];
+  double bb = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    float bi = b[i];
+    x[i] = 0.0;
+    r[i] = bi;
+    rhat[i] = bi;
+    bb += (double)bi * (double)bi;
+  }
+  double s2 = block_sum_d(bb, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s2;
+  if (!last_block(&counters[0])) return;
+  double BB = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->rho = BB;
+    sc->bnorm2 = BB;
+    sc->rnorm2 = BB;
+    sc->rref2 = BB;
+    sc->tol2 = rtol * rtol * BB;
+    sc->alpha = sc->omega = 1.0;
+    sc->beta = 0.0;
+    sc->iters = 0;
+    sc->maxiter = maxiter;
+    sc->replace = 0;
+    sc->restart = 1;
+    sc->breakdowns = 0;
+    sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
+    counters[0] = 0u;
+  }
+}
+
+// p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
+// v_new = A y; alpha = rho / (rhat . v_new)
+template <int NDOF, int G>
+__global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __restrict__ adj_ptr,
+                                                     const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                     const float* __restrict__ vals, const float* __restrict__ dinv,
+                                                     const float* __restrict__ r, const float* __restrict__ rhat,
+                                                     const float* __restrict__ pold, const float* __restrict__ vold,
+                                                     float* __restrict__ pnew, float* __restrict__ y,
+                                                     float* __restrict__ vnew, double* part, unsigned* counters,
+                                                     KScalars* sc) {
+  __shared__ double sh[32];
+  if (sc->done || sc->replace) return;
+  const bool rs = sc->restart != 0;
+  const float beta = rs ? 0.f : (float)sc->beta;
+  const float omega = rs ? 0.f : (float)sc->omega;
+  auto pval = [&](int64_t d) -> float {
+    return rs ? __ldg(r + d) : fmaf(beta, fmaf(-omega, __ldg(vold + d), __ldg(pold + d)), __ldg(r + d));
+  };
+  double dot = 0.0;
+  FOLGB_NODE_LOOP(NDOF, G) {
+    FOLGB_NODE_SETUP(NDOF)
+    float acc[NDOF];
+    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(dinv + d) * pval(d); },
+                              acc);
+    if (active && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        const int64_t d = (int64_t)NDOF * n + i;
+        const float pn = pval(d);
+        pnew[d] = pn;
+        y[d] = dinv[d] * pn;
+        vnew[d] = acc[i];
+        dot += (double)rhat[d] * (double)acc[i];
+      }
+    }
+  }
+  double s = block_sum_d(dot, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (!last_block(&counters[1])) return;
+  double RV = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->restart = 0;
+    if (RV == 0.0 || !isfinite(RV)) {
+      sc->breakdowns += 1;
+      if (sc->breakdowns > 2) sc->done = 3;
+      else sc->replace = 1;
+    } else {
+      sc->alpha = sc->rho / RV;
+    }
+    counters[1] = 0u;
+  }
+}
+
+// s = r - alpha v_new, z = D^-1 s, t = A z; omega = (t . s) / (t . t)
+template <int NDOF, int G>
+__global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __restrict__ adj_ptr,
+                                                     const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                     const float* __restrict__ vals, const float* __restrict__ dinv,
+                                                     const float* __restrict__ r, const float* __restrict__ vnew,
+                                                     float* __restrict__ z, float* __restrict__ t, double* part,
+                                                     unsigned* counters, KScalars* sc) {
+  __shared__ double sh[32];
+  if (sc->done || sc->replace) return;
+  const float af = (float)sc->alpha;
+  auto sval = [&](int64_t d) -> float { return fmaf(-af, __ldg(vnew + d), __ldg(r + d)); };
+  double ts = 0.0, tt = 0.0;
+  FOLGB_NODE_LOOP(NDOF, G) {
+    FOLGB_NODE_SETUP(NDOF)
+    float acc[NDOF];
+    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(dinv + d) * sval(d); },
+                              acc);
+    if (active && lane == 0) {
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) {
+        const int64_t d = (int64_t)NDOF * n + i;
+        const float sv = sval(d);
+        z[d] = dinv[d] * sv;
+        t[d] = acc[i];
+        ts += (double)acc[i] * (double)sv;
+        tt += (double)acc[i] * (double)acc[i];
+      }
+    }
+  }
+  double s1 = block_sum_d(ts, sh);
+  double s2 = block_sum_d(tt, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s1;
+    part[gridDim.x + blockIdx.x] = s2;
+  }
+  if (!last_block(&counters[4])) return;
+  double TS = sum_partials(part, gridDim.x, sh);
+  double TT = sum_partials(part + gridDim.x, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    sc->omega = (TT > 0.0 && isfinite(TT)) ? TS / TT : 0.0;
+    counters[4] = 0u;
+  }
+}
+
+// s = r - alpha v, x += alpha y + omega z, r = s - omega t; rho_new = rhat . r
+__global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restrict__ x, float* __restrict__ r,
+                                                     const float* __restrict__ rhat, const float* __restrict__ vnew,
+                                                     const float* __restrict__ y, const float* __restrict__ z,
+                                                     const float* __restrict__ t, double* part, unsigned* counters,
+                                                     KScalars* sc) {
+  __shared__ double sh[32];
+  if (sc->done || sc->replace) return;
+  const double alpha = sc->alpha, omega = sc->omega;
+  const float af = (float)alpha, of = (float)omega;
+  double rhr = 0.0, rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float s = fmaf(-af, vnew[i], r[i]);
+    x[i] = fma(omega, (double)z[i], fma(alpha, (double)y[i], x[i]));
+    const float ri = fmaf(-of, t[i], s);
+    r[i] = ri;
+    rhr += (double)rhat[i] * (double)ri;
+    rr += (double)ri * (double)ri;
+  }
+  double s1 = block_sum_d(rhr, sh);
+  double s2 = block_sum_d(rr, sh);
+  if (threadIdx.x == 0) {
+    part[blockIdx.x] = s1;
+    part[gridDim.x + blockIdx.x] = s2;
+  }
+  if (!last_block(&counters[2])) return;
+  double RH = sum_partials(part, gridDim.x, sh);
+  double RR = sum_partials(part + gridDim.x, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    const double rho_old = sc->rho;
+    sc->beta = (omega != 0.0 && rho_old != 0.0) ? (RH / rho_old) * (alpha / omega) : 0.0;
+    sc->rho = RH;
+    sc->rnorm2 = RR;
+    sc->iters += 1;
+    sc->breakdowns = 0;
+    if (!isfinite(RR)) sc->done = 3;
+    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RH == 0.0 || omega == 0.0) sc->replace = 1;
+    if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
+    counters[2] = 0u;
+  }
+}
+
+template <int NDOF>
+static int group_width(int maxdeg) {
+  int g = 1;
+  while (g < maxdeg && g < 32) g <<= 1;
+  return g < 4 ? 4 : g;
+}
+
+template <int NDOF, class F>
+static int with_group(int maxdeg, F&& f) {
+  switch (group_width<NDOF>(maxdeg)) {
+    case 4: return f(std::integral_constant<int, 4>{});
+    case 8: return f(std::integral_constant<int, 8>{});
+    case 16: return f(std::integral_constant<int, 16>{});
+    default: return f(std::integral_constant<int, 32>{});
+  }
+}
+
+template <class F>
+static int with_ndof(int ndof, F&& f) {
+  switch (ndof) {
+    case 1: return f(std::integral_constant<int, 1>{});
+    case 2: return f(std::integral_constant<int, 2>{});
+    case 3: return f(std::integral_constant<int, 3>{});
+  }
+  return FOLGB_ERR_INVALID_ARGUMENT;
+}
+
+static int spmv_blocks(const folgb_plan* p, int G) {
+  int64_t threads = p->N * (int64_t)G;
+  int64_t blocks = (threads + 255) / 256;
+  int64_t cap = (int64_t)num_sms() * 8;
+  return (int)(blocks < cap ? blocks : cap);
+}
+
+__global__ void k_adam(float* __restrict__ x, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
+                       int64_t n, const int* step, float lr, float b1, float b2, float eps) {
+  const int t = *step + 1;
+  const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float gi = g[i];
+    const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
+    const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+    m[i] = mi;
+    v[i] = vi;
+    x[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
+  }
+}
+
+__global__ void k_step_inc(int* step) { *step += 1; }
+
+enum { SOLVER_CG = 0, SOLVER_BICGSTAB = 1 };
+
+static int krylov_solve(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
+                        float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
+                        double* rel_residual, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+  if (!p || !vals || !dinv || !rhs || !x || maxiter <= 0 || !(rtol >= 0.0)) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
+  KWork w;
+  size_t need = layout_krylov(p, workspace, workspace_bytes, &w);
+  if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
+  if (check_every <= 0) check_every = 32;
+  const int64_t n = (int64_t)p->ndof * p->N;
+  int vb = (int)((n + 255) / 256);
+  if (vb > kVecBlocks) vb = kVecBlocks;
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, 8 * sizeof(unsigned), s));
+  if (solver == SOLVER_CG)
+    k_pcg_init<<<vb, 256, 0, s>>>(n, rhs, dinv, w.x, w.r, w.z, w.p0, w.part, w.counters, w.sc, rtol, maxiter);
+  else
+    k_bicg_init<<<vb, 256, 0, s>>>(n, rhs, w.x, w.r, w.rhat, w.part, w.counters, w.sc, rtol, maxiter);
+  FOLGB_LAUNCH_CHECK();
+  KScalars host{};
+  float *pa = w.p0, *pb = w.p1, *va = w.v0, *vb_ = w.v1;
+  int rc = with_ndof(p->ndof, [&](auto nd) -> int {
+    constexpr int NDOF = decltype(nd)::value;
+    return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
+      constexpr int G = decltype(gw)::value;
+      const int sb = spmv_blocks(p, G);
+      int guard = 0;
+      while (true) {
+        for (int k = 0; k < check_every; ++k) {
+          if (solver == SOLVER_CG) {
+            trace_begin(KID_PCG_SPMV, s);
+            k_pcg_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, w.z, pa, pb,
+                                                    w.q, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_SPMV, s);
+            trace_begin(KID_PCG_UPDATE, s);
+            k_pcg_update<<<vb, 256, 0, s>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_UPDATE, s);
+            std::swap(pa, pb);
+          } else {
+            trace_begin(KID_PCG_SPMV, s);
+            k_bicg_p_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, dinv, w.r,
+                                                       w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
+            k_bicg_s_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, dinv, w.r,
+                                                       vb_, w.z, w.t, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_SPMV, s);
+            trace_begin(KID_PCG_UPDATE, s);
+            k_bicg_update<<<vb, 256, 0, s>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_UPDATE, s);
+            std::swap(pa, pb);
+            std::swap(va, vb_);
+          }
+        }
+        FOLGB_LAUNCH_CHECK();
+        FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
+        FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
+        if (host.done) break;
+        if (host.replace) {
+          if (solver == SOLVER_CG)
+            k_true_residual<NDOF, G, false><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, rhs,
+                                                                dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
+          else
+            k_true_residual<NDOF, G, true><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, rhs,
+                                                               dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
+          FOLGB_LAUNCH_CHECK();
+          FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
+          FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
+          if (host.done) break;
+          if (host.iters >= maxiter) {
+            host.done = 2;
+            break;
+          }
+        }
+        // hard cap on host rounds (each round runs >= 1 iteration or a replacement)
+        if (++guard > 4 * (maxiter / check_every + 8)) {
+          host.done = 2;
+          break;
+        }
+      }
+      k_to_float<<<vb, 256, 0, s>>>(n, w.x, x);
+      FOLGB_LAUNCH_CHECK();
+      return (int)FOLGB_OK;
+    });
+  });
+  if (rc) return rc;
+  if (iterations) *iterations = host.iters;
+  if (rel_residual) *rel_residual = host.bnorm2 > 0 ? std::sqrt(host.rnorm2 / host.bnorm2) : 0.0;
+  if (host.done == 3) return FOLGB_ERR_NAN;
+  if (host.done != 1) return FOLGB_ERR_NOT_CONVERGED;
+  return FOLGB_OK;
+}
+
+}  // namespace folgb
+
+using namespace folgb;
+
+extern "C" int folgb_spmv(const folgb_plan* p, const float* vals, const float* x, float* y, void* stream) {
+  if (!p || !vals || !x || !y) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
+  cudaStream_t s = (cudaStream_t)stream;
+  return with_ndof(p->ndof, [&](auto nd) -> int {
+    constexpr int NDOF = decltype(nd)::value;
+    return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
+      constexpr int G = decltype(gw)::value;
+      k_spmv<NDOF, G><<<spmv_blocks(p, G), 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, x, y);
+      FOLGB_LAUNCH_CHECK();
+      return (int)FOLGB_OK;
+    });
+  });
+}
+
+extern "C" int folgb_pcg(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
+                         double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations, double* rel_residual,
+                         void* workspace, size_t workspace_bytes, void* stream) {
+  return krylov_solve(p, SOLVER_CG, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                      workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int folgb_bicgstab(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
+                              double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
+                              double* rel_residual, void* workspace, size_t workspace_bytes, void* stream) {
+  return krylov_solve(p, SOLVER_BICGSTAB, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                      workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int folgb_adam_step(float* params, const float* grads, float* m, float* v, int64_t n, int32_t* step,
+                               float lr, float beta1, float beta2, float eps, void* stream) {
+  if (!params || !grads || !m || !v || !step || n < 0) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (n == 0) return FOLGB_OK;
+  cudaStream_t s = (cudaStream_t)stream;
+  int blocks = (int)((n + 255) / 256);
+  int cap = num_sms() * 8;
+  if (blocks > cap) blocks = cap;
+  k_adam<<<blocks, 256, 0, s>>>(params, grads, m, v, n, step, lr, beta1, beta2, eps);
+  k_step_inc<<<1, 1, 0, s>>>(step);
+  FOLGB_LAUNCH_CHECK();
+  return FOLGB_OK;
+}

@@ -181,6 +181,7 @@ class FiniteElementLoss:
         p.num_gp = int(self.num_gp)
         p.control_layout = capi.CONTROL_ELEMENT if s.get("control_layout", "nodal") == "element" else capi.CONTROL_NODAL
         p.shear_mode = capi.SHEAR_CONSISTENT if s.get("voigt_shear_mode", "reference") == "consistent" else capi.SHEAR_REFERENCE
+        p.kernel_variant = 1 if s.get("kernel_variant", "auto") == "generic" else 0
         p.young_modulus = float(mat.get("young_modulus", 1.0))
         p.poisson_ratio = float(mat.get("poisson_ratio", 0.3))
         bf = np.zeros(3)
@@ -338,7 +339,8 @@ class FiniteElementLoss:
     def ComputeJacobianMatrixAndResidualVector(self, total_control_vars, total_primal_vars,
                                                transpose_jacobian: bool = False, with_matrix: bool = True):
         torch = _torch()
-        plan = self._get_csr_plan()
+        # the residual alone needs no CSR tables
+        plan = self._get_csr_plan() if with_matrix else self._plan
         ctrl = _dev(total_control_vars).reshape(-1)
         u = _dev(total_primal_vars).reshape(-1)
         residual = torch.empty(self.total_number_of_dofs, dtype=torch.float32, device="cuda")

@@ -67,13 +67,15 @@ class FiniteElementSolver(Solver):
                                                             self.fe_solver_settings["linear_solver_settings"])
         name = self.linear_solver_settings["solver"]
         known = ["PETSc-bcgsl", "PETSc-tfqmr", "PETSc-minres", "PETSc-gmres", "JAX-direct", "JAX-bicgstab",
-                 "GB300-pcg"]
+                 "GB300-pcg", "GB300-bicgstab"]
         if name not in known:
             raise ValueError(f"linear solver {name} does exist, available options are {known}")
-        self.LinearSolve = self.PCGLinearSolver
+        # CG for the SPD systems it was asked for; every other name keeps the
+        # reference's default behaviour (a Krylov method that tolerates
+        # nonsymmetric / indefinite tangents): Jacobi-BiCGSTAB.
+        self.LinearSolve = self.PCGLinearSolver if name == "GB300-pcg" else self.BiCGSTABLinearSolver
 
-    def PCGLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
-        """Solve tangent_matrix dx = -residual with Jacobi-PCG; returns dx."""
+    def _krylov(self, fn_name, tangent_matrix, residual_vector):
         torch = _torch()
         plan = tangent_matrix.plan
         b = -_dev(residual_vector)
@@ -81,14 +83,24 @@ class FiniteElementSolver(Solver):
         ws = plan.workspace(capi.OP_PCG)
         iters, rel = C.c_int32(), C.c_double()
         s = self.linear_solver_settings
-        rc = plan.lib.folgb_pcg(plan.handle, capi.ptr(tangent_matrix.data), capi.ptr(tangent_matrix.inv_diag),
-                                capi.ptr(b), capi.ptr(x), float(s["tol"]), int(s["maxiter"]),
-                                int(s.get("check_every", 32)), C.byref(iters), C.byref(rel), capi.ptr(ws), ws.numel(),
-                                capi.stream_handle())
-        self.last_linear_info = {"iterations": iters.value, "relative_residual": rel.value, "status": rc}
+        fn = getattr(plan.lib, fn_name)
+        rc = fn(plan.handle, capi.ptr(tangent_matrix.data), capi.ptr(tangent_matrix.inv_diag), capi.ptr(b),
+                capi.ptr(x), float(s["tol"]), int(s["maxiter"]), int(s.get("check_every", 32)), C.byref(iters),
+                C.byref(rel), capi.ptr(ws), ws.numel(), capi.stream_handle())
+        self.last_linear_info = {"solver": fn_name, "iterations": iters.value, "relative_residual": rel.value,
+                                 "status": rc}
         if rc not in (capi.OK, capi.ERR_NOT_CONVERGED):
-            capi.check("folgb_pcg", rc)
+            capi.check(fn_name, rc)
         return x
+
+    def PCGLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
+        """Solve tangent_matrix dx = -residual with Jacobi-PCG (x0 = 0); returns dx."""
+        return self._krylov("folgb_pcg", tangent_matrix, residual_vector)
+
+    def BiCGSTABLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
+        """Solve tangent_matrix dx = -residual with Jacobi-BiCGSTAB (x0 = 0); returns dx.
+        (fe_solver.py:60-67 passes x0 = current dofs; dx starts from 0 here.)"""
+        return self._krylov("folgb_bicgstab", tangent_matrix, residual_vector)
 
 
 class FiniteElementLinearResidualBasedSolver(FiniteElementSolver):

@@ -61,7 +61,8 @@ typedef struct folgb_physics {
   int32_t num_gp;         /* Gauss order 1..3 ("num_gp", fe_loss.py:68-83)     */
   int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
   int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */
-  int32_t reserved;
+  int32_t kernel_variant; /* 0: fastest kernel for the element (sum-factorised
+                             hex8 2x2x2 elasticity); 1: the generic Gauss loop */
   double young_modulus;   /* material_dict young_modulus (elastic D scale)     */
   double poisson_ratio;   /* material_dict poisson_ratio                       */
   double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */
@@ -153,14 +154,26 @@ int folgb_assemble(const folgb_plan* plan, const float* control, const float* do
                    void* stream);
 
 /* Jacobi-preconditioned CG on the plan's CSR (x0 = 0), replacing
- * FiniteElementSolver.LinearSolve (fe_solver.py:60-78).  Vectors are FP32,
- * inner products and norms FP64.  Solves A x = rhs to ||r|| <= rtol ||rhs||.
- * Runs on the stream; it returns after the solve (it reads the residual norm
- * every check_every iterations).  iterations / rel_residual may be NULL. */
+ * FiniteElementSolver.LinearSolve (fe_solver.py:60-78) for symmetric positive
+ * definite systems.  Matrix and Krylov vectors FP32, inner products, norms and
+ * the iterate FP64; reliable updates recompute the true residual b - A x in
+ * FP64, and convergence (||b - A x|| <= rtol ||rhs||) is judged on it.
+ * The call returns after the solve: it reads the device flags every
+ * check_every iterations.  Returns FOLGB_ERR_NOT_CONVERGED at maxiter (x holds
+ * the last iterate).  iterations / rel_residual may be NULL. */
 int folgb_pcg(const folgb_plan* plan, const float* csr_values, const float* inv_diag,
               const float* rhs, float* x, double rtol, int32_t maxiter, int32_t check_every,
               int32_t* iterations, double* rel_residual,
               void* workspace, size_t workspace_bytes, void* stream);
+
+/* Jacobi-preconditioned BiCGSTAB with the same precision scheme, for
+ * nonsymmetric or indefinite systems: the reference's default linear solver
+ * (jax.scipy.sparse.linalg.bicgstab, fe_solver.py:60-67).  Same arguments and
+ * workspace as folgb_pcg. */
+int folgb_bicgstab(const folgb_plan* plan, const float* csr_values, const float* inv_diag,
+                   const float* rhs, float* x, double rtol, int32_t maxiter, int32_t check_every,
+                   int32_t* iterations, double* rel_residual,
+                   void* workspace, size_t workspace_bytes, void* stream);
 
 /* y = A x on the plan's CSR (FP32). */
 int folgb_spmv(const folgb_plan* plan, const float* csr_values, const float* x, float* y,

@@ -256,7 +256,7 @@ def linear_elastic_element(etype, X, de, ue, num_gp=2, young=1.0, nu=0.3, body_f
     nen, dim = ELEMENTS[etype]
     ndof = dim
     D = isotropic_D(dim, young, nu)
-    b = np.zeros(dim) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()
+    b = np.zeros(dim) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()[:dim]
     pts, wts = gauss_rule(etype, num_gp)
     E = X.shape[0]
     dt = np.result_type(X, de, ue)
@@ -375,7 +375,7 @@ def neohooke_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None,
     V = _V3 if d == 3 else _V2
     m_ref = np.array([1.0 if p == q else 2.0 for p, q in V])
     m_use = m_ref if shear_mode == "reference" else np.ones(len(V))
-    b = np.zeros(d) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()
+    b = np.zeros(d) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()[:d]
     pts, wts = gauss_rule(etype, num_gp)
     E = X.shape[0]
     dt = np.result_type(X, de, ue)

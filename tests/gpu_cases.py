@@ -8,14 +8,16 @@ from oracle import fe_oracle as fo
 ETYPE_NAME = {"quad4": "quad", "hex8": "hexahedron", "tet4": "tetra"}
 
 
-def make_mesh(etype, n, seed=0, jitter=0.02):
+def make_mesh(etype, n, seed=0, jitter=0.08):
+    """Structured mesh with nodes displaced by N(0, (jitter * h)^2), h = 1/n."""
     rng = np.random.default_rng(seed)
+    amp = jitter / n
     if etype == "quad4":
         m = M.create_2D_square_mesh(1.0, n + 1)
-        m.nodes_coordinates = m.nodes_coordinates + jitter * rng.standard_normal(m.nodes_coordinates.shape) * np.array([1, 1, 0])
+        m.nodes_coordinates = m.nodes_coordinates + amp * rng.standard_normal(m.nodes_coordinates.shape) * np.array([1, 1, 0])
     else:
         m = M.create_3D_box_mesh(n, n, n)
-        m.nodes_coordinates = m.nodes_coordinates + jitter * rng.standard_normal(m.nodes_coordinates.shape)
+        m.nodes_coordinates = m.nodes_coordinates + amp * rng.standard_normal(m.nodes_coordinates.shape)
         if etype == "tet4":
             m = M.split_hex_to_tets(m)
     return m

@@ -57,7 +57,8 @@ def test_loss_adjoint_matches_oracle(cuda, etype, physics, n, layout):
     B = 2
     nctrl = gl.GetNumberOfControls()
     ctrl = 0.5 + rng.random((B, nctrl))
-    u = 0.05 * rng.standard_normal((B, gl.GetTotalNumberOfDOFs()))
+    # displacement noise scaled to the element size: strains of a few percent
+    u = (0.03 / n) * rng.standard_normal((B, gl.GetTotalNumberOfDOFs()))
     mean, (mn, mx, _), losses, du, dc = gl.ComputeBatchLossAndGrad(ctrl, u)
     gl.CheckDeviceStatus()
     omean, _, olosses, odu, odc = ol.batch_loss_and_grads(ctrl, u)
@@ -65,6 +66,31 @@ def test_loss_adjoint_matches_oracle(cuda, etype, physics, n, layout):
     assert rel_fro(du.cpu().numpy(), odu) < TOL
     assert rel_fro(dc.cpu().numpy(), odc) < TOL
     assert np.all(du.cpu().numpy()[:, ol.dirichlet_indices] == 0)
+
+
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+@pytest.mark.parametrize("bf", [None, [0.3, -0.2, 0.1]])
+def test_hex8_sum_factorised_matches_generic_and_oracle(cuda, layout, bf):
+    """The sum-factorised hex8 kernel and the generic Gauss loop agree with
+    each other and with the oracle (loss, both gradients, residual)."""
+    m = make_mesh("hex8", 5, seed=21, jitter=0.15)
+    s = _settings("hex8", "elastic", layout, 1.0, bf)
+    fast = gpu_loss("hex8", "elastic", m, s)
+    generic = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": "generic"})
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(22)
+    ctrl = 0.5 + rng.random((2, fast.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((2, fast.GetTotalNumberOfDOFs()))
+    a = fast.ComputeBatchLossAndGrad(ctrl, u)
+    g = generic.ComputeBatchLossAndGrad(ctrl, u)
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, y, z in zip(a[2:], g[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+        assert rel_fro(y.cpu().numpy(), z) < TOL
+    uf = ol.full_dof_vector(u[0])
+    _, Rf = fast.ComputeJacobianMatrixAndResidualVector(ctrl[0], uf, with_matrix=False)
+    _, Ro = ol.csr(ctrl[0], uf)
+    assert rel_fro(Rf.cpu().numpy(), Ro) < TOL
 
 
 @pytest.mark.parametrize("exponent,bf", [(1.5, None), (1.0, [0.3, -0.2, 0.1]), (2.0, [0.1, 0.2, 0.3])])
@@ -120,7 +146,7 @@ def test_csr_pattern_bit_exact_and_values(cuda, etype, physics, n, transpose):
     gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
     rng = np.random.default_rng(10)
     ctrl = 0.5 + rng.random(m.GetNumberOfNodes())
-    u = ol.full_dof_vector(0.05 * rng.standard_normal(ol.total_dofs))
+    u = ol.full_dof_vector((0.03 / n) * rng.standard_normal(ol.total_dofs))
     jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, u, transpose_jacobian=transpose)
     gl.CheckDeviceStatus()
     A, Ro = ol.csr(ctrl, u, transpose=transpose)
@@ -151,7 +177,7 @@ def test_linear_solve_matches_direct(cuda, etype, physics, n):
     s = _settings(etype, physics)
     gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
     ctrl = 0.5 + np.random.default_rng(15).random(m.GetNumberOfNodes())
-    solver = FiniteElementLinearResidualBasedSolver("lin", gl, {"linear_solver_settings": {"tol": 1e-8, "maxiter": 5000}})
+    solver = FiniteElementLinearResidualBasedSolver("lin", gl, {"linear_solver_settings": {"solver": "GB300-pcg", "tol": 1e-8, "maxiter": 5000}})
     solver.Initialize()
     x = solver.Solve(ctrl, np.zeros(ol.total_dofs)).cpu().numpy()
     xo = fo.linear_solve(ol, ctrl, np.zeros(ol.total_dofs))
@@ -196,7 +222,8 @@ def test_inverted_element_and_nan_are_reported(cuda):
     assert e.value.code == _capi.ERR_NONPOSITIVE_DETJ
     m2 = make_mesh("hex8", 2, seed=18)
     gl2 = gpu_loss("hex8", "elastic", m2, _settings("hex8", "elastic"))
-    u[0, 5] = np.nan
+    free = gl2.non_dirichlet_indices[len(gl2.non_dirichlet_indices) // 2]
+    u[0, free] = np.nan
     gl2.ComputeBatchLossAndGrad(ctrl, u)
     with pytest.raises(_capi.FolgbError) as e:
         gl2.CheckDeviceStatus()
@@ -212,3 +239,24 @@ def test_invalid_arguments_raise(cuda):
     m.elements_nodes["quad"][0, 0] = 10 ** 6          # node id out of range
     with pytest.raises(_capi.FolgbError):
         gpu_loss("quad4", "thermal", m, _settings("quad4", "thermal"))
+
+
+@pytest.mark.parametrize("shear", ["reference", "consistent"])
+def test_bicgstab_on_indefinite_neohooke_tangent(cuda, shear):
+    """The reference NH model is not stress-free at C = I (S = -mu I), so its
+    tangent is indefinite near u = 0: Jacobi-BiCGSTAB (the reference's default
+    solver) against an FP64 direct solve."""
+    from folax_gb300.solvers import FiniteElementSolver
+    m = make_mesh("tet4", 3, seed=19)
+    s = _settings("tet4", "neohooke", shear=shear)
+    gl, ol = gpu_loss("tet4", "neohooke", m, s), oracle_loss("tet4", "neohooke", m, s)
+    ctrl = 0.5 + np.random.default_rng(20).random(m.GetNumberOfNodes())
+    u = ol.full_dof_vector(np.zeros(ol.total_dofs), 0.5)
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, u)
+    solver = FiniteElementSolver("b", gl, {"linear_solver_settings": {"solver": "JAX-bicgstab", "tol": 1e-9,
+                                                                       "maxiter": 4000}})
+    solver.Initialize()
+    dx = solver.LinearSolve(jac, R).cpu().numpy()
+    A, Ro = ol.csr(ctrl, u)
+    assert solver.last_linear_info["status"] == 0, solver.last_linear_info
+    assert rel_fro(dx, fo.direct_solve(A, -Ro)) < 1e-5
