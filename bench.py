@@ -98,10 +98,9 @@ class Clocks:
         try:
             fd, self.path = tempfile.mkstemp(suffix=".csv")
             os.close(fd)
-            self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
-                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+                                          "--format=csv,noheader,nounits", "-lms", "100", "-f", self.path],
+                                         stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
 
@@ -113,7 +112,6 @@ class Clocks:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
-        self.fh.close()
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for line in open(self.path):
@@ -274,8 +272,15 @@ def main():
     torch.cuda.synchronize()
     barrier()
     torch.cuda.synchronize()
+    # clocks are sampled from before a one-second untimed soak (steady clocks,
+    # enough samples) to the end of the timed region
     clocks = Clocks(local)
     clocks.start()
+    t_end = time.perf_counter() + 1.0
+    while time.perf_counter() < t_end:
+        for _ in range(20):
+            fused()
+        torch.cuda.synchronize()
     ms = timed(fused, args.steps)
     clk = clocks.stop()
     torch.cuda.synchronize()
