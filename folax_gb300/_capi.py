@@ -19,11 +19,13 @@ ERR_NOT_CONVERGED = 4
 ERR_CUDA = 5
 ERR_WORKSPACE = 6
 ERR_NO_PATTERN = 7
+ERR_TOO_LARGE = 8
 
 STATUS_NAMES = {
     OK: "ok", ERR_INVALID_ARGUMENT: "invalid argument", ERR_NONPOSITIVE_DETJ: "non-positive detJ",
     ERR_NAN: "non-finite value", ERR_NOT_CONVERGED: "not converged", ERR_CUDA: "CUDA error",
     ERR_WORKSPACE: "workspace too small", ERR_NO_PATTERN: "plan has no CSR pattern",
+    ERR_TOO_LARGE: "problem larger than the fixed scratch",
 }
 
 QUAD4, HEX8, TET4 = 0, 1, 2
@@ -61,6 +63,7 @@ PROTOTYPES = {
     "folgb_workspace_bytes": (sz, [vp, i32, i32]),
     "folgb_loss_adjoint": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_loss_adjoint_plain": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_loss_adjoint_noalloc": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp]),
     "folgb_csr_pattern": (C.c_int, [vp, vp, vp, vp]),
     "folgb_assemble": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_pcg": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),

@@ -36,7 +36,8 @@ enum {
   FOLGB_ERR_NOT_CONVERGED = 4,    /* PCG hit maxiter above tolerance         */
   FOLGB_ERR_CUDA = 5,             /* a CUDA runtime call failed              */
   FOLGB_ERR_WORKSPACE = 6,        /* workspace NULL or smaller than required */
-  FOLGB_ERR_NO_PATTERN = 7        /* plan built without the CSR tables       */
+  FOLGB_ERR_NO_PATTERN = 7,       /* plan built without the CSR tables       */
+  FOLGB_ERR_TOO_LARGE = 8         /* problem exceeds a fixed-size scratch    */
 };
 
 /* element types (fol/geometries/__init__.py:18-21) */
@@ -134,6 +135,25 @@ int folgb_loss_adjoint_plain(const folgb_plan* plan, int32_t batch,
                              float* losses, float* dloss_ddofs, float* dloss_dcontrol,
                              int32_t* device_status, void* workspace, size_t workspace_bytes,
                              void* stream);
+
+/* folgb_loss_adjoint for callers that cannot allocate device memory when they
+ * evaluate the loss (a framework custom call with no scratch-buffer slot, a
+ * fixed memory budget, code running inside an allocator hook).  No
+ * counterpart in the reference.  Same arguments and results as
+ * folgb_loss_adjoint minus the workspace: the scratch is a fixed array inside
+ * the library's device image, 32 MiB on every GPU that loads the library,
+ * held until exit (enough for 64^3 hex8 elasticity, batch 1: the size
+ * folgb_workspace_bytes(plan, FOLGB_OP_LOSS_ADJOINT, batch) reports must fit).
+ * Larger problems return FOLGB_ERR_TOO_LARGE.  The array is shared
+ * by all calls on a device, so calls that overlap on the GPU race; order them
+ * on one stream.  The first call on each device looks up the array's address
+ * (cudaGetSymbolAddress); make it before any stream capture.  Calls no
+ * allocator. */
+int folgb_loss_adjoint_noalloc(const folgb_plan* plan, int32_t batch,
+                               const float* control, int64_t control_stride,
+                               const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
+                               float* losses, float* dloss_ddofs, float* dloss_dcontrol,
+                               int32_t* device_status, void* stream);
 
 /* Copies the plan's CSR pattern (canonical: sorted column indices, one entry
  * per connected dof pair, the pattern scipy.sparse.csr_array builds from the
