@@ -81,7 +81,7 @@ __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const Batch
 
 struct BatchWS {
   float* g;
-  float* gde;
+  int rec;
   float* partials;
   unsigned* counters;
   float* scale;
@@ -91,8 +91,8 @@ static size_t layout_batch(const folgb_batch_plan* bp, void* base, size_t cap, B
   const folgb_plan* p = bp->mesh;
   Bump b(base, cap);
   BatchWS t;
-  t.g = b.take<float>((size_t)p->E * p->nen * p->ndof);
-  t.gde = p->ctrl_layout == FOLGB_CONTROL_NODAL ? b.take<float>((size_t)p->E * p->nen) : nullptr;
+  t.rec = loss_record(p);
+  t.g = b.take<float>((size_t)p->E * p->nen * t.rec);
   t.partials = b.take<float>((size_t)bp->ntiles);
   t.counters = b.take<unsigned>(1);
   t.scale = b.take<float>((size_t)bp->I);
@@ -210,7 +210,7 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
   A.ctrl_layout = p->ctrl_layout;
   A.mat = p->mat;
   A.g = w.g;
-  A.gde = w.gde;
+  A.rec = w.rec;
   A.dctrl_elem = elem_ctrl ? dloss_dcontrol : nullptr;
   A.partials = w.partials;
   A.counters = w.counters;
@@ -231,7 +231,7 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
   });
   if (rc) return rc;
   if (dloss_ddofs || dloss_dcontrol) {
-    rc = launch_gather(p, 1, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, 0,
+    rc = launch_gather(p, 1, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, 0,
                        elem_ctrl ? nullptr : dloss_dcontrol, 0, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, bp->d_node_inst, bp->d_elem_inst);
   }

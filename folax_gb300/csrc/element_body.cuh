@@ -54,8 +54,11 @@ struct VecArgs {
   int apply_dirichlet;
   int ctrl_layout;
   MatConst mat;
-  float* g;           // [B][E][nen*ndof] element vectors
-  float* gde;         // [B][E][nen] (nodal control) or NULL
+  // element results: one record of `rec` floats per (instance, element, node)
+  // = ndof vector components (+ the nodal control sensitivity), local-node-major:
+  // record (b, e, a) starts at ((b*nen + a)*E + e)*rec
+  float* g;
+  int rec;
   float* dctrl_elem;  // [B][E] element-layout control gradient or NULL
   float* partials;    // [B][gridDim.x]
   unsigned* counters; // [B]
@@ -312,16 +315,18 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
       }
     }
     if (!isfinite(energy)) bad |= 2;
-    // element vector (16-byte stores; ND is a multiple of 4 for every element)
-    float4* gout = reinterpret_cast<float4*>(A.g + ((int64_t)b * A.E + e) * ND);
+    // one record per (element, node), local-node-major ([b][a][e]): ndof
+    // vector components, then the nodal control sensitivity when present
+    const bool nodal_gde = (MODE == MODE_LOSS) && A.ctrl_layout == FOLGB_CONTROL_NODAL;
 #pragma unroll
-    for (int i = 0; i < ND / 4; ++i) gout[i] = make_float4(g[4 * i], g[4 * i + 1], g[4 * i + 2], g[4 * i + 3]);
+    for (int a = 0; a < NEN; ++a) {
+      float* rec = A.g + (((int64_t)b * NEN + a) * A.E + e) * A.rec;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) rec[c] = g[a * NDOF + c];
+      if (nodal_gde) rec[NDOF] = gd[a];
+    }
     if (MODE == MODE_LOSS) {
-      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) {
-        float4* go = reinterpret_cast<float4*>(A.gde + ((int64_t)b * A.E + e) * NEN);
-#pragma unroll
-        for (int i = 0; i < NEN / 4; ++i) go[i] = make_float4(gd[4 * i], gd[4 * i + 1], gd[4 * i + 2], gd[4 * i + 3]);
-      } else if (A.dctrl_elem) {
+      if (!nodal_gde && A.dctrl_elem) {
         float s = 0.f;
 #pragma unroll
         for (int a = 0; a < NEN; ++a) s += gd[a];

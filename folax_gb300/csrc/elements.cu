@@ -44,9 +44,11 @@ struct GatherArgs {
   int nen;
   const int* inc_ptr;
   const int* inc_slot;
+  const int* inc_padded;  // [N][pad] slots, -1 padded (pad 4 or 8), or NULL
   const unsigned char* dmask;
-  const float* g;      // [B][E*nen][ndof] element vectors
-  const float* gde;    // [B][E*nen] or NULL
+  const float* g;      // [B][nen][E] records of `rec` floats (local-node-major)
+  int rec;             // record width: ndof, + 1 when it carries the control sensitivity
+  int with_gde;        // record component ndof is the nodal control sensitivity
   const float* scale;  // [B] or NULL (scale 1)
   float* out;          // [B][ndof*N] or NULL
   int64_t out_stride;
@@ -58,28 +60,84 @@ struct GatherArgs {
   const int* elem_inst;  // batched meshes: instance of each element, or NULL
 };
 
-// Deterministic transpose-gather: every node sums its incident element slots
-// in ascending element order (no float atomics).  Dirichlet dofs get 0
-// (fe_loss.py:91-100 overwrites them, so their gradient is zero; the BC
-// residual rows are zeroed by fe_loss.py:191-207).
-template <int NDOF>
+// Deterministic transpose-gather: node n sums the records of its incident
+// (element, local node) slots in ascending element order (no float atomics).
+// Every index and record load of a node is issued before the sums (vector
+// loads: records are 4/8/16 bytes, and when no node has more than 4 or 8
+// incidences the slot list is read from a -1 padded table with int4 loads),
+// so a node costs two memory latencies, not one per slot.
+// Dirichlet dofs get 0 (fe_loss.py:91-100 overwrites them, so their gradient
+// is zero; the BC residual rows are zeroed by fe_loss.py:191-207).
+template <int REC>
+__device__ __forceinline__ void load_rec(const float* __restrict__ p, float (&v)[REC]) {
+  if constexpr (REC == 4) {
+    const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = t.x;
+    v[1] = t.y;
+    v[2] = t.z;
+    v[3] = t.w;
+  } else if constexpr (REC == 2) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    v[0] = t.x;
+    v[1] = t.y;
+  } else {
+    v[0] = __ldg(p);
+  }
+}
+
+template <int NDOF, int REC, bool GDE, int CH>
+__device__ __forceinline__ void sum_slots(const float* __restrict__ g, const int (&slot)[CH], float (&acc)[NDOF],
+                                          float& accd) {
+  float v[CH][REC];
+#pragma unroll
+  for (int k = 0; k < CH; ++k) {
+    if (slot[k] >= 0) load_rec<REC>(g + (int64_t)slot[k] * REC, v[k]);
+    else {
+#pragma unroll
+      for (int c = 0; c < REC; ++c) v[k][c] = 0.f;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < CH; ++k) {
+#pragma unroll
+    for (int c = 0; c < NDOF; ++c) acc[c] += v[k][c];
+    if constexpr (GDE) accd += v[k][NDOF];
+  }
+}
+
+// PAD = 4 or 8: padded slot table; PAD = 0: CSR slot list in chunks of 8.
+template <int NDOF, int REC, bool GDE, int PAD>
 __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
   const int b = blockIdx.y;
   const float scb = A.scale ? A.scale[b] : 1.f;
-  const int64_t sbase = (int64_t)b * A.E * A.nen;
+  const float* g = A.g + (int64_t)b * A.E * A.nen * REC;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < A.N; n += stride) {
-    const int s0 = __ldg(A.inc_ptr + n), s1 = __ldg(A.inc_ptr + n + 1);
     float acc[NDOF];
 #pragma unroll
     for (int c = 0; c < NDOF; ++c) acc[c] = 0.f;
     float accd = 0.f;
-    for (int k = s0; k < s1; ++k) {
-      const int64_t slot = sbase + __ldg(A.inc_slot + k);
-      const float* gv = A.g + slot * NDOF;
+    if constexpr (PAD > 0) {
+      int slot[PAD];
+      const int4* sp = reinterpret_cast<const int4*>(A.inc_padded + n * PAD);
 #pragma unroll
-      for (int c = 0; c < NDOF; ++c) acc[c] += gv[c];
-      if (A.gde) accd += A.gde[slot];
+      for (int k = 0; k < PAD / 4; ++k) {
+        const int4 t = __ldg(sp + k);
+        slot[4 * k] = t.x;
+        slot[4 * k + 1] = t.y;
+        slot[4 * k + 2] = t.z;
+        slot[4 * k + 3] = t.w;
+      }
+      sum_slots<NDOF, REC, GDE, PAD>(g, slot, acc, accd);
+    } else {
+      constexpr int CH = 8;
+      const int s0 = __ldg(A.inc_ptr + n), s1 = __ldg(A.inc_ptr + n + 1);
+      for (int k0 = s0; k0 < s1; k0 += CH) {
+        int slot[CH];
+#pragma unroll
+        for (int k = 0; k < CH; ++k) slot[k] = (k0 + k < s1) ? __ldg(A.inc_slot + k0 + k) : -1;
+        sum_slots<NDOF, REC, GDE, CH>(g, slot, acc, accd);
+      }
     }
     const float sc = A.node_inst ? A.scale[__ldg(A.node_inst + n)] : scb;
     if (A.out) {
@@ -123,7 +181,8 @@ struct MatArgs {
   int epb;         // elements per block
   float* Ke;       // [B][E][nen][nen][ndof][ndof]
   float* Fe;       // plain: [B][E][nd] or NULL
-  float* gde;      // plain, nodal control: [B][E][nen]
+  float* g;        // plain, nodal control: records (component ndof = control sensitivity)
+  int rec;
   float* dctrl_elem;  // plain, element control: [B][E]
   float exponent, inv_batch;
   int* status;
@@ -428,7 +487,8 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
         gd = fmaf(rec[R::O_SED], gp.N[q][a], gd);
         fw = fmaf(rec[R::O_WD], gp.N[q][a], fw);
       }
-      if (A.ctrl_layout == FOLGB_CONTROL_NODAL) A.gde[((int64_t)b * A.E + e) * NEN + a] = gd;
+      if (A.ctrl_layout == FOLGB_CONTROL_NODAL)
+        A.g[(((int64_t)b * NEN + a) * A.E + e) * A.rec + NDOF] = gd;
       if (A.Fe) {
 #pragma unroll
         for (int i = 0; i < NDOF; ++i)
@@ -540,9 +600,12 @@ __global__ void __launch_bounds__(256) k_plain_backward(const VecArgs A, const f
     }
 #pragma unroll
     for (int i = 0; i < ND; ++i) energy = fmaf(ue[i], r[i], energy);
-    float4* gout = reinterpret_cast<float4*>(A.g + ((int64_t)b * A.E + e) * ND);
 #pragma unroll
-    for (int i = 0; i < ND / 4; ++i) gout[i] = make_float4(r[4 * i], r[4 * i + 1], r[4 * i + 2], r[4 * i + 3]);
+    for (int a = 0; a < NEN; ++a) {
+      float* rec = A.g + (((int64_t)b * NEN + a) * A.E + e) * A.rec;
+#pragma unroll
+      for (int c = 0; c < NDOF; ++c) rec[c] = r[a * NDOF + c];
+    }
   }
   float be = block_sum(energy, red);
   finish_loss(be, A, b, red);
@@ -553,7 +616,7 @@ __global__ void __launch_bounds__(256) k_plain_backward(const VecArgs A, const f
 // ---------------------------------------------------------------------------
 struct LossWS {
   float* g;
-  float* gde;
+  int rec;
   float* partials;
   unsigned* counters;
   float* scale;
@@ -562,25 +625,30 @@ struct LossWS {
 };
 
 static int loss_blocks(const folgb_plan* p) { return (int)((p->E + 255) / 256); }
+// partial-sum slots: enough for the smallest element-kernel block (64 threads)
+static int loss_partial_slots(const folgb_plan* p) { return (int)((p->E + 63) / 64); }
+
+// record width of the loss path: ndof components (+ the nodal control sensitivity)
+static int loss_rec(const folgb_plan* p) { return loss_record(p); }
 
 static size_t layout_loss(const folgb_plan* p, int B, bool plain, void* base, size_t cap, LossWS* w) {
   Bump bp(base, cap);
   const int64_t ND = (int64_t)p->nen * p->ndof;
-  float* g = bp.take<float>((size_t)B * p->E * ND);
-  float* gde = p->ctrl_layout == FOLGB_CONTROL_NODAL ? bp.take<float>((size_t)B * p->E * p->nen) : nullptr;
-  float* partials = bp.take<float>((size_t)B * loss_blocks(p));
+  const int rec = loss_rec(p);
+  float* g = bp.take<float>((size_t)B * p->E * p->nen * rec);
+  float* partials = bp.take<float>((size_t)B * loss_partial_slots(p));
   unsigned* counters = bp.take<unsigned>((size_t)B);
   float* scale = bp.take<float>((size_t)B);
   float* Ke = plain ? bp.take<float>((size_t)B * p->E * ND * ND) : nullptr;
   float* Fe = (plain && p->mat.has_bf) ? bp.take<float>((size_t)B * p->E * ND) : nullptr;
-  if (w) *w = LossWS{g, gde, partials, counters, scale, Ke, Fe};
+  if (w) *w = LossWS{g, rec, partials, counters, scale, Ke, Fe};
   return align_up(bp.off);
 }
 
 static size_t layout_assemble(const folgb_plan* p, void* base, size_t cap, float** g, float** Ke) {
   Bump bp(base, cap);
   const int64_t ND = (int64_t)p->nen * p->ndof;
-  float* gg = bp.take<float>((size_t)p->E * ND);
+  float* gg = bp.take<float>((size_t)p->E * p->nen * residual_record(p));
   float* kk = bp.take<float>((size_t)p->E * ND * ND);
   if (g) *g = gg;
   if (Ke) *Ke = kk;
@@ -613,7 +681,7 @@ static int launch_matrix(const MatArgs& A0, int B, int npts, cudaStream_t s) {
   return FOLGB_OK;
 }
 
-int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, const float* scale, float* out,
+int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
                   cudaStream_t s, const int* node_inst, const int* elem_inst) {
   GatherArgs G;
@@ -624,9 +692,11 @@ int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, 
   G.nen = p->nen;
   G.inc_ptr = p->d_inc_ptr;
   G.inc_slot = p->d_inc_slot;
+  G.inc_padded = p->d_inc_padded;
   G.dmask = p->d_dmask;
   G.g = g;
-  G.gde = gde;
+  G.rec = rec;
+  G.with_gde = with_gde;
   G.scale = scale;
   G.out = out;
   G.out_stride = out_stride;
@@ -634,19 +704,41 @@ int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, 
   G.dctrl_stride = dctrl_stride;
   G.dctrl_elem = dctrl_elem;
   G.rescale_elem = rescale_elem;
+  if (rec != padded_record(p->ndof + (with_gde ? 1 : 0))) return FOLGB_ERR_INVALID_ARGUMENT;
   int64_t work = p->N > p->E ? p->N : p->E;
   int blocks = (int)((work + 255) / 256);
   int cap = num_sms() * 8;
   if (blocks > cap) blocks = cap;
   dim3 grid((unsigned)blocks, (unsigned)B);
+  auto go = [&](auto nd, auto rc_, auto gde) -> int {
+    constexpr int NDOF = decltype(nd)::value, REC = decltype(rc_)::value;
+    constexpr bool GDE = decltype(gde)::value;
+    switch (p->inc_pad) {
+      case 4: k_node_gather<NDOF, REC, GDE, 4><<<grid, 256, 0, s>>>(G); break;
+      case 8: k_node_gather<NDOF, REC, GDE, 8><<<grid, 256, 0, s>>>(G); break;
+      default: k_node_gather<NDOF, REC, GDE, 0><<<grid, 256, 0, s>>>(G); break;
+    }
+    return (int)FOLGB_OK;
+  };
+  using I1 = std::integral_constant<int, 1>;
+  using I2 = std::integral_constant<int, 2>;
+  using I3 = std::integral_constant<int, 3>;
+  using I4 = std::integral_constant<int, 4>;
+  using T = std::true_type;
+  using F = std::false_type;
   trace_begin(KID_GATHER, s);
-  switch (p->ndof) {
-    case 1: k_node_gather<1><<<grid, 256, 0, s>>>(G); break;
-    case 2: k_node_gather<2><<<grid, 256, 0, s>>>(G); break;
-    case 3: k_node_gather<3><<<grid, 256, 0, s>>>(G); break;
+  int rcode;
+  switch (p->ndof * 2 + (with_gde ? 1 : 0)) {
+    case 2: rcode = go(I1{}, I1{}, F{}); break;
+    case 3: rcode = go(I1{}, I2{}, T{}); break;
+    case 4: rcode = go(I2{}, I2{}, F{}); break;
+    case 5: rcode = go(I2{}, I4{}, T{}); break;
+    case 6: rcode = go(I3{}, I4{}, F{}); break;
+    case 7: rcode = go(I3{}, I4{}, T{}); break;
     default: return FOLGB_ERR_INVALID_ARGUMENT;
   }
   trace_end(KID_GATHER, s);
+  if (rcode) return rcode;
   FOLGB_LAUNCH_CHECK();
   return FOLGB_OK;
 }
@@ -670,7 +762,7 @@ static VecArgs make_vec_args(const folgb_plan* p, int B, const float* control, i
   A.ctrl_layout = p->ctrl_layout;
   A.mat = p->mat;
   A.g = w.g;
-  A.gde = w.gde;
+  A.rec = w.rec;
   A.dctrl_elem = dctrl_elem;
   A.partials = w.partials;
   A.counters = w.counters;
@@ -718,7 +810,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
                             elem_ctrl ? dloss_dcontrol : nullptr, device_status);
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
-  if (p->phys.kernel_variant == 0 && launch_hex8_fast(p, A, grid, MODE_LOSS, s)) {
+  if (p->phys.kernel_variant != 1 && launch_hex8_fast(p, A, grid, MODE_LOSS, s)) {
     FOLGB_LAUNCH_CHECK();
   } else {
     rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
@@ -732,7 +824,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   }
   if (rc) return rc;
   if (dloss_ddofs || dloss_dcontrol) {
-    rc = launch_gather(p, B, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
+    rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
                        elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr);
   }
@@ -771,7 +863,8 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   M.epb = 0;
   M.Ke = w.Ke;
   M.Fe = w.Fe;
-  M.gde = w.gde;
+  M.g = w.g;
+  M.rec = w.rec;
   M.dctrl_elem = elem_ctrl ? dloss_dcontrol : nullptr;
   M.exponent = (float)p->phys.loss_exponent;
   M.inv_batch = 1.f / (float)B;
@@ -796,7 +889,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   });
   if (rc) return rc;
   if (dloss_ddofs || dloss_dcontrol) {
-    rc = launch_gather(p, B, w.g, elem_ctrl ? nullptr : w.gde, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
+    rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
                        elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr);
   }
@@ -812,9 +905,8 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   size_t need = layout_assemble(p, workspace, workspace_bytes, &g, &Ke);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  LossWS w{g, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  LossWS w{g, residual_record(p), nullptr, nullptr, nullptr, nullptr, nullptr};
   VecArgs A = make_vec_args(p, 1, control, 0, dofs, 0, 0, w, nullptr, nullptr, device_status);
-  A.gde = nullptr;
   MatArgs M;
   M.E = p->E;
   M.conn = p->d_conn;
@@ -833,7 +925,8 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   M.epb = 0;
   M.Ke = Ke;
   M.Fe = nullptr;
-  M.gde = nullptr;
+  M.g = nullptr;
+  M.rec = residual_record(p);
   M.dctrl_elem = nullptr;
   M.exponent = 1.f;
   M.inv_batch = 1.f;
@@ -843,7 +936,7 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   int rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
     if (residual) {
-      if (!(p->phys.kernel_variant == 0 && launch_hex8_fast(p, A, grid, MODE_RESIDUAL, s))) {
+      if (!(p->phys.kernel_variant != 1 && launch_hex8_fast(p, A, grid, MODE_RESIDUAL, s))) {
         trace_begin(KID_ELEM_RESIDUAL, s);
         k_elem_vector<ET, PH, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
         trace_end(KID_ELEM_RESIDUAL, s);
@@ -855,7 +948,8 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   });
   if (rc) return rc;
   if (residual) {
-    rc = launch_gather(p, 1, g, nullptr, nullptr, residual, 0, nullptr, 0, nullptr, 0, s, nullptr, nullptr);
+    rc = launch_gather(p, 1, g, residual_record(p), 0, nullptr, residual, 0, nullptr, 0, nullptr, 0, s, nullptr,
+                       nullptr);
     if (rc) return rc;
   }
   if (csr_values || inv_diag) {
@@ -881,4 +975,54 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
     FOLGB_LAUNCH_CHECK();
   }
   return FOLGB_OK;
+}
+
+namespace folgb {
+int hex8_variant_count();
+}
+
+// Times every kernel variant of the plan's loss + adjoint path on the given
+// inputs (2 warm-up and `repeats` timed calls each, CUDA events on the stream)
+// and keeps the fastest in the plan.  Synchronises the stream.
+extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control, int64_t control_stride,
+                              const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                              float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
+                              void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants) {
+  if (!p || !chosen) return FOLGB_ERR_INVALID_ARGUMENT;
+  const bool tunable = p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && p->phys.num_gp == 2 &&
+                       p->phys.kernel_variant == 0;  // a forced variant is not retuned
+  const int nv = tunable ? hex8_variant_count() : 1;
+  if (repeats <= 0) repeats = 5;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t a, b;
+  FOLGB_CUDA_TRY(cudaEventCreate(&a));
+  FOLGB_CUDA_TRY(cudaEventCreate(&b));
+  int best = 0;
+  float best_ms = 0.f;
+  int rc = FOLGB_OK;
+  for (int v = 0; v < nv && rc == FOLGB_OK; ++v) {
+    p->hex8_variant = v;
+    for (int k = 0; k < 2 && rc == FOLGB_OK; ++k)
+      rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
+                              dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
+    cudaEventRecord(a, s);
+    for (int k = 0; k < repeats && rc == FOLGB_OK; ++k)
+      rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
+                              dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
+    cudaEventRecord(b, s);
+    if (cudaEventSynchronize(b) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, a, b);
+    ms /= repeats;
+    if (ms_per_variant && v < max_variants) ms_per_variant[v] = ms;
+    if (v == 0 || ms < best_ms) {
+      best = v;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  p->hex8_variant = best;
+  *chosen = best;
+  return rc;
 }

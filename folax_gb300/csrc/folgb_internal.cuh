@@ -3,8 +3,9 @@
 // Data layout in HBM (built once per mesh by folgb_plan_create):
 //   conn      int32 [E][nen]          element -> node ids (16/32-byte rows)
 //   xyz4      float4[N]               node coordinates padded to 16 bytes
-//   inc_ptr   int32 [N+1]             node -> incident element slots (CSR)
-//   inc_slot  int32 [E*nen]           slot = e*nen + a, ascending e per node
+//   inc_ptr   int32 [N+1]             node -> incident (element, local node) (CSR)
+//   inc_slot  int32 [E*nen]           record index a*E + e, ascending e per node
+//   element results ("records"): [B][nen][E] x 1/2/4 floats, local-node-major
 //   dmask     uint8 [N]               bit c set if dof (node, c) is Dirichlet
 //   dval      float [ndof*N]          Dirichlet value (read only where masked)
 //   gp        GPTable                 Gauss points: w, N, dN/dxi (fp32)
@@ -62,6 +63,9 @@ struct folgb_plan {
   float4* d_xyz4 = nullptr;
   int* d_inc_ptr = nullptr;
   int* d_inc_slot = nullptr;
+  int inc_pad = 0;          // 4 or 8 when every node has at most that many incidences, else 0
+  int* d_inc_padded = nullptr;  // [N][inc_pad] incident slots, -1 padded (vector loads)
+  int hex8_variant = 0;    // sum-factorised hex8 kernel variant (autotuned)
   unsigned char* d_dmask = nullptr;
   float* d_dval = nullptr;
   folgb::GPTable* d_gp = nullptr;
@@ -115,8 +119,16 @@ struct Bump {
 
 int num_sms();
 
+// Element-result records: one per (instance, element, node), [b][a][e],
+// padded to 1, 2 or 4 floats so the gather reads them with one vector load.
+// Components [0, ndof) hold the vector; component ndof the nodal control
+// sensitivity when the loss path has one.
+inline int padded_record(int n) { return n <= 1 ? 1 : (n <= 2 ? 2 : 4); }
+inline int loss_record(const folgb_plan* p);
+inline int residual_record(const folgb_plan* p);
+
 // deterministic node gather of element vectors (elements.cu)
-int launch_gather(const folgb_plan* p, int B, const float* g, const float* gde, const float* scale, float* out,
+int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
                   cudaStream_t s, const int* node_inst, const int* elem_inst);
 
@@ -379,4 +391,9 @@ enum KernelId {
 };
 void trace_begin(int kid, cudaStream_t s);
 void trace_end(int kid, cudaStream_t s);
+
+inline int loss_record(const folgb_plan* p) {
+  return padded_record(p->ndof + (p->ctrl_layout == FOLGB_CONTROL_NODAL ? 1 : 0));
+}
+inline int residual_record(const folgb_plan* p) { return padded_record(p->ndof); }
 }  // namespace folgb

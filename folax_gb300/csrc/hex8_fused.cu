@@ -102,8 +102,13 @@ __device__ __forceinline__ void butterfly4_t(const float (&v)[4], float& A, floa
   D += qp - qm;
 }
 
-template <int CL, int MODE>
-__global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
+// Kernel variants (chosen per plan by the autotuner in launch_hex8_fast):
+//   ACC 0: keep the 36 per-direction point sums, adjoint butterflies at the end;
+//   ACC 1: accumulate the dual Hadamard coefficients point by point
+//          (21 accumulators instead of 36: fewer registers, ~14% more adds);
+//   BLOCK: threads per block (sets the register cap through __launch_bounds__).
+template <int CL, int MODE, bool BF, int ACC, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_hex8_elastic(const VecArgs A) {
   __shared__ float red[32];
   const int b = blockIdx.y;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -115,7 +120,8 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
     load_nodes<8>(A.conn, e, nodes);
     const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
     const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
-    float X[3][8], U[3][8], de[8];
+    float X[3][8], U[3][8];
+    float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
 #pragma unroll
     for (int L = 0; L < 8; ++L) {
       const int n = nodes[LEX[L]];
@@ -129,17 +135,15 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
         const int64_t d = 3 * (int64_t)n + c;
         U[c][L] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
       }
-      if (CL == FOLGB_CONTROL_NODAL) de[L] = __ldg(ctrl + n);
+      if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = __ldg(ctrl + n);
     }
-    float egp[8];
-    if (CL == FOLGB_CONTROL_NODAL) {
+    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
+    else egp[0] = __ldg(ctrl + e);
+    float bfe = 0.f;  // u . b at the nodes, weighted below (body force only)
+    float ub[BF ? 8 : 1];
+    if constexpr (BF) {
 #pragma unroll
-      for (int L = 0; L < 8; ++L) egp[L] = de[L];
-      interp8(egp);
-    } else {
-      const float ev = __ldg(ctrl + e);
-#pragma unroll
-      for (int q = 0; q < 8; ++q) egp[q] = ev;
+      for (int L = 0; L < 8; ++L) ub[L] = U[0][L] * A.mat.bf[0] + U[1][L] * A.mat.bf[1] + U[2][L] * A.mat.bf[2];
     }
     // reference derivatives of the geometry and of the displacement
     Deriv12 DX[3], DU[3];
@@ -150,15 +154,23 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
       wht8(U[i]);
       deriv12(U[i], DU[i]);
     }
-    // per-direction adjoint accumulators S[i][dir][4]
-    float S[3][3][4];
+    float S[ACC == 0 ? 3 : 1][3][4];   // ACC 0: per-direction point sums
+    float Dd[ACC == 1 ? 3 : 1][8];     // ACC 1: dual Hadamard coefficients (raw)
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
+    for (int i = 0; i < 3; ++i) {
+      if (ACC == 0) {
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+        for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int t = 0; t < 4; ++t) S[i][k][t] = 0.f;
-    float wsed[8], wdet[8];
+          for (int t = 0; t < 4; ++t) S[i][k][t] = 0.f;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) Dd[i][k] = 0.f;
+      }
+    }
+    float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+    float wdet[BF ? 8 : 1];
+    float sedsum = 0.f;
     const MatConst& mt = A.mat;
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
@@ -178,7 +190,7 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
       const float det = det_inv<3>(J, Ji);
       bad |= !(det > 0.f);
       const float wd = det;  // Gauss weight 1
-      wdet[q] = wd;
+      if constexpr (BF) wdet[q] = wd;
       float H[3][3];
 #pragma unroll
       for (int i = 0; i < 3; ++i)
@@ -188,9 +200,11 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
       const float g01 = H[0][1] + H[1][0], g12 = H[1][2] + H[2][1], g02 = H[0][2] + H[2][0];
       const float sed = mt.lam * tr * tr + 2.f * mt.mu * (H[0][0] * H[0][0] + H[1][1] * H[1][1] + H[2][2] * H[2][2]) +
                         mt.mu * (g01 * g01 + g12 * g12 + g02 * g02);
-      const float ew = egp[q] * wd;
+      const float eq = (CL == FOLGB_CONTROL_NODAL) ? egp[q] : egp[0];
+      const float ew = eq * wd;
       energy = fmaf(ew, sed, energy);
-      wsed[q] = wd * sed;
+      if constexpr (CL == FOLGB_CONTROL_NODAL) wsed[q] = wd * sed;
+      else sedsum = fmaf(wd, sed, sedsum);
       // w detJ sigma
       const float lt = ew * mt.lam * tr, tm = 2.f * ew * mt.mu, sm = ew * mt.mu;
       float sg[3][3];
@@ -200,15 +214,31 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
       sg[0][1] = sg[1][0] = sm * g01;
       sg[1][2] = sg[2][1] = sm * g12;
       sg[0][2] = sg[2][0] = sm * g02;
-      // T[i][k] = sum_j sg[i][j] Ji[k][j]; scatter into the direction sums
+      const float sx = tx ? 1.f : -1.f, sy = ty ? 1.f : -1.f, sz = tz ? 1.f : -1.f;
 #pragma unroll
       for (int i = 0; i < 3; ++i) {
         const float t0 = sg[i][0] * Ji[0][0] + sg[i][1] * Ji[0][1] + sg[i][2] * Ji[0][2];
         const float t1 = sg[i][0] * Ji[1][0] + sg[i][1] * Ji[1][1] + sg[i][2] * Ji[1][2];
         const float t2 = sg[i][0] * Ji[2][0] + sg[i][1] * Ji[2][1] + sg[i][2] * Ji[2][2];
-        S[i][0][ix] += t0;
-        S[i][1][iy] += t1;
-        S[i][2][iz] += t2;
+        if (ACC == 0) {
+          S[i][0][ix] += t0;
+          S[i][1][iy] += t1;
+          S[i][2][iz] += t2;
+        } else {
+          // lex b: 1 xi, 2 eta, 3 xi eta, 4 zeta, 5 xi zeta, 6 eta zeta, 7 xi eta zeta
+          Dd[i][1] += t0;
+          Dd[i][3] = fmaf(sy, t0, Dd[i][3]);
+          Dd[i][5] = fmaf(sz, t0, Dd[i][5]);
+          Dd[i][7] = fmaf(sy * sz, t0, Dd[i][7]);
+          Dd[i][2] += t1;
+          Dd[i][3] = fmaf(sx, t1, Dd[i][3]);
+          Dd[i][6] = fmaf(sz, t1, Dd[i][6]);
+          Dd[i][7] = fmaf(sx * sz, t1, Dd[i][7]);
+          Dd[i][4] += t2;
+          Dd[i][5] = fmaf(sx, t2, Dd[i][5]);
+          Dd[i][6] = fmaf(sy, t2, Dd[i][6]);
+          Dd[i][7] = fmaf(sx * sy, t2, Dd[i][7]);
+        }
       }
     }
     // adjoint: per component, dual Hadamard coefficients then the transposed transform
@@ -217,75 +247,68 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       float d[8];
+      if (ACC == 0) {
 #pragma unroll
-      for (int k = 0; k < 8; ++k) d[k] = 0.f;
-      float A1 = 0.f, B1 = 0.f, C1 = 0.f, D1 = 0.f;
-      butterfly4_t(S[i][0], A1, B1, C1, D1);  // xi: (1, xi eta, xi zeta, xi eta zeta)
-      d[1] += s * A1;
-      d[3] += sg_ * B1;
-      d[5] += sg_ * C1;
-      d[7] += sg2 * D1;
-      float A2 = 0.f, B2 = 0.f, C2 = 0.f, D2 = 0.f;
-      butterfly4_t(S[i][1], A2, B2, C2, D2);  // eta: (eta, xi eta, eta zeta, xi eta zeta)
-      d[2] += s * A2;
-      d[3] += sg_ * B2;
-      d[6] += sg_ * C2;
-      d[7] += sg2 * D2;
-      float A3 = 0.f, B3 = 0.f, C3 = 0.f, D3 = 0.f;
-      butterfly4_t(S[i][2], A3, B3, C3, D3);  // zeta: (zeta, xi zeta, eta zeta, xi eta zeta)
-      d[4] += s * A3;
-      d[5] += sg_ * B3;
-      d[6] += sg_ * C3;
-      d[7] += sg2 * D3;
+        for (int k = 0; k < 8; ++k) d[k] = 0.f;
+        float A1 = 0.f, B1 = 0.f, C1 = 0.f, D1 = 0.f;
+        butterfly4_t(S[i][0], A1, B1, C1, D1);  // xi: (1, xi eta, xi zeta, xi eta zeta)
+        d[1] += A1;
+        d[3] += B1;
+        d[5] += C1;
+        d[7] += D1;
+        float A2 = 0.f, B2 = 0.f, C2 = 0.f, D2 = 0.f;
+        butterfly4_t(S[i][1], A2, B2, C2, D2);  // eta: (eta, xi eta, eta zeta, xi eta zeta)
+        d[2] += A2;
+        d[3] += B2;
+        d[6] += C2;
+        d[7] += D2;
+        float A3 = 0.f, B3 = 0.f, C3 = 0.f, D3 = 0.f;
+        butterfly4_t(S[i][2], A3, B3, C3, D3);  // zeta: (zeta, xi zeta, eta zeta, xi eta zeta)
+        d[4] += A3;
+        d[5] += B3;
+        d[6] += C3;
+        d[7] += D3;
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) d[k] = Dd[i][k];
+      }
+      d[0] = 0.f;
+      d[1] *= s;
+      d[2] *= s;
+      d[4] *= s;
+      d[3] *= sg_;
+      d[5] *= sg_;
+      d[6] *= sg_;
+      d[7] *= sg2;
       wht8_t(d);
 #pragma unroll
       for (int L = 0; L < 8; ++L) g[L][i] = d[L];
     }
-    if (mt.has_bf) {
-      float W[8];
+    if constexpr (BF) {
+      interp8(wdet);  // nodal weights sum_q w detJ N_a(q)
 #pragma unroll
-      for (int q = 0; q < 8; ++q) W[q] = wdet[q];
-      interp8(W);
+      for (int L = 0; L < 8; ++L) {
 #pragma unroll
-      for (int L = 0; L < 8; ++L)
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float f = W[L] * mt.bf[i];
-          g[L][i] -= f;
-          // u was transformed in place: recompute the nodal value from the dofs
-          const int n = nodes[LEX[L]];
-          const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
-          const int64_t dd = 3 * (int64_t)n + i;
-          const float uv = ((m >> i) & 1u) ? __ldg(A.dval + dd) : __ldg(dofs + dd);
-          energy = fmaf(-f, uv, energy);
-        }
+        for (int i = 0; i < 3; ++i) g[L][i] = fmaf(-wdet[L], mt.bf[i], g[L][i]);
+        bfe = fmaf(wdet[L], ub[L], bfe);
+      }
+      energy -= bfe;
     }
     if (!isfinite(energy)) bad |= 2;
-    // element vector in node order, 16-byte stores
-    float out[24];
+    // 16-byte records, local-node-major ([b][a][e]): the 3 vector components
+    // and the nodal control sensitivity (or padding); for each local node the
+    // warp's stores are contiguous
+    constexpr bool nodal_gde = (MODE == MODE_LOSS) && (CL == FOLGB_CONTROL_NODAL);
+    if constexpr (nodal_gde) interp8(wsed);
+    float4* out = reinterpret_cast<float4*>(A.g);
 #pragma unroll
-    for (int L = 0; L < 8; ++L)
-#pragma unroll
-      for (int i = 0; i < 3; ++i) out[3 * LEX[L] + i] = g[L][i];
-    float4* gout = reinterpret_cast<float4*>(A.g + ((int64_t)b * A.E + e) * 24);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) gout[k] = make_float4(out[4 * k], out[4 * k + 1], out[4 * k + 2], out[4 * k + 3]);
-    if (MODE == MODE_LOSS) {
-      if (CL == FOLGB_CONTROL_NODAL) {
-        interp8(wsed);
-        float gn[8];
-#pragma unroll
-        for (int L = 0; L < 8; ++L) gn[LEX[L]] = wsed[L];
-        float4* go = reinterpret_cast<float4*>(A.gde + ((int64_t)b * A.E + e) * 8);
-        go[0] = make_float4(gn[0], gn[1], gn[2], gn[3]);
-        go[1] = make_float4(gn[4], gn[5], gn[6], gn[7]);
-      } else if (A.dctrl_elem) {
-        float sum = 0.f;
-#pragma unroll
-        for (int q = 0; q < 8; ++q) sum += wsed[q];
-        A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sum * A.inv_batch : sum;
-      }
+    for (int L = 0; L < 8; ++L) {
+      float w = 0.f;
+      if constexpr (nodal_gde) w = wsed[L];
+      out[((int64_t)b * 8 + LEX[L]) * A.E + e] = make_float4(g[L][0], g[L][1], g[L][2], w);
     }
+    if (MODE == MODE_LOSS && CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
+      A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
   }
   report_bad(bad, A.status);
   if (MODE == MODE_LOSS) {
@@ -294,20 +317,48 @@ __global__ void __launch_bounds__(256) k_hex8_elastic(const VecArgs A) {
   }
 }
 
+template <int CL, int MODE, int ACC, int BLOCK>
+static void launch_variant(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
+  dim3 g2((unsigned)((A.E + BLOCK - 1) / BLOCK), grid.y);
+  if (bf) k_hex8_elastic<CL, MODE, true, ACC, BLOCK><<<g2, BLOCK, 0, s>>>(A);
+  else k_hex8_elastic<CL, MODE, false, ACC, BLOCK><<<g2, BLOCK, 0, s>>>(A);
+}
+
+template <int CL, int MODE>
+static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cudaStream_t s) {
+  switch (variant) {
+    case 0: launch_variant<CL, MODE, 0, 256>(A, grid, bf, s); break;
+    case 1: launch_variant<CL, MODE, 0, 128>(A, grid, bf, s); break;
+    case 2: launch_variant<CL, MODE, 1, 256>(A, grid, bf, s); break;
+    case 3: launch_variant<CL, MODE, 1, 128>(A, grid, bf, s); break;
+    case 4: launch_variant<CL, MODE, 0, 64>(A, grid, bf, s); break;
+    default: launch_variant<CL, MODE, 1, 64>(A, grid, bf, s); break;
+  }
+}
+
+// Number of sum-factorised variants the autotuner may choose from.
+constexpr int kHex8Variants = 6;
+
 // Launches the sum-factorised kernel when it applies (hex8, linear
-// elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.
+// elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's
+// block count is recomputed for the variant's block size; the caller's
+// partial-sum buffers are sized for the smallest block (128 threads).
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2) return 0;
+  const int variant = p->hex8_variant;
+  const bool bf = p->mat.has_bf != 0;
   trace_begin(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
   if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
-    if (mode == MODE_LOSS) k_hex8_elastic<FOLGB_CONTROL_NODAL, MODE_LOSS><<<grid, 256, 0, s>>>(A);
-    else k_hex8_elastic<FOLGB_CONTROL_NODAL, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
+    if (mode == MODE_LOSS) launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_LOSS>(A, grid, bf, variant, s);
+    else launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_RESIDUAL>(A, grid, bf, variant, s);
   } else {
-    if (mode == MODE_LOSS) k_hex8_elastic<FOLGB_CONTROL_ELEMENT, MODE_LOSS><<<grid, 256, 0, s>>>(A);
-    else k_hex8_elastic<FOLGB_CONTROL_ELEMENT, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
+    if (mode == MODE_LOSS) launch_cl_mode<FOLGB_CONTROL_ELEMENT, MODE_LOSS>(A, grid, bf, variant, s);
+    else launch_cl_mode<FOLGB_CONTROL_ELEMENT, MODE_RESIDUAL>(A, grid, bf, variant, s);
   }
   trace_end(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
   return 1;
 }
+
+int hex8_variant_count() { return kHex8Variants; }
 
 }  // namespace folgb

@@ -9,7 +9,7 @@
 // workspace; folgb_loss_adjoint_noalloc instead uses a fixed scratch array
 // that is part of this library's device image:
 //
-//   * kNoAllocScratchBytes (32 MiB) of device memory, held by every GPU that
+//   * kNoAllocScratchBytes (48 MiB) of device memory, held by every GPU that
 //     loads the library until the process exits;
 //   * enough for the hex8 elasticity loss on a 64^3 mesh (batch 1); larger
 //     problems are rejected with FOLGB_ERR_TOO_LARGE before any work;
@@ -28,7 +28,7 @@
 
 namespace {
 
-constexpr size_t kNoAllocScratchBytes = size_t(32) << 20;
+constexpr size_t kNoAllocScratchBytes = size_t(48) << 20;
 constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];

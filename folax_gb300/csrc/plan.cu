@@ -301,6 +301,8 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
   p->E = num_elements;
   p->N = num_nodes;
   p->ctrl_layout = phys->control_layout;
+  // kernel_variant >= 2 pins sum-factorised variant (kernel_variant - 2)
+  p->hex8_variant = phys->kernel_variant >= 2 ? phys->kernel_variant - 2 : 0;
   if ((rc = fill_material(*phys, dim, p->mat)) || !build_gp_table(p->etype, phys->num_gp, p->h_gp)) {
     delete p;
     return rc ? rc : FOLGB_ERR_INVALID_ARGUMENT;
@@ -310,6 +312,23 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     x4[n] = make_float4((float)xyz[3 * n], (float)xyz[3 * n + 1], (float)xyz[3 * n + 2], 0.f);
   std::vector<int> inc_ptr, inc_slot;
   build_incidence(c32, num_elements, nen, num_nodes, inc_ptr, inc_slot);
+  // the device lists hold record indices a*E + e: element results are stored
+  // local-node-major, so a warp of consecutive nodes reads consecutive records
+  std::vector<int> inc_rec(inc_slot.size());
+  for (size_t k = 0; k < inc_slot.size(); ++k)
+    inc_rec[k] = (int)((inc_slot[k] % nen) * num_elements + inc_slot[k] / nen);
+  // padded copy of the incidence lists for vector loads when every node has
+  // at most 4 or 8 incident element slots (structured quad / hex meshes)
+  int maxinc = 0;
+  for (int64_t n = 0; n < num_nodes; ++n) maxinc = std::max(maxinc, inc_ptr[n + 1] - inc_ptr[n]);
+  const int pad = maxinc <= 4 ? 4 : (maxinc <= 8 ? 8 : 0);
+  p->inc_pad = pad;
+  std::vector<int> inc_padded;
+  if (pad) {
+    inc_padded.assign((size_t)num_nodes * pad, -1);
+    for (int64_t n = 0; n < num_nodes; ++n)
+      for (int k = inc_ptr[n]; k < inc_ptr[n + 1]; ++k) inc_padded[(size_t)n * pad + (k - inc_ptr[n])] = inc_rec[k];
+  }
   std::vector<unsigned char> dmask(num_nodes, 0);
   std::vector<float> dval(ndofs, 0.f);
   p->dir_dofs.assign(dirichlet_dofs, dirichlet_dofs + num_dirichlet);
@@ -321,7 +340,8 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
   }
   if ((rc = upload(&p->d_conn, c32.data(), c32.size())) || (rc = upload(&p->d_xyz4, x4.data(), x4.size())) ||
       (rc = upload(&p->d_inc_ptr, inc_ptr.data(), inc_ptr.size())) ||
-      (rc = upload(&p->d_inc_slot, inc_slot.data(), inc_slot.size())) ||
+      (rc = upload(&p->d_inc_slot, inc_rec.data(), inc_rec.size())) ||
+      (pad && (rc = upload(&p->d_inc_padded, inc_padded.data(), inc_padded.size()))) ||
       (rc = upload(&p->d_dmask, dmask.data(), dmask.size())) || (rc = upload(&p->d_dval, dval.data(), dval.size())) ||
       (rc = upload(&p->d_gp, &p->h_gp, 1))) {
     folgb_plan_destroy(p);
@@ -337,7 +357,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
 
 extern "C" int folgb_plan_destroy(folgb_plan* p) {
   if (!p) return FOLGB_OK;
-  void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_dmask, p->d_dval, p->d_gp,
+  void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_inc_padded, p->d_dmask, p->d_dval, p->d_gp,
                   p->d_adj_ptr, p->d_adj, p->d_rowptr, p->d_colind, p->d_pair_row, p->d_pair_ptr,
                   p->d_pair_slot};
   for (void* q : ptrs)

@@ -28,6 +28,10 @@ from . import _capi as capi
 from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
+# sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
+HEX8_VARIANTS = 6
+HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
+                      "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 
@@ -181,7 +185,8 @@ class FiniteElementLoss:
         p.num_gp = int(self.num_gp)
         p.control_layout = capi.CONTROL_ELEMENT if s.get("control_layout", "nodal") == "element" else capi.CONTROL_NODAL
         p.shear_mode = capi.SHEAR_CONSISTENT if s.get("voigt_shear_mode", "reference") == "consistent" else capi.SHEAR_REFERENCE
-        p.kernel_variant = 1 if s.get("kernel_variant", "auto") == "generic" else 0
+        kv = s.get("kernel_variant", "auto")
+        p.kernel_variant = 1 if kv == "generic" else (2 + int(kv) if isinstance(kv, int) else 0)
         p.young_modulus = float(mat.get("young_modulus", 1.0))
         p.poisson_ratio = float(mat.get("poisson_ratio", 0.3))
         bf = np.zeros(3)
@@ -314,6 +319,26 @@ class FiniteElementLoss:
         capi.check("folgb_loss_adjoint_plain" if plain else "folgb_loss_adjoint", rc)
         mean = losses.mean()
         return mean, (losses.min(), losses.max(), mean), losses, du, dp
+
+    def Autotune(self, batch_params, batch_dofs, repeats: int = 5):
+        """Time the plan's kernel variants on these inputs and keep the fastest
+        (folgb_autotune).  Returns {"chosen": v, "ms": [per-variant times]}."""
+        torch = _torch()
+        P, U, B = self._batched(batch_params, batch_dofs)
+        losses = torch.empty(B, dtype=torch.float32, device="cuda")
+        du = torch.empty_like(U)
+        dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda")
+        ws = self._plan.workspace(capi.OP_LOSS_ADJOINT, B)
+        chosen = C.c_int32()
+        times = (C.c_float * 8)()
+        rc = self._plan.lib.folgb_autotune(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1],
+                                           capi.ptr(U), U.shape[1], capi.ptr(losses), capi.ptr(du), capi.ptr(dp),
+                                           capi.ptr(ws), ws.numel(), repeats, capi.stream_handle(), C.byref(chosen),
+                                           C.cast(times, C.c_void_p), 8)
+        capi.check("folgb_autotune", rc)
+        n = HEX8_VARIANTS if (self.element_type == "hexahedron" and self.physics == capi.ELASTIC
+                              and self.num_gp == 2) else 1
+        return {"chosen": chosen.value, "ms": [times[i] for i in range(n)]}
 
     def ComputeBatchLoss(self, batch_params, batch_dofs):
         mean, stats, _, _, _ = self.ComputeBatchLossAndGrad(batch_params, batch_dofs, grads=False)

@@ -63,7 +63,9 @@ typedef struct folgb_physics {
   int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
   int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */
   int32_t kernel_variant; /* 0: fastest kernel for the element (sum-factorised
-                             hex8 2x2x2 elasticity); 1: the generic Gauss loop */
+                             hex8 2x2x2 elasticity, variant set by
+                             folgb_autotune); 1: the generic Gauss loop;
+                             2 + v: sum-factorised variant v (0..5) */
   double young_modulus;   /* material_dict young_modulus (elastic D scale)     */
   double poisson_ratio;   /* material_dict poisson_ratio                       */
   double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */
@@ -141,7 +143,7 @@ int folgb_loss_adjoint_plain(const folgb_plan* plan, int32_t batch,
  * fixed memory budget, code running inside an allocator hook).  No
  * counterpart in the reference.  Same arguments and results as
  * folgb_loss_adjoint minus the workspace: the scratch is a fixed array inside
- * the library's device image, 32 MiB on every GPU that loads the library,
+ * the library's device image, 48 MiB on every GPU that loads the library,
  * held until exit (enough for 64^3 hex8 elasticity, batch 1: the size
  * folgb_workspace_bytes(plan, FOLGB_OP_LOSS_ADJOINT, batch) reports must fit).
  * Larger problems return FOLGB_ERR_TOO_LARGE.  The array is shared
@@ -154,6 +156,18 @@ int folgb_loss_adjoint_noalloc(const folgb_plan* plan, int32_t batch,
                                const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
                                float* losses, float* dloss_ddofs, float* dloss_dcontrol,
                                int32_t* device_status, void* stream);
+
+/* Autotuner (no counterpart in the reference): times every kernel variant of
+ * the plan's fused loss + adjoint on the caller's inputs (elements per block
+ * and accumulation scheme of the sum-factorised hex8 kernel; plans with one
+ * variant are a no-op) and keeps the fastest in the plan.  Arguments as
+ * folgb_loss_adjoint with apply_dirichlet = 1; repeats timed calls per variant
+ * (<= 0: 5).  *chosen gets the variant index, ms_per_variant[v] (may be NULL)
+ * the mean time of variant v.  Synchronises the stream. */
+int folgb_autotune(folgb_plan* plan, int32_t batch, const float* control, int64_t control_stride,
+                   const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                   float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
+                   void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants);
 
 /* Copies the plan's CSR pattern (canonical: sorted column indices, one entry
  * per connected dof pair, the pattern scipy.sparse.csr_array builds from the

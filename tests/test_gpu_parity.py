@@ -93,6 +93,38 @@ def test_hex8_sum_factorised_matches_generic_and_oracle(cuda, layout, bf):
     assert rel_fro(Rf.cpu().numpy(), Ro) < TOL
 
 
+@pytest.mark.parametrize("variant", [0, 1, 2, 3, 4, 5])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_hex8_every_variant_matches_oracle(cuda, variant, layout):
+    """Each autotuner candidate (block size x accumulation scheme) is exact."""
+    m = make_mesh("hex8", 4, seed=23, jitter=0.15)
+    s = _settings("hex8", "elastic", layout, 1.0, [0.2, 0.0, -0.1])
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(24)
+    ctrl = 0.5 + rng.random((3, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((3, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+
+
+def test_autotune_keeps_results_exact(cuda):
+    m = make_mesh("hex8", 6, seed=25)
+    s = _settings("hex8", "elastic", "element")
+    gl, ol = gpu_loss("hex8", "elastic", m, s), oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(26)
+    ctrl = 0.5 + rng.random((1, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
+    info = gl.Autotune(ctrl, u, repeats=2)
+    assert 0 <= info["chosen"] < 6 and len(info["ms"]) == 6 and min(info["ms"]) > 0
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+
+
 @pytest.mark.parametrize("exponent,bf", [(1.5, None), (1.0, [0.3, -0.2, 0.1]), (2.0, [0.1, 0.2, 0.3])])
 def test_loss_exponent_body_force_broadcast(cuda, exponent, bf):
     m = make_mesh("hex8", 3, seed=3)

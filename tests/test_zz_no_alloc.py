@@ -74,7 +74,7 @@ def test_noalloc_rejects_problems_larger_than_its_scratch(cuda):
     torch = cuda
     lib = _capi.load()
     loss = _case("hex8", "elastic", 16, "element", seed=34)
-    B = 400  # 400 x 4096 elements x 24 floats: far above 32 MiB
+    B = 400  # 400 x 4096 elements x 32 floats: far above 48 MiB
     ctrl = np.ones((1, loss.GetNumberOfControls()))
     u = np.zeros((B, loss.GetTotalNumberOfDOFs()))
     rc, *_ = _call(torch, lib, loss, ctrl, u, noalloc=True)
