@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--plain-steps", type=int, default=5)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
+    ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     return ap.parse_args()
 
 
@@ -166,6 +167,180 @@ def cpu_baseline_port(n_sample=12, seed=7):
                       f"{reps} repetitions, {dt * 1e3:.1f} ms each"}
 
 
+def _events_ms(torch, fn, steps, flush=None):
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for a, b in ev:
+        if flush is not None:
+            flush.zero_()
+        a.record()
+        fn()
+        b.record()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / steps
+
+
+def extra_pcg(args, loss, ctrl):
+    """C1: CSR stiffness assembly + Jacobi-PCG (rtol 1e-8, fp64 dots) on the
+    64^3 hex8 workload; time per iteration and SpMV bandwidth."""
+    import ctypes as C
+    import torch
+    from folax_gb300 import _capi
+    from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
+    lib = _capi.load()
+    u0 = loss.ApplyDirichletBCOnDofVector(torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda"))
+    c = ctrl[0]
+    loss.ComputeJacobianMatrixAndResidualVector(c, u0)          # builds the CSR tables once
+    torch.cuda.synchronize()
+    ms_asm = _events_ms(torch, lambda: loss.ComputeJacobianMatrixAndResidualVector(c, u0), 3)
+    jac, r = loss.ComputeJacobianMatrixAndResidualVector(c, u0)
+    solver = FiniteElementLinearResidualBasedSolver("pcg", loss, {"linear_solver_settings": {
+        "solver": "GB300-pcg", "tol": 1e-8, "maxiter": 20000, "check_every": 64}})
+    solver.Initialize()
+    lib.folgb_trace_enable(1)
+    lib.folgb_trace_reset()
+    t0 = time.perf_counter()
+    dx = solver.LinearSolve(jac, r)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    n_s, t_s, n_u, t_u = C.c_int64(), C.c_double(), C.c_int64(), C.c_double()
+    lib.folgb_trace_read(_capi.KERNEL_IDS["pcg_spmv"], C.byref(n_s), C.byref(t_s))
+    lib.folgb_trace_read(_capi.KERNEL_IDS["pcg_update"], C.byref(n_u), C.byref(t_u))
+    lib.folgb_trace_enable(0)
+    info = solver.last_linear_info
+    it = max(1, info["iterations"])
+    # true residual of the returned solution, fp64 on the host
+    A = jac.to_scipy()
+    res = np.linalg.norm(A @ dx.double().cpu().numpy() + r.double().cpu().numpy()) / np.linalg.norm(
+        r.double().cpu().numpy())
+    plan = jac.plan
+    N = plan.num_nodes
+    nnz = plan.nnz
+    pairs = nnz // 9
+    spmv_bytes = 4 * nnz + 4 * pairs + 4 * (N + 1) + 4 * 3 * N + 8 * 3 * N
+    spmv_ms = t_s.value / max(1, n_s.value)
+    peaks = measured_peaks() or {}
+    return {"dofs": plan.total_dofs, "nnz": nnz, "assembly_ms": ms_asm, "iterations": info["iterations"],
+            "status": info["status"], "solve_ms": wall * 1e3, "ms_per_iteration": wall * 1e3 / it,
+            "kernel_ms_per_iteration": (t_s.value + t_u.value) / it, "spmv_ms": spmv_ms,
+            "spmv_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
+            "spmv_hbm_frac": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+            "true_relative_residual": float(res),
+            "note": "Jacobi-PCG, fp32 matrix/vectors, fp64 dots, norms and iterate, reliable updates; "
+                    "wall time includes one host flag read per 64 iterations"}
+
+
+def extra_batched(args, n_inst=512, seed=11):
+    """C3: 512 quad4 thermal instances, side n ~ U{16..128}, own Fourier
+    conductivity each: fused loss + adjoint + Adam on the nodal field as one
+    CUDA graph, against the same step as per-instance launches."""
+    import torch
+    from folax_gb300 import fields
+    from folax_gb300.batched import AdamState, BatchedFELoss, capture_step
+    from folax_gb300.loss import ThermalLoss2DQuad
+    from folax_gb300.mesh import create_2D_square_mesh
+    rng = np.random.default_rng(seed)
+    sizes = rng.integers(16, 129, n_inst)
+    meshes = [create_2D_square_mesh(1.0, int(n) + 1) for n in sizes]
+    settings = {"dirichlet_bc_dict": {"T": {"left": 1.0, "right": 0.0}}, "control_layout": "element", "num_gp": 2}
+    t0 = time.perf_counter()
+    bl = BatchedFELoss("quad", "thermal", meshes, settings, elements_per_tile=1024)
+    t_plan = time.perf_counter() - t0
+    ctrl = torch.tensor(np.concatenate([fields.fourier_conductivity(
+        fields.element_centroids(m.nodes_coordinates, m.elements_nodes["quad"]), seed + i)
+        for i, m in enumerate(meshes)]), dtype=torch.float32, device="cuda")
+    T = torch.rand(bl.total_dofs, device="cuda", generator=torch.Generator(device="cuda").manual_seed(seed))
+    out = (torch.empty(n_inst, device="cuda"), torch.empty_like(T), torch.empty_like(ctrl))
+    adam = AdamState(T, lr=1e-3)
+
+    def step():
+        bl.ComputeLossAndGrad(ctrl, T, out=out)
+        adam.update(T, out[1])
+
+    g, _ = capture_step(step, warmup=3)
+    steps = 20
+    ms_graph = _events_ms(torch, g.replay, steps)
+    # per-instance launches: the same work, one loss object and launch set per instance
+    per = []
+    offs_c, offs_d = bl.control_offsets, bl.dof_offsets
+    for i, m in enumerate(meshes):
+        L = ThermalLoss2DQuad("i", dict(settings), m)
+        L.Initialize()
+        ci = ctrl[offs_c[i]:offs_c[i + 1]][None]
+        Ti = T[offs_d[i]:offs_d[i + 1]].clone()[None]
+        per.append((L, ci, Ti, AdamState(Ti[0], lr=1e-3)))
+
+    def per_step():
+        for L, ci, Ti, st in per:
+            _, _, _, du, _ = L.ComputeBatchLossAndGrad(ci, Ti)
+            st.update(Ti[0], du[0])
+
+    per_step()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    per_steps = 3
+    for _ in range(per_steps):
+        per_step()
+    torch.cuda.synchronize()
+    ms_per = (time.perf_counter() - t0) * 1e3 / per_steps
+    E = bl.num_elements
+    return {"instances": n_inst, "elements": E, "nodes": bl.num_nodes, "plan_s": t_plan,
+            "graph_ms_per_step": ms_graph, "graph_melem_s": E / (ms_graph * 1e-3) / 1e6,
+            "per_instance_ms_per_step": ms_per, "per_instance_melem_s": E / (ms_per * 1e-3) / 1e6,
+            "speedup_batched_vs_per_instance": ms_per / ms_graph,
+            "step": "fused loss + adjoint (one persistent launch + gather) + Adam on the nodal field, one CUDA graph",
+            "per_instance_step": "the same, one eager launch set per instance (wall clock)"}
+
+
+def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=24):
+    """C4: tet4 Neo-Hookean (6-tet split of a 64^3 hex grid, 1 Gauss point),
+    mu/lambda scaled by the two-phase field, batch 16: fused loss + adjoint
+    throughput; and the time of one Newton iteration (CSR tangent + BiCGSTAB)
+    on a 24^3 split."""
+    import torch
+    from folax_gb300 import fields
+    from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
+    from folax_gb300.mesh import create_3D_box_mesh, split_hex_to_tets
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    bc = {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.05}}
+    mesh = split_hex_to_tets(create_3D_box_mesh(n, n, n))
+    Ev = fields.two_phase_voxels(n, seed)
+    E_t = np.repeat(Ev, 6).astype(np.float32)
+    settings = {"dirichlet_bc_dict": bc, "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
+                "control_layout": "element"}
+    loss = NeoHookeMechanicalLoss3DTetra("nh", settings, mesh)
+    loss.Initialize()
+    rng = np.random.default_rng(seed)
+    u = np.zeros((batch, mesh.GetNumberOfNodes(), 3), dtype=np.float32)
+    u[:, :, 2] = 0.05 * mesh.nodes_coordinates[None, :, 2]
+    u += (0.002 * rng.standard_normal(u.shape)).astype(np.float32)
+    U = torch.tensor(u.reshape(batch, -1), device="cuda")
+    Cb = torch.tensor(np.repeat(E_t[None], batch, 0), device="cuda")
+    for _ in range(3):
+        loss.ComputeBatchLossAndGrad(Cb, U)
+    torch.cuda.synchronize()
+    ms = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
+    E = len(mesh.elements_nodes["tetra"])
+    # one Newton iteration on a smaller split: assembly + BiCGSTAB (rtol 1e-6)
+    m2 = split_hex_to_tets(create_3D_box_mesh(newton_n, newton_n, newton_n))
+    E2 = np.repeat(fields.two_phase_voxels(newton_n, seed), 6).astype(np.float32)
+    l2 = NeoHookeMechanicalLoss3DTetra("nh2", dict(settings), m2)
+    l2.Initialize()
+    solver = FiniteElementNonLinearResidualBasedSolver("nl", l2, {
+        "linear_solver_settings": {"solver": "JAX-bicgstab", "tol": 1e-6, "maxiter": 20000, "check_every": 64},
+        "nonlinear_solver_settings": {"load_incr": 1, "maxiter": 1}})
+    solver.Initialize()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    solver.Solve(E2, np.zeros(l2.GetTotalNumberOfDOFs(), dtype=np.float32))
+    torch.cuda.synchronize()
+    t_newton = time.perf_counter() - t0
+    h = solver.history[-1] if solver.history else {}
+    return {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6,
+            "newton": {"mesh": f"{newton_n}^3 hex split into {len(m2.elements_nodes['tetra'])} tets",
+                       "dofs": l2.GetTotalNumberOfDOFs(), "ms_per_newton_iteration": t_newton * 1e3,
+                       "linear": h.get("linear"), "residual_norm": h.get("res_norm")}}
+
+
 def _oracle_chunk(args):
     """Worker of the reference arm: loss + element gradients for a slab of elements."""
     xyz, conn, ctrl, u = args
@@ -272,6 +447,10 @@ def main():
     for _ in range(args.warmup):
         fused()
     torch.cuda.synchronize()
+    # the step as a CUDA graph (the same kernels; no host launch overhead)
+    from folax_gb300.batched import capture_step
+    graph, _ = capture_step(fused, warmup=1)
+    step = graph.replay
     barrier()
     torch.cuda.synchronize()
     # clocks are sampled from before a one-second untimed soak (steady clocks,
@@ -281,10 +460,11 @@ def main():
     t_end = time.perf_counter() + (0.0 if args.no_soak else 1.0)
     while time.perf_counter() < t_end:
         for _ in range(20):
-            fused()
+            step()
         torch.cuda.synchronize()
-    ms = timed(fused, args.steps)
+    ms = timed(step, args.steps)
     clk = clocks.stop()
+    ms_eager = timed(fused, args.steps)
     torch.cuda.synchronize()
     barrier()
     if world > 1:
@@ -345,13 +525,27 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     fp32_achieved = FLOPS_PER_ELEMENT * nE / (elem_ms * 1e-3) / 1e12
 
+    extras = None
+    if rank == 0 and not args.no_extras:
+        extras = {}
+        for name, fn in (("pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
+                         ("batched_quad4_512", lambda: extra_batched(args)),
+                         ("neohooke_tet4_batch16", lambda: extra_neohooke(args))):
+            try:
+                extras[name] = fn()
+            except Exception as exc:  # report, do not hide, a failed extra
+                extras[name] = {"error": f"{type(exc).__name__}: {exc}"}
+            torch.cuda.empty_cache()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_port()
     if rank == 0:
         line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
                 "value": value, "unit": "M elements/s", "n_gpus": world, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+                "warmup": args.warmup, "ms_per_step": ms, "ms_per_step_eager_api": ms_eager,
+                "timing": "CUDA-graph replay of the fused step (memset + element kernel + gather); "
+                          "ms_per_step_eager_api = the same step through the Python API call",
+                "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded two-phase voxels, noisy uniaxial u)",
                 "config": workload_config(args.n, B),
                 "plain": {"value": value_plain, "unit": "M elements/s", "ms_per_step": ms_plain,
@@ -370,7 +564,8 @@ def main():
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
                 "clocks": clk,
-                "gpu_launches": 2 * args.steps}
+                "gpu_launches": 2 * args.steps,
+                "extras": extras}
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
