@@ -329,16 +329,22 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=24):
         "linear_solver_settings": {"solver": "JAX-bicgstab", "tol": 1e-6, "maxiter": 20000, "check_every": 64},
         "nonlinear_solver_settings": {"load_incr": 1, "maxiter": 1}})
     solver.Initialize()
+    out = {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6}
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    solver.Solve(E2, np.zeros(l2.GetTotalNumberOfDOFs(), dtype=np.float32))
+    try:
+        solver.Solve(E2, np.zeros(l2.GetTotalNumberOfDOFs(), dtype=np.float32))
+        err = None
+    except Exception as exc:
+        err = f"{type(exc).__name__}: {exc}"
     torch.cuda.synchronize()
     t_newton = time.perf_counter() - t0
     h = solver.history[-1] if solver.history else {}
-    return {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6,
-            "newton": {"mesh": f"{newton_n}^3 hex split into {len(m2.elements_nodes['tetra'])} tets",
-                       "dofs": l2.GetTotalNumberOfDOFs(), "ms_per_newton_iteration": t_newton * 1e3,
-                       "linear": h.get("linear"), "residual_norm": h.get("res_norm")}}
+    out["newton"] = {"mesh": f"{newton_n}^3 hex split into {len(m2.elements_nodes['tetra'])} tets",
+                     "dofs": l2.GetTotalNumberOfDOFs(), "ms_per_newton_iteration": t_newton * 1e3,
+                     "linear": h.get("linear") or solver.last_linear_info, "residual_norm": h.get("res_norm"),
+                     "error": err}
+    return out
 
 
 def _oracle_chunk(args):

@@ -5,8 +5,9 @@
 //
 // SpMV reads the canonical CSR values but indexes columns through the node
 // adjacency (one column index per ndof x ndof block), so the index stream is
-// 1/ndof^2 of a scalar CSR's.  One group of G lanes handles one node's ndof
-// rows; lane j of the group owns neighbour j.
+// 1/ndof^2 of a scalar CSR's.  One group of G lanes handles the ndof rows of
+// kRowsU consecutive nodes; lane k of the group owns the flat row positions
+// k, k + G, ... (neighbour-major, component-minor), so value loads coalesce.
 //
 // Precision: matrix and Krylov vectors in fp32, every inner product and norm
 // accumulated in fp64, the iterate x kept in fp64.  fp32 SpMV bounds how far
@@ -33,7 +34,7 @@ struct KScalars {
   double alpha, beta, omega;
   int iters, done, replace, maxiter, restart, breakdowns;
 };
-// done: 1 converged (true residual), 2 maxiter, 3 repeated breakdown / non-finite
+// done: 1 converged (true residual), 2 maxiter, 3 non-finite, 4 repeated breakdown or divergence
 
 struct KWork {
   float *r, *z, *p0, *p1, *q;   // PCG: r, z, p (two buffers), q = A p
@@ -46,6 +47,8 @@ struct KWork {
 
 constexpr int kVecBlocks = 1024;
 constexpr double kReplaceDrop2 = 1e-6;  // replace when |r|^2 <= 1e-6 |r_true|^2
+constexpr int kMaxBreakdowns = 8;       // consecutive breakdown restarts before giving up
+constexpr double kDiverge2 = 1e12;      // stop when |r_true|^2 > 1e12 |b|^2 (diverged)
 
 static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork* w) {
   Bump bp(base, cap);
@@ -90,56 +93,85 @@ __device__ __forceinline__ double sum_partials(const double* part, int n, double
   return block_sum_d(s, sh);
 }
 
-// Per-node row product over the node adjacency: acc[i] = sum_j sum_l
-// A(ndof*n+i, ndof*m_j+l) * col(m_j, l), computed by a group of G lanes and
-// reduced with shuffles.  Called warp-uniformly (inactive lanes pass deg 0).
-template <int NDOF, int G, class T, class Col>
-__device__ __forceinline__ void node_rows(const int* __restrict__ adj, const float* __restrict__ vals, int a0,
-                                          int deg, const int (&rb)[NDOF], int lane, Col col, T (&acc)[NDOF]) {
+// Row products over the node adjacency for U nodes at once.  The canonical
+// CSR stores node n's ndof rows back to back, each ndof*deg(n) long and
+// neighbour-major, so with a0 = adj_ptr[n] the value of row (n, i) at flat
+// position w = ndof*j + l (neighbour j, component l) sits at
+// ndof*ndof*a0 + i*ndof*deg + w: no rowptr read is needed.  A group of G
+// lanes serves U consecutive nodes; lane k takes the flat positions
+// w = k, k + G, ... of all ndof rows, so every value load of the group is
+// contiguous (coalesced), and the loads of all U nodes are issued before any
+// is used.
+template <int NDOF, int G, int U, class T, class Col>
+__device__ __forceinline__ void rows_multi(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
+                                           const float* __restrict__ vals, int maxdeg, int64_t base, int lane,
+                                           Col col, T (&acc)[U][NDOF], bool (&active)[U]) {
+  int a0[U], len[U];
 #pragma unroll
-  for (int i = 0; i < NDOF; ++i) acc[i] = T(0);
-  for (int j = lane; j < deg; j += G) {
-    const int m = __ldg(adj + a0 + j);
-    T cv[NDOF];
+  for (int u = 0; u < U; ++u) {
+    const int64_t n = base + u;
+    active[u] = n < N;
+    a0[u] = active[u] ? __ldg(adj_ptr + n) : 0;
+    len[u] = active[u] ? NDOF * (__ldg(adj_ptr + n + 1) - a0[u]) : 0;
 #pragma unroll
-    for (int l = 0; l < NDOF; ++l) cv[l] = col((int64_t)NDOF * m + l);
+    for (int i = 0; i < NDOF; ++i) acc[u][i] = T(0);
+  }
+  const int maxlen = NDOF * maxdeg;
+  for (int w0 = 0; w0 < maxlen; w0 += G) {
+    const int w = w0 + lane;
+    const int j = w / NDOF, l = w - NDOF * j;
+    int m[U];
+    float v[U][NDOF];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool on = w < len[u];
+      m[u] = on ? __ldg(adj + a0[u] + j) : 0;
+      const float* vr = vals + (int64_t)NDOF * NDOF * a0[u] + w;
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) v[u][i] = on ? __ldg(vr + (int64_t)i * len[u]) : 0.f;
+    }
+    T xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = (w < len[u]) ? col((int64_t)NDOF * m[u] + l) : T(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) acc[u][i] += (T)v[u][i] * xv[u];
+  }
+#pragma unroll
+  for (int u = 0; u < U; ++u)
 #pragma unroll
     for (int i = 0; i < NDOF; ++i)
 #pragma unroll
-      for (int l = 0; l < NDOF; ++l) acc[i] += (T)__ldg(vals + rb[i] + NDOF * j + l) * cv[l];
-  }
-#pragma unroll
-  for (int i = 0; i < NDOF; ++i)
-#pragma unroll
-    for (int o = G / 2; o > 0; o >>= 1) acc[i] += __shfl_xor_sync(0xffffffffu, acc[i], o, G);
+      for (int o = G / 2; o > 0; o >>= 1) acc[u][i] += __shfl_xor_sync(0xffffffffu, acc[u][i], o, G);
 }
 
-// Warp-uniform loop over nodes: every lane runs the same number of rounds so
-// the group shuffles always see the whole warp.
-#define FOLGB_NODE_LOOP(NDOF, G)                                                                 \
-  const int lane = threadIdx.x % G;                                                              \
-  const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;                    \
-  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;                                 \
-  for (int64_t n = group; __any_sync(0xffffffffu, n < N); n += ngroups)
+constexpr int kRowsU = 4;  // nodes per lane group per round
 
-#define FOLGB_NODE_SETUP(NDOF)                                                    \
-  const bool active = n < N;                                                      \
-  const int a0 = active ? __ldg(adj_ptr + n) : 0;                                 \
-  const int deg = active ? __ldg(adj_ptr + n + 1) - a0 : 0;                       \
-  int rb[NDOF];                                                                   \
-  _Pragma("unroll") for (int i = 0; i < NDOF; ++i) rb[i] = active ? __ldg(rowptr + (int64_t)NDOF * n + i) : 0;
+// Warp-uniform loop over node blocks: every lane runs the same number of
+// rounds so the group shuffles always see the whole warp.
+#define FOLGB_NODE_BLOCKS(G)                                                              \
+  const int lane = threadIdx.x % G;                                                       \
+  const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;             \
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;                          \
+  for (int64_t base = group * kRowsU; __any_sync(0xffffffffu, base < N); base += ngroups * kRowsU)
 
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_spmv(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
-                                              const int* __restrict__ rowptr, const float* __restrict__ vals,
+                                              int maxdeg, const float* __restrict__ vals,
                                               const float* __restrict__ x, float* __restrict__ y) {
-  FOLGB_NODE_LOOP(NDOF, G) {
-    FOLGB_NODE_SETUP(NDOF)
-    float acc[NDOF];
-    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(x + d); }, acc);
-    if (active && lane == 0) {
+  FOLGB_NODE_BLOCKS(G) {
+    float acc[kRowsU][NDOF];
+    bool act[kRowsU];
+    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                       [&](int64_t d) { return __ldg(x + d); }, acc, act);
+    if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) y[(int64_t)NDOF * n + i] = acc[i];
+      for (int u = 0; u < kRowsU; ++u)
+        if (act[u]) {
+#pragma unroll
+          for (int i = 0; i < NDOF; ++i) y[(int64_t)NDOF * (base + u) + i] = acc[u][i];
+        }
     }
   }
 }
@@ -149,7 +181,7 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t N, const int* __restrict__
 // ---------------------------------------------------------------------------
 template <int NDOF, int G, bool BICG>
 __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __restrict__ adj_ptr,
-                                                       const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                       const int* __restrict__ adj, int maxdeg,
                                                        const float* __restrict__ vals, const float* __restrict__ b,
                                                        const float* __restrict__ dinv, const double* __restrict__ x,
                                                        float* __restrict__ r, float* __restrict__ z,
@@ -157,22 +189,27 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
                                                        KScalars* sc) {
   __shared__ double sh[32];
   double rz = 0.0, rr = 0.0;
-  FOLGB_NODE_LOOP(NDOF, G) {
-    FOLGB_NODE_SETUP(NDOF)
-    double acc[NDOF];
-    node_rows<NDOF, G, double>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return x[d]; }, acc);
-    if (active && lane == 0) {
+  FOLGB_NODE_BLOCKS(G) {
+    double acc[kRowsU][NDOF];
+    bool act[kRowsU];
+    rows_multi<NDOF, G, kRowsU, double>(N, adj_ptr, adj, vals, maxdeg, base, lane, [&](int64_t d) { return x[d]; },
+                                        acc, act);
+    if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = (int64_t)NDOF * n + i;
-        const double ri = (double)b[d] - acc[i];
-        const float rf = (float)ri;
-        r[d] = rf;
-        const float zf = dinv[d] * rf;
-        if (!BICG) z[d] = zf;
-        else rhat[d] = rf;
-        rz += (double)rf * (double)zf;
-        rr += ri * ri;
+      for (int u = 0; u < kRowsU; ++u) {
+        if (!act[u]) continue;
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = (int64_t)NDOF * (base + u) + i;
+          const double ri = (double)b[d] - acc[u][i];
+          const float rf = (float)ri;
+          r[d] = rf;
+          const float zf = dinv[d] * rf;
+          if (!BICG) z[d] = zf;
+          else rhat[d] = rf;
+          rz += (double)rf * (double)zf;
+          rr += ri * ri;
+        }
       }
     }
   }
@@ -198,6 +235,7 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
     }
     if (!isfinite(RR)) sc->done = 3;
     else if (RR <= sc->tol2) sc->done = 1;
+    else if (RR > kDiverge2 * sc->bnorm2) sc->done = 4;
     counters[3] = 0u;
   }
 }
@@ -255,7 +293,7 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
 
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
-                                                  const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                  const int* __restrict__ adj, int maxdeg,
                                                   const float* __restrict__ vals, const float* __restrict__ z,
                                                   const float* __restrict__ pold, float* __restrict__ pnew,
                                                   float* __restrict__ q, double* part, unsigned* counters,
@@ -264,19 +302,24 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restri
   if (sc->done || sc->replace) return;
   const float beta = (float)sc->beta;
   double dot = 0.0;
-  FOLGB_NODE_LOOP(NDOF, G) {
-    FOLGB_NODE_SETUP(NDOF)
-    float acc[NDOF];
-    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane,
-                              [&](int64_t d) { return fmaf(beta, __ldg(pold + d), __ldg(z + d)); }, acc);
-    if (active && lane == 0) {
+  FOLGB_NODE_BLOCKS(G) {
+    float acc[kRowsU][NDOF];
+    bool act[kRowsU];
+    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                       [&](int64_t d) { return fmaf(beta, __ldg(pold + d), __ldg(z + d)); }, acc,
+                                       act);
+    if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = (int64_t)NDOF * n + i;
-        const float pn = fmaf(beta, pold[d], z[d]);
-        pnew[d] = pn;
-        q[d] = acc[i];
-        dot += (double)pn * (double)acc[i];
+      for (int u = 0; u < kRowsU; ++u) {
+        if (!act[u]) continue;
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = (int64_t)NDOF * (base + u) + i;
+          const float pn = fmaf(beta, pold[d], z[d]);
+          pnew[d] = pn;
+          q[d] = acc[u][i];
+          dot += (double)pn * (double)acc[u][i];
+        }
       }
     }
   }
@@ -289,7 +332,8 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restri
       // breakdown: restart from the true residual; give up if it repeats
       sc->alpha = 0.0;
       sc->breakdowns += 1;
-      if (sc->breakdowns > 2) sc->done = 3;
+      if (!isfinite(PQ)) sc->done = 3;
+      else if (sc->breakdowns > kMaxBreakdowns) sc->done = 4;
       else sc->replace = 1;
     } else {
       sc->alpha = sc->rho / PQ;
@@ -333,7 +377,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __re
     sc->iters += 1;
     sc->breakdowns = 0;
     if (!isfinite(RR)) sc->done = 3;
-    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2) sc->replace = 1;
+    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2) sc->replace = 1;
     if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
     counters[2] = 0u;
   }
@@ -379,9 +423,11 @@ __global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __re
 
 // p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
 // v_new = A y; alpha = rho / (rhat . v_new)
+// p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
+// v_new = A y; alpha = rho / (rhat . v_new)
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __restrict__ adj_ptr,
-                                                     const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                     const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
                                                      const float* __restrict__ r, const float* __restrict__ rhat,
                                                      const float* __restrict__ pold, const float* __restrict__ vold,
@@ -397,20 +443,24 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
     return rs ? __ldg(r + d) : fmaf(beta, fmaf(-omega, __ldg(vold + d), __ldg(pold + d)), __ldg(r + d));
   };
   double dot = 0.0;
-  FOLGB_NODE_LOOP(NDOF, G) {
-    FOLGB_NODE_SETUP(NDOF)
-    float acc[NDOF];
-    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(dinv + d) * pval(d); },
-                              acc);
-    if (active && lane == 0) {
+  FOLGB_NODE_BLOCKS(G) {
+    float acc[kRowsU][NDOF];
+    bool act[kRowsU];
+    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                       [&](int64_t d) { return __ldg(dinv + d) * pval(d); }, acc, act);
+    if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = (int64_t)NDOF * n + i;
-        const float pn = pval(d);
-        pnew[d] = pn;
-        y[d] = dinv[d] * pn;
-        vnew[d] = acc[i];
-        dot += (double)rhat[d] * (double)acc[i];
+      for (int u = 0; u < kRowsU; ++u) {
+        if (!act[u]) continue;
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = (int64_t)NDOF * (base + u) + i;
+          const float pn = pval(d);
+          pnew[d] = pn;
+          y[d] = dinv[d] * pn;
+          vnew[d] = acc[u][i];
+          dot += (double)rhat[d] * (double)acc[u][i];
+        }
       }
     }
   }
@@ -422,7 +472,8 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
     sc->restart = 0;
     if (RV == 0.0 || !isfinite(RV)) {
       sc->breakdowns += 1;
-      if (sc->breakdowns > 2) sc->done = 3;
+      if (!isfinite(RV)) sc->done = 3;
+      else if (sc->breakdowns > kMaxBreakdowns) sc->done = 4;
       else sc->replace = 1;
     } else {
       sc->alpha = sc->rho / RV;
@@ -434,7 +485,7 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
 // s = r - alpha v_new, z = D^-1 s, t = A z; omega = (t . s) / (t . t)
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __restrict__ adj_ptr,
-                                                     const int* __restrict__ adj, const int* __restrict__ rowptr,
+                                                     const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
                                                      const float* __restrict__ r, const float* __restrict__ vnew,
                                                      float* __restrict__ z, float* __restrict__ t, double* part,
@@ -444,20 +495,24 @@ __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __res
   const float af = (float)sc->alpha;
   auto sval = [&](int64_t d) -> float { return fmaf(-af, __ldg(vnew + d), __ldg(r + d)); };
   double ts = 0.0, tt = 0.0;
-  FOLGB_NODE_LOOP(NDOF, G) {
-    FOLGB_NODE_SETUP(NDOF)
-    float acc[NDOF];
-    node_rows<NDOF, G, float>(adj, vals, a0, deg, rb, lane, [&](int64_t d) { return __ldg(dinv + d) * sval(d); },
-                              acc);
-    if (active && lane == 0) {
+  FOLGB_NODE_BLOCKS(G) {
+    float acc[kRowsU][NDOF];
+    bool act[kRowsU];
+    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                       [&](int64_t d) { return __ldg(dinv + d) * sval(d); }, acc, act);
+    if (lane == 0) {
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) {
-        const int64_t d = (int64_t)NDOF * n + i;
-        const float sv = sval(d);
-        z[d] = dinv[d] * sv;
-        t[d] = acc[i];
-        ts += (double)acc[i] * (double)sv;
-        tt += (double)acc[i] * (double)acc[i];
+      for (int u = 0; u < kRowsU; ++u) {
+        if (!act[u]) continue;
+#pragma unroll
+        for (int i = 0; i < NDOF; ++i) {
+          const int64_t d = (int64_t)NDOF * (base + u) + i;
+          const float sv = sval(d);
+          z[d] = dinv[d] * sv;
+          t[d] = acc[u][i];
+          ts += (double)acc[u][i] * (double)sv;
+          tt += (double)acc[u][i] * (double)acc[u][i];
+        }
       }
     }
   }
@@ -476,7 +531,6 @@ __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __res
   }
 }
 
-// s = r - alpha v, x += alpha y + omega z, r = s - omega t; rho_new = rhat . r
 __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restrict__ x, float* __restrict__ r,
                                                      const float* __restrict__ rhat, const float* __restrict__ vnew,
                                                      const float* __restrict__ y, const float* __restrict__ z,
@@ -512,7 +566,9 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
     sc->iters += 1;
     sc->breakdowns = 0;
     if (!isfinite(RR)) sc->done = 3;
-    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RH == 0.0 || omega == 0.0) sc->replace = 1;
+    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2 || RH == 0.0 ||
+             omega == 0.0)
+      sc->replace = 1;
     if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
     counters[2] = 0u;
   }
@@ -521,7 +577,7 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
 template <int NDOF>
 static int group_width(int maxdeg) {
   int g = 1;
-  while (g < maxdeg && g < 32) g <<= 1;
+  while (g < NDOF * maxdeg && g < 32) g <<= 1;
   return g < 4 ? 4 : g;
 }
 
@@ -546,7 +602,7 @@ static int with_ndof(int ndof, F&& f) {
 }
 
 static int spmv_blocks(const folgb_plan* p, int G) {
-  int64_t threads = p->N * (int64_t)G;
+  int64_t threads = ((p->N + kRowsU - 1) / kRowsU) * (int64_t)G;
   int64_t blocks = (threads + 255) / 256;
   int64_t cap = (int64_t)num_sms() * 8;
   return (int)(blocks < cap ? blocks : cap);
@@ -600,7 +656,7 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         for (int k = 0; k < check_every; ++k) {
           if (solver == SOLVER_CG) {
             trace_begin(KID_PCG_SPMV, s);
-            k_pcg_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, w.z, pa, pb,
+            k_pcg_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
                                                     w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, s);
             trace_begin(KID_PCG_UPDATE, s);
@@ -609,9 +665,9 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
             std::swap(pa, pb);
           } else {
             trace_begin(KID_PCG_SPMV, s);
-            k_bicg_p_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, dinv, w.r,
+            k_bicg_p_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
                                                        w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
-            k_bicg_s_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, dinv, w.r,
+            k_bicg_s_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
                                                        vb_, w.z, w.t, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, s);
             trace_begin(KID_PCG_UPDATE, s);
@@ -627,10 +683,10 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         if (host.done) break;
         if (host.replace) {
           if (solver == SOLVER_CG)
-            k_true_residual<NDOF, G, false><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, rhs,
+            k_true_residual<NDOF, G, false><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
                                                                 dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
           else
-            k_true_residual<NDOF, G, true><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, rhs,
+            k_true_residual<NDOF, G, true><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
                                                                dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
           FOLGB_LAUNCH_CHECK();
           FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
@@ -672,7 +728,7 @@ extern "C" int folgb_spmv(const folgb_plan* p, const float* vals, const float* x
     constexpr int NDOF = decltype(nd)::value;
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
       constexpr int G = decltype(gw)::value;
-      k_spmv<NDOF, G><<<spmv_blocks(p, G), 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->d_rowptr, vals, x, y);
+      k_spmv<NDOF, G><<<spmv_blocks(p, G), 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, x, y);
       FOLGB_LAUNCH_CHECK();
       return (int)FOLGB_OK;
     });
