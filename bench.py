@@ -14,10 +14,11 @@ Workload (one "step" = one pass of the hot path over one batch):
 Metric: M elements/s of fused loss + adjoint.  Reported beside it: the plain
 GPU path (element matrices materialised in HBM, separate backward pass), the
 end-to-end number through the public API with host buffers, the dominant
-kernel's roofline, and the FP64 oracle port timed on the host cores.
+kernel's roofline, and the C FP64 oracle timed on the host cores.
 
-`--impl reference` times the oracle port (the reference is JAX, absent here)
-with every host core on a bounded sample of the same workload.
+`--impl reference` times the C FP64 oracle (the reference's element algorithm;
+the reference itself is JAX, absent here) with every host core on the whole
+workload.
 """
 from __future__ import annotations
 
@@ -56,6 +57,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
+    ap.add_argument("--hex8-variant", type=int, default=None,
+                    help="force one hex8 kernel variant (0-5) instead of autotuning (profiling runs)")
+    ap.add_argument("--extras", default="pcg,batched,neohooke",
+                    help="comma list of the extra measurements to run (pcg, batched, neohooke)")
     return ap.parse_args()
 
 
@@ -140,9 +145,49 @@ def measured_peaks():
         return None
 
 
-def cpu_baseline_port(n_sample=12, seed=7):
-    """FP64 oracle port (NumPy, one thread) on a bounded sample: a 12^3 hex8
-    mesh with the same physics; returns M elements/s of loss + adjoint."""
+def _c_oracle(n, seed, threads):
+    """The C oracle (FP64, OpenMP) set up on the bench workload: returns
+    (oracle, control, full dof vector)."""
+    from oracle import c_oracle
+    mesh, settings, E, u = workload(n, seed)
+    L = c_oracle.CLossOracle("hex8", "elastic", mesh.nodes_coordinates, mesh.elements_nodes["hexahedron"],
+                             dirichlet=settings["dirichlet_bc_dict"], node_sets=mesh.node_sets,
+                             control_layout="element", threads=threads)
+    return L, E.astype(np.float64), L.py.full_dof_vector(u.astype(np.float64))
+
+
+def _host_threads():
+    return len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else (os.cpu_count() or 1)
+
+
+def cpu_baseline_port(n, seed, budget_s=10.0):
+    """C oracle (FP64 restatement of the reference's element algorithm, OpenMP
+    over every host core) on the full bench workload: loss + adjoint of the
+    whole mesh per repetition, as many repetitions as fit in about budget_s.
+    Falls back to the NumPy oracle on a 12^3 sample when the C oracle does not
+    build."""
+    threads = _host_threads()
+    try:
+        L, ctrl, u = _c_oracle(n, seed, threads)
+    except Exception as exc:  # noqa: BLE001
+        return _cpu_baseline_numpy(reason=f"C oracle unavailable ({type(exc).__name__}: {exc})")
+    L.loss_adjoint(ctrl, u)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        L.loss_adjoint(ctrl, u)
+        reps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    E = n ** 3
+    return {"value": E / dt / 1e6, "unit": "M elements/s", "cores": L.max_threads, "kind": "port",
+            "sample": f"C FP64 oracle (OpenMP, {L.max_threads} threads), hex8 elastic loss+adjoint of the whole "
+                      f"{n}^3 mesh ({E} elements), {reps} repetitions, {dt * 1e3:.1f} ms each"}
+
+
+def _cpu_baseline_numpy(n_sample=12, seed=7, reason=""):
+    """NumPy FP64 oracle, one thread, on a 12^3 sample (fallback)."""
     from oracle import fe_oracle as fo
     from folax_gb300 import fields
     from folax_gb300.mesh import create_3D_box_mesh
@@ -164,7 +209,7 @@ def cpu_baseline_port(n_sample=12, seed=7):
     E = n_sample ** 3
     return {"value": E / dt / 1e6, "unit": "M elements/s", "cores": 1, "kind": "port",
             "sample": f"NumPy FP64 oracle, hex8 elastic loss+adjoint on a {n_sample}^3 mesh ({E} elements), "
-                      f"{reps} repetitions, {dt * 1e3:.1f} ms each"}
+                      f"{reps} repetitions, {dt * 1e3:.1f} ms each. {reason}"}
 
 
 def _events_ms(torch, fn, steps, flush=None):
@@ -291,11 +336,13 @@ def extra_batched(args, n_inst=512, seed=11):
             "per_instance_step": "the same, one eager launch set per instance (wall clock)"}
 
 
-def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=24):
+def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
     """C4: tet4 Neo-Hookean (6-tet split of a 64^3 hex grid, 1 Gauss point),
     mu/lambda scaled by the two-phase field, batch 16: fused loss + adjoint
     throughput; and the time of one Newton iteration (CSR tangent + BiCGSTAB)
-    on a 24^3 split."""
+    on a 12^3 split.  The Neo-Hookean tangent of this model is indefinite at
+    the undeformed state (its stress there is -mu I), so Jacobi BiCGSTAB needs
+    thousands of iterations beyond ~16^3 and the Newton solve stays small."""
     import torch
     from folax_gb300 import fields
     from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
@@ -320,7 +367,7 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=24):
     torch.cuda.synchronize()
     ms = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
     E = len(mesh.elements_nodes["tetra"])
-    # one Newton iteration on a smaller split: assembly + BiCGSTAB (rtol 1e-6)
+    # one Newton iteration on a small split: assembly + BiCGSTAB (rtol 1e-6)
     m2 = split_hex_to_tets(create_3D_box_mesh(newton_n, newton_n, newton_n))
     E2 = np.repeat(fields.two_phase_voxels(newton_n, seed), 6).astype(np.float32)
     l2 = NeoHookeMechanicalLoss3DTetra("nh2", dict(settings), m2)
@@ -347,57 +394,37 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=24):
     return out
 
 
-def _oracle_chunk(args):
-    """Worker of the reference arm: loss + element gradients for a slab of elements."""
-    xyz, conn, ctrl, u = args
-    from oracle import fe_oracle as fo
-    X = xyz[conn]
-    de = np.repeat(ctrl[:, None], 8, axis=1)
-    dofidx = (3 * conn[:, :, None] + np.arange(3)).reshape(len(conn), -1)
-    en, re, _, dE = fo.linear_elastic_element("hex8", X, de, u[dofidx], 2, 1.0, 0.3, None)
-    return float(en.sum()), re, dE.sum(axis=1)
-
-
 def run_reference(args):
-    """Oracle port on every host core (process pool, spawn) over a bounded
-    sample of the 64^3 workload: each step evaluates a fixed slab of elements
-    (loss + per-element gradients + nodal scatter)."""
-    import multiprocessing as mp
+    """The reference's algorithm on the host cores: the C oracle (FP64,
+    OpenMP over every core; the reference itself is JAX, which is not
+    installed) evaluates loss + adjoint of the whole bench mesh each step.
+    Rank 0 only; other ranks exit without work."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    mesh, settings, E, u = workload(args.n, args.seed)
-    conn = mesh.elements_nodes["hexahedron"]
-    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    sample = min(len(conn), 2048 * cores)
-    chunks = np.array_split(np.arange(sample), cores)
-    xyz = mesh.nodes_coordinates
-    ud = u.astype(np.float64)
-    work = [(xyz, conn[c], E[c].astype(np.float64), ud) for c in chunks]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        def step():
-            res = pool.map(_oracle_chunk, work)
-            g = np.zeros(3 * len(xyz))
-            for c, (_, re, _) in zip(chunks, res):
-                idx = (3 * conn[c][:, :, None] + np.arange(3)).ravel()
-                np.add.at(g, idx, re.ravel())
-            return sum(r[0] for r in res)
-        for _ in range(max(1, args.warmup)):
-            step()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            step()
-        dt = (time.perf_counter() - t0) / args.steps
-    value = sample / dt / 1e6
+    threads = _host_threads()
+    try:
+        L, ctrl, u = _c_oracle(args.n, args.seed, threads)
+    except Exception as exc:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": f"C oracle did not build: {type(exc).__name__}"}))
+        return
+    for _ in range(max(1, args.warmup)):
+        L.loss_adjoint(ctrl, u)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        L.loss_adjoint(ctrl, u)
+    dt = (time.perf_counter() - t0) / args.steps
+    E = args.n ** 3
+    value = E / dt / 1e6
     line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
             "impl": "reference", "value": value, "unit": "M elements/s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded two-phase voxels, noisy uniaxial u)",
             "config": workload_config(args.n, 1),
-            "cpu_baseline": {"value": value, "unit": "M elements/s", "cores": cores, "kind": "port",
-                             "sample": f"FP64 NumPy oracle port (the reference is JAX, not installed), "
-                                       f"{sample} of {len(conn)} elements per step over {cores} processes"},
+            "cpu_baseline": {"value": value, "unit": "M elements/s", "cores": L.max_threads, "kind": "port",
+                             "sample": f"C FP64 oracle restating the reference's element algorithm (the reference "
+                                       f"is JAX, not installed): the whole {args.n}^3 mesh ({E} elements) per step, "
+                                       f"{L.max_threads} OpenMP threads"},
             "e2e": {"value": value, "unit": "M elements/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -425,6 +452,8 @@ def main():
             dist.barrier()
 
     mesh, settings, E_h, u_h = workload(args.n, args.seed)
+    if args.hex8_variant is not None:
+        settings["kernel_variant"] = int(args.hex8_variant)
     loss = MechanicalLoss3DHexa("bench", settings, mesh)
     loss.Initialize()
     lib = _capi.load()
@@ -493,7 +522,9 @@ def main():
     # plain path
     for _ in range(2):
         plain()
-    ms_plain = timed(plain, args.plain_steps)
+    ms_plain_eager = timed(plain, args.plain_steps)
+    graph_plain, _ = capture_step(plain, warmup=1)
+    ms_plain = timed(graph_plain.replay, args.plain_steps)
     value_plain = B * nE / (ms_plain * 1e-3) / 1e6
 
     # end to end through the public API with host buffers
@@ -534,9 +565,12 @@ def main():
     extras = None
     if rank == 0 and not args.no_extras:
         extras = {}
-        for name, fn in (("pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
-                         ("batched_quad4_512", lambda: extra_batched(args)),
-                         ("neohooke_tet4_batch16", lambda: extra_neohooke(args))):
+        wanted = set(args.extras.split(","))
+        for key, name, fn in (("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
+                              ("batched", "batched_quad4_512", lambda: extra_batched(args)),
+                              ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args))):
+            if key not in wanted:
+                continue
             try:
                 extras[name] = fn()
             except Exception as exc:  # report, do not hide, a failed extra
@@ -544,7 +578,7 @@ def main():
             torch.cuda.empty_cache()
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline_port()
+        cpu = cpu_baseline_port(args.n, args.seed)
     if rank == 0:
         line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
                 "value": value, "unit": "M elements/s", "n_gpus": world, "steps": args.steps,
@@ -555,6 +589,8 @@ def main():
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded two-phase voxels, noisy uniaxial u)",
                 "config": workload_config(args.n, B),
                 "plain": {"value": value_plain, "unit": "M elements/s", "ms_per_step": ms_plain,
+                          "ms_per_step_eager_api": ms_plain_eager,
+                          "timing": "CUDA-graph replay, like the fused step",
                           "speedup_fused_vs_plain": value / value_plain},
                 "kernels": {"elem_loss_ms": elem_ms, "gather_ms": gather_ms,
                             "autotune": {"chosen_variant": tune["chosen"], "ms_per_variant": tune["ms"],

@@ -997,11 +997,12 @@ extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control
   cudaEvent_t a, b;
   FOLGB_CUDA_TRY(cudaEventCreate(&a));
   FOLGB_CUDA_TRY(cudaEventCreate(&b));
-  int best = 0;
+  // an untunable plan is timed as it stands (its variant, forced or not, is kept)
+  int best = p->hex8_variant;
   float best_ms = 0.f;
   int rc = FOLGB_OK;
   for (int v = 0; v < nv && rc == FOLGB_OK; ++v) {
-    p->hex8_variant = v;
+    if (tunable) p->hex8_variant = v;
     for (int k = 0; k < 2 && rc == FOLGB_OK; ++k)
       rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
                               dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
@@ -1015,7 +1016,7 @@ extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control
     cudaEventElapsedTime(&ms, a, b);
     ms /= repeats;
     if (ms_per_variant && v < max_variants) ms_per_variant[v] = ms;
-    if (v == 0 || ms < best_ms) {
+    if (tunable && (v == 0 || ms < best_ms)) {
       best = v;
       best_ms = ms;
     }

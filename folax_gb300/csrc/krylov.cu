@@ -6,7 +6,7 @@
 // SpMV reads the canonical CSR values but indexes columns through the node
 // adjacency (one column index per ndof x ndof block), so the index stream is
 // 1/ndof^2 of a scalar CSR's.  One group of G lanes handles the ndof rows of
-// kRowsU consecutive nodes; lane k of the group owns the flat row positions
+// a few consecutive nodes; lane k of the group owns the flat row positions
 // k, k + G, ... (neighbour-major, component-minor), so value loads coalesce.
 //
 // Precision: matrix and Krylov vectors in fp32, every inner product and norm
@@ -102,17 +102,54 @@ __device__ __forceinline__ double sum_partials(const double* part, int n, double
 // w = k, k + G, ... of all ndof rows, so every value load of the group is
 // contiguous (coalesced), and the loads of all U nodes are issued before any
 // is used.
-template <int NDOF, int G, int U, class T, class Col>
-__device__ __forceinline__ void rows_multi(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
+//
+// The U*ndof per-lane partial sums are then reduced by halving: at each
+// shuffle step a lane keeps half of its values (the upper half when its lane
+// bit for that step is set) and adds the partner's copy of that half, so the
+// group needs VP - 1 shuffles (VP = U*ndof rounded up to a power of two)
+// instead of U*ndof*log2(G), and lane k ends up holding the row sum of value
+// index k / (G / VP).  The row epilogues (vector updates, dot products) then
+// run on U*ndof lanes in parallel instead of serially on one lane.
+template <int NDOF>
+struct RowsU {
+  static constexpr int U = NDOF == 3 ? 5 : (NDOF == 2 ? 4 : 8);  // nodes per group per round
+  static constexpr int V = U * NDOF;                              // rows per group per round
+  static constexpr int VP = V <= 4 ? 4 : (V <= 8 ? 8 : 16);       // V rounded up to a power of two
+};
+
+template <int G, int C, int O, class T, int VP>
+__device__ __forceinline__ void halving_reduce(T (&v)[VP], int lane) {
+  if constexpr (C > 1) {
+    const bool up = (lane & O) != 0;
+#pragma unroll
+    for (int k = 0; k < C / 2; ++k) {
+      const T send = up ? v[k] : v[k + C / 2];
+      const T keep = up ? v[k + C / 2] : v[k];
+      v[k] = keep + __shfl_xor_sync(0xffffffffu, send, O, G);
+    }
+    halving_reduce<G, C / 2, O / 2>(v, lane);
+  } else if constexpr (O >= 1) {
+    v[0] += __shfl_xor_sync(0xffffffffu, v[0], O, G);
+    halving_reduce<G, 1, O / 2>(v, lane);
+  }
+}
+
+// Returns true on the lane that owns a row of this round; then *sum is the
+// row's product and *dof its index (node-major: ndof*node + component).
+template <int NDOF, int G, class T, class Col>
+__device__ __forceinline__ bool rows_multi(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
                                            const float* __restrict__ vals, int maxdeg, int64_t base, int lane,
-                                           Col col, T (&acc)[U][NDOF], bool (&active)[U]) {
+                                           Col col, T& sum, int64_t& dof) {
+  constexpr int U = RowsU<NDOF>::U, V = RowsU<NDOF>::V, VP = RowsU<NDOF>::VP;
+  static_assert(VP <= G, "lane group narrower than the rows it reduces");
   int a0[U], len[U];
+  T acc[U][NDOF];
 #pragma unroll
   for (int u = 0; u < U; ++u) {
     const int64_t n = base + u;
-    active[u] = n < N;
-    a0[u] = active[u] ? __ldg(adj_ptr + n) : 0;
-    len[u] = active[u] ? NDOF * (__ldg(adj_ptr + n + 1) - a0[u]) : 0;
+    const bool act = n < N;
+    a0[u] = act ? __ldg(adj_ptr + n) : 0;
+    len[u] = act ? NDOF * (__ldg(adj_ptr + n + 1) - a0[u]) : 0;
 #pragma unroll
     for (int i = 0; i < NDOF; ++i) acc[u][i] = T(0);
   }
@@ -138,41 +175,36 @@ __device__ __forceinline__ void rows_multi(int64_t N, const int* __restrict__ ad
 #pragma unroll
       for (int i = 0; i < NDOF; ++i) acc[u][i] += (T)v[u][i] * xv[u];
   }
+  T flat[VP];
 #pragma unroll
-  for (int u = 0; u < U; ++u)
-#pragma unroll
-    for (int i = 0; i < NDOF; ++i)
-#pragma unroll
-      for (int o = G / 2; o > 0; o >>= 1) acc[u][i] += __shfl_xor_sync(0xffffffffu, acc[u][i], o, G);
+  for (int k = 0; k < VP; ++k) flat[k] = k < V ? acc[k / NDOF][k % NDOF] : T(0);
+  halving_reduce<G, VP, G / 2>(flat, lane);
+  constexpr int kSub = G / VP;  // lanes sharing one value index
+  const int idx = lane / kSub;
+  sum = flat[0];
+  dof = (int64_t)NDOF * base + idx;
+  return (lane % kSub) == 0 && idx < V && dof < (int64_t)NDOF * N;
 }
-
-constexpr int kRowsU = 4;  // nodes per lane group per round
 
 // Warp-uniform loop over node blocks: every lane runs the same number of
 // rounds so the group shuffles always see the whole warp.
-#define FOLGB_NODE_BLOCKS(G)                                                              \
-  const int lane = threadIdx.x % G;                                                       \
-  const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;             \
-  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;                          \
-  for (int64_t base = group * kRowsU; __any_sync(0xffffffffu, base < N); base += ngroups * kRowsU)
+#define FOLGB_NODE_BLOCKS(NDOF, G)                                                               \
+  constexpr int kU = RowsU<NDOF>::U;                                                             \
+  const int lane = threadIdx.x % G;                                                              \
+  const int64_t group = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / G;                    \
+  const int64_t ngroups = ((int64_t)gridDim.x * blockDim.x) / G;                                 \
+  for (int64_t base = group * kU; __any_sync(0xffffffffu, base < N); base += ngroups * kU)
 
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_spmv(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
                                               int maxdeg, const float* __restrict__ vals,
                                               const float* __restrict__ x, float* __restrict__ y) {
-  FOLGB_NODE_BLOCKS(G) {
-    float acc[kRowsU][NDOF];
-    bool act[kRowsU];
-    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                       [&](int64_t d) { return __ldg(x + d); }, acc, act);
-    if (lane == 0) {
-#pragma unroll
-      for (int u = 0; u < kRowsU; ++u)
-        if (act[u]) {
-#pragma unroll
-          for (int i = 0; i < NDOF; ++i) y[(int64_t)NDOF * (base + u) + i] = acc[u][i];
-        }
-    }
+  FOLGB_NODE_BLOCKS(NDOF, G) {
+    float sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                   [&](int64_t k) { return __ldg(x + k); }, sum, d))
+      y[d] = sum;
   }
 }
 
@@ -188,32 +220,33 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
                                                        float* __restrict__ rhat, double* part, unsigned* counters,
                                                        KScalars* sc) {
   __shared__ double sh[32];
-  double rz = 0.0, rr = 0.0;
-  FOLGB_NODE_BLOCKS(G) {
-    double acc[kRowsU][NDOF];
-    bool act[kRowsU];
-    rows_multi<NDOF, G, kRowsU, double>(N, adj_ptr, adj, vals, maxdeg, base, lane, [&](int64_t d) { return x[d]; },
-                                        acc, act);
-    if (lane == 0) {
-#pragma unroll
-      for (int u = 0; u < kRowsU; ++u) {
-        if (!act[u]) continue;
-#pragma unroll
-        for (int i = 0; i < NDOF; ++i) {
-          const int64_t d = (int64_t)NDOF * (base + u) + i;
-          const double ri = (double)b[d] - acc[u][i];
-          const float rf = (float)ri;
-          r[d] = rf;
-          const float zf = dinv[d] * rf;
-          if (!BICG) z[d] = zf;
-          else rhat[d] = rf;
-          rz += (double)rf * (double)zf;
-          rr += ri * ri;
-        }
+  // BiCGSTAB keeps its shadow residual and directions across a residual
+  // replacement; only a breakdown (replace == 2) restarts it from rhat = r.
+  const bool restart = BICG && sc->replace == 2;
+  float rzf = 0.f;
+  double rr = 0.0;
+  FOLGB_NODE_BLOCKS(NDOF, G) {
+    double sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, double>(N, adj_ptr, adj, vals, maxdeg, base, lane, [&](int64_t k) { return x[k]; },
+                                    sum, d)) {
+      const double ri = (double)b[d] - sum;
+      const float rf = (float)ri;
+      r[d] = rf;
+      if (!BICG) {
+        const float zf = dinv[d] * rf;
+        z[d] = zf;
+        rzf = fmaf(rf, zf, rzf);
+      } else if (restart) {
+        rhat[d] = rf;
+        rzf = fmaf(rf, rf, rzf);
+      } else {
+        rzf = fmaf(rhat[d], rf, rzf);
       }
+      rr = fma(ri, ri, rr);
     }
   }
-  double s1 = block_sum_d(rz, sh);
+  double s1 = block_sum_d((double)rzf, sh);
   double s2 = block_sum_d(rr, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s1;
@@ -226,11 +259,10 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
     sc->rnorm2 = RR;
     sc->rref2 = RR;
     sc->replace = 0;
+    sc->rho = RZ;  // PCG: r . z;  BiCGSTAB: rhat . r
     if (BICG) {
-      sc->rho = RR;  // rhat = r
-      sc->restart = 1;
+      if (restart) sc->restart = 1;
     } else {
-      sc->rho = RZ;
       sc->beta = 0.0;  // restart the search direction: p = z
     }
     if (!isfinite(RR)) sc->done = 3;
@@ -301,29 +333,19 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restri
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
   const float beta = (float)sc->beta;
-  double dot = 0.0;
-  FOLGB_NODE_BLOCKS(G) {
-    float acc[kRowsU][NDOF];
-    bool act[kRowsU];
-    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                       [&](int64_t d) { return fmaf(beta, __ldg(pold + d), __ldg(z + d)); }, acc,
-                                       act);
-    if (lane == 0) {
-#pragma unroll
-      for (int u = 0; u < kRowsU; ++u) {
-        if (!act[u]) continue;
-#pragma unroll
-        for (int i = 0; i < NDOF; ++i) {
-          const int64_t d = (int64_t)NDOF * (base + u) + i;
-          const float pn = fmaf(beta, pold[d], z[d]);
-          pnew[d] = pn;
-          q[d] = acc[u][i];
-          dot += (double)pn * (double)acc[u][i];
-        }
-      }
+  float dot = 0.f;  // this lane's rows only (a handful); fp64 from the block sum on
+  FOLGB_NODE_BLOCKS(NDOF, G) {
+    float sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                   [&](int64_t k) { return fmaf(beta, __ldg(pold + k), __ldg(z + k)); }, sum, d)) {
+      const float pn = fmaf(beta, pold[d], z[d]);
+      pnew[d] = pn;
+      q[d] = sum;
+      dot = fmaf(pn, sum, dot);
     }
   }
-  double s = block_sum_d(dot, sh);
+  double s = block_sum_d((double)dot, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (!last_block(&counters[1])) return;
   double PQ = sum_partials(part, gridDim.x, sh);
@@ -351,18 +373,18 @@ __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __re
   if (sc->done || sc->replace) return;
   const double alpha = sc->alpha;
   const float af = (float)alpha;
-  double rz = 0.0, rr = 0.0;
+  float rz = 0.f, rr = 0.f;  // per-thread partials over a few entries
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] = fma(alpha, (double)p[i], x[i]);
     const float ri = fmaf(-af, q[i], r[i]);
     r[i] = ri;
     const float zi = dinv[i] * ri;
     z[i] = zi;
-    rz += (double)ri * (double)zi;
-    rr += (double)ri * (double)ri;
+    rz = fmaf(ri, zi, rz);
+    rr = fmaf(ri, ri, rr);
   }
-  double s1 = block_sum_d(rz, sh);
-  double s2 = block_sum_d(rr, sh);
+  double s1 = block_sum_d((double)rz, sh);
+  double s2 = block_sum_d((double)rr, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s1;
     part[gridDim.x + blockIdx.x] = s2;
@@ -423,8 +445,6 @@ __global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __re
 
 // p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
 // v_new = A y; alpha = rho / (rhat . v_new)
-// p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
-// v_new = A y; alpha = rho / (rhat . v_new)
 template <int NDOF, int G>
 __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                      const int* __restrict__ adj, int maxdeg,
@@ -442,29 +462,20 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
   auto pval = [&](int64_t d) -> float {
     return rs ? __ldg(r + d) : fmaf(beta, fmaf(-omega, __ldg(vold + d), __ldg(pold + d)), __ldg(r + d));
   };
-  double dot = 0.0;
-  FOLGB_NODE_BLOCKS(G) {
-    float acc[kRowsU][NDOF];
-    bool act[kRowsU];
-    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                       [&](int64_t d) { return __ldg(dinv + d) * pval(d); }, acc, act);
-    if (lane == 0) {
-#pragma unroll
-      for (int u = 0; u < kRowsU; ++u) {
-        if (!act[u]) continue;
-#pragma unroll
-        for (int i = 0; i < NDOF; ++i) {
-          const int64_t d = (int64_t)NDOF * (base + u) + i;
-          const float pn = pval(d);
-          pnew[d] = pn;
-          y[d] = dinv[d] * pn;
-          vnew[d] = acc[u][i];
-          dot += (double)rhat[d] * (double)acc[u][i];
-        }
-      }
+  float dot = 0.f;
+  FOLGB_NODE_BLOCKS(NDOF, G) {
+    float sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                   [&](int64_t k) { return __ldg(dinv + k) * pval(k); }, sum, d)) {
+      const float pn = pval(d);
+      pnew[d] = pn;
+      y[d] = dinv[d] * pn;
+      vnew[d] = sum;
+      dot = fmaf(rhat[d], sum, dot);
     }
   }
-  double s = block_sum_d(dot, sh);
+  double s = block_sum_d((double)dot, sh);
   if (threadIdx.x == 0) part[blockIdx.x] = s;
   if (!last_block(&counters[1])) return;
   double RV = sum_partials(part, gridDim.x, sh);
@@ -474,7 +485,7 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
       sc->breakdowns += 1;
       if (!isfinite(RV)) sc->done = 3;
       else if (sc->breakdowns > kMaxBreakdowns) sc->done = 4;
-      else sc->replace = 1;
+      else sc->replace = 2;
     } else {
       sc->alpha = sc->rho / RV;
     }
@@ -494,30 +505,21 @@ __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __res
   if (sc->done || sc->replace) return;
   const float af = (float)sc->alpha;
   auto sval = [&](int64_t d) -> float { return fmaf(-af, __ldg(vnew + d), __ldg(r + d)); };
-  double ts = 0.0, tt = 0.0;
-  FOLGB_NODE_BLOCKS(G) {
-    float acc[kRowsU][NDOF];
-    bool act[kRowsU];
-    rows_multi<NDOF, G, kRowsU, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                       [&](int64_t d) { return __ldg(dinv + d) * sval(d); }, acc, act);
-    if (lane == 0) {
-#pragma unroll
-      for (int u = 0; u < kRowsU; ++u) {
-        if (!act[u]) continue;
-#pragma unroll
-        for (int i = 0; i < NDOF; ++i) {
-          const int64_t d = (int64_t)NDOF * (base + u) + i;
-          const float sv = sval(d);
-          z[d] = dinv[d] * sv;
-          t[d] = acc[u][i];
-          ts += (double)acc[u][i] * (double)sv;
-          tt += (double)acc[u][i] * (double)acc[u][i];
-        }
-      }
+  float ts = 0.f, tt = 0.f;
+  FOLGB_NODE_BLOCKS(NDOF, G) {
+    float sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                   [&](int64_t k) { return __ldg(dinv + k) * sval(k); }, sum, d)) {
+      const float sv = sval(d);
+      z[d] = dinv[d] * sv;
+      t[d] = sum;
+      ts = fmaf(sum, sv, ts);
+      tt = fmaf(sum, sum, tt);
     }
   }
-  double s1 = block_sum_d(ts, sh);
-  double s2 = block_sum_d(tt, sh);
+  double s1 = block_sum_d((double)ts, sh);
+  double s2 = block_sum_d((double)tt, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s1;
     part[gridDim.x + blockIdx.x] = s2;
@@ -540,17 +542,17 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
   if (sc->done || sc->replace) return;
   const double alpha = sc->alpha, omega = sc->omega;
   const float af = (float)alpha, of = (float)omega;
-  double rhr = 0.0, rr = 0.0;
+  float rhr = 0.f, rr = 0.f;  // per-thread partials over a few entries
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const float s = fmaf(-af, vnew[i], r[i]);
     x[i] = fma(omega, (double)z[i], fma(alpha, (double)y[i], x[i]));
     const float ri = fmaf(-of, t[i], s);
     r[i] = ri;
-    rhr += (double)rhat[i] * (double)ri;
-    rr += (double)ri * (double)ri;
+    rhr = fmaf(rhat[i], ri, rhr);
+    rr = fmaf(ri, ri, rr);
   }
-  double s1 = block_sum_d(rhr, sh);
-  double s2 = block_sum_d(rr, sh);
+  double s1 = block_sum_d((double)rhr, sh);
+  double s2 = block_sum_d((double)rr, sh);
   if (threadIdx.x == 0) {
     part[blockIdx.x] = s1;
     part[gridDim.x + blockIdx.x] = s2;
@@ -566,9 +568,8 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
     sc->iters += 1;
     sc->breakdowns = 0;
     if (!isfinite(RR)) sc->done = 3;
-    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2 || RH == 0.0 ||
-             omega == 0.0)
-      sc->replace = 1;
+    else if (RH == 0.0 || omega == 0.0) sc->replace = 2;  // breakdown: restart
+    else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2) sc->replace = 1;
     if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
     counters[2] = 0u;
   }
@@ -578,17 +579,26 @@ template <int NDOF>
 static int group_width(int maxdeg) {
   int g = 1;
   while (g < NDOF * maxdeg && g < 32) g <<= 1;
-  return g < 4 ? 4 : g;
+  return g < RowsU<NDOF>::VP ? RowsU<NDOF>::VP : g;
 }
 
 template <int NDOF, class F>
 static int with_group(int maxdeg, F&& f) {
+  constexpr int VP = RowsU<NDOF>::VP;  // group_width never returns less
   switch (group_width<NDOF>(maxdeg)) {
-    case 4: return f(std::integral_constant<int, 4>{});
-    case 8: return f(std::integral_constant<int, 8>{});
-    case 16: return f(std::integral_constant<int, 16>{});
-    default: return f(std::integral_constant<int, 32>{});
+    case 4:
+      if constexpr (VP <= 4) return f(std::integral_constant<int, 4>{});
+      break;
+    case 8:
+      if constexpr (VP <= 8) return f(std::integral_constant<int, 8>{});
+      break;
+    case 16:
+      if constexpr (VP <= 16) return f(std::integral_constant<int, 16>{});
+      break;
+    default:
+      break;
   }
+  return f(std::integral_constant<int, 32>{});
 }
 
 template <class F>
@@ -601,8 +611,10 @@ static int with_ndof(int ndof, F&& f) {
   return FOLGB_ERR_INVALID_ARGUMENT;
 }
 
+template <int NDOF>
 static int spmv_blocks(const folgb_plan* p, int G) {
-  int64_t threads = ((p->N + kRowsU - 1) / kRowsU) * (int64_t)G;
+  constexpr int U = RowsU<NDOF>::U;
+  int64_t threads = ((p->N + U - 1) / U) * (int64_t)G;
   int64_t blocks = (threads + 255) / 256;
   int64_t cap = (int64_t)num_sms() * 8;
   return (int)(blocks < cap ? blocks : cap);
@@ -650,7 +662,7 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
     constexpr int NDOF = decltype(nd)::value;
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
       constexpr int G = decltype(gw)::value;
-      const int sb = spmv_blocks(p, G);
+      const int sb = spmv_blocks<NDOF>(p, G);
       int guard = 0;
       while (true) {
         for (int k = 0; k < check_every; ++k) {
@@ -728,7 +740,7 @@ extern "C" int folgb_spmv(const folgb_plan* p, const float* vals, const float* x
     constexpr int NDOF = decltype(nd)::value;
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
       constexpr int G = decltype(gw)::value;
-      k_spmv<NDOF, G><<<spmv_blocks(p, G), 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, x, y);
+      k_spmv<NDOF, G><<<spmv_blocks<NDOF>(p, G), 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, x, y);
       FOLGB_LAUNCH_CHECK();
       return (int)FOLGB_OK;
     });

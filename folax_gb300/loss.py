@@ -339,8 +339,9 @@ class FiniteElementLoss:
                                            capi.ptr(ws), ws.numel(), repeats, capi.stream_handle(), C.byref(chosen),
                                            C.cast(times, C.c_void_p), 8)
         capi.check("folgb_autotune", rc)
-        n = HEX8_VARIANTS if (self.element_type == "hexahedron" and self.physics == capi.ELASTIC
-                              and self.num_gp == 2) else 1
+        tunable = (self.element_type == "hexahedron" and self.physics == capi.ELASTIC and self.num_gp == 2
+                   and self.loss_settings.get("kernel_variant", "auto") == "auto")
+        n = HEX8_VARIANTS if tunable else 1
         return {"chosen": chosen.value, "ms": [times[i] for i in range(n)]}
 
     def ComputeBatchLoss(self, batch_params, batch_dofs):

@@ -62,3 +62,16 @@ def rel_fro(a, b):
     b = np.asarray(b, dtype=np.float64)
     den = np.linalg.norm(b)
     return np.linalg.norm(a - b) / (den if den > 0 else 1.0)
+
+
+def c_oracle_loss(etype, physics, m, settings):
+    """The C FP64 oracle (thermal / elastic) with the same arguments."""
+    from oracle import c_oracle
+    mat = settings.get("material_dict", {})
+    return c_oracle.CLossOracle(etype, physics, m.nodes_coordinates, m.elements_nodes[ETYPE_NAME[etype]],
+                                dirichlet=settings["dirichlet_bc_dict"], node_sets=m.node_sets,
+                                num_gp=settings.get("num_gp", 1 if etype == "tet4" else 2),
+                                young=mat.get("young_modulus", 1.0), nu=mat.get("poisson_ratio", 0.3),
+                                body_force=settings.get("body_foce"), beta=settings.get("beta", 0.0),
+                                c=settings.get("c", 1.0), exponent=settings.get("loss_function_exponent", 1.0),
+                                control_layout=settings.get("control_layout", "nodal"))

@@ -125,6 +125,17 @@ def test_autotune_keeps_results_exact(cuda):
         assert rel_fro(x.cpu().numpy(), z) < TOL
 
 
+def test_autotune_keeps_a_forced_variant(cuda):
+    m = make_mesh("hex8", 4, seed=27)
+    s = _settings("hex8", "elastic", "element")
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 3})
+    rng = np.random.default_rng(28)
+    ctrl = 0.5 + rng.random((1, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
+    info = gl.Autotune(ctrl, u, repeats=2)
+    assert info["chosen"] == 3 and len(info["ms"]) == 1 and info["ms"][0] > 0
+
+
 @pytest.mark.parametrize("exponent,bf", [(1.5, None), (1.0, [0.3, -0.2, 0.1]), (2.0, [0.1, 0.2, 0.3])])
 def test_loss_exponent_body_force_broadcast(cuda, exponent, bf):
     m = make_mesh("hex8", 3, seed=3)
