@@ -43,6 +43,10 @@ FLUSH_BYTES = 512 * 1024 * 1024
 # grad u (72 FMA), stress (~20), B^T sigma (72 FMA), energy and dE (~25):
 # 4 x 72 x 2 + 75 = 651 flops, x 8 points = 5,208 flops; plus gathers ~0.
 FLOPS_PER_ELEMENT = 5208.0
+# DRAM bytes (read + write) of one k_hex8_elastic launch on the 64^3 workload,
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, variant 0):
+# 17,491,200 + 2,304.  Other mesh sizes report null.
+NCU_TRAFFIC_BYTES = {64: 17_493_504}
 
 
 def parse():
@@ -58,7 +62,7 @@ def parse():
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     ap.add_argument("--hex8-variant", type=int, default=None,
-                    help="force one hex8 kernel variant (0-5) instead of autotuning (profiling runs)")
+                    help="force one hex8 kernel variant (0-9) instead of autotuning (profiling runs)")
     ap.add_argument("--extras", default="pcg,batched,neohooke",
                     help="comma list of the extra measurements to run (pcg, batched, neohooke)")
     return ap.parse_args()
@@ -261,12 +265,21 @@ def extra_pcg(args, loss, ctrl):
     N = plan.num_nodes
     nnz = plan.nnz
     pairs = nnz // 9
-    spmv_bytes = 4 * nnz + 4 * pairs + 4 * (N + 1) + 4 * 3 * N + 8 * 3 * N
-    spmv_ms = t_s.value / max(1, n_s.value)
+    # plain SpMV y = A x (folgb_spmv), timed alone: values, adjacency, x and y
+    xv = torch.randn(plan.total_dofs, device="cuda")
+    yv = torch.empty_like(xv)
+    spmv = lambda: _capi.check("folgb_spmv", lib.folgb_spmv(plan.handle, _capi.ptr(jac.data), _capi.ptr(xv),
+                                                          _capi.ptr(yv), _capi.stream_handle()))
+    for _ in range(3):
+        spmv()
+    spmv_ms = _events_ms(torch, spmv, 20)
+    spmv_bytes = 4 * nnz + 4 * pairs + 4 * (N + 1) + 4 * 3 * N + 4 * 3 * N
     peaks = measured_peaks() or {}
     return {"dofs": plan.total_dofs, "nnz": nnz, "assembly_ms": ms_asm, "iterations": info["iterations"],
             "status": info["status"], "solve_ms": wall * 1e3, "ms_per_iteration": wall * 1e3 / it,
-            "kernel_ms_per_iteration": (t_s.value + t_u.value) / it, "spmv_ms": spmv_ms,
+            "kernel_ms_per_iteration": (t_s.value + t_u.value) / it,
+            "pcg_spmv_kernel_ms": t_s.value / max(1, n_s.value), "pcg_update_kernel_ms": t_u.value / max(1, n_u.value),
+            "pcg_launches": [n_s.value, n_u.value], "spmv_ms": spmv_ms,
             "spmv_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
             "spmv_hbm_frac": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
             "true_relative_residual": float(res),
@@ -596,7 +609,10 @@ def main():
                             "autotune": {"chosen_variant": tune["chosen"], "ms_per_variant": tune["ms"],
                                          "variants": HEX8_VARIANT_NAMES}},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm, "traffic": None,
+                             "frac": achieved / hbm,
+                             "traffic": NCU_TRAFFIC_BYTES.get(args.n),
+                             "traffic_unit": "bytes per launch (ncu dram read + write)",
+                             "algorithmic_bytes": alg_bytes,
                              "kernel": "k_hex8_elastic (sum-factorised hex8 2x2x2)",
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                              "fp32": {"achieved_tflops": fp32_achieved, "nominal_peak_tflops": fp32_peak,

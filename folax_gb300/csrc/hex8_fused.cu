@@ -106,9 +106,13 @@ __device__ __forceinline__ void butterfly4_t(const float (&v)[4], float& A, floa
 //   ACC 0: keep the 36 per-direction point sums, adjoint butterflies at the end;
 //   ACC 1: accumulate the dual Hadamard coefficients point by point
 //          (21 accumulators instead of 36: fewer registers, ~14% more adds);
-//   BLOCK: threads per block (sets the register cap through __launch_bounds__).
-template <int CL, int MODE, bool BF, int ACC, int BLOCK>
-__global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_hex8_elastic(const VecArgs A) {
+//   BLOCK: threads per block; the register cap is 128 (512 resident threads
+//          per SM) through __launch_bounds__, or REGS for the
+//          k_hex8_elastic_regs wrapper: each SM sub-partition holds 16,384
+//          registers, so 96 registers give 5 resident warps per partition
+//          (20 per SM) and 80 give 6 (24 per SM), at the price of spills.
+template <int CL, int MODE, bool BF, int ACC>
+__device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
   __shared__ float red[32];
   const int b = blockIdx.y;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -317,11 +321,28 @@ __global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_hex8_elastic(const VecAr
   }
 }
 
+template <int CL, int MODE, bool BF, int ACC, int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 512 / BLOCK) k_hex8_elastic(const VecArgs A) {
+  hex8_elastic_body<CL, MODE, BF, ACC>(A);
+}
+
+template <int CL, int MODE, bool BF, int ACC, int REGS>
+__global__ void __maxnreg__(REGS) k_hex8_elastic_regs(const VecArgs A) {
+  hex8_elastic_body<CL, MODE, BF, ACC>(A);
+}
+
 template <int CL, int MODE, int ACC, int BLOCK>
 static void launch_variant(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
   dim3 g2((unsigned)((A.E + BLOCK - 1) / BLOCK), grid.y);
   if (bf) k_hex8_elastic<CL, MODE, true, ACC, BLOCK><<<g2, BLOCK, 0, s>>>(A);
   else k_hex8_elastic<CL, MODE, false, ACC, BLOCK><<<g2, BLOCK, 0, s>>>(A);
+}
+
+template <int CL, int MODE, int ACC, int REGS>
+static void launch_variant_regs(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
+  dim3 g2((unsigned)((A.E + 127) / 128), grid.y);
+  if (bf) k_hex8_elastic_regs<CL, MODE, true, ACC, REGS><<<g2, 128, 0, s>>>(A);
+  else k_hex8_elastic_regs<CL, MODE, false, ACC, REGS><<<g2, 128, 0, s>>>(A);
 }
 
 template <int CL, int MODE>
@@ -332,17 +353,21 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
     case 2: launch_variant<CL, MODE, 1, 256>(A, grid, bf, s); break;
     case 3: launch_variant<CL, MODE, 1, 128>(A, grid, bf, s); break;
     case 4: launch_variant<CL, MODE, 0, 64>(A, grid, bf, s); break;
-    default: launch_variant<CL, MODE, 1, 64>(A, grid, bf, s); break;
+    case 5: launch_variant<CL, MODE, 1, 64>(A, grid, bf, s); break;
+    case 6: launch_variant_regs<CL, MODE, 0, 96>(A, grid, bf, s); break;
+    case 7: launch_variant_regs<CL, MODE, 1, 96>(A, grid, bf, s); break;
+    case 8: launch_variant_regs<CL, MODE, 0, 80>(A, grid, bf, s); break;
+    default: launch_variant_regs<CL, MODE, 1, 80>(A, grid, bf, s); break;
   }
 }
 
 // Number of sum-factorised variants the autotuner may choose from.
-constexpr int kHex8Variants = 6;
+constexpr int kHex8Variants = 10;
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's
 // block count is recomputed for the variant's block size; the caller's
-// partial-sum buffers are sized for the smallest block (128 threads).
+// partial-sum buffers are sized for the smallest block (64 threads).
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2) return 0;
   const int variant = p->hex8_variant;

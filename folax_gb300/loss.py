@@ -29,9 +29,11 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 6
+HEX8_VARIANTS = 10
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
-                      "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients"]
+                      "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
+                      "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
+                      "128 thr, 80 regs, point sums", "128 thr, 80 regs, dual coefficients"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 
@@ -44,6 +46,8 @@ def _dev(x, dtype=None):
     torch = _torch()
     dtype = dtype or torch.float32
     if isinstance(x, torch.Tensor):
+        if x.is_cuda and x.dtype == dtype and x.is_contiguous():
+            return x  # already usable: no conversion call on the hot path
         return x.to(device="cuda", dtype=dtype).contiguous()
     return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda").contiguous()
 
@@ -76,15 +80,21 @@ class Plan:
         self.num_nodes = len(xyz3)
         self.has_csr = bool(build_csr)
         self._ws = {}
+        self._ws_fit = {}  # (op, batch) -> a buffer known to be large enough
         self._pattern = None
 
     def workspace(self, op: int, batch: int = 1):
+        buf = self._ws_fit.get((op, batch))
+        if buf is not None:
+            return buf
         torch = _torch()
         n = int(self.lib.folgb_workspace_bytes(self.handle, op, batch))
         buf = self._ws.get(op)
         if buf is None or buf.numel() < n:
             buf = torch.empty(max(n, 256), dtype=torch.uint8, device="cuda")
             self._ws[op] = buf
+            self._ws_fit = {k: v for k, v in self._ws_fit.items() if k[0] != op}
+        self._ws_fit[(op, batch)] = buf
         return buf
 
     def set_dirichlet_values(self, values: np.ndarray, load_increment: float = 1.0):
@@ -333,11 +343,11 @@ class FiniteElementLoss:
         dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda")
         ws = self._plan.workspace(capi.OP_LOSS_ADJOINT, B)
         chosen = C.c_int32()
-        times = (C.c_float * 8)()
+        times = (C.c_float * 16)()
         rc = self._plan.lib.folgb_autotune(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1],
                                            capi.ptr(U), U.shape[1], capi.ptr(losses), capi.ptr(du), capi.ptr(dp),
                                            capi.ptr(ws), ws.numel(), repeats, capi.stream_handle(), C.byref(chosen),
-                                           C.cast(times, C.c_void_p), 8)
+                                           C.cast(times, C.c_void_p), 16)
         capi.check("folgb_autotune", rc)
         tunable = (self.element_type == "hexahedron" and self.physics == capi.ELASTIC and self.num_gp == 2
                    and self.loss_settings.get("kernel_variant", "auto") == "auto")
