@@ -75,6 +75,11 @@ PROTOTYPES = {
     "folgb_batch_plan_destroy": (C.c_int, [vp]),
     "folgb_batch_workspace_bytes": (sz, [vp]),
     "folgb_batch_loss_adjoint": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_fourier_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, i32, vp, i64, f64, f64, f64, f64, f64]),
+    "folgb_fourier_destroy": (C.c_int, [vp]),
+    "folgb_fourier_forward": (C.c_int, [vp, i32, vp, vp, vp]),
+    "folgb_fourier_workspace_bytes": (sz, [vp, i32]),
+    "folgb_fourier_backward": (C.c_int, [vp, i32, vp, vp, vp, vp, sz, vp]),
     "folgb_trace_enable": (C.c_int, [i32]),
     "folgb_trace_reset": (C.c_int, []),
     "folgb_trace_read": (C.c_int, [i32, C.POINTER(i64), C.POINTER(f64)]),
@@ -123,7 +128,19 @@ def ptr(t) -> int | None:
     return t.ctypes.data
 
 
+_RAW_STREAM = None
+
+
 def stream_handle(stream=None) -> int:
+    """cudaStream_t of `stream`, or of torch's current stream on the current
+    device (through torch's raw-stream query when it has one: ~0.2 us instead
+    of ~3 us for building a Stream object on every call)."""
+    global _RAW_STREAM
     import torch
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return s.cuda_stream
+    if stream is not None:
+        return stream.cuda_stream
+    if _RAW_STREAM is None:
+        raw = getattr(torch._C, "_cuda_getCurrentRawStream", None)
+        _RAW_STREAM = (lambda: raw(torch.cuda.current_device())) if raw is not None else \
+            (lambda: torch.cuda.current_stream().cuda_stream)
+    return _RAW_STREAM()

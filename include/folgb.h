@@ -246,6 +246,32 @@ int folgb_batch_loss_adjoint(const folgb_batch_plan* plan, const float* control,
                              float* dloss_ddofs, float* dloss_dcontrol, int32_t* device_status,
                              void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- nodal Fourier control ----------------------------------------------
+ * FourierControl (fol/controls/fourier_control.py:14-59) on the device: the
+ * map from Fourier coefficients to the nodal material field that precedes the
+ * loss in a FOL training step, and its vector-Jacobian product.  Replaces
+ * FourierControl.ComputeControlledVariables (:49-59) and the jax.grad of the
+ * loss with respect to the coefficients through it.
+ * Coefficients: [batch][1 + nx*ny*nz], the constant term first, then
+ * meshgrid(x_freqs, y_freqs, z_freqs, indexing="ij") flattened row-major
+ * (:44-45); scaled as coeffs * (scale_max - scale_min) + scale_min (:51-52).
+ * xyz: node coordinates (HOST, num_nodes x 3, doubles). */
+typedef struct folgb_fourier folgb_fourier;
+int folgb_fourier_create(folgb_fourier** control, const double* x_freqs, int32_t nx,
+                         const double* y_freqs, int32_t ny, const double* z_freqs, int32_t nz,
+                         const double* xyz, int64_t num_nodes, double min_value, double max_value,
+                         double beta, double scale_min, double scale_max);
+int folgb_fourier_destroy(folgb_fourier* control);
+/* values[b][n] = (max - min) * sigmoid(beta * (K_b(x_n) - 0.5)) + min. */
+int folgb_fourier_forward(const folgb_fourier* control, int32_t batch, const float* coeffs,
+                          float* values, void* stream);
+size_t folgb_fourier_workspace_bytes(const folgb_fourier* control, int32_t batch);
+/* dcoeffs[b][q] = sum_n dvalues[b][n] * d values[b][n] / d coeffs[b][q]
+ * (deterministic: per-block partials summed in a fixed order). */
+int folgb_fourier_backward(const folgb_fourier* control, int32_t batch, const float* coeffs,
+                           const float* dvalues, float* dcoeffs, void* workspace,
+                           size_t workspace_bytes, void* stream);
+
 /* ---- opt-in kernel tracing ------------------------------------------------
  * CUDA events recorded on the launching stream around every kernel of the
  * entry points above, summed per kernel id.  The reference's only tracing is

@@ -617,6 +617,43 @@ class FELossOracle:
 
 
 # ----------------------------------------------------------------------------
+# Nodal Fourier control (fol/controls/fourier_control.py:24-59)
+# ----------------------------------------------------------------------------
+
+def fourier_frequencies(x_freqs, y_freqs, z_freqs):
+    """meshgrid(x, y, z, indexing="ij") flattened row-major (fourier_control.py:44-45)."""
+    mx, my, mz = np.meshgrid(np.asarray(x_freqs, float), np.asarray(y_freqs, float), np.asarray(z_freqs, float),
+                             indexing="ij")
+    return np.stack([mx.ravel(), my.ravel(), mz.ravel()], axis=1)
+
+
+def fourier_basis(freqs, xyz):
+    """(F, N): cos(fx pi x) cos(fy pi y) cos(fz pi z) per frequency and node (:53-57)."""
+    X = np.asarray(xyz, dtype=np.float64)
+    return (np.cos(np.pi * freqs[:, 0:1] * X[None, :, 0]) * np.cos(np.pi * freqs[:, 1:2] * X[None, :, 1])
+            * np.cos(np.pi * freqs[:, 2:3] * X[None, :, 2]))
+
+
+def fourier_control_values(coeffs, freqs, xyz, vmin=1e-6, vmax=1.0, beta=1.0, scale_min=0.0, scale_max=1.0):
+    """ComputeControlledVariables (:49-59): coeffs (B, F+1) -> nodal values (B, N)."""
+    v = np.atleast_2d(np.asarray(coeffs, dtype=np.float64)) * (scale_max - scale_min) + scale_min
+    K = v[:, :1] / 2.0 + v[:, 1:] @ fourier_basis(freqs, xyz)
+    return (vmax - vmin) / (1.0 + np.exp(-beta * (K - 0.5))) + vmin
+
+
+def fourier_control_vjp(coeffs, dvalues, freqs, xyz, vmin=1e-6, vmax=1.0, beta=1.0, scale_min=0.0,
+                        scale_max=1.0):
+    """d(sum dvalues * values)/d coeffs (B, F+1): what jax.grad through the
+    control gives for a loss whose nodal-control gradient is dvalues."""
+    v = np.atleast_2d(np.asarray(coeffs, dtype=np.float64)) * (scale_max - scale_min) + scale_min
+    Phi = fourier_basis(freqs, xyz)
+    K = v[:, :1] / 2.0 + v[:, 1:] @ Phi
+    s = 1.0 / (1.0 + np.exp(-beta * (K - 0.5)))
+    g = np.atleast_2d(dvalues) * (vmax - vmin) * beta * s * (1.0 - s)
+    return (scale_max - scale_min) * np.concatenate([0.5 * g.sum(axis=1, keepdims=True), g @ Phi.T], axis=1)
+
+
+# ----------------------------------------------------------------------------
 # Solvers
 # ----------------------------------------------------------------------------
 

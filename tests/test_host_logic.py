@@ -68,14 +68,32 @@ def test_update_default_dict_drops_unknown_keys():
     assert d == {"a": 1, "b": 3}
 
 
-def test_fourier_control_matches_formula():
+def test_oracle_fourier_control_matches_formula():
     m = M.create_2D_square_mesh(1.0, 4)
-    fc = fields.FourierControl("E", {"x_freqs": np.array([2, 4]), "y_freqs": np.array([2]), "z_freqs": np.array([0]),
-                                     "beta": 20, "min": 0.1, "max": 1.0}, m)
-    fc.Initialize()
-    assert fc.GetNumberOfVariables() == 3
+    freqs = fo.fourier_frequencies([2, 4], [2], [0])
     v = np.array([0.3, 0.5, -0.2])
-    X = m.nodes_coordinates
+    X = np.zeros((m.GetNumberOfNodes(), 3))
+    X[:, :2] = m.nodes_coordinates[:, :2]
     K = 0.15 + 0.5 * np.cos(2 * np.pi * X[:, 0]) * np.cos(2 * np.pi * X[:, 1]) \
         - 0.2 * np.cos(4 * np.pi * X[:, 0]) * np.cos(2 * np.pi * X[:, 1])
-    np.testing.assert_allclose(fc.ComputeControlledVariables(v), 0.9 / (1 + np.exp(-20 * (K - 0.5))) + 0.1)
+    got = fo.fourier_control_values(v, freqs, X, vmin=0.1, vmax=1.0, beta=20)
+    np.testing.assert_allclose(got[0], 0.9 / (1 + np.exp(-20 * (K - 0.5))) + 0.1)
+
+
+def test_oracle_fourier_control_vjp_matches_central_differences():
+    rng = np.random.default_rng(8)
+    X = rng.random((40, 3))
+    freqs = fo.fourier_frequencies([1, 2], [0, 3], [1])
+    c = 0.3 * rng.standard_normal((2, len(freqs) + 1))
+    dv = rng.standard_normal((2, 40))
+    kw = dict(vmin=0.1, vmax=2.0, beta=3.0, scale_min=-0.5, scale_max=1.5)
+    g = fo.fourier_control_vjp(c, dv, freqs, X, **kw)
+    h = 1e-6
+    for b in range(2):
+        for q in range(c.shape[1]):
+            cp, cm = c.copy(), c.copy()
+            cp[b, q] += h
+            cm[b, q] -= h
+            fd = (np.sum(dv[b] * fo.fourier_control_values(cp[b], freqs, X, **kw)[0])
+                  - np.sum(dv[b] * fo.fourier_control_values(cm[b], freqs, X, **kw)[0])) / (2 * h)
+            assert abs(fd - g[b, q]) < 1e-7 * max(1.0, abs(fd))
