@@ -352,10 +352,12 @@ def extra_batched(args, n_inst=512, seed=11):
 def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
     """C4: tet4 Neo-Hookean (6-tet split of a 64^3 hex grid, 1 Gauss point),
     mu/lambda scaled by the two-phase field, batch 16: fused loss + adjoint
-    throughput; and the time of one Newton iteration (CSR tangent + BiCGSTAB)
-    on a 12^3 split.  The Neo-Hookean tangent of this model is indefinite at
-    the undeformed state (its stress there is -mu I), so Jacobi BiCGSTAB needs
-    thousands of iterations beyond ~16^3 and the Newton solve stays small."""
+    throughput; and the time of one Newton iteration (CSR tangent + Jacobi
+    BiCGSTAB with fp64 Krylov vectors, rtol 1e-6) on a 12^3 split.  The
+    Neo-Hookean model is not stress-free at C = I (S = -mu I): its first
+    tangent is indefinite and ill-conditioned, fp32 recurrences diverge on it,
+    and a full undamped Newton solve from u = 0 inverts elements beyond ~6^3,
+    so one iteration is timed."""
     import torch
     from folax_gb300 import fields
     from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra

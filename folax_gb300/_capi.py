@@ -32,7 +32,8 @@ QUAD4, HEX8, TET4 = 0, 1, 2
 THERMAL, ELASTIC, NEOHOOKE = 0, 1, 2
 CONTROL_NODAL, CONTROL_ELEMENT = 0, 1
 SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
-OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN = 0, 1, 2, 3
+OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4
+KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
 
 
 class FolgbError(RuntimeError):
@@ -69,6 +70,8 @@ PROTOTYPES = {
     "folgb_assemble": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_pcg": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
     "folgb_bicgstab": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
+    "folgb_krylov": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz,
+                               vp]),
     "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
     "folgb_adam_step": (C.c_int, [vp, vp, vp, vp, i64, vp, f32, f32, f32, f32, vp]),
     "folgb_batch_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), i32, vp, vp, vp, vp, vp, vp, i64, i32]),

@@ -656,6 +656,7 @@ static size_t layout_assemble(const folgb_plan* p, void* base, size_t cap, float
 }
 
 size_t pcg_workspace_bytes(const folgb_plan* p);
+size_t krylov64_workspace_bytes(const folgb_plan* p);
 
 static int mat_epb(int rec_size, int npts) {
   const int budget = 96 * 1024;
@@ -791,6 +792,7 @@ extern "C" size_t folgb_workspace_bytes(const folgb_plan* p, int32_t op, int32_t
     case FOLGB_OP_PLAIN: return layout_loss(p, batch, true, nullptr, 0, nullptr);
     case FOLGB_OP_ASSEMBLE: return layout_assemble(p, nullptr, 0, nullptr, nullptr);
     case FOLGB_OP_PCG: return pcg_workspace_bytes(p);
+    case FOLGB_OP_KRYLOV64: return krylov64_workspace_bytes(p);
   }
   return 0;
 }

@@ -36,12 +36,15 @@ struct KScalars {
 };
 // done: 1 converged (true residual), 2 maxiter, 3 non-finite, 4 repeated breakdown or divergence
 
+// Krylov vectors in VT (float, or double for ill-conditioned / indefinite
+// systems such as the Neo-Hookean tangent); the iterate is always fp64.
+template <class VT>
 struct KWork {
-  float *r, *z, *p0, *p1, *q;   // PCG: r, z, p (two buffers), q = A p
-  float *rhat, *v0, *v1, *y, *t;  // BiCGSTAB extras
-  double* x;                    // fp64 iterate
-  double* part;                 // [2][65536]
-  unsigned* counters;           // [8]
+  VT *r, *z, *p0, *p1, *q;   // PCG: r, z, p (two buffers), q = A p
+  VT *rhat, *v0, *v1, *y, *t;  // BiCGSTAB extras
+  double* x;                 // fp64 iterate
+  double* part;              // [2][65536]
+  unsigned* counters;        // [8]
   KScalars* sc;
 };
 
@@ -50,20 +53,21 @@ constexpr double kReplaceDrop2 = 1e-6;  // replace when |r|^2 <= 1e-6 |r_true|^2
 constexpr int kMaxBreakdowns = 8;       // consecutive breakdown restarts before giving up
 constexpr double kDiverge2 = 1e12;      // stop when |r_true|^2 > 1e12 |b|^2 (diverged)
 
-static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork* w) {
+template <class VT>
+static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork<VT>* w) {
   Bump bp(base, cap);
   const size_t n = (size_t)p->ndof * p->N;
-  KWork t;
-  t.r = bp.take<float>(n);
-  t.z = bp.take<float>(n);
-  t.p0 = bp.take<float>(n);
-  t.p1 = bp.take<float>(n);
-  t.q = bp.take<float>(n);
-  t.rhat = bp.take<float>(n);
-  t.v0 = bp.take<float>(n);
-  t.v1 = bp.take<float>(n);
-  t.y = bp.take<float>(n);
-  t.t = bp.take<float>(n);
+  KWork<VT> t;
+  t.r = bp.take<VT>(n);
+  t.z = bp.take<VT>(n);
+  t.p0 = bp.take<VT>(n);
+  t.p1 = bp.take<VT>(n);
+  t.q = bp.take<VT>(n);
+  t.rhat = bp.take<VT>(n);
+  t.v0 = bp.take<VT>(n);
+  t.v1 = bp.take<VT>(n);
+  t.y = bp.take<VT>(n);
+  t.t = bp.take<VT>(n);
   t.x = bp.take<double>(n);
   t.part = bp.take<double>(2 * 65536);
   t.counters = bp.take<unsigned>(8);
@@ -72,7 +76,11 @@ static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork* 
   return align_up(bp.off);
 }
 
-size_t pcg_workspace_bytes(const folgb_plan* p) { return layout_krylov(p, nullptr, 0, nullptr); }
+size_t pcg_workspace_bytes(const folgb_plan* p) { return layout_krylov<float>(p, nullptr, 0, nullptr); }
+size_t krylov64_workspace_bytes(const folgb_plan* p) { return layout_krylov<double>(p, nullptr, 0, nullptr); }
+
+__device__ __forceinline__ float vfma(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double vfma(double a, double b, double c) { return fma(a, b, c); }
 
 __device__ __forceinline__ bool last_block(unsigned* counter) {
   __shared__ bool last;
@@ -211,19 +219,19 @@ __global__ void __launch_bounds__(256) k_spmv(int64_t N, const int* __restrict__
 // ---------------------------------------------------------------------------
 // shared: fp64 true residual r = b - A x (reliable update / restart)
 // ---------------------------------------------------------------------------
-template <int NDOF, int G, bool BICG>
+template <int NDOF, int G, bool BICG, class VT>
 __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __restrict__ adj_ptr,
                                                        const int* __restrict__ adj, int maxdeg,
                                                        const float* __restrict__ vals, const float* __restrict__ b,
                                                        const float* __restrict__ dinv, const double* __restrict__ x,
-                                                       float* __restrict__ r, float* __restrict__ z,
-                                                       float* __restrict__ rhat, double* part, unsigned* counters,
+                                                       VT* __restrict__ r, VT* __restrict__ z,
+                                                       VT* __restrict__ rhat, double* part, unsigned* counters,
                                                        KScalars* sc) {
   __shared__ double sh[32];
   // BiCGSTAB keeps its shadow residual and directions across a residual
   // replacement; only a breakdown (replace == 2) restarts it from rhat = r.
   const bool restart = BICG && sc->replace == 2;
-  float rzf = 0.f;
+  VT rzf = VT(0);
   double rr = 0.0;
   FOLGB_NODE_BLOCKS(NDOF, G) {
     double sum;
@@ -231,17 +239,17 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
     if (rows_multi<NDOF, G, double>(N, adj_ptr, adj, vals, maxdeg, base, lane, [&](int64_t k) { return x[k]; },
                                     sum, d)) {
       const double ri = (double)b[d] - sum;
-      const float rf = (float)ri;
+      const VT rf = (VT)ri;
       r[d] = rf;
       if (!BICG) {
-        const float zf = dinv[d] * rf;
+        const VT zf = (VT)dinv[d] * rf;
         z[d] = zf;
-        rzf = fmaf(rf, zf, rzf);
+        rzf = vfma(rf, zf, rzf);
       } else if (restart) {
         rhat[d] = rf;
-        rzf = fmaf(rf, rf, rzf);
+        rzf = vfma(rf, rf, rzf);
       } else {
-        rzf = fmaf(rhat[d], rf, rzf);
+        rzf = vfma(rhat[d], rf, rzf);
       }
       rr = fma(ri, ri, rr);
     }
@@ -280,10 +288,10 @@ __global__ void k_to_float(int64_t n, const double* __restrict__ x, float* __res
 // ---------------------------------------------------------------------------
 // Jacobi PCG
 // ---------------------------------------------------------------------------
+template <class VT>
 __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* __restrict__ dinv,
-                           double* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
-                           float* __restrict__ p0, double* part, unsigned* counters, KScalars* sc, double rtol,
-                           int maxiter) {
+                           double* __restrict__ x, VT* __restrict__ r, VT* __restrict__ z, VT* __restrict__ p0,
+                           double* part, unsigned* counters, KScalars* sc, double rtol, int maxiter) {
   __shared__ double sh[32];
   double rz = 0.0, bb = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
@@ -292,7 +300,7 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
     x[i] = 0.0;
     r[i] = bi;
     z[i] = zi;
-    p0[i] = 0.f;
+    p0[i] = VT(0);
     rz += (double)bi * (double)zi;
     bb += (double)bi * (double)bi;
   }
@@ -323,26 +331,26 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
   }
 }
 
-template <int NDOF, int G>
+template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                   const int* __restrict__ adj, int maxdeg,
-                                                  const float* __restrict__ vals, const float* __restrict__ z,
-                                                  const float* __restrict__ pold, float* __restrict__ pnew,
-                                                  float* __restrict__ q, double* part, unsigned* counters,
+                                                  const float* __restrict__ vals, const VT* __restrict__ z,
+                                                  const VT* __restrict__ pold, VT* __restrict__ pnew,
+                                                  VT* __restrict__ q, double* part, unsigned* counters,
                                                   KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
-  const float beta = (float)sc->beta;
-  float dot = 0.f;  // this lane's rows only (a handful); fp64 from the block sum on
+  const VT beta = (VT)sc->beta;
+  VT dot = VT(0);  // this lane's rows only (a handful); fp64 from the block sum on
   FOLGB_NODE_BLOCKS(NDOF, G) {
-    float sum;
+    VT sum;
     int64_t d;
-    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                   [&](int64_t k) { return fmaf(beta, __ldg(pold + k), __ldg(z + k)); }, sum, d)) {
-      const float pn = fmaf(beta, pold[d], z[d]);
+    if (rows_multi<NDOF, G, VT>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                [&](int64_t k) { return vfma(beta, __ldg(pold + k), __ldg(z + k)); }, sum, d)) {
+      const VT pn = vfma(beta, pold[d], z[d]);
       pnew[d] = pn;
       q[d] = sum;
-      dot = fmaf(pn, sum, dot);
+      dot = vfma(pn, sum, dot);
     }
   }
   double s = block_sum_d((double)dot, sh);
@@ -364,24 +372,24 @@ __global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restri
   }
 }
 
+template <class VT>
 __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __restrict__ dinv,
-                                                    double* __restrict__ x, float* __restrict__ r,
-                                                    float* __restrict__ z, const float* __restrict__ p,
-                                                    const float* __restrict__ q, double* part, unsigned* counters,
-                                                    KScalars* sc) {
+                                                    double* __restrict__ x, VT* __restrict__ r, VT* __restrict__ z,
+                                                    const VT* __restrict__ p, const VT* __restrict__ q, double* part,
+                                                    unsigned* counters, KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
   const double alpha = sc->alpha;
-  const float af = (float)alpha;
-  float rz = 0.f, rr = 0.f;  // per-thread partials over a few entries
+  const VT af = (VT)alpha;
+  VT rz = VT(0), rr = VT(0);  // per-thread partials over a few entries
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     x[i] = fma(alpha, (double)p[i], x[i]);
-    const float ri = fmaf(-af, q[i], r[i]);
+    const VT ri = vfma(-af, q[i], r[i]);
     r[i] = ri;
-    const float zi = dinv[i] * ri;
+    const VT zi = (VT)dinv[i] * ri;
     z[i] = zi;
-    rz = fmaf(ri, zi, rz);
-    rr = fmaf(ri, ri, rr);
+    rz = vfma(ri, zi, rz);
+    rr = vfma(ri, ri, rr);
   }
   double s1 = block_sum_d((double)rz, sh);
   double s2 = block_sum_d((double)rr, sh);
@@ -409,8 +417,9 @@ __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __re
 // Jacobi BiCGSTAB (right preconditioned): y = D^-1 p, z = D^-1 s,
 // x += alpha y + omega z.  Three kernels per iteration.
 // ---------------------------------------------------------------------------
-__global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __restrict__ x, float* __restrict__ r,
-                            float* __restrict__ rhat, double* part, unsigned* counters, KScalars* sc, double rtol,
+template <class VT>
+__global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __restrict__ x, VT* __restrict__ r,
+                            VT* __restrict__ rhat, double* part, unsigned* counters, KScalars* sc, double rtol,
                             int maxiter) {
   __shared__ double sh[32];
   double bb = 0.0;
@@ -445,34 +454,34 @@ __global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __re
 
 // p_new = r + beta (p_old - omega v_old) (p_new = r on restart), y = D^-1 p_new,
 // v_new = A y; alpha = rho / (rhat . v_new)
-template <int NDOF, int G>
+template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                      const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
-                                                     const float* __restrict__ r, const float* __restrict__ rhat,
-                                                     const float* __restrict__ pold, const float* __restrict__ vold,
-                                                     float* __restrict__ pnew, float* __restrict__ y,
-                                                     float* __restrict__ vnew, double* part, unsigned* counters,
+                                                     const VT* __restrict__ r, const VT* __restrict__ rhat,
+                                                     const VT* __restrict__ pold, const VT* __restrict__ vold,
+                                                     VT* __restrict__ pnew, VT* __restrict__ y,
+                                                     VT* __restrict__ vnew, double* part, unsigned* counters,
                                                      KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
   const bool rs = sc->restart != 0;
-  const float beta = rs ? 0.f : (float)sc->beta;
-  const float omega = rs ? 0.f : (float)sc->omega;
-  auto pval = [&](int64_t d) -> float {
-    return rs ? __ldg(r + d) : fmaf(beta, fmaf(-omega, __ldg(vold + d), __ldg(pold + d)), __ldg(r + d));
+  const VT beta = rs ? VT(0) : (VT)sc->beta;
+  const VT omega = rs ? VT(0) : (VT)sc->omega;
+  auto pval = [&](int64_t d) -> VT {
+    return rs ? __ldg(r + d) : vfma(beta, vfma(-omega, __ldg(vold + d), __ldg(pold + d)), __ldg(r + d));
   };
-  float dot = 0.f;
+  VT dot = VT(0);
   FOLGB_NODE_BLOCKS(NDOF, G) {
-    float sum;
+    VT sum;
     int64_t d;
-    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                   [&](int64_t k) { return __ldg(dinv + k) * pval(k); }, sum, d)) {
-      const float pn = pval(d);
+    if (rows_multi<NDOF, G, VT>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                [&](int64_t k) { return (VT)__ldg(dinv + k) * pval(k); }, sum, d)) {
+      const VT pn = pval(d);
       pnew[d] = pn;
-      y[d] = dinv[d] * pn;
+      y[d] = (VT)dinv[d] * pn;
       vnew[d] = sum;
-      dot = fmaf(rhat[d], sum, dot);
+      dot = vfma(rhat[d], sum, dot);
     }
   }
   double s = block_sum_d((double)dot, sh);
@@ -494,28 +503,28 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
 }
 
 // s = r - alpha v_new, z = D^-1 s, t = A z; omega = (t . s) / (t . t)
-template <int NDOF, int G>
+template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                      const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
-                                                     const float* __restrict__ r, const float* __restrict__ vnew,
-                                                     float* __restrict__ z, float* __restrict__ t, double* part,
+                                                     const VT* __restrict__ r, const VT* __restrict__ vnew,
+                                                     VT* __restrict__ z, VT* __restrict__ t, double* part,
                                                      unsigned* counters, KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
-  const float af = (float)sc->alpha;
-  auto sval = [&](int64_t d) -> float { return fmaf(-af, __ldg(vnew + d), __ldg(r + d)); };
-  float ts = 0.f, tt = 0.f;
+  const VT af = (VT)sc->alpha;
+  auto sval = [&](int64_t d) -> VT { return vfma(-af, __ldg(vnew + d), __ldg(r + d)); };
+  VT ts = VT(0), tt = VT(0);
   FOLGB_NODE_BLOCKS(NDOF, G) {
-    float sum;
+    VT sum;
     int64_t d;
-    if (rows_multi<NDOF, G, float>(N, adj_ptr, adj, vals, maxdeg, base, lane,
-                                   [&](int64_t k) { return __ldg(dinv + k) * sval(k); }, sum, d)) {
-      const float sv = sval(d);
-      z[d] = dinv[d] * sv;
+    if (rows_multi<NDOF, G, VT>(N, adj_ptr, adj, vals, maxdeg, base, lane,
+                                [&](int64_t k) { return (VT)__ldg(dinv + k) * sval(k); }, sum, d)) {
+      const VT sv = sval(d);
+      z[d] = (VT)dinv[d] * sv;
       t[d] = sum;
-      ts = fmaf(sum, sv, ts);
-      tt = fmaf(sum, sum, tt);
+      ts = vfma(sum, sv, ts);
+      tt = vfma(sum, sum, tt);
     }
   }
   double s1 = block_sum_d((double)ts, sh);
@@ -533,23 +542,24 @@ __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __res
   }
 }
 
-__global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restrict__ x, float* __restrict__ r,
-                                                     const float* __restrict__ rhat, const float* __restrict__ vnew,
-                                                     const float* __restrict__ y, const float* __restrict__ z,
-                                                     const float* __restrict__ t, double* part, unsigned* counters,
+template <class VT>
+__global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restrict__ x, VT* __restrict__ r,
+                                                     const VT* __restrict__ rhat, const VT* __restrict__ vnew,
+                                                     const VT* __restrict__ y, const VT* __restrict__ z,
+                                                     const VT* __restrict__ t, double* part, unsigned* counters,
                                                      KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
   const double alpha = sc->alpha, omega = sc->omega;
-  const float af = (float)alpha, of = (float)omega;
-  float rhr = 0.f, rr = 0.f;  // per-thread partials over a few entries
+  const VT af = (VT)alpha, of = (VT)omega;
+  VT rhr = VT(0), rr = VT(0);  // per-thread partials over a few entries
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float s = fmaf(-af, vnew[i], r[i]);
+    const VT s = vfma(-af, vnew[i], r[i]);
     x[i] = fma(omega, (double)z[i], fma(alpha, (double)y[i], x[i]));
-    const float ri = fmaf(-of, t[i], s);
+    const VT ri = vfma(-of, t[i], s);
     r[i] = ri;
-    rhr = fmaf(rhat[i], ri, rhr);
-    rr = fmaf(ri, ri, rr);
+    rhr = vfma(rhat[i], ri, rhr);
+    rr = vfma(ri, ri, rr);
   }
   double s1 = block_sum_d((double)rhr, sh);
   double s2 = block_sum_d((double)rr, sh);
@@ -638,13 +648,14 @@ __global__ void k_step_inc(int* step) { *step += 1; }
 
 enum { SOLVER_CG = 0, SOLVER_BICGSTAB = 1 };
 
+template <class VT>
 static int krylov_solve(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
                         float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
                         double* rel_residual, void* workspace, size_t workspace_bytes, cudaStream_t s) {
   if (!p || !vals || !dinv || !rhs || !x || maxiter <= 0 || !(rtol >= 0.0)) return FOLGB_ERR_INVALID_ARGUMENT;
   if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
-  KWork w;
-  size_t need = layout_krylov(p, workspace, workspace_bytes, &w);
+  KWork<VT> w;
+  size_t need = layout_krylov<VT>(p, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   if (check_every <= 0) check_every = 32;
   const int64_t n = (int64_t)p->ndof * p->N;
@@ -652,12 +663,12 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
   if (vb > kVecBlocks) vb = kVecBlocks;
   FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, 8 * sizeof(unsigned), s));
   if (solver == SOLVER_CG)
-    k_pcg_init<<<vb, 256, 0, s>>>(n, rhs, dinv, w.x, w.r, w.z, w.p0, w.part, w.counters, w.sc, rtol, maxiter);
+    k_pcg_init<VT><<<vb, 256, 0, s>>>(n, rhs, dinv, w.x, w.r, w.z, w.p0, w.part, w.counters, w.sc, rtol, maxiter);
   else
-    k_bicg_init<<<vb, 256, 0, s>>>(n, rhs, w.x, w.r, w.rhat, w.part, w.counters, w.sc, rtol, maxiter);
+    k_bicg_init<VT><<<vb, 256, 0, s>>>(n, rhs, w.x, w.r, w.rhat, w.part, w.counters, w.sc, rtol, maxiter);
   FOLGB_LAUNCH_CHECK();
   KScalars host{};
-  float *pa = w.p0, *pb = w.p1, *va = w.v0, *vb_ = w.v1;
+  VT *pa = w.p0, *pb = w.p1, *va = w.v0, *vb_ = w.v1;
   int rc = with_ndof(p->ndof, [&](auto nd) -> int {
     constexpr int NDOF = decltype(nd)::value;
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
@@ -668,22 +679,22 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         for (int k = 0; k < check_every; ++k) {
           if (solver == SOLVER_CG) {
             trace_begin(KID_PCG_SPMV, s);
-            k_pcg_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
+            k_pcg_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
                                                     w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, s);
             trace_begin(KID_PCG_UPDATE, s);
-            k_pcg_update<<<vb, 256, 0, s>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
+            k_pcg_update<VT><<<vb, 256, 0, s>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_UPDATE, s);
             std::swap(pa, pb);
           } else {
             trace_begin(KID_PCG_SPMV, s);
-            k_bicg_p_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
+            k_bicg_p_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
                                                        w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
-            k_bicg_s_spmv<NDOF, G><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
+            k_bicg_s_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
                                                        vb_, w.z, w.t, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, s);
             trace_begin(KID_PCG_UPDATE, s);
-            k_bicg_update<<<vb, 256, 0, s>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
+            k_bicg_update<VT><<<vb, 256, 0, s>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
             trace_end(KID_PCG_UPDATE, s);
             std::swap(pa, pb);
             std::swap(va, vb_);
@@ -695,10 +706,10 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         if (host.done) break;
         if (host.replace) {
           if (solver == SOLVER_CG)
-            k_true_residual<NDOF, G, false><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
+            k_true_residual<NDOF, G, false, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
                                                                 dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
           else
-            k_true_residual<NDOF, G, true><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
+            k_true_residual<NDOF, G, true, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
                                                                dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
           FOLGB_LAUNCH_CHECK();
           FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
@@ -750,15 +761,30 @@ extern "C" int folgb_spmv(const folgb_plan* p, const float* vals, const float* x
 extern "C" int folgb_pcg(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
                          double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations, double* rel_residual,
                          void* workspace, size_t workspace_bytes, void* stream) {
-  return krylov_solve(p, SOLVER_CG, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+  return krylov_solve<float>(p, SOLVER_CG, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
                       workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int folgb_bicgstab(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
                               double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
                               double* rel_residual, void* workspace, size_t workspace_bytes, void* stream) {
-  return krylov_solve(p, SOLVER_BICGSTAB, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
-                      workspace, workspace_bytes, (cudaStream_t)stream);
+  return krylov_solve<float>(p, SOLVER_BICGSTAB, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations,
+                             rel_residual, workspace, workspace_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int folgb_krylov(const folgb_plan* p, int32_t method, int32_t vector_bits, const float* vals,
+                            const float* dinv, const float* rhs, float* x, double rtol, int32_t maxiter,
+                            int32_t check_every, int32_t* iterations, double* rel_residual, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  if (method != FOLGB_KRYLOV_CG && method != FOLGB_KRYLOV_BICGSTAB) return FOLGB_ERR_INVALID_ARGUMENT;
+  const int solver = method == FOLGB_KRYLOV_CG ? SOLVER_CG : SOLVER_BICGSTAB;
+  if (vector_bits == 32)
+    return krylov_solve<float>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                               workspace, workspace_bytes, (cudaStream_t)stream);
+  if (vector_bits == 64)
+    return krylov_solve<double>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                                workspace, workspace_bytes, (cudaStream_t)stream);
+  return FOLGB_ERR_INVALID_ARGUMENT;
 }
 
 extern "C" int folgb_adam_step(float* params, const float* grads, float* m, float* v, int64_t n, int32_t* step,

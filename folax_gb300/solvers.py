@@ -58,7 +58,7 @@ class FiniteElementSolver(Solver):
         self.fe_loss_function = fe_loss_function
         self.fe_solver_settings = fe_solver_settings
         self.linear_solver_settings = {"solver": "JAX-bicgstab", "tol": 1e-6, "atol": 1e-6, "maxiter": 1000,
-                                       "pre-conditioner": "ilu", "check_every": 32}
+                                       "pre-conditioner": "ilu", "check_every": 32, "vector_precision": "auto"}
         self.last_linear_info = None
 
     def Initialize(self) -> None:
@@ -75,32 +75,45 @@ class FiniteElementSolver(Solver):
         # nonsymmetric / indefinite tangents): Jacobi-BiCGSTAB.
         self.LinearSolve = self.PCGLinearSolver if name == "GB300-pcg" else self.BiCGSTABLinearSolver
 
-    def _krylov(self, fn_name, tangent_matrix, residual_vector):
+    def _vector_bits(self) -> int:
+        """Krylov vector precision: "fp32", "fp64", or "auto" (fp64 for the
+        Neo-Hookean tangent, which is indefinite near u = 0 and defeats fp32
+        recurrences; fp32 otherwise)."""
+        v = self.linear_solver_settings.get("vector_precision", "auto")
+        if v == "auto":
+            return 64 if getattr(self.fe_loss_function, "physics", None) == capi.NEOHOOKE else 32
+        if v not in ("fp32", "fp64"):
+            raise ValueError(f"vector_precision must be auto, fp32 or fp64, not {v}")
+        return 64 if v == "fp64" else 32
+
+    def _krylov(self, method, tangent_matrix, residual_vector):
         torch = _torch()
         plan = tangent_matrix.plan
         b = -_dev(residual_vector)
         x = torch.empty_like(b)
-        ws = plan.workspace(capi.OP_PCG)
+        bits = self._vector_bits()
+        ws = plan.workspace(capi.OP_KRYLOV64 if bits == 64 else capi.OP_PCG)
         iters, rel = C.c_int32(), C.c_double()
         s = self.linear_solver_settings
-        fn = getattr(plan.lib, fn_name)
-        rc = fn(plan.handle, capi.ptr(tangent_matrix.data), capi.ptr(tangent_matrix.inv_diag), capi.ptr(b),
-                capi.ptr(x), float(s["tol"]), int(s["maxiter"]), int(s.get("check_every", 32)), C.byref(iters),
-                C.byref(rel), capi.ptr(ws), ws.numel(), capi.stream_handle())
-        self.last_linear_info = {"solver": fn_name, "iterations": iters.value, "relative_residual": rel.value,
-                                 "status": rc}
+        rc = plan.lib.folgb_krylov(plan.handle, method, bits, capi.ptr(tangent_matrix.data),
+                                   capi.ptr(tangent_matrix.inv_diag), capi.ptr(b), capi.ptr(x), float(s["tol"]),
+                                   int(s["maxiter"]), int(s.get("check_every", 32)), C.byref(iters), C.byref(rel),
+                                   capi.ptr(ws), ws.numel(), capi.stream_handle())
+        name = ("folgb_pcg" if method == capi.KRYLOV_CG else "folgb_bicgstab") + ("" if bits == 32 else "_fp64")
+        self.last_linear_info = {"solver": name, "iterations": iters.value, "relative_residual": rel.value,
+                                 "status": rc, "vector_bits": bits}
         if rc not in (capi.OK, capi.ERR_NOT_CONVERGED):
-            capi.check(fn_name, rc)
+            capi.check(name, rc)
         return x
 
     def PCGLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
         """Solve tangent_matrix dx = -residual with Jacobi-PCG (x0 = 0); returns dx."""
-        return self._krylov("folgb_pcg", tangent_matrix, residual_vector)
+        return self._krylov(capi.KRYLOV_CG, tangent_matrix, residual_vector)
 
     def BiCGSTABLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
         """Solve tangent_matrix dx = -residual with Jacobi-BiCGSTAB (x0 = 0); returns dx.
         (fe_solver.py:60-67 passes x0 = current dofs; dx starts from 0 here.)"""
-        return self._krylov("folgb_bicgstab", tangent_matrix, residual_vector)
+        return self._krylov(capi.KRYLOV_BICGSTAB, tangent_matrix, residual_vector)
 
 
 class FiniteElementLinearResidualBasedSolver(FiniteElementSolver):

@@ -102,7 +102,7 @@ int folgb_plan_set_dirichlet_values(folgb_plan* plan, const double* values, doub
 
 /* Operation ids for folgb_workspace_bytes. */
 enum { FOLGB_OP_LOSS_ADJOINT = 0, FOLGB_OP_ASSEMBLE = 1, FOLGB_OP_PCG = 2,
-       FOLGB_OP_PLAIN = 3 };
+       FOLGB_OP_PLAIN = 3, FOLGB_OP_KRYLOV64 = 4 };
 size_t folgb_workspace_bytes(const folgb_plan* plan, int32_t op, int32_t batch);
 
 /* Fused FE loss + adjoint for a batch of instances on one mesh.
@@ -208,6 +208,19 @@ int folgb_bicgstab(const folgb_plan* plan, const float* csr_values, const float*
                    const float* rhs, float* x, double rtol, int32_t maxiter, int32_t check_every,
                    int32_t* iterations, double* rel_residual,
                    void* workspace, size_t workspace_bytes, void* stream);
+
+/* Either solver with the Krylov vectors in fp32 (vector_bits 32: the same as
+ * folgb_pcg / folgb_bicgstab, workspace FOLGB_OP_PCG) or fp64 (vector_bits
+ * 64, workspace FOLGB_OP_KRYLOV64).  The matrix, preconditioner and rhs stay
+ * fp32.  fp64 vectors keep BiCGSTAB convergent on the indefinite,
+ * ill-conditioned Neo-Hookean tangents where fp32 recurrences diverge (the
+ * reference runs the same solver in fp32 JAX by default).  method:
+ * FOLGB_KRYLOV_CG or FOLGB_KRYLOV_BICGSTAB. */
+enum { FOLGB_KRYLOV_CG = 0, FOLGB_KRYLOV_BICGSTAB = 1 };
+int folgb_krylov(const folgb_plan* plan, int32_t method, int32_t vector_bits,
+                 const float* csr_values, const float* inv_diag, const float* rhs, float* x,
+                 double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
+                 double* rel_residual, void* workspace, size_t workspace_bytes, void* stream);
 
 /* y = A x on the plan's CSR (FP32). */
 int folgb_spmv(const folgb_plan* plan, const float* csr_values, const float* x, float* y,

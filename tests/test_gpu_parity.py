@@ -303,3 +303,70 @@ def test_bicgstab_on_indefinite_neohooke_tangent(cuda, shear):
     A, Ro = ol.csr(ctrl, u)
     assert solver.last_linear_info["status"] == 0, solver.last_linear_info
     assert rel_fro(dx, fo.direct_solve(A, -Ro)) < 1e-5
+
+
+@pytest.mark.parametrize("bits", [32, 64])
+def test_krylov_vector_precision_on_spd_system(cuda, bits):
+    """folgb_krylov: CG with fp32 or fp64 Krylov vectors on an SPD stiffness."""
+    from folax_gb300.solvers import FiniteElementSolver
+    m = make_mesh("hex8", 6, seed=51)
+    s = _settings("hex8", "elastic", "element")
+    gl, ol = gpu_loss("hex8", "elastic", m, s), oracle_loss("hex8", "elastic", m, s)
+    ctrl = 0.5 + np.random.default_rng(52).random(gl.GetNumberOfControls())
+    u = ol.full_dof_vector(np.zeros(ol.total_dofs))
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, u)
+    solver = FiniteElementSolver("cg", gl, {"linear_solver_settings": {
+        "solver": "GB300-pcg", "tol": 1e-8, "maxiter": 5000, "vector_precision": f"fp{bits}"}})
+    solver.Initialize()
+    dx = solver.LinearSolve(jac, R).cpu().numpy()
+    assert solver.last_linear_info["status"] == 0 and solver.last_linear_info["vector_bits"] == bits
+    A, Ro = ol.csr(ctrl, u)
+    assert rel_fro(dx, fo.direct_solve(A, -Ro)) < 1e-5
+
+
+def test_fp64_vector_bicgstab_on_12cubed_neohooke_tangent(cuda):
+    """The first Newton tangent of the Neo-Hookean tet split of a 12^3 grid
+    (two-phase E, reference shear): fp32 BiCGSTAB recurrences diverge on it;
+    with fp64 vectors the solve reaches rtol 1e-6 against the GPU's own matrix."""
+    from folax_gb300 import fields
+    from folax_gb300.mesh import create_3D_box_mesh, split_hex_to_tets
+    from folax_gb300.solvers import FiniteElementSolver
+    n = 12
+    m = split_hex_to_tets(create_3D_box_mesh(n, n, n))
+    s = {"dirichlet_bc_dict": {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.05}},
+         "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3}, "control_layout": "element"}
+    gl = gpu_loss("tet4", "neohooke", m, s)
+    E = np.repeat(fields.two_phase_voxels(n, 2024), 6)
+    u = gl.ApplyDirichletBCOnDofVector(np.zeros(gl.GetTotalNumberOfDOFs()))
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(E, u)
+    solver = FiniteElementSolver("b", gl, {"linear_solver_settings": {"solver": "JAX-bicgstab", "tol": 1e-6,
+                                                                       "maxiter": 20000, "check_every": 64}})
+    solver.Initialize()
+    dx = solver.LinearSolve(jac, R).double().cpu().numpy()
+    info = solver.last_linear_info
+    assert info["vector_bits"] == 64 and info["status"] == 0, info
+    A = jac.to_scipy()
+    r = R.double().cpu().numpy()
+    assert np.linalg.norm(A @ dx + r) / np.linalg.norm(r) < 2e-6
+
+
+def test_newton_neohooke_reference_shear_two_phase_matches_oracle(cuda):
+    """Newton (load_incr 1) on the reference Neo-Hookean model, 6^3 tet split,
+    two-phase E: the GPU path (fp32 assembly, fp64-vector BiCGSTAB) converges
+    to the oracle's root (FP64 assembly, direct solves)."""
+    from folax_gb300 import fields
+    from folax_gb300.mesh import create_3D_box_mesh, split_hex_to_tets
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    n = 6
+    m = split_hex_to_tets(create_3D_box_mesh(n, n, n))
+    s = {"dirichlet_bc_dict": {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.05}},
+         "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3}, "control_layout": "element"}
+    gl, ol = gpu_loss("tet4", "neohooke", m, s), oracle_loss("tet4", "neohooke", m, s)
+    E = np.repeat(fields.two_phase_voxels(n, 2024), 6)
+    solver = FiniteElementNonLinearResidualBasedSolver("nl", gl, {
+        "linear_solver_settings": {"tol": 1e-9, "maxiter": 20000, "check_every": 64},
+        "nonlinear_solver_settings": {"load_incr": 1, "maxiter": 12, "abs_tol": 1e-7, "rel_tol": 1e-8}})
+    solver.Initialize()
+    x = solver.Solve(E, np.zeros(ol.total_dofs)).double().cpu().numpy()
+    xo, _ = fo.newton_solve(ol, E, np.zeros(ol.total_dofs), load_incr=1, maxiter=12, abs_tol=1e-7, rel_tol=1e-8)
+    assert rel_fro(x, xo) < 1e-4
