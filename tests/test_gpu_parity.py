@@ -327,7 +327,9 @@ def test_krylov_vector_precision_on_spd_system(cuda, bits):
 def test_fp64_vector_bicgstab_on_12cubed_neohooke_tangent(cuda):
     """The first Newton tangent of the Neo-Hookean tet split of a 12^3 grid
     (two-phase E, reference shear): fp32 BiCGSTAB recurrences diverge on it;
-    with fp64 vectors the solve reaches rtol 1e-6 against the GPU's own matrix."""
+    with fp64 vectors the solve converges (rtol 1e-6 on the fp64 iterate) and
+    the returned fp32 solution's residual against the GPU's own matrix is at
+    the fp32 rounding floor of the exact solution."""
     from folax_gb300 import fields
     from folax_gb300.mesh import create_3D_box_mesh, split_hex_to_tets
     from folax_gb300.solvers import FiniteElementSolver
@@ -347,7 +349,12 @@ def test_fp64_vector_bicgstab_on_12cubed_neohooke_tangent(cuda):
     assert info["vector_bits"] == 64 and info["status"] == 0, info
     A = jac.to_scipy()
     r = R.double().cpu().numpy()
-    assert np.linalg.norm(A @ dx + r) / np.linalg.norm(r) < 2e-6
+    # the solution comes back in fp32: its rounding alone leaves a residual
+    # floor on this ill-conditioned system, measured on the exact solution
+    x_star = fo.direct_solve(A, -r)
+    floor = np.linalg.norm(A @ x_star.astype(np.float32).astype(np.float64) + r) / np.linalg.norm(r)
+    res = np.linalg.norm(A @ dx + r) / np.linalg.norm(r)
+    assert res < 1e-6 + 2.0 * floor, (res, floor)
 
 
 def test_newton_neohooke_reference_shear_two_phase_matches_oracle(cuda):
