@@ -391,6 +391,7 @@ enum KernelId {
 };
 void trace_begin(int kid, cudaStream_t s);
 void trace_end(int kid, cudaStream_t s);
+bool trace_active();
 
 inline int loss_record(const folgb_plan* p) {
   return padded_record(p->ndof + (p->ctrl_layout == FOLGB_CONTROL_NODAL ? 1 : 0));

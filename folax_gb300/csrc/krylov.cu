@@ -33,6 +33,7 @@ struct KScalars {
   double rho, bnorm2, rnorm2, rref2, tol2;
   double alpha, beta, omega;
   int iters, done, replace, maxiter, restart, breakdowns;
+  int rounds;  // device-resident solve: executions of the loop body
 };
 // done: 1 converged (true residual), 2 maxiter, 3 non-finite, 4 repeated breakdown or divergence
 
@@ -228,6 +229,9 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
                                                        VT* __restrict__ rhat, double* part, unsigned* counters,
                                                        KScalars* sc) {
   __shared__ double sh[32];
+  // runs only when an iteration kernel asked for it (in the device-resident
+  // loop it is launched after every chunk)
+  if (!sc->replace || sc->done) return;
   // BiCGSTAB keeps its shadow residual and directions across a residual
   // replacement; only a breakdown (replace == 2) restarts it from rhat = r.
   const bool restart = BICG && sc->replace == 2;
@@ -326,6 +330,7 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
     sc->replace = 0;
     sc->restart = 0;
     sc->breakdowns = 0;
+    sc->rounds = 0;
     sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
     counters[0] = 0u;
   }
@@ -447,6 +452,7 @@ __global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __re
     sc->replace = 0;
     sc->restart = 1;
     sc->breakdowns = 0;
+    sc->rounds = 0;
     sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
     counters[0] = 0u;
   }
@@ -585,6 +591,18 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
   }
 }
 
+// Loop control of the device-resident solve (a CUDA-graph WHILE node whose
+// body is one chunk of iterations + the true-residual kernel + this kernel):
+// the same exits as the host loop, and a hard cap on body executions so the
+// loop always ends.
+__global__ void k_krylov_continue(KScalars* sc, cudaGraphConditionalHandle loop, int maxiter, int max_rounds) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (!sc->done && !sc->replace && sc->iters >= maxiter) sc->done = 2;
+  sc->rounds += 1;
+  if (!sc->done && sc->rounds >= max_rounds) sc->done = 2;
+  cudaGraphSetConditional(loop, sc->done ? 0u : 1u);
+}
+
 template <int NDOF>
 static int group_width(int maxdeg) {
   int g = 1;
@@ -674,43 +692,104 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
       constexpr int G = decltype(gw)::value;
       const int sb = spmv_blocks<NDOF>(p, G);
-      int guard = 0;
-      while (true) {
-        for (int k = 0; k < check_every; ++k) {
+      // one chunk of iterations on stream cs (an even count keeps the p / v
+      // ping-pong buffers aligned from one chunk to the next)
+      auto chunk = [&](int count, cudaStream_t cs) {
+        for (int k = 0; k < count; ++k) {
           if (solver == SOLVER_CG) {
-            trace_begin(KID_PCG_SPMV, s);
-            k_pcg_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
-                                                    w.q, w.part, w.counters, w.sc);
-            trace_end(KID_PCG_SPMV, s);
-            trace_begin(KID_PCG_UPDATE, s);
-            k_pcg_update<VT><<<vb, 256, 0, s>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
-            trace_end(KID_PCG_UPDATE, s);
+            trace_begin(KID_PCG_SPMV, cs);
+            k_pcg_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
+                                                     w.q, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_SPMV, cs);
+            trace_begin(KID_PCG_UPDATE, cs);
+            k_pcg_update<VT><<<vb, 256, 0, cs>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_UPDATE, cs);
             std::swap(pa, pb);
           } else {
-            trace_begin(KID_PCG_SPMV, s);
-            k_bicg_p_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
-                                                       w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
-            k_bicg_s_spmv<NDOF, G, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
-                                                       vb_, w.z, w.t, w.part, w.counters, w.sc);
-            trace_end(KID_PCG_SPMV, s);
-            trace_begin(KID_PCG_UPDATE, s);
-            k_bicg_update<VT><<<vb, 256, 0, s>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
-            trace_end(KID_PCG_UPDATE, s);
+            trace_begin(KID_PCG_SPMV, cs);
+            k_bicg_p_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
+                                                        w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
+            k_bicg_s_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
+                                                        vb_, w.z, w.t, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_SPMV, cs);
+            trace_begin(KID_PCG_UPDATE, cs);
+            k_bicg_update<VT><<<vb, 256, 0, cs>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
+            trace_end(KID_PCG_UPDATE, cs);
             std::swap(pa, pb);
             std::swap(va, vb_);
           }
         }
+      };
+      auto true_residual = [&](cudaStream_t cs) {
+        if (solver == SOLVER_CG)
+          k_true_residual<NDOF, G, false, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals,
+                                                                 rhs, dinv, w.x, w.r, w.z, w.rhat, w.part,
+                                                                 w.counters, w.sc);
+        else
+          k_true_residual<NDOF, G, true, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals,
+                                                                rhs, dinv, w.x, w.r, w.z, w.rhat, w.part,
+                                                                w.counters, w.sc);
+      };
+      const int K = (check_every + 1) & ~1;
+      const int max_rounds = 4 * (maxiter / K + 8);
+      // Device-resident solve: the whole iteration loop is one CUDA graph (a
+      // WHILE node over [K iterations, true residual, loop control]), launched
+      // once; the host reads the scalars at the end only.  Not while tracing
+      // (the events would be captured) or while the caller's stream is being
+      // captured itself; any graph API failure falls back to the host loop.
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      bool resident = !trace_active() && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
+                      cap == cudaStreamCaptureStatusNone;
+      if (resident) {
+        cudaStream_t cs = nullptr;
+        cudaGraph_t g = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
+                  cudaGraphCreate(&g, 0) == cudaSuccess;
+        cudaGraphConditionalHandle loop{};
+        cudaGraph_t body = nullptr;
+        if (ok) ok = cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
+        if (ok) {
+          cudaGraphNodeParams np{};
+          np.type = cudaGraphNodeTypeConditional;
+          np.conditional.handle = loop;
+          np.conditional.type = cudaGraphCondTypeWhile;
+          np.conditional.size = 1;
+          cudaGraphNode_t node;
+          ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
+          if (ok) body = np.conditional.phGraph_out[0];
+        }
+        if (ok) ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
+                                                   cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+        if (ok) {
+          chunk(K, cs);
+          true_residual(cs);
+          k_krylov_continue<<<1, 32, 0, cs>>>(w.sc, loop, maxiter, max_rounds);
+          cudaGraph_t captured = nullptr;
+          const bool launched_ok = cudaGetLastError() == cudaSuccess;
+          ok = cudaStreamEndCapture(cs, &captured) == cudaSuccess && launched_ok;
+        }
+        if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
+        if (ok) {
+          FOLGB_CUDA_TRY(cudaGraphLaunch(exec, s));
+          FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
+          FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
+        }
+        if (exec) cudaGraphExecDestroy(exec);
+        if (g) cudaGraphDestroy(g);
+        if (cs) cudaStreamDestroy(cs);
+        cudaGetLastError();  // a failed graph set-up is not the caller's error
+        resident = ok;
+      }
+      int guard = 0;
+      while (!resident) {
+        chunk(check_every, s);
         FOLGB_LAUNCH_CHECK();
         FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
         FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
         if (host.done) break;
         if (host.replace) {
-          if (solver == SOLVER_CG)
-            k_true_residual<NDOF, G, false, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
-                                                                dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
-          else
-            k_true_residual<NDOF, G, true, VT><<<sb, 256, 0, s>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, rhs,
-                                                               dinv, w.x, w.r, w.z, w.rhat, w.part, w.counters, w.sc);
+          true_residual(s);
           FOLGB_LAUNCH_CHECK();
           FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
           FOLGB_CUDA_TRY(cudaStreamSynchronize(s));

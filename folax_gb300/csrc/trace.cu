@@ -33,6 +33,11 @@ cudaEvent_t get_event() {
 }
 }  // namespace
 
+bool trace_active() {
+  std::lock_guard<std::mutex> g(mu);
+  return enabled;
+}
+
 void trace_begin(int kid, cudaStream_t s) {
   if (!enabled || kid < 0 || kid >= KID_COUNT) return;
   std::lock_guard<std::mutex> g(mu);
