@@ -42,6 +42,10 @@ class FolgbError(RuntimeError):
         self.code = code
 
 
+class Monomial(C.Structure):
+    _fields_ = [("coeff", C.c_double), ("control_power", C.c_int32), ("dof_power", C.c_int32 * 3)]
+
+
 class Physics(C.Structure):
     _fields_ = [
         ("element_type", C.c_int32), ("physics", C.c_int32), ("num_gp", C.c_int32),
@@ -78,6 +82,8 @@ PROTOTYPES = {
     "folgb_batch_plan_destroy": (C.c_int, [vp]),
     "folgb_batch_workspace_bytes": (sz, [vp]),
     "folgb_batch_loss_adjoint": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_response_workspace_bytes": (sz, [vp]),
+    "folgb_response": (C.c_int, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_fourier_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, i32, vp, i64, f64, f64, f64, f64, f64]),
     "folgb_fourier_destroy": (C.c_int, [vp]),
     "folgb_fourier_forward": (C.c_int, [vp, i32, vp, vp, vp]),

@@ -43,6 +43,39 @@ def element_centroids(xyz: np.ndarray, conn: np.ndarray) -> np.ndarray:
     return xyz[conn].mean(axis=1)
 
 
+class IdentityControl:
+    """fol/controls/identity_control.py: the controlled variables are the
+    control variables (a nodal or element field given directly)."""
+
+    def __init__(self, control_name: str, control_settings: dict, num_vars: int):
+        self._name = control_name
+        self.settings = control_settings
+        self.num_vars = int(num_vars)
+        self.initialized = False
+
+    def GetName(self):
+        return self._name
+
+    def Initialize(self, reinitialize=False):
+        self.num_control_vars = self.num_vars
+        self.num_controlled_vars = self.num_vars
+        self.initialized = True
+
+    def GetNumberOfVariables(self):
+        return self.num_vars
+
+    def GetNumberOfControlledVariables(self):
+        return self.num_vars
+
+    def ComputeControlledVariables(self, variable_vector):
+        from .loss import _dev
+        return _dev(variable_vector)
+
+    def ComputeBatchControlledVariables(self, batch_variable_vector):
+        from .loss import _dev
+        return _dev(batch_variable_vector).reshape(-1, self.num_vars)
+
+
 class FourierControl:
     """Nodal Fourier control (fol/controls/fourier_control.py:14-59):
     K(x) = v0/2 + sum_f v_f cos(fx pi x) cos(fy pi y) cos(fz pi z),

@@ -127,6 +127,20 @@ class FiniteElementLinearResidualBasedSolver(FiniteElementSolver):
         return u + du
 
 
+class AdjointFiniteElementSolver(FiniteElementSolver):
+    """adjoint_fe_solver.py:11-23: solves K^T_BC adjoint = -dJ/du for a
+    FiniteElementResponse (folax_gb300.response)."""
+
+    def __init__(self, adj_fe_solver_name: str, fe_response, adj_fe_solver_settings: dict = {}):
+        super().__init__(adj_fe_solver_name, fe_response.fe_loss, adj_fe_solver_settings)
+        self.fe_response = fe_response
+
+    def Solve(self, current_control_vars, current_dofs, current_adjoint_dofs=None):
+        jac, rhs = self.fe_response.ComputeAdjointJacobianMatrixAndRHSVector(current_control_vars, current_dofs)
+        # the linear solver negates its right-hand side (adjoint_fe_solver.py:21-22)
+        return self.LinearSolve(jac, -rhs, current_adjoint_dofs)
+
+
 class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBasedSolver):
     """Newton-Raphson with load stepping (fe_nonlinear_residual_based_solver.py:76-170).
 

@@ -259,6 +259,36 @@ int folgb_batch_loss_adjoint(const folgb_batch_plan* plan, const float* control,
                              float* dloss_ddofs, float* dloss_dcontrol, int32_t* device_status,
                              void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- adjoint sensitivities of an integral response ------------------------
+ * FiniteElementResponse (fol/responses/fe_response.py:17-526) for thermal and
+ * linear-elastic plans: J = sum_e sum_gp w detJ f(d_gp, u_gp) with d_gp, u_gp
+ * the control and dofs interpolated at the Gauss point (:92-120) and f a
+ * polynomial, sum_k coeff_k * d^control_power_k * prod_i u_i^dof_power_k[i]
+ * (the host parses the reference's response formula string into monomials).
+ * Any output may be NULL:
+ *   value        device scalar J (ComputeValue, :208-225);
+ *   adjoint_rhs  -(dJ/du) with zeros on Dirichlet dofs
+ *                (ComputeAdjointJacobianMatrixAndRHSVector, :244-283; the
+ *                matrix is folgb_assemble with transpose = 1);
+ *   dcontrol     dJ/dcontrol + adjoint . dR/dcontrol
+ *                (ComputeAdjointNodalControlDerivatives, :486-526);
+ *   dxyz         [3 N] dJ/dx + adjoint . dR/dx
+ *                (ComputeAdjointNodalShapeDerivatives, :365-406).
+ * dcontrol and dxyz need the adjoint dofs (the AdjointFiniteElementSolver
+ * solution).  dofs and adjoint are used as given (no Dirichlet overwrite).
+ * Neo-Hookean plans return FOLGB_ERR_INVALID_ARGUMENT. */
+typedef struct {
+  double coeff;
+  int32_t control_power;
+  int32_t dof_power[3];
+} folgb_monomial;
+enum { FOLGB_MAX_MONOMIALS = 16 };
+size_t folgb_response_workspace_bytes(const folgb_plan* plan);
+int folgb_response(const folgb_plan* plan, int32_t num_monomials, const folgb_monomial* monomials,
+                   const float* control, const float* dofs, const float* adjoint, float* value,
+                   float* adjoint_rhs, float* dcontrol, float* dxyz, void* workspace,
+                   size_t workspace_bytes, void* stream);
+
 /* ---- nodal Fourier control ----------------------------------------------
  * FourierControl (fol/controls/fourier_control.py:14-59) on the device: the
  * map from Fourier coefficients to the nodal material field that precedes the

@@ -737,25 +737,42 @@ def _complex_step(fun, x, h=1e-30):
     return np.stack(cols, axis=-1)
 
 
-class QuadResponseOracle:
-    """Response R = sum_e sum_gp w detJ (E_gp^2) U_x,gp on a quad4 elastic loss
-    (the "(E**2)*U[0]" response of tests/unit/test_sensitivity_analysis.py:477,
-    evaluated as in fe_response.py:92-120)."""
+class ResponseOracle:
+    """Integral response J = sum_e sum_gp w detJ f(d_gp, u_gp) over a thermal or
+    elastic loss (fe_response.py:92-120), f = sum_k c_k d^p_k prod_i u_i^q_ki
+    given as monomials [(c, p, (q_0, q_1, q_2)), ...], and its adjoint
+    sensitivities (fe_response.py:244-526) by complex-step differentiation of
+    the element value and the element residual."""
 
-    def __init__(self, loss: FELossOracle):
-        assert loss.etype == "quad4" and loss.physics == "elastic"
+    def __init__(self, loss: FELossOracle, monomials):
+        assert loss.physics in ("thermal", "elastic")
         self.loss = loss
+        self.monomials = [(float(c), int(p), tuple(int(v) for v in q)) for c, p, q in monomials]
+
+    def f(self, d, u):
+        out = 0.0
+        for c, p, q in self.monomials:
+            term = c * d ** p
+            for i in range(len(u)):
+                term = term * u[i] ** q[i]
+            out = out + term
+        return out
 
     def element_value(self, X, de, ue):
-        pts, wts = gauss_rule("quad4", self.loss.num_gp)
+        L = self.loss
+        pts, wts = gauss_rule(L.etype, L.num_gp)
         val = 0.0
         for xi, w in zip(pts, wts):
-            Nv = shape_values("quad4", xi)
-            detJ = _det(jacobian("quad4", X, xi))
-            egp = Nv @ de
-            ux = (N_matrix(Nv, 2) @ ue)[0]
-            val = val + w * detJ * egp ** 2 * ux
+            Nv = shape_values(L.etype, xi)
+            detJ = _det(jacobian(L.etype, X, xi))
+            uq = N_matrix(Nv, L.ndof) @ ue
+            val = val + w * detJ * self.f(Nv @ de, uq)
         return val
+
+    def _de(self, ctrl, e, nodes):
+        if self.loss.control_layout == "element":
+            return np.full(len(nodes), np.asarray(ctrl)[e], dtype=np.result_type(np.asarray(ctrl), float))
+        return np.asarray(ctrl)[nodes]
 
     def _per_element(self, fn, ctrl, u, adj=None):
         L = self.loss
@@ -763,18 +780,21 @@ class QuadResponseOracle:
         for e in range(len(L.conn)):
             nodes = L.conn[e]
             X = L.xyz[nodes]
-            de = np.asarray(ctrl)[nodes]
-            dofs = (2 * nodes[:, None] + np.arange(2)).ravel()
+            dofs = (L.ndof * nodes[:, None] + np.arange(L.ndof)).ravel()
             ue = np.asarray(u)[dofs]
             ae = None if adj is None else np.asarray(adj)[dofs]
-            out.append(fn(X, de, ue, ae))
+            out.append(fn(X, self._de(ctrl, e, nodes), ue, ae))
         return np.array(out)
+
+    def value(self, ctrl, u):
+        """ComputeValue (fe_response.py:208-225)."""
+        return float(np.sum(self._per_element(lambda X, de, ue, _: self.element_value(X, de, ue), ctrl, u)))
 
     def adjoint_jacobian_and_rhs(self, ctrl, u):
         """ComputeAdjointJacobianMatrixAndRHSVector (fe_response.py:244-283)."""
         L = self.loss
         g = self._per_element(lambda X, de, ue, _: _complex_step(lambda v: self.element_value(X, de, v), ue), ctrl, u)
-        rhs = L._assemble_nodal(g, 2)
+        rhs = L._assemble_nodal(g, L.ndof)
         rhs[L.dirichlet_indices] = 0.0
         rhs *= -1.0
         A, _ = L.csr(ctrl, u, transpose=True)
@@ -782,17 +802,23 @@ class QuadResponseOracle:
 
     def _residual(self, X, de, ue):
         L = self.loss
-        return linear_elastic_element("quad4", X, de, ue, L.num_gp, L.young, L.nu, L.body_force)[1]
+        if L.physics == "thermal":
+            return thermal_element(L.etype, X, de, ue, L.num_gp, L.beta, L.c)[1]
+        return linear_elastic_element(L.etype, X, de, ue, L.num_gp, L.young, L.nu, L.body_force)[1]
 
     def nodal_control_derivatives(self, ctrl, u, adj):
-        """ComputeAdjointNodalControlDerivatives (fe_response.py:486-526)."""
+        """ComputeAdjointNodalControlDerivatives (fe_response.py:486-526); for
+        element controls the per-element sums."""
         L = self.loss
 
         def per(X, de, ue, ae):
             dR = _complex_step(lambda d: self.element_value(X, d, ue), de)
             dres = _complex_step(lambda d: self._residual(X, d, ue), de)   # (nd, nen)
             return dR + ae @ dres
-        return L._assemble_nodal(self._per_element(per, ctrl, u, adj), 1)
+        g = self._per_element(per, ctrl, u, adj)
+        if L.control_layout == "element":
+            return g.sum(axis=1)
+        return L._assemble_nodal(g, 1)
 
     def nodal_shape_derivatives(self, ctrl, u, adj):
         """ComputeAdjointNodalShapeDerivatives (fe_response.py:365-406)."""
@@ -803,3 +829,12 @@ class QuadResponseOracle:
             dres = _complex_step(lambda x: self._residual(x, de, ue), X)   # (nd, nen*3)
             return dR + ae @ dres
         return L._assemble_nodal(self._per_element(per, ctrl, u, adj), 3)
+
+
+class QuadResponseOracle(ResponseOracle):
+    """The "(E**2)*U[0]" response on a quad4 elastic loss
+    (tests/unit/test_sensitivity_analysis.py:477)."""
+
+    def __init__(self, loss: FELossOracle):
+        assert loss.etype == "quad4" and loss.physics == "elastic"
+        super().__init__(loss, [(1.0, 2, (1, 0, 0))])
