@@ -50,6 +50,7 @@ struct VecArgs {
   const float* dofs;
   int64_t dofs_stride;
   const unsigned char* dmask;
+  const unsigned char* elem_bc;  // [E] element touches a Dirichlet dof
   const float* dval;
   int apply_dirichlet;
   int ctrl_layout;
@@ -133,11 +134,12 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
     float eval = 0.f;
     const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
     const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+    const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
       float4 x = __ldg(A.xyz4 + nodes[a]);
       X[a][0] = x.x; X[a][1] = x.y; X[a][2] = x.z;
-      unsigned m = A.apply_dirichlet ? __ldg(A.dmask + nodes[a]) : 0u;
+      unsigned m = bc ? __ldg(A.dmask + nodes[a]) : 0u;
 #pragma unroll
       for (int c = 0; c < NDOF; ++c) {
         int64_t d = (int64_t)NDOF * nodes[a] + c;
@@ -339,6 +341,62 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
 
 // __syncthreads_or returns whether any thread's predicate is non-zero (not
 // the bitwise OR), so each flag gets its own reduction.
+// Warp-level variants of the epilogue: no block barrier, so warps that finish
+// early do not wait for the slowest warp of their block.
+__device__ __forceinline__ void report_bad_warp(int bad, int* status) {
+  const unsigned detj = __any_sync(0xffffffffu, bad & 1), nan = __any_sync(0xffffffffu, bad & 2);
+  if ((threadIdx.x & 31) == 0 && status && (detj || nan))
+    atomicOr(status, (detj ? 1 << FOLGB_ERR_NONPOSITIVE_DETJ : 0) | (nan ? 1 << FOLGB_ERR_NAN : 0));
+}
+
+// Loss epilogue without barriers: each warp adds its 32 energies with a fixed
+// shuffle tree and posts the sum in shared memory; the last warp of the block
+// to post (a shared counter) adds the block's warp sums in warp order and
+// posts the block sum; the last block (a global counter) adds the block sums
+// in block order.  The order of every sum is fixed, whichever warp or block
+// finishes last.  wcount must be zeroed before any warp can post.
+__device__ __forceinline__ void finish_loss_warp(float energy, int bad, const VecArgs& A, int b, float* wsum,
+                                                 unsigned* wcount) {
+  report_bad_warp(bad, A.status);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) energy += __shfl_xor_sync(0xffffffffu, energy, o);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int nblk = gridDim.x;
+  int last = 0;
+  if (lane == 0) {
+    wsum[warp] = energy;
+    __threadfence_block();
+    last = atomicAdd(wcount, 1u) == (unsigned)nw - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence_block();
+  float v = (lane < nw) ? ((volatile float*)wsum)[lane] : 0.f;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  last = 0;
+  if (lane == 0) {
+    A.partials[(int64_t)b * nblk + blockIdx.x] = v;
+    __threadfence();
+    last = atomicAdd(A.counters + b, 1u) == (unsigned)nblk - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, last, 0)) return;
+  __threadfence();
+  float s = 0.f;
+  const volatile float* pv = A.partials + (int64_t)b * nblk;
+  for (int i = lane; i < nblk; i += 32) s += pv[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if (lane == 0) {
+    const float p = A.exponent;
+    const float Lp = (p == 1.f) ? s : powf(s, p);
+    const float sc = (p == 1.f) ? A.inv_batch : p * powf(s, p - 1.f) * A.inv_batch;
+    A.losses[b] = Lp;
+    A.scale[b] = sc;
+    if (!isfinite(Lp) && A.status) atomicOr(A.status, 1 << FOLGB_ERR_NAN);
+    A.counters[b] = 0u;  // ready for the next launch
+  }
+}
+
 __device__ __forceinline__ void report_bad(int bad, int* status) {
   const int detj = __syncthreads_or(bad & 1);
   const int nan = __syncthreads_or(bad & 2);

@@ -24,6 +24,7 @@ template <int ET, int PH, int MODE>
 __global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
   __shared__ GPTable gp;
   __shared__ float red[32];
+  pdl_launch_dependents();
   load_gp_table(gp, A.gp);
   __syncthreads();
   const int b = blockIdx.y;
@@ -109,9 +110,9 @@ __device__ __forceinline__ void sum_slots(const float* __restrict__ g, const int
 template <int NDOF, int REC, bool GDE, int PAD>
 __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
   const int b = blockIdx.y;
-  const float scb = A.scale ? A.scale[b] : 1.f;
   const float* g = A.g + (int64_t)b * A.E * A.nen * REC;
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  float scb = 1.f;
   for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < A.N; n += stride) {
     float acc[NDOF];
 #pragma unroll
@@ -128,10 +129,12 @@ __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
         slot[4 * k + 2] = t.z;
         slot[4 * k + 3] = t.w;
       }
+      pdl_wait_primary();  // the incidence slots do not depend on the element kernel; the records do
       sum_slots<NDOF, REC, GDE, PAD>(g, slot, acc, accd);
     } else {
       constexpr int CH = 8;
       const int s0 = __ldg(A.inc_ptr + n), s1 = __ldg(A.inc_ptr + n + 1);
+      pdl_wait_primary();
       for (int k0 = s0; k0 < s1; k0 += CH) {
         int slot[CH];
 #pragma unroll
@@ -139,6 +142,7 @@ __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
         sum_slots<NDOF, REC, GDE, CH>(g, slot, acc, accd);
       }
     }
+    if (A.scale) scb = A.scale[b];
     const float sc = A.node_inst ? A.scale[__ldg(A.node_inst + n)] : scb;
     if (A.out) {
       const unsigned m = __ldg(A.dmask + n);
@@ -149,6 +153,8 @@ __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
     if (A.dctrl) A.dctrl[(int64_t)b * A.dctrl_stride + n] = sc * accd;
   }
   if (A.rescale_elem && A.dctrl_elem) {
+    pdl_wait_primary();
+    if (A.scale) scb = A.scale[b];
     for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += stride)
       A.dctrl_elem[(int64_t)b * A.E + e] *= A.elem_inst ? A.scale[__ldg(A.elem_inst + e)] : scb;
   }
@@ -684,7 +690,7 @@ static int launch_matrix(const MatArgs& A0, int B, int npts, cudaStream_t s) {
 
 int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
-                  cudaStream_t s, const int* node_inst, const int* elem_inst) {
+                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl) {
   GatherArgs G;
   G.node_inst = node_inst;
   G.elem_inst = elem_inst;
@@ -714,11 +720,19 @@ int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_
   auto go = [&](auto nd, auto rc_, auto gde) -> int {
     constexpr int NDOF = decltype(nd)::value, REC = decltype(rc_)::value;
     constexpr bool GDE = decltype(gde)::value;
-    switch (p->inc_pad) {
-      case 4: k_node_gather<NDOF, REC, GDE, 4><<<grid, 256, 0, s>>>(G); break;
-      case 8: k_node_gather<NDOF, REC, GDE, 8><<<grid, 256, 0, s>>>(G); break;
-      default: k_node_gather<NDOF, REC, GDE, 0><<<grid, 256, 0, s>>>(G); break;
-    }
+    auto kernel = p->inc_pad == 4 ? k_node_gather<NDOF, REC, GDE, 4>
+                  : (p->inc_pad == 8 ? k_node_gather<NDOF, REC, GDE, 8> : k_node_gather<NDOF, REC, GDE, 0>);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = pdl ? 1 : 0;
+    FOLGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, kernel, G));
     return (int)FOLGB_OK;
   };
   using I1 = std::integral_constant<int, 1>;
@@ -758,6 +772,7 @@ static VecArgs make_vec_args(const folgb_plan* p, int B, const float* control, i
   A.dofs = dofs;
   A.dofs_stride = dstride;
   A.dmask = p->d_dmask;
+  A.elem_bc = p->d_elem_bc;
   A.dval = p->d_dval;
   A.apply_dirichlet = apply_dirichlet;
   A.ctrl_layout = p->ctrl_layout;
@@ -828,7 +843,8 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   if (dloss_ddofs || dloss_dcontrol) {
     rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
                        elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
-                       (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr);
+                       (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr,
+                       trace_active() ? 0 : 1);
   }
   return rc;
 }

@@ -67,6 +67,7 @@ struct folgb_plan {
   int* d_inc_padded = nullptr;  // [N][inc_pad] incident slots, -1 padded (vector loads)
   int hex8_variant = 0;    // sum-factorised hex8 kernel variant (autotuned)
   unsigned char* d_dmask = nullptr;
+  unsigned char* d_elem_bc = nullptr;  // [E] 1 if a node of the element has a Dirichlet dof
   float* d_dval = nullptr;
   folgb::GPTable* d_gp = nullptr;
   std::vector<int64_t> dir_dofs;
@@ -128,9 +129,18 @@ inline int loss_record(const folgb_plan* p);
 inline int residual_record(const folgb_plan* p);
 
 // deterministic node gather of element vectors (elements.cu)
+// pdl = 1: launched as a programmatic dependent of the element kernel just
+// before it on the stream (its incidence loads overlap that kernel's tail).
 int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
-                  cudaStream_t s, const int* node_inst, const int* elem_inst);
+                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl = 0);
+
+// Programmatic dependent launch: the primary kernel lets the next kernel on
+// the stream start early; the dependent waits for the primary's completion
+// (and memory) before touching its results.  Both are no-ops without the
+// launch attribute.
+__device__ __forceinline__ void pdl_launch_dependents() { asm volatile("griddepcontrol.launch_dependents;"); }
+__device__ __forceinline__ void pdl_wait_primary() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
 
 // ---------------------------------------------------------------------------
 // element traits

@@ -113,7 +113,13 @@ __device__ __forceinline__ void butterfly4_t(const float (&v)[4], float& A, floa
 //          (20 per SM) and 80 give 6 (24 per SM), at the price of spills.
 template <int CL, int MODE, bool BF, int ACC>
 __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
-  __shared__ float red[32];
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  pdl_launch_dependents();  // the gather may start its independent loads during this kernel's tail
+  if (MODE == MODE_LOSS) {
+    if (threadIdx.x == 0) wcount = 0u;
+    __syncthreads();
+  }
   const int b = blockIdx.y;
   const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   float energy = 0.f;
@@ -124,6 +130,7 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
     load_nodes<8>(A.conn, e, nodes);
     const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
     const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+    const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
     float X[3][8], U[3][8];
     float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
 #pragma unroll
@@ -133,7 +140,7 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
       X[0][L] = x.x;
       X[1][L] = x.y;
       X[2][L] = x.z;
-      const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
+      const unsigned m = bc ? __ldg(A.dmask + n) : 0u;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const int64_t d = 3 * (int64_t)n + c;
@@ -314,11 +321,8 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
     if (MODE == MODE_LOSS && CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
       A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
   }
-  report_bad(bad, A.status);
-  if (MODE == MODE_LOSS) {
-    float be = block_sum(energy, red);
-    finish_loss(be, A, b, red);
-  }
+  if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount);
+  else report_bad_warp(bad, A.status);
 }
 
 template <int CL, int MODE, bool BF, int ACC, int BLOCK>

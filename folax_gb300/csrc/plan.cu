@@ -338,7 +338,13 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     dmask[d / ndof] |= (unsigned char)(1u << (d % ndof));
     dval[d] = (float)dirichlet_values[i];  // later entries win, as numpy/XLA .at[].set
   }
+  // per-element Dirichlet flag: kernels read the nodal masks only for the
+  // elements that touch a constrained node (3 % of a 64^3 box)
+  std::vector<unsigned char> elem_bc(num_elements, 0);
+  for (int64_t e = 0; e < num_elements; ++e)
+    for (int a = 0; a < nen; ++a) elem_bc[e] |= dmask[c32[(size_t)e * nen + a]] ? 1 : 0;
   if ((rc = upload(&p->d_conn, c32.data(), c32.size())) || (rc = upload(&p->d_xyz4, x4.data(), x4.size())) ||
+      (rc = upload(&p->d_elem_bc, elem_bc.data(), elem_bc.size())) ||
       (rc = upload(&p->d_inc_ptr, inc_ptr.data(), inc_ptr.size())) ||
       (rc = upload(&p->d_inc_slot, inc_rec.data(), inc_rec.size())) ||
       (pad && (rc = upload(&p->d_inc_padded, inc_padded.data(), inc_padded.size()))) ||
@@ -357,7 +363,8 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
 
 extern "C" int folgb_plan_destroy(folgb_plan* p) {
   if (!p) return FOLGB_OK;
-  void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_inc_padded, p->d_dmask, p->d_dval, p->d_gp,
+  void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_inc_padded, p->d_dmask, p->d_elem_bc,
+                  p->d_dval, p->d_gp,
                   p->d_adj_ptr, p->d_adj, p->d_rowptr, p->d_colind, p->d_pair_row, p->d_pair_ptr,
                   p->d_pair_slot};
   for (void* q : ptrs)
