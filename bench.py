@@ -44,9 +44,13 @@ FLUSH_BYTES = 512 * 1024 * 1024
 # 4 x 72 x 2 + 75 = 651 flops, x 8 points = 5,208 flops; plus gathers ~0.
 FLOPS_PER_ELEMENT = 5208.0
 # DRAM bytes (read + write) of one k_hex8_elastic launch on the 64^3 workload,
-# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum, variant 0):
-# 17,491,200 + 2,304.  Other mesh sizes report null.
-NCU_TRAFFIC_BYTES = {64: 17_493_504}
+# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of the
+# autotuned variant, 128 threads / 96 registers): 17,498,624 + 108,544.  Other
+# mesh sizes report null.
+NCU_TRAFFIC_BYTES = {64: 17_607_168}
+# Warp instructions of the same launch (smsp__inst_executed.sum): the kernel's
+# real limit is instruction issue (4 warp instructions per clock per SM).
+NCU_WARP_INSTRUCTIONS = {64: 16_144_605}
 
 
 def parse():
@@ -140,6 +144,18 @@ class Clocks:
         os.unlink(self.path)
         return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
                 "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def issue_roofline(n, elem_ms, clk, peaks):
+    """Instruction-issue roofline of the element kernel: ncu's warp-instruction
+    count over 152 SMs x 4 issue slots per clock at the sampled SM clock."""
+    wi = NCU_WARP_INSTRUCTIONS.get(n)
+    if wi is None:
+        return None
+    mhz = (clk or {}).get("sm_mhz") or (peaks or {}).get("sm_max_mhz", 2070.0)
+    bound_us = wi / (152 * 4 * mhz * 1e6) * 1e6
+    return {"warp_instructions": wi, "issue_bound_us": bound_us, "measured_us": elem_ms * 1e3,
+            "frac": bound_us / (elem_ms * 1e3), "sm_mhz": mhz}
 
 
 def measured_peaks():
@@ -619,7 +635,9 @@ def main():
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                              "fp32": {"achieved_tflops": fp32_achieved, "nominal_peak_tflops": fp32_peak,
                                       "frac": fp32_achieved / fp32_peak,
-                                      "flops_per_element": FLOPS_PER_ELEMENT}},
+                                      "flops_per_element": FLOPS_PER_ELEMENT,
+                                      "note": "naive-algorithm flop count; the sum-factorised kernel executes fewer"},
+                             "issue": issue_roofline(args.n, elem_ms, clk, peaks)},
                 "e2e": {"value": B * nE / (ms_e2e * 1e-3) / 1e6, "unit": "M elements/s", "ms_per_step": ms_e2e,
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
