@@ -67,8 +67,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     ap.add_argument("--hex8-variant", type=int, default=None,
                     help="force one hex8 kernel variant (0-9) instead of autotuning (profiling runs)")
-    ap.add_argument("--extras", default="pcg,batched,neohooke",
-                    help="comma list of the extra measurements to run (pcg, batched, neohooke)")
+    ap.add_argument("--extras", default="small,pcg,batched,neohooke",
+                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke)")
     return ap.parse_args()
 
 
@@ -301,6 +301,43 @@ def extra_pcg(args, loss, ctrl):
             "true_relative_residual": float(res),
             "note": "Jacobi-PCG, fp32 matrix/vectors, fp64 dots, norms and iterate, reliable updates; "
                     "wall time includes one host flag read per 64 iterations"}
+
+
+def extra_small_thermal(args, n=50, seed=5):
+    """C0 on the GPU: quad4 steady heat conduction on the unit square, 50 x 50
+    elements, k = 0.1 + 0.9 sigmoid(16 Fourier modes) per element, T = 1 at
+    x = 0, T = 0 at x = 1: CSR assembly + Jacobi-PCG (rtol 1e-8, fp32 vectors:
+    the single-cluster solver), as a linear FE solve (fe_linear_residual_based
+    _solver.py:15-22) through the public API."""
+    import torch
+    from folax_gb300 import fields
+    from folax_gb300.loss import ThermalLoss2DQuad
+    from folax_gb300.mesh import create_2D_square_mesh
+    from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
+    m = create_2D_square_mesh(1.0, n + 1)
+    k = fields.fourier_conductivity(fields.element_centroids(m.nodes_coordinates, m.elements_nodes["quad"]), seed)
+    loss = ThermalLoss2DQuad("c0", {"dirichlet_bc_dict": {"T": {"left": 1.0, "right": 0.0}},
+                                    "control_layout": "element", "num_gp": 2}, m)
+    loss.Initialize()
+    solver = FiniteElementLinearResidualBasedSolver("c0", loss, {"linear_solver_settings": {
+        "solver": "GB300-pcg", "tol": 1e-8, "maxiter": 20000, "vector_precision": "fp32"}})
+    solver.Initialize()
+    kt = torch.tensor(k, dtype=torch.float32, device="cuda")
+    T0 = torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda")
+    for _ in range(3):
+        solver.Solve(kt, T0)
+    torch.cuda.synchronize()
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        T = solver.Solve(kt, T0)
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) / reps * 1e3
+    info = solver.last_linear_info
+    return {"mesh": f"{n}x{n} quad4", "dofs": loss.GetTotalNumberOfDOFs(), "ms_per_solve": ms,
+            "iterations": info["iterations"], "status": info["status"],
+            "ms_per_iteration": ms / max(1, info["iterations"]),
+            "note": "wall time of assembly + Dirichlet + PCG + update through the solver API, one host sync per solve"}
 
 
 def extra_batched(args, n_inst=512, seed=11):
@@ -597,7 +634,8 @@ def main():
     if rank == 0 and not args.no_extras:
         extras = {}
         wanted = set(args.extras.split(","))
-        for key, name, fn in (("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
+        for key, name, fn in (("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
+                              ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
                               ("batched", "batched_quad4_512", lambda: extra_batched(args)),
                               ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args))):
             if key not in wanted:

@@ -23,6 +23,8 @@
 #include <cmath>
 #include <type_traits>
 
+#include <cooperative_groups.h>
+
 #include "folgb_internal.cuh"
 
 using namespace folgb;
@@ -666,6 +668,297 @@ __global__ void k_step_inc(int* step) { *step += 1; }
 
 enum { SOLVER_CG = 0, SOLVER_BICGSTAB = 1 };
 
+// ---------------------------------------------------------------------------
+// Cluster-resident solver for small systems: the whole solve is ONE launch of
+// one thread-block cluster (kClusterCTAs CTAs on as many SMs).  Each CTA owns a
+// contiguous range of nodes (rows); vectors live in global memory (L2), the
+// iteration's phases are separated by hardware cluster barriers, and every
+// reduction is done by each CTA posting its block sum in shared memory and
+// every CTA adding all CTAs' sums in rank order over distributed shared
+// memory -- so all CTAs hold bit-identical scalars and take the same branch.
+// No host round trip, no kernel boundary, no spin-wait.  Same algorithm,
+// precision scheme and exits as the multi-kernel solver above.
+// ---------------------------------------------------------------------------
+constexpr int kClusterCTAs = 16;          // non-portable size (opt-in); 8, the portable one, as fallback
+constexpr int kClusterThreads = 512;
+constexpr int64_t kClusterMaxDofs = 16384;  // measured crossover: ~2x faster at 2.6k-6.6k dofs, slower at 47k
+
+template <class VT>
+struct ClusterArgs {
+  int64_t N;
+  const int* adj_ptr;
+  const int* adj;
+  int maxdeg;
+  const float* vals;
+  const float* dinv;
+  const float* b;
+  VT *r, *z, *p, *q, *rhat, *v, *y, *t;
+  double* x;
+  float* xout;
+  KScalars* sc;
+  double rtol;
+  int maxiter;
+};
+
+// sum of K doubles over the cluster; every thread of every CTA gets the same
+// totals (block sums added in rank order)
+template <int K>
+__device__ __forceinline__ void cluster_sum(double (&v)[K], double* sh, double (*slot)[4], int& parity) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double s = block_sum_d(v[k], sh);
+    if (threadIdx.x == 0) slot[parity][k] = s;
+  }
+  cluster.sync();
+  // lane r of every warp fetches rank r's sums (one remote latency, not nr),
+  // then a fixed shuffle tree adds them: the same order in every warp and CTA
+  const int nr = (int)cluster.num_blocks(), lane = threadIdx.x & 31;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double tot = lane < nr ? cluster.map_shared_rank(&slot[parity][0], lane)[k] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    v[k] = tot;
+  }
+  parity ^= 1;
+}
+
+// rows of this CTA's node range [n0, n1): epi(dof, row sum) on the owner lanes
+template <int NDOF, int G, class T, class VT, class Col, class Epi>
+__device__ __forceinline__ void cta_rows(const ClusterArgs<VT>& A, int64_t n0, int64_t n1, Col col, Epi epi) {
+  constexpr int U = RowsU<NDOF>::U;
+  const int lane = threadIdx.x % G;
+  const int64_t group = threadIdx.x / G, ngroups = blockDim.x / G;
+  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += ngroups * U) {
+    T sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, T>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
+  }
+}
+
+template <int NDOF, int G, class VT, bool BICG>
+__global__ void __launch_bounds__(kClusterThreads, 1) k_krylov_cluster(const ClusterArgs<VT> A) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  __shared__ double sh[32];
+  __shared__ double slot[2][4];
+  int parity = 0;
+  const int rank = (int)cluster.block_rank(), nr = (int)cluster.num_blocks();
+  const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
+  const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
+  const int64_t tid = threadIdx.x, nth = blockDim.x;
+  // ---- init: x = 0, r = b (BiCGSTAB: rhat = r; CG: z = D^-1 r, p = 0)
+  double red[2] = {0.0, 0.0};
+  for (int64_t d = d0 + tid; d < d1; d += nth) {
+    const float bi = A.b[d];
+    A.x[d] = 0.0;
+    A.r[d] = (VT)bi;
+    if (BICG) {
+      A.rhat[d] = (VT)bi;
+    } else {
+      const VT zi = (VT)A.dinv[d] * (VT)bi;
+      A.z[d] = zi;
+      A.p[d] = VT(0);
+      red[1] += (double)bi * (double)zi;
+    }
+    red[0] += (double)bi * (double)bi;
+  }
+  cluster_sum<2>(red, sh, slot, parity);
+  const double bb = red[0];
+  const double tol2 = A.rtol * A.rtol * bb;
+  double rho = BICG ? bb : red[1], rref2 = bb, rnorm2 = bb;
+  double alpha = 1.0, beta = 0.0, omega = 1.0;
+  int done = (bb == 0.0) ? 1 : (!isfinite(bb) ? 3 : 0);
+  int iters = 0, breakdowns = 0, replace = 0;
+  bool restart = true;
+  while (!done) {
+    if (!replace) {
+      if constexpr (BICG) {
+        // A: p = r + beta (p - omega v) (p = r on restart), y = D^-1 p
+        const VT vb = (VT)beta, vo = (VT)omega;
+        for (int64_t d = d0 + tid; d < d1; d += nth) {
+          const VT pn = restart ? A.r[d] : vfma(vb, vfma(-vo, A.v[d], A.p[d]), A.r[d]);
+          A.p[d] = pn;
+          A.y[d] = (VT)A.dinv[d] * pn;
+        }
+        cluster.sync();
+        // B: v = A y, rhat . v
+        double dv[1] = {0.0};
+        cta_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return A.y[k]; }, [&](int64_t d, VT sum) {
+          A.v[d] = sum;
+          dv[0] += (double)A.rhat[d] * (double)sum;
+        });
+        cluster_sum<1>(dv, sh, slot, parity);
+        const double RV = dv[0];
+        restart = false;
+        if (RV == 0.0 || !isfinite(RV)) {
+          ++breakdowns;
+          if (!isfinite(RV)) done = 3;
+          else if (breakdowns > kMaxBreakdowns) done = 4;
+          else replace = 2;
+          continue;
+        }
+        alpha = rho / RV;
+        // C: s = r - alpha v (kept in q), z = D^-1 s
+        const VT va = (VT)alpha;
+        for (int64_t d = d0 + tid; d < d1; d += nth) {
+          const VT sv = vfma(-va, A.v[d], A.r[d]);
+          A.q[d] = sv;
+          A.z[d] = (VT)A.dinv[d] * sv;
+        }
+        cluster.sync();
+        // D: t = A z, t . s, t . t
+        double dt[2] = {0.0, 0.0};
+        cta_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return A.z[k]; }, [&](int64_t d, VT sum) {
+          A.t[d] = sum;
+          dt[0] += (double)sum * (double)A.q[d];
+          dt[1] += (double)sum * (double)sum;
+        });
+        cluster_sum<2>(dt, sh, slot, parity);
+        omega = (dt[1] > 0.0 && isfinite(dt[1])) ? dt[0] / dt[1] : 0.0;
+        // E: x += alpha y + omega z, r = s - omega t, rhat . r, r . r
+        const VT vom = (VT)omega;
+        double de[2] = {0.0, 0.0};
+        for (int64_t d = d0 + tid; d < d1; d += nth) {
+          A.x[d] = fma(omega, (double)A.z[d], fma(alpha, (double)A.y[d], A.x[d]));
+          const VT ri = vfma(-vom, A.t[d], A.q[d]);
+          A.r[d] = ri;
+          de[0] += (double)A.rhat[d] * (double)ri;
+          de[1] += (double)ri * (double)ri;
+        }
+        cluster_sum<2>(de, sh, slot, parity);
+        const double RH = de[0], RR = de[1];
+        beta = (omega != 0.0 && rho != 0.0) ? (RH / rho) * (alpha / omega) : 0.0;
+        rho = RH;
+        rnorm2 = RR;
+        ++iters;
+        breakdowns = 0;
+        if (!isfinite(RR)) done = 3;
+        else if (RH == 0.0 || omega == 0.0) replace = 2;
+        else if (RR <= tol2 || RR <= kReplaceDrop2 * rref2 || RR > kDiverge2 * bb) replace = 1;
+        if (!done && iters >= A.maxiter) replace = replace ? replace : 1;
+      } else {
+        // A: p = z + beta p
+        const VT vb = (VT)beta;
+        for (int64_t d = d0 + tid; d < d1; d += nth) A.p[d] = vfma(vb, A.p[d], A.z[d]);
+        cluster.sync();
+        // B: q = A p, p . q
+        double dq[1] = {0.0};
+        cta_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return A.p[k]; }, [&](int64_t d, VT sum) {
+          A.q[d] = sum;
+          dq[0] += (double)A.p[d] * (double)sum;
+        });
+        cluster_sum<1>(dq, sh, slot, parity);
+        const double PQ = dq[0];
+        if (!(PQ > 0.0) || !isfinite(PQ)) {
+          ++breakdowns;
+          if (!isfinite(PQ)) done = 3;
+          else if (breakdowns > kMaxBreakdowns) done = 4;
+          else replace = 1;
+          continue;
+        }
+        alpha = rho / PQ;
+        // C: x += alpha p, r -= alpha q, z = D^-1 r, r . z, r . r
+        const VT va = (VT)alpha;
+        double dc[2] = {0.0, 0.0};
+        for (int64_t d = d0 + tid; d < d1; d += nth) {
+          A.x[d] = fma(alpha, (double)A.p[d], A.x[d]);
+          const VT ri = vfma(-va, A.q[d], A.r[d]);
+          A.r[d] = ri;
+          const VT zi = (VT)A.dinv[d] * ri;
+          A.z[d] = zi;
+          dc[0] += (double)ri * (double)zi;
+          dc[1] += (double)ri * (double)ri;
+        }
+        cluster_sum<2>(dc, sh, slot, parity);
+        const double RZ = dc[0], RR = dc[1];
+        beta = RZ / rho;
+        rho = RZ;
+        rnorm2 = RR;
+        ++iters;
+        breakdowns = 0;
+        if (!isfinite(RR)) done = 3;
+        else if (RR <= tol2 || RR <= kReplaceDrop2 * rref2 || RR > kDiverge2 * bb) replace = 1;
+        if (!done && iters >= A.maxiter) replace = replace ? replace : 1;
+      }
+      if (done || !replace) continue;
+    }
+    // reliable update: r = b - A x in fp64 (x of every CTA is visible: the
+    // last cluster sum ordered it); a breakdown (replace == 2) also restarts
+    // BiCGSTAB's shadow residual
+    const bool fresh = BICG && replace == 2;
+    double dr[2] = {0.0, 0.0};
+    cta_rows<NDOF, G, double>(A, n0, n1, [&](int64_t k) { return A.x[k]; }, [&](int64_t d, double sum) {
+      const double ri = (double)A.b[d] - sum;
+      const VT rv = (VT)ri;
+      A.r[d] = rv;
+      if (!BICG) {
+        const VT zi = (VT)A.dinv[d] * rv;
+        A.z[d] = zi;
+        dr[0] += (double)rv * (double)zi;
+      } else if (fresh) {
+        A.rhat[d] = rv;
+        dr[0] += (double)rv * (double)rv;
+      } else {
+        dr[0] += (double)A.rhat[d] * (double)rv;
+      }
+      dr[1] += ri * ri;
+    });
+    cluster_sum<2>(dr, sh, slot, parity);
+    rho = dr[0];
+    rref2 = rnorm2 = dr[1];
+    if (fresh) restart = true;
+    if (!BICG) beta = 0.0;
+    replace = 0;
+    if (!isfinite(dr[1])) done = 3;
+    else if (dr[1] <= tol2) done = 1;
+    else if (dr[1] > kDiverge2 * bb) done = 4;
+    else if (iters >= A.maxiter) done = 2;
+  }
+  for (int64_t d = d0 + tid; d < d1; d += nth) A.xout[d] = (float)A.x[d];
+  if (rank == 0 && threadIdx.x == 0) {
+    A.sc->iters = iters;
+    A.sc->done = done;
+    A.sc->rnorm2 = rnorm2;
+    A.sc->bnorm2 = bb;
+  }
+}
+
+// one launch of the cluster solver; returns false if the launch was refused
+// (the caller then uses the multi-kernel path)
+template <int NDOF, int G, class VT>
+static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStream_t s) {
+  auto kernel = solver == SOLVER_CG ? k_krylov_cluster<NDOF, G, VT, false> : k_krylov_cluster<NDOF, G, VT, true>;
+  for (int ctas : {kClusterCTAs, 8}) {
+    if (ctas > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+      cudaGetLastError();
+      continue;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(ctas);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = ctas;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kernel, &cfg) != cudaSuccess || nclusters < 1) {
+      cudaGetLastError();
+      continue;
+    }
+    if (cudaLaunchKernelEx(&cfg, kernel, A) == cudaSuccess) return true;
+    cudaGetLastError();
+  }
+  return false;
+}
+
 template <class VT>
 static int krylov_solve(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
                         float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
@@ -740,6 +1033,37 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
       cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
       bool resident = !trace_active() && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
                       cap == cudaStreamCaptureStatusNone;
+      // small systems: the whole solve in one cluster launch (fp32 vectors:
+      // with fp64 vectors the per-nonzero fp64 arithmetic of a few SMs is
+      // slower than the all-SM multi-kernel path)
+      if (resident && n <= kClusterMaxDofs && sizeof(VT) == sizeof(float)) {
+        ClusterArgs<VT> ca;
+        ca.N = p->N;
+        ca.adj_ptr = p->d_adj_ptr;
+        ca.adj = p->d_adj;
+        ca.maxdeg = p->maxdeg;
+        ca.vals = vals;
+        ca.dinv = dinv;
+        ca.b = rhs;
+        ca.r = w.r;
+        ca.z = w.z;
+        ca.p = w.p0;
+        ca.q = w.q;
+        ca.rhat = w.rhat;
+        ca.v = w.v0;
+        ca.y = w.y;
+        ca.t = w.t;
+        ca.x = w.x;
+        ca.xout = x;
+        ca.sc = w.sc;
+        ca.rtol = rtol;
+        ca.maxiter = maxiter;
+        if (launch_cluster_solver<NDOF, G, VT>(solver, ca, s)) {
+          FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
+          FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
+          return (int)FOLGB_OK;
+        }
+      }
       if (resident) {
         cudaStream_t cs = nullptr;
         cudaGraph_t g = nullptr;

@@ -383,11 +383,12 @@ def test_newton_neohooke_reference_shear_two_phase_matches_oracle(cuda):
 def test_device_resident_krylov_loop_matches_host_loop(cuda, solver_name):
     """The solve loop as one CUDA graph (WHILE node, no host sync until the
     end) runs the same kernels in the same order as the host-driven loop
-    (forced here by enabling kernel tracing): bit-identical results."""
+    (forced here by enabling kernel tracing): bit-identical results.  32^3
+    hex8 (107,811 dofs) is above the size the single-cluster solver takes."""
     from folax_gb300 import _capi
     from folax_gb300.solvers import FiniteElementSolver
     torch = cuda
-    m = make_mesh("hex8", 8, seed=61)
+    m = make_mesh("hex8", 32, seed=61)
     s = _settings("hex8", "elastic", "element")
     gl = gpu_loss("hex8", "elastic", m, s)
     ctrl = 0.5 + np.random.default_rng(62).random(gl.GetNumberOfControls())
@@ -407,3 +408,31 @@ def test_device_resident_krylov_loop_matches_host_loop(cuda, solver_name):
     info_host = dict(solver.last_linear_info)
     assert info_dev["status"] == 0 and info_dev["iterations"] == info_host["iterations"]
     assert torch.equal(x_dev, x_host)
+
+
+@pytest.mark.parametrize("solver_name,etype,physics,n", [("GB300-pcg", "hex8", "elastic", 8),
+                                                        ("GB300-pcg", "quad4", "thermal", 50),
+                                                        ("JAX-bicgstab", "tet4", "elastic", 6),
+                                                        ("JAX-bicgstab", "quad4", "elastic", 24)])
+def test_cluster_solver_matches_direct_solve(cuda, solver_name, etype, physics, n):
+    """Systems up to 16,384 dofs with fp32 Krylov vectors are solved in one
+    thread-block-cluster launch (all phases separated by cluster barriers,
+    reductions over distributed shared memory): against an FP64 direct solve,
+    and deterministic."""
+    from folax_gb300.solvers import FiniteElementSolver
+    torch = cuda
+    m = make_mesh(etype, n, seed=63)
+    s = _settings(etype, physics, "nodal")
+    gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
+    ctrl = 0.5 + np.random.default_rng(64).random(gl.GetNumberOfControls())
+    u = ol.full_dof_vector(np.zeros(ol.total_dofs))
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, u)
+    solver = FiniteElementSolver("k", gl, {"linear_solver_settings": {"solver": solver_name, "tol": 1e-8,
+                                                                       "maxiter": 20000, "vector_precision": "fp32"}})
+    solver.Initialize()
+    x1 = solver.LinearSolve(jac, R)
+    assert solver.last_linear_info["status"] == 0, solver.last_linear_info
+    x2 = solver.LinearSolve(jac, R)
+    assert torch.equal(x1, x2)
+    A, Ro = ol.csr(ctrl, u)
+    assert rel_fro(x1.cpu().numpy(), fo.direct_solve(A, -Ro)) < 1e-5
