@@ -102,10 +102,42 @@ __device__ __forceinline__ void butterfly4_t(const float (&v)[4], float& A, floa
   D += qp - qm;
 }
 
+// ---- packed fp32 pairs (Blackwell FFMA2/FMUL2/FADD2: two IEEE fp32 operations
+// per instruction, each rounded as the scalar one).  ACC 2 runs the Gauss
+// points in pairs (t_xi = 0, 1 at the same t_eta, t_zeta), so every per-point
+// operation issues once for two points.
+__device__ __forceinline__ float2 f2(float a) { return make_float2(a, a); }
+__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, f2(-1.f), a); }  // exact a - b
+// a*b - c*d with the scalar expression's rounding: fl(fl(a*b) - fl(c*d))
+__device__ __forceinline__ float2 cross2(float2 a, float2 b, float2 c, float2 d) { return sub2(mul2(a, b), mul2(c, d)); }
+
+// inverse and determinant of a pair of 3x3 matrices (the operations of det_inv<3>)
+__device__ __forceinline__ float2 det_inv_pair(const float2 (&J)[3][3], float2 (&Ji)[3][3]) {
+  const float2 c00 = cross2(J[1][1], J[2][2], J[1][2], J[2][1]);
+  const float2 c01 = cross2(J[1][2], J[2][0], J[1][0], J[2][2]);
+  const float2 c02 = cross2(J[1][0], J[2][1], J[1][1], J[2][0]);
+  const float2 det = add2(add2(mul2(J[0][0], c00), mul2(J[0][1], c01)), mul2(J[0][2], c02));
+  const float2 r = make_float2(1.0f / det.x, 1.0f / det.y);
+  Ji[0][0] = mul2(c00, r);
+  Ji[1][0] = mul2(c01, r);
+  Ji[2][0] = mul2(c02, r);
+  Ji[0][1] = mul2(cross2(J[0][2], J[2][1], J[0][1], J[2][2]), r);
+  Ji[1][1] = mul2(cross2(J[0][0], J[2][2], J[0][2], J[2][0]), r);
+  Ji[2][1] = mul2(cross2(J[0][1], J[2][0], J[0][0], J[2][1]), r);
+  Ji[0][2] = mul2(cross2(J[0][1], J[1][2], J[0][2], J[1][1]), r);
+  Ji[1][2] = mul2(cross2(J[0][2], J[1][0], J[0][0], J[1][2]), r);
+  Ji[2][2] = mul2(cross2(J[0][0], J[1][1], J[0][1], J[1][0]), r);
+  return det;
+}
+
 // Kernel variants (chosen per plan by the autotuner in launch_hex8_fast):
 //   ACC 0: keep the 36 per-direction point sums, adjoint butterflies at the end;
 //   ACC 1: accumulate the dual Hadamard coefficients point by point
 //          (21 accumulators instead of 36: fewer registers, ~14% more adds);
+//   ACC 2: as ACC 0 with the Gauss points in packed fp32 pairs;
 //   BLOCK: threads per block; the register cap is 128 (512 resident threads
 //          per SM) through __launch_bounds__, or REGS for the
 //          k_hex8_elastic_regs wrapper: each SM sub-partition holds 16,384
@@ -165,11 +197,11 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
       wht8(U[i]);
       deriv12(U[i], DU[i]);
     }
-    float S[ACC == 0 ? 3 : 1][3][4];   // ACC 0: per-direction point sums
+    float S[ACC != 1 ? 3 : 1][3][4];   // ACC 0 / 2: per-direction point sums
     float Dd[ACC == 1 ? 3 : 1][8];     // ACC 1: dual Hadamard coefficients (raw)
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
-      if (ACC == 0) {
+      if (ACC != 1) {
 #pragma unroll
         for (int k = 0; k < 3; ++k)
 #pragma unroll
@@ -183,6 +215,81 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
     float wdet[BF ? 8 : 1];
     float sedsum = 0.f;
     const MatConst& mt = A.mat;
+    if constexpr (ACC == 2) {
+      // Gauss points in pairs q = (0|1) + 2 ty + 4 tz: dxi is shared by the pair,
+      // deta / dzeta and every per-point quantity are packed (t_xi = 0, 1)
+      float2 en2 = f2(0.f), sed2sum = f2(0.f);
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int t = 0; t < 4; ++t) S[i][k][t] = 0.f;
+#pragma unroll
+      for (int pr = 0; pr < 4; ++pr) {
+        const int ty = pr & 1, tz = pr >> 1;
+        const int ix = ty + 2 * tz;
+        float2 J[3][3], Gm[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          J[i][0] = f2(DX[i].dxi[ix]);
+          J[i][1] = make_float2(DX[i].deta[2 * tz], DX[i].deta[2 * tz + 1]);
+          J[i][2] = make_float2(DX[i].dzeta[2 * ty], DX[i].dzeta[2 * ty + 1]);
+          Gm[i][0] = f2(DU[i].dxi[ix]);
+          Gm[i][1] = make_float2(DU[i].deta[2 * tz], DU[i].deta[2 * tz + 1]);
+          Gm[i][2] = make_float2(DU[i].dzeta[2 * ty], DU[i].dzeta[2 * ty + 1]);
+        }
+        float2 Ji[3][3];
+        const float2 wd = det_inv_pair(J, Ji);  // Gauss weight 1
+        bad |= !(wd.x > 0.f) | !(wd.y > 0.f);
+        if constexpr (BF) {
+          wdet[2 * pr] = wd.x;
+          wdet[2 * pr + 1] = wd.y;
+        }
+        float2 H[3][3];
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+          for (int j = 0; j < 3; ++j) H[i][j] = fma2(Gm[i][2], Ji[2][j], fma2(Gm[i][1], Ji[1][j], mul2(Gm[i][0], Ji[0][j])));
+        const float2 tr = add2(add2(H[0][0], H[1][1]), H[2][2]);
+        const float2 g01 = add2(H[0][1], H[1][0]), g12 = add2(H[1][2], H[2][1]), g02 = add2(H[0][2], H[2][0]);
+        const float2 sq = fma2(H[2][2], H[2][2], fma2(H[1][1], H[1][1], mul2(H[0][0], H[0][0])));
+        const float2 gg = fma2(g02, g02, fma2(g12, g12, mul2(g01, g01)));
+        const float2 sed = fma2(f2(mt.mu), gg, fma2(f2(2.f * mt.mu), sq, mul2(f2(mt.lam), mul2(tr, tr))));
+        const float2 eq = (CL == FOLGB_CONTROL_NODAL) ? make_float2(egp[2 * pr], egp[2 * pr + 1]) : f2(egp[0]);
+        const float2 ew = mul2(eq, wd);
+        en2 = fma2(ew, sed, en2);
+        if constexpr (CL == FOLGB_CONTROL_NODAL) {
+          const float2 ws = mul2(wd, sed);
+          wsed[2 * pr] = ws.x;
+          wsed[2 * pr + 1] = ws.y;
+        } else {
+          sed2sum = fma2(wd, sed, sed2sum);
+        }
+        // w detJ sigma
+        const float2 lt = mul2(mul2(ew, f2(mt.lam)), tr), tm = mul2(ew, f2(2.f * mt.mu)), sm = mul2(ew, f2(mt.mu));
+        float2 sg[3][3];
+        sg[0][0] = fma2(tm, H[0][0], lt);
+        sg[1][1] = fma2(tm, H[1][1], lt);
+        sg[2][2] = fma2(tm, H[2][2], lt);
+        sg[0][1] = sg[1][0] = mul2(sm, g01);
+        sg[1][2] = sg[2][1] = mul2(sm, g12);
+        sg[0][2] = sg[2][0] = mul2(sm, g02);
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float2 t0 = fma2(sg[i][2], Ji[0][2], fma2(sg[i][1], Ji[0][1], mul2(sg[i][0], Ji[0][0])));
+          const float2 t1 = fma2(sg[i][2], Ji[1][2], fma2(sg[i][1], Ji[1][1], mul2(sg[i][0], Ji[1][0])));
+          const float2 t2 = fma2(sg[i][2], Ji[2][2], fma2(sg[i][1], Ji[2][1], mul2(sg[i][0], Ji[2][0])));
+          S[i][0][ix] += t0.x + t0.y;       // dxi shared by the pair
+          S[i][1][2 * tz] += t1.x;           // deta index t_xi + 2 t_zeta
+          S[i][1][2 * tz + 1] += t1.y;
+          S[i][2][2 * ty] += t2.x;           // dzeta index t_xi + 2 t_eta
+          S[i][2][2 * ty + 1] += t2.y;
+        }
+      }
+      energy += en2.x + en2.y;
+      sedsum += sed2sum.x + sed2sum.y;
+    } else {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int tx = q & 1, ty = (q >> 1) & 1, tz = (q >> 2) & 1;
@@ -252,13 +359,14 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
         }
       }
     }
+    }  // ACC != 2
     // adjoint: per component, dual Hadamard coefficients then the transposed transform
     float g[8][3];
     const float s = 0.125f, sg_ = 0.125f * kG, sg2 = 0.125f * kG2;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       float d[8];
-      if (ACC == 0) {
+      if (ACC != 1) {
 #pragma unroll
         for (int k = 0; k < 8; ++k) d[k] = 0.f;
         float A1 = 0.f, B1 = 0.f, C1 = 0.f, D1 = 0.f;
@@ -361,12 +469,15 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
     case 6: launch_variant_regs<CL, MODE, 0, 96>(A, grid, bf, s); break;
     case 7: launch_variant_regs<CL, MODE, 1, 96>(A, grid, bf, s); break;
     case 8: launch_variant_regs<CL, MODE, 0, 80>(A, grid, bf, s); break;
-    default: launch_variant_regs<CL, MODE, 1, 80>(A, grid, bf, s); break;
+    case 9: launch_variant_regs<CL, MODE, 1, 80>(A, grid, bf, s); break;
+    case 10: launch_variant<CL, MODE, 2, 256>(A, grid, bf, s); break;
+    case 11: launch_variant<CL, MODE, 2, 128>(A, grid, bf, s); break;
+    default: launch_variant_regs<CL, MODE, 2, 96>(A, grid, bf, s); break;
   }
 }
 
 // Number of sum-factorised variants the autotuner may choose from.
-constexpr int kHex8Variants = 10;
+constexpr int kHex8Variants = 13;
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's

@@ -29,11 +29,13 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 10
+HEX8_VARIANTS = 13
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
                       "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
                       "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
-                      "128 thr, 80 regs, point sums", "128 thr, 80 regs, dual coefficients"]
+                      "128 thr, 80 regs, point sums", "128 thr, 80 regs, dual coefficients",
+                      "256 thr, paired points (f32x2)", "128 thr, paired points (f32x2)",
+                      "128 thr, 96 regs, paired points (f32x2)"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 
