@@ -11,7 +11,8 @@ from .mesh import Mesh, create_2D_square_mesh, create_3D_box_mesh, split_hex_to_
 _LAZY = {
     "loss": ("FiniteElementLoss", "ThermalLoss2DQuad", "ThermalLoss3DHexa", "ThermalLoss3DTetra",
              "MechanicalLoss2DQuad", "MechanicalLoss3DHexa", "MechanicalLoss3DTetra",
-             "NeoHookeMechanicalLoss2DQuad", "NeoHookeMechanicalLoss3DHexa", "NeoHookeMechanicalLoss3DTetra"),
+             "NeoHookeMechanicalLoss2DQuad", "NeoHookeMechanicalLoss3DHexa", "NeoHookeMechanicalLoss3DTetra",
+             "SaintVenantMechanicalLoss2DQuad", "SaintVenantMechanicalLoss3DHexa", "SaintVenantMechanicalLoss3DTetra"),
     "solvers": ("FiniteElementLinearResidualBasedSolver", "FiniteElementNonLinearResidualBasedSolver"),
 }
 

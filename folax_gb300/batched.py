@@ -18,10 +18,12 @@ import numpy as np
 from . import _capi as capi
 from .loss import _ETYPE, _dev, _torch
 
-_PHYSICS = {"thermal": capi.THERMAL, "elastic": capi.ELASTIC, "neohooke": capi.NEOHOOKE}
+_PHYSICS = {"thermal": capi.THERMAL, "elastic": capi.ELASTIC, "neohooke": capi.NEOHOOKE,
+            "saint_venant": capi.SAINT_VENANT}
 _NDOF = {("quad", "thermal"): 1, ("hexahedron", "thermal"): 1, ("tetra", "thermal"): 1,
          ("quad", "elastic"): 2, ("hexahedron", "elastic"): 3, ("tetra", "elastic"): 3,
-         ("quad", "neohooke"): 2, ("hexahedron", "neohooke"): 3, ("tetra", "neohooke"): 3}
+         ("quad", "neohooke"): 2, ("hexahedron", "neohooke"): 3, ("tetra", "neohooke"): 3,
+         ("quad", "saint_venant"): 2, ("hexahedron", "saint_venant"): 3, ("tetra", "saint_venant"): 3}
 
 
 class BatchedFELoss:

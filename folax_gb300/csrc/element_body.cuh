@@ -24,16 +24,19 @@ struct Tag {
 
 template <class F>
 int dispatch(int et, int ph, F&& f) {
-  switch (et * 3 + ph) {
+  switch (et * 4 + ph) {
     case 0: return f(Tag<FOLGB_QUAD4, FOLGB_THERMAL>{});
     case 1: return f(Tag<FOLGB_QUAD4, FOLGB_ELASTIC>{});
     case 2: return f(Tag<FOLGB_QUAD4, FOLGB_NEOHOOKE>{});
-    case 3: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
-    case 4: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
-    case 5: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
-    case 6: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
-    case 7: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
-    case 8: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
+    case 3: return f(Tag<FOLGB_QUAD4, FOLGB_SAINT_VENANT>{});
+    case 4: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
+    case 5: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
+    case 6: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
+    case 7: return f(Tag<FOLGB_HEX8, FOLGB_SAINT_VENANT>{});
+    case 8: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
+    case 9: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
+    case 10: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
+    case 11: return f(Tag<FOLGB_TET4, FOLGB_SAINT_VENANT>{});
   }
   return FOLGB_ERR_INVALID_ARGUMENT;
 }
@@ -264,6 +267,47 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
               g[a * DIM + i] -= f;
               energy = fmaf(-f, ue[a * DIM + i], energy);
             }
+        }
+      } else if constexpr (PH == FOLGB_SAINT_VENANT) {
+        float H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+            H[i][j] = s;
+          }
+        SVKState<DIM> st;
+        svk_state<DIM>(H, mt.mu_f * egp, mt.lam_f * egp, mt.mu_f, mt.lam_f, st);
+        float P[DIM][DIM];  // first Piola-Kirchhoff stress F S
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int p = 0; p < DIM; ++p) s = fmaf(st.F[k][p], st.S[p][j], s);
+            P[k][j] = s;
+          }
+        energy = fmaf(wd, st.psi, energy);
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
+            g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
+          }
+          gd[a] = fmaf(wd * st.dpsi_de, gp.N[q][a], gd[a]);
+        }
+        if (MODE == MODE_RESIDUAL && mt.has_bf) {
+#pragma unroll
+          for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
         }
       } else {  // neo-Hooke
         float H[DIM][DIM];

@@ -188,6 +188,59 @@ __device__ __forceinline__ float det_inv<3>(const float (&J)[3][3], float (&Ji)[
   return det;
 }
 
+// Saint-Venant-Kirchhoff material at one Gauss point
+// (constitutive_material_models/saint_venant.py:13-31): E = (F^T F - I)/2,
+// computed as (H + H^T + H^T H)/2 to keep small strains accurate in fp32,
+// psi = lam/2 tr(E)^2 + mu E:E, S = lam tr(E) I + 2 mu E.  dpsi_de is the
+// energy per unit Young's modulus (lam and mu are proportional to it).
+template <int D>
+struct SVKState {
+  float F[D][D];
+  float S[D][D];
+  float psi, dpsi_de;
+};
+
+template <int D>
+__device__ __forceinline__ void svk_state(const float (&H)[D][D], float mu, float lam, float mu1, float lam1,
+                                          SVKState<D>& st) {
+  float E[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float hh = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) hh = fmaf(H[k][i], H[k][j], hh);
+      E[i][j] = 0.5f * (H[i][j] + H[j][i] + hh);
+      st.F[i][j] = H[i][j] + (i == j ? 1.f : 0.f);
+    }
+  float tr = 0.f, ee = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    tr += E[i][i];
+#pragma unroll
+    for (int j = 0; j < D; ++j) ee = fmaf(E[i][j], E[i][j], ee);
+  }
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) st.S[i][j] = 2.f * mu * E[i][j] + (i == j ? lam * tr : 0.f);
+  st.psi = 0.5f * lam * tr * tr + mu * ee;
+  st.dpsi_de = 0.5f * lam1 * tr * tr + mu1 * ee;
+}
+
+// dS for a symmetric increment dC of C = F^T F (dE = dC / 2)
+template <int D>
+__device__ __forceinline__ void svk_dS(float mu, float lam, const float (&dC)[D][D], float (&dS)[D][D]) {
+  float tr = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) tr += 0.5f * dC[i][i];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) dS[i][j] = mu * dC[i][j] + (i == j ? lam * tr : 0.f);
+}
+
 // Neo-Hookean kinematics and stress at one Gauss point, written to avoid the
 // fp32 cancellation of det(C) near C = I: J - 1 comes from the invariant
 // expansion of det(I + H) and ln J from log1p.

@@ -258,7 +258,7 @@ int check_physics(const folgb_physics* phys, int& nen, int& dim, int& ndof) {
     case FOLGB_TET4: nen = 4; dim = 3; break;
     default: return FOLGB_ERR_INVALID_ARGUMENT;
   }
-  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_NEOHOOKE) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_SAINT_VENANT) return FOLGB_ERR_INVALID_ARGUMENT;
   if (phys->control_layout != FOLGB_CONTROL_NODAL && phys->control_layout != FOLGB_CONTROL_ELEMENT)
     return FOLGB_ERR_INVALID_ARGUMENT;
   if (phys->num_gp < 1 || phys->num_gp > 3) return FOLGB_ERR_INVALID_ARGUMENT;

@@ -516,3 +516,36 @@ class NeoHookeMechanicalLoss2DQuad(NeoHookeMechanicalLoss):
         loss_settings.setdefault("num_gp", 2)
         super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["Ux", "Uy"], element_type="quad"),
                          fe_mesh)
+
+
+class SaintVenantMechanicalLoss(FiniteElementLoss):
+    """mechanical_saint_venant.py:18-296: Saint-Venant-Kirchhoff, energy
+    sum w detJ psi(E) (psi = lam/2 tr(E)^2 + mu E:E, Lame constants from the
+    Young's modulus control), residual B(F)^T S - Fe, tangent B^T C B plus the
+    geometric stiffness."""
+    physics = capi.SAINT_VENANT
+
+    def Initialize(self, reinitialize=False) -> None:
+        if "material_dict" not in self.loss_settings:
+            raise ValueError("material_dict should provided in the loss settings !")
+        super().Initialize(reinitialize)
+
+
+class SaintVenantMechanicalLoss3DTetra(SaintVenantMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="tetra"), fe_mesh)
+
+
+class SaintVenantMechanicalLoss3DHexa(SaintVenantMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["Ux", "Uy", "Uz"],
+                                     element_type="hexahedron"), fe_mesh)
+
+
+class SaintVenantMechanicalLoss2DQuad(SaintVenantMechanicalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["Ux", "Uy"], element_type="quad"),
+                         fe_mesh)

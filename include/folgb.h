@@ -46,7 +46,8 @@ enum { FOLGB_QUAD4 = 0, FOLGB_HEX8 = 1, FOLGB_TET4 = 2 };
 enum {
   FOLGB_THERMAL = 0,  /* thermal.py:28-49                 */
   FOLGB_ELASTIC = 1,  /* mechanical.py:98-117             */
-  FOLGB_NEOHOOKE = 2  /* mechanical_neohooke_AD.py:254-293 */
+  FOLGB_NEOHOOKE = 2, /* mechanical_neohooke_AD.py:254-293 */
+  FOLGB_SAINT_VENANT = 3 /* mechanical_saint_venant.py:263-296 */
 };
 /* control layout: nodal values gathered by connectivity (fe_loss.py:160), or
  * one value per element used as de = value * 1 (partition of unity). */
@@ -58,7 +59,7 @@ enum { FOLGB_SHEAR_REFERENCE = 0, FOLGB_SHEAR_CONSISTENT = 1 };
 
 typedef struct folgb_physics {
   int32_t element_type;   /* FOLGB_QUAD4 / HEX8 / TET4                         */
-  int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE                */
+  int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE / SAINT_VENANT */
   int32_t num_gp;         /* Gauss order 1..3 ("num_gp", fe_loss.py:68-83)     */
   int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
   int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */

@@ -433,6 +433,75 @@ def neohooke_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None,
     return energy, re, Ke, fcons, dEn
 
 
+def saint_venant_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None, want_tangent=True):
+    """Saint-Venant-Kirchhoff element (mechanical_saint_venant.py:263-296 with
+    constitutive_material_models/saint_venant.py:13-31).
+
+    Per Gauss point: lam, mu from the interpolated Young's modulus (3-D Lame
+    constants, also in 2-D, :274-276), F = I + H, E = (F^T F - I)/2,
+    psi = lam/2 tr(E)^2 + mu E:E, S = lam tr(E) I + 2 mu E.  Returns
+    (energy, re, Ke, fint, dEnergy/dde) with energy = sum_gp w detJ psi,
+    fint = sum_gp w detJ B^T S_voigt (= d energy / d ue), re = fint - Fe and
+    Ke = B^T C B + the geometric stiffness (d re / d ue)."""
+    X, de, ue, squeeze = _as_batch(X, de, ue)
+    nen, d = ELEMENTS[etype]
+    if num_gp is None:
+        num_gp = 1 if etype == "tet4" else 2
+    V = _V3 if d == 3 else _V2
+    b = np.zeros(d) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()[:d]
+    pts, wts = gauss_rule(etype, num_gp)
+    E = X.shape[0]
+    dt = np.result_type(X, de, ue)
+    nd = d * nen
+    energy = np.zeros(E, dtype=dt)
+    fint = np.zeros((E, nd), dtype=dt)
+    Fe = np.zeros((E, nd), dtype=dt)
+    Ke = np.zeros((E, nd, nd), dtype=dt) if want_tangent else None
+    dEn = np.zeros((E, nen), dtype=dt)
+    U = ue.reshape(E, nen, d)
+    eye = np.eye(d)
+    for xi, w in zip(pts, wts):
+        Nv = shape_values(etype, xi)
+        dNdx, detJ = global_grads(etype, X, xi)
+        wd = w * detJ
+        egp = de @ Nv
+        mu, lam = lame(egp, nu)
+        mu1, lam1 = lame(1.0, nu)
+        H = np.einsum("eai,eaj->eij", U, dNdx)
+        F = eye + H
+        Es = 0.5 * (np.einsum("eki,ekj->eij", F, F) - eye)
+        trE = np.einsum("eii->e", Es)
+        EE = np.einsum("eij,eij->e", Es, Es)
+        psi = 0.5 * lam * trE ** 2 + mu * EE
+        S = lam[:, None, None] * trE[:, None, None] * eye + 2.0 * mu[:, None, None] * Es
+        B = nl_B(F, dNdx)
+        Sv = np.stack([S[:, p, q] for p, q in V], axis=1)
+        fint += wd[:, None] * np.einsum("evi,ev->ei", B, Sv)
+        energy += wd * psi
+        Fe += wd[:, None] * (N_matrix(Nv, d).T @ b)[None]
+        dEn += (wd * (0.5 * lam1 * trE ** 2 + mu1 * EE))[:, None] * Nv[None]
+        if want_tangent:
+            G = np.einsum("eap,epq,ebq->eab", dNdx, S, dNdx)
+            Kg = np.zeros((E, nd, nd), dtype=dt)
+            for k in range(d):
+                Kg[:, k::d, k::d] = G
+            Km = np.zeros((E, nd, nd), dtype=dt)
+            for bnode in range(nen):
+                for l in range(d):
+                    dF = np.zeros((E, d, d), dtype=dt)
+                    dF[:, l, :] = dNdx[:, bnode, :]
+                    dE = 0.5 * (np.einsum("eki,ekj->eij", dF, F) + np.einsum("eki,ekj->eij", F, dF))
+                    dS = (lam[:, None, None] * np.einsum("eii->e", dE)[:, None, None] * eye
+                          + 2.0 * mu[:, None, None] * dE)
+                    dSv = np.stack([dS[:, p, q] for p, q in V], axis=1)
+                    Km[:, :, d * bnode + l] = np.einsum("evi,ev->ei", B, dSv)
+            Ke += wd[:, None, None] * (Km + Kg)
+    re = fint - Fe
+    if squeeze:
+        return energy[0], re[0], (Ke[0] if want_tangent else None), fint[0], dEn[0]
+    return energy, re, Ke, fint, dEn
+
+
 # ----------------------------------------------------------------------------
 # Mesh generators (structured, seeded) — node/element ordering of the reference
 # ----------------------------------------------------------------------------
@@ -456,7 +525,8 @@ def square_mesh(L, N):
 #   fol/loss_functions/fe_loss.py
 # ----------------------------------------------------------------------------
 
-PHYSICS_NDOF = {"thermal": lambda dim: 1, "elastic": lambda dim: dim, "neohooke": lambda dim: dim}
+PHYSICS_NDOF = {"thermal": lambda dim: 1, "elastic": lambda dim: dim, "neohooke": lambda dim: dim,
+                "saint_venant": lambda dim: dim}
 
 
 class FELossOracle:
@@ -521,6 +591,8 @@ class FELossOracle:
             en, re, Ke, dEn = linear_elastic_element(self.etype, X, de, ue, self.num_gp,
                                                      self.young, self.nu, self.body_force)
             return en, re, Ke, re, dEn
+        if self.physics == "saint_venant":
+            return saint_venant_element(self.etype, X, de, ue, self.num_gp, self.nu, self.body_force, want_tangent)
         en, re, Ke, fcons, dEn = neohooke_element(self.etype, X, de, ue, self.num_gp, self.nu,
                                                   self.body_force, self.shear_mode, want_tangent)
         return en, re, Ke, fcons, dEn

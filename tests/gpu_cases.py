@@ -39,7 +39,10 @@ def gpu_loss(etype, physics, m, settings):
            ("tet4", "thermal"): L.ThermalLoss3DTetra, ("quad4", "elastic"): L.MechanicalLoss2DQuad,
            ("hex8", "elastic"): L.MechanicalLoss3DHexa, ("tet4", "elastic"): L.MechanicalLoss3DTetra,
            ("quad4", "neohooke"): L.NeoHookeMechanicalLoss2DQuad, ("hex8", "neohooke"): L.NeoHookeMechanicalLoss3DHexa,
-           ("tet4", "neohooke"): L.NeoHookeMechanicalLoss3DTetra}[(etype, physics)]
+           ("tet4", "neohooke"): L.NeoHookeMechanicalLoss3DTetra,
+           ("quad4", "saint_venant"): L.SaintVenantMechanicalLoss2DQuad,
+           ("hex8", "saint_venant"): L.SaintVenantMechanicalLoss3DHexa,
+           ("tet4", "saint_venant"): L.SaintVenantMechanicalLoss3DTetra}[(etype, physics)]
     loss = cls("loss", dict(settings), m)
     loss.Initialize()
     return loss

@@ -20,6 +20,22 @@ def test_linear_elastic_element_golden(etype):
     np.testing.assert_allclose(re, arr(g["residual"]), rtol=1e-4 if etype == "tet4" else 1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("etype", ["tet4", "hex8"])
+def test_saint_venant_at_zero_strain_is_the_linear_golden(etype):
+    """test_saint_venant_mechanical_loss.py evaluates the Saint-Venant element
+    at u = 1 (a rigid translation: F = I, E = 0).  There its tangent is the
+    linear-elastic stiffness (3-D Lame constants) and its residual -F_e, so
+    the linear-elastic golden vectors (test_mechanical_loss.py, same E, nu and
+    body force) pin it."""
+    g = golden("mechanical_linear.json")[etype]
+    nen, dim = fo.ELEMENTS[etype]
+    en, re, K, fint, dE = fo.saint_venant_element(etype, arr(g["xyz"]), np.ones(nen), np.ones(nen * dim), NGP[etype],
+                                                  0.3, arr(g["body_force"]).ravel())
+    np.testing.assert_allclose(K, arr(g["stiffness"]), rtol=1e-5, atol=1e-6)
+    np.testing.assert_allclose(re, arr(g["residual"]), rtol=1e-4 if etype == "tet4" else 1e-5, atol=1e-6)
+    assert abs(en) < 1e-12 and np.abs(fint).max() < 1e-12
+
+
 @pytest.mark.parametrize("etype", ["tet4", "hex8", "quad4"])
 def test_neohooke_element_golden(etype):
     """tests/unit/test_neo_hooke_mechanical_loss_AD.py: K_e = jacfwd(r_e), r_e."""

@@ -107,3 +107,27 @@ def test_newton_neohooke_converges():
     L, ctrl, u = _small("tet4", "neohooke", n=2)
     u1, hist = fo.newton_solve(L, ctrl, np.zeros(L.total_dofs), load_incr=2, maxiter=10)
     assert hist[-1][2] < 1e-8 or hist[-1][3] < 1e-8
+
+
+@pytest.mark.parametrize("etype", ["tet4", "hex8", "quad4"])
+def test_saint_venant_element_consistency(etype):
+    """Saint-Venant element: internal force = d energy / d u and tangent =
+    d residual / d u (complex step), energy control derivative = d energy / d e."""
+    rng = np.random.default_rng(9)
+    nen, dim = fo.ELEMENTS[etype]
+    if etype == "quad4":
+        X = np.array([[0.0, 0.0, 0.0], [1.1, 0.1, 0.0], [1.0, 0.9, 0.0], [0.1, 1.2, 0.0]])
+    elif etype == "tet4":
+        X = np.array([[0.0, 0.0, 0.0], [1.0, 0.1, 0.0], [0.1, 1.0, 0.1], [0.0, 0.2, 1.1]])
+    else:
+        X = np.array(fo._HEX_SIGNS) * 0.5 + 0.5 + 0.05 * rng.standard_normal((8, 3))
+    de = 0.5 + rng.random(nen)
+    ue = 0.1 * rng.standard_normal(nen * dim)
+    bf = np.array([0.3, -0.2, 0.1])
+    en, re, K, fint, dEn = fo.saint_venant_element(etype, X, de, ue, None, 0.3, bf)
+    dE_du = fo._complex_step(lambda v: fo.saint_venant_element(etype, X, de, v, None, 0.3, bf, False)[0], ue)
+    np.testing.assert_allclose(fint, dE_du, rtol=1e-10, atol=1e-12)
+    dR = fo._complex_step(lambda v: fo.saint_venant_element(etype, X, de, v, None, 0.3, bf, False)[1], ue)
+    np.testing.assert_allclose(K, dR, rtol=1e-10, atol=1e-12)
+    dE_de = fo._complex_step(lambda d: fo.saint_venant_element(etype, X, d, ue, None, 0.3, bf, False)[0], de)
+    np.testing.assert_allclose(dEn, dE_de, rtol=1e-10, atol=1e-12)
