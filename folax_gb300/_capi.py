@@ -29,7 +29,7 @@ STATUS_NAMES = {
 }
 
 QUAD4, HEX8, TET4 = 0, 1, 2
-THERMAL, ELASTIC, NEOHOOKE, SAINT_VENANT = 0, 1, 2, 3
+THERMAL, ELASTIC, NEOHOOKE, SAINT_VENANT, TRANSIENT_THERMAL = 0, 1, 2, 3, 4
 CONTROL_NODAL, CONTROL_ELEMENT = 0, 1
 SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
 OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4
@@ -53,6 +53,7 @@ class Physics(C.Structure):
         ("young_modulus", C.c_double), ("poisson_ratio", C.c_double),
         ("body_force", C.c_double * 3), ("beta", C.c_double), ("c", C.c_double),
         ("loss_exponent", C.c_double),
+        ("rho_cp", C.c_double), ("time_step", C.c_double), ("material_beta", C.c_double),
     ]
 
 
@@ -65,6 +66,7 @@ PROTOTYPES = {
     "folgb_plan_destroy": (C.c_int, [vp]),
     "folgb_plan_info": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
     "folgb_plan_set_dirichlet_values": (C.c_int, [vp, vp, f64]),
+    "folgb_plan_set_nodal_field": (C.c_int, [vp, vp]),
     "folgb_workspace_bytes": (sz, [vp, i32, i32]),
     "folgb_loss_adjoint": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_loss_adjoint_plain": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),

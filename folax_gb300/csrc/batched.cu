@@ -206,6 +206,7 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
   A.dofs_stride = 0;
   A.dmask = p->d_dmask;
   A.elem_bc = p->d_elem_bc;
+  A.k0 = p->d_k0;
   A.dval = p->d_dval;
   A.apply_dirichlet = apply_dirichlet;
   A.ctrl_layout = p->ctrl_layout;

@@ -24,19 +24,22 @@ struct Tag {
 
 template <class F>
 int dispatch(int et, int ph, F&& f) {
-  switch (et * 4 + ph) {
+  switch (et * 5 + ph) {
     case 0: return f(Tag<FOLGB_QUAD4, FOLGB_THERMAL>{});
     case 1: return f(Tag<FOLGB_QUAD4, FOLGB_ELASTIC>{});
     case 2: return f(Tag<FOLGB_QUAD4, FOLGB_NEOHOOKE>{});
     case 3: return f(Tag<FOLGB_QUAD4, FOLGB_SAINT_VENANT>{});
-    case 4: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
-    case 5: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
-    case 6: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
-    case 7: return f(Tag<FOLGB_HEX8, FOLGB_SAINT_VENANT>{});
-    case 8: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
-    case 9: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
-    case 10: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
-    case 11: return f(Tag<FOLGB_TET4, FOLGB_SAINT_VENANT>{});
+    case 4: return f(Tag<FOLGB_QUAD4, FOLGB_TRANSIENT_THERMAL>{});
+    case 5: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
+    case 6: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
+    case 7: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
+    case 8: return f(Tag<FOLGB_HEX8, FOLGB_SAINT_VENANT>{});
+    case 9: return f(Tag<FOLGB_HEX8, FOLGB_TRANSIENT_THERMAL>{});
+    case 10: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
+    case 11: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
+    case 12: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
+    case 13: return f(Tag<FOLGB_TET4, FOLGB_SAINT_VENANT>{});
+    case 14: return f(Tag<FOLGB_TET4, FOLGB_TRANSIENT_THERMAL>{});
   }
   return FOLGB_ERR_INVALID_ARGUMENT;
 }
@@ -54,6 +57,7 @@ struct VecArgs {
   int64_t dofs_stride;
   const unsigned char* dmask;
   const unsigned char* elem_bc;  // [E] element touches a Dirichlet dof
+  const float* k0;               // [N] nodal material field (transient thermal)
   const float* dval;
   int apply_dirichlet;
   int ctrl_layout;
@@ -134,6 +138,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
     float X[NEN][3];
     float ue[ND];
     float de[NEN];
+    float ke[PH == FOLGB_TRANSIENT_THERMAL ? NEN : 1];
     float eval = 0.f;
     const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
     const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
@@ -149,6 +154,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         ue[a * NDOF + c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
       }
       if (A.ctrl_layout == FOLGB_CONTROL_NODAL) de[a] = __ldg(ctrl + nodes[a]);
+      if constexpr (PH == FOLGB_TRANSIENT_THERMAL) ke[a] = __ldg(A.k0 + nodes[a]);
     }
     if (A.ctrl_layout != FOLGB_CONTROL_NODAL) eval = __ldg(ctrl + e);
     float g[ND];
@@ -174,6 +180,9 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
       float det = det_inv<DIM>(J, Ji);
       bad |= !(det > 0.f);
       const float wd = gp.w[q] * det;
+      // dN/dx = dN/dxi J^-1; the transient thermal element uses J^-1 dN/dxi^T
+      // instead (transient_thermal.py:57-59), the same for symmetric J
+      constexpr bool kTransposedInverse = PH == FOLGB_TRANSIENT_THERMAL;
       float dNdx[NEN][DIM];
 #pragma unroll
       for (int a = 0; a < NEN; ++a)
@@ -181,7 +190,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int j = 0; j < DIM; ++j) {
           float s = 0.f;
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], Ji[k][j], s);
+          for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], kTransposedInverse ? Ji[j][k] : Ji[k][j], s);
           dNdx[a][j] = s;
         }
       float egp;
@@ -267,6 +276,37 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
               g[a * DIM + i] -= f;
               energy = fmaf(-f, ue[a * DIM + i], energy);
             }
+        }
+      } else if constexpr (PH == FOLGB_TRANSIENT_THERMAL) {
+        // egp is the current temperature at the point (the nodal control)
+        float Tn = 0.f, kq = 0.f, gT[DIM];
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gT[j] = 0.f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          Tn = fmaf(gp.N[q][a], ue[a], Tn);
+          kq = fmaf(gp.N[q][a], ke[a], kq);
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
+        }
+        const float Kc = kq * (1.f + mt.mbeta * powf(Tn, mt.c));
+        const float dKdT = kq * mt.mbeta * mt.c * powf(Tn, mt.c - 1.f);
+        float gg = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gg = fmaf(gT[j], gT[j], gg);
+        const float diff = Tn - egp, rc = mt.rho_cp;
+        energy = fmaf(wd, 0.5f * Kc * gg + 0.5f * rc / mt.dt * diff * diff, energy);
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+          float gn = 0.f;
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) gn = fmaf(dNdx[a][j], gT[j], gn);
+          if (MODE == MODE_LOSS) {
+            g[a] = fmaf(wd, Kc * gn + (0.5f * dKdT * gg + rc / mt.dt * diff) * gp.N[q][a], g[a]);
+            gd[a] = fmaf(-wd * rc / mt.dt * diff, gp.N[q][a], gd[a]);
+          } else {
+            g[a] = fmaf(wd, rc * diff * gp.N[q][a] + mt.dt * Kc * gn, g[a]);
+          }
         }
       } else if constexpr (PH == FOLGB_SAINT_VENANT) {
         float H[DIM][DIM];

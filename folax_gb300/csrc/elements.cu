@@ -179,6 +179,7 @@ struct MatArgs {
   const float* dofs;
   int64_t dofs_stride;
   const unsigned char* dmask;
+  const float* k0;
   const float* dval;
   int apply_dirichlet;
   int ctrl_layout;
@@ -199,10 +200,12 @@ struct MatRec {
   static constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM;
   static constexpr int NV = Voigt<DIM>::NV;
   static constexpr int GEO = NEN * DIM + 3;  // dNdx, wd, coef, sedw
-  static constexpr int EXTRA = (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT) ? (2 * DIM * DIM + NV * NV) : 0;
+  static constexpr int EXTRA = (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT) ? (2 * DIM * DIM + NV * NV)
+                               : (PH == FOLGB_TRANSIENT_THERMAL ? NEN + 2 + DIM : 0);
   static constexpr int SIZE = GEO + EXTRA;
   static constexpr int O_WD = NEN * DIM, O_COEF = O_WD + 1, O_SED = O_WD + 2;
   static constexpr int O_F = GEO, O_M = GEO + DIM * DIM, O_HM = GEO + 2 * DIM * DIM;
+  static constexpr int O_N = GEO, O_K = GEO + NEN, O_DK = GEO + NEN + 1, O_GT = GEO + NEN + 2;  // transient
 };
 
 template <int ET, int PH, int MMODE>
@@ -257,7 +260,9 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       for (int j = 0; j < DIM; ++j) {
         float s = 0.f;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], Ji[k][j], s);
+        // the transient thermal element uses J^-1 dN/dxi^T (transient_thermal.py:57-59)
+        for (int k = 0; k < DIM; ++k)
+          s = fmaf(gp.dN[q][a][k], PH == FOLGB_TRANSIENT_THERMAL ? Ji[j][k] : Ji[k][j], s);
         dNdx[a][j] = s;
         rec[a * DIM + j] = s;
       }
@@ -269,7 +274,8 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       egp = __ldg(ctrl + e);
     }
     rec[R::O_WD] = wd;
-    const bool need_u = (PH == FOLGB_NEOHOOKE) || (PH == FOLGB_SAINT_VENANT) || (MMODE == MAT_PLAIN) ||
+    const bool need_u = (PH == FOLGB_NEOHOOKE) || (PH == FOLGB_SAINT_VENANT) || (PH == FOLGB_TRANSIENT_THERMAL) ||
+                        (MMODE == MAT_PLAIN) ||
                         (PH == FOLGB_THERMAL && mt.beta != 0.f);
     float ue[ND];
     if (need_u) {
@@ -324,6 +330,24 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
         sed = mt.lam * tr * tr + 2.f * mt.mu * sq + mt.mu * sh2;
       }
       rec[R::O_SED] = wd * sed;
+    } else if constexpr (PH == FOLGB_TRANSIENT_THERMAL) {
+      float Tn = 0.f, kq = 0.f, gT[DIM];
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) gT[j] = 0.f;
+#pragma unroll
+      for (int a = 0; a < NEN; ++a) {
+        Tn = fmaf(gp.N[q][a], ue[a], Tn);
+        kq = fmaf(gp.N[q][a], __ldg(A.k0 + nodes[a]), kq);
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
+        rec[R::O_N + a] = gp.N[q][a];
+      }
+      rec[R::O_COEF] = wd;
+      rec[R::O_SED] = 0.f;
+      rec[R::O_K] = kq * (1.f + mt.mbeta * powf(Tn, mt.c));
+      rec[R::O_DK] = kq * mt.mbeta * mt.c * powf(Tn, mt.c - 1.f);
+#pragma unroll
+      for (int j = 0; j < DIM; ++j) rec[R::O_GT + j] = gT[j];
     } else if constexpr (PH == FOLGB_SAINT_VENANT) {
       float H[DIM][DIM];
 #pragma unroll
@@ -437,6 +461,15 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       const float coef = rec[R::O_COEF];
       if constexpr (PH == FOLGB_THERMAL) {
         K[0][0] = fmaf(coef, dot, K[0][0]);
+      } else if constexpr (PH == FOLGB_TRANSIENT_THERMAL) {
+        // Me + dt (dK/dT N_a (grad T . grad N_b) + K grad N_a . grad N_b), as
+        // transient_thermal.py:64-76 writes it
+        float gTb = 0.f;
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) gTb = fmaf(rec[R::O_GT + j], dNb[j], gTb);
+        const float Na = rec[R::O_N + ra], Nb = rec[R::O_N + rb];
+        const float v = mt.rho_cp * Na * Nb + mt.dt * (rec[R::O_DK] * Na * gTb + rec[R::O_K] * dot);
+        K[0][0] = fmaf(coef, v, K[0][0]);
       } else if constexpr (PH == FOLGB_ELASTIC) {
 #pragma unroll
         for (int i = 0; i < DIM; ++i)
@@ -812,6 +845,7 @@ static VecArgs make_vec_args(const folgb_plan* p, int B, const float* control, i
   A.dofs_stride = dstride;
   A.dmask = p->d_dmask;
   A.elem_bc = p->d_elem_bc;
+  A.k0 = p->d_k0;
   A.dval = p->d_dval;
   A.apply_dirichlet = apply_dirichlet;
   A.ctrl_layout = p->ctrl_layout;
@@ -895,7 +929,8 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
                                         void* stream) {
   int rc = check_loss_args(p, B, control, dofs, losses);
   if (rc) return rc;
-  if (p->physics == FOLGB_NEOHOOKE || p->physics == FOLGB_SAINT_VENANT) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (p->physics == FOLGB_NEOHOOKE || p->physics == FOLGB_SAINT_VENANT ||
+      p->physics == FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
   LossWS w;
   size_t need = layout_loss(p, B, true, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
@@ -912,6 +947,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   M.dofs = dofs;
   M.dofs_stride = dofs_stride;
   M.dmask = p->d_dmask;
+  M.k0 = p->d_k0;
   M.dval = p->d_dval;
   M.apply_dirichlet = apply_dirichlet;
   M.ctrl_layout = p->ctrl_layout;
@@ -932,7 +968,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
   rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
-    if constexpr (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT) {
+    if constexpr (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT || PH == FOLGB_TRANSIENT_THERMAL) {
       return (int)FOLGB_ERR_INVALID_ARGUMENT;
     } else {
       int r = launch_matrix<ET, PH, MAT_PLAIN>(M, B, npts, s);
@@ -974,6 +1010,7 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
   M.dofs = dofs;
   M.dofs_stride = 0;
   M.dmask = p->d_dmask;
+  M.k0 = p->d_k0;
   M.dval = p->d_dval;
   M.apply_dirichlet = 0;
   M.ctrl_layout = p->ctrl_layout;

@@ -47,6 +47,7 @@ struct MatConst {
   float bf[3];          // body force
   int has_bf;
   int shear_ref;        // 1: reference (doubled) shear for the FE residual/tangent
+  float rho_cp, dt, mbeta;  // transient thermal: rho cp, time step, material beta
 };
 
 }  // namespace folgb
@@ -68,6 +69,7 @@ struct folgb_plan {
   int hex8_variant = 0;    // sum-factorised hex8 kernel variant (autotuned)
   unsigned char* d_dmask = nullptr;
   unsigned char* d_elem_bc = nullptr;  // [E] 1 if a node of the element has a Dirichlet dof
+  float* d_k0 = nullptr;               // [N] nodal material field (transient thermal k0)
   float* d_dval = nullptr;
   folgb::GPTable* d_gp = nullptr;
   std::vector<int64_t> dir_dofs;
@@ -150,7 +152,9 @@ template <> struct ElemT<FOLGB_QUAD4> { static constexpr int NEN = 4, DIM = 2; }
 template <> struct ElemT<FOLGB_HEX8>  { static constexpr int NEN = 8, DIM = 3; };
 template <> struct ElemT<FOLGB_TET4>  { static constexpr int NEN = 4, DIM = 3; };
 
-template <int PH, int DIM> struct NdofT { static constexpr int V = (PH == FOLGB_THERMAL) ? 1 : DIM; };
+template <int PH, int DIM> struct NdofT {
+  static constexpr int V = (PH == FOLGB_THERMAL || PH == FOLGB_TRANSIENT_THERMAL) ? 1 : DIM;
+};
 
 // ---------------------------------------------------------------------------
 // small dense helpers (fp32)

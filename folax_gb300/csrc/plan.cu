@@ -150,6 +150,9 @@ int fill_material(const folgb_physics& p, int dim, MatConst& m) {
   for (int i = 0; i < 3; ++i) m.bf[i] = (float)p.body_force[i];
   m.has_bf = (p.body_force[0] != 0.0 || p.body_force[1] != 0.0 || p.body_force[2] != 0.0) ? 1 : 0;
   m.shear_ref = p.shear_mode == FOLGB_SHEAR_REFERENCE ? 1 : 0;
+  m.rho_cp = (float)p.rho_cp;
+  m.dt = (float)p.time_step;
+  m.mbeta = (float)p.material_beta;
   return FOLGB_OK;
 }
 
@@ -258,11 +261,15 @@ int check_physics(const folgb_physics* phys, int& nen, int& dim, int& ndof) {
     case FOLGB_TET4: nen = 4; dim = 3; break;
     default: return FOLGB_ERR_INVALID_ARGUMENT;
   }
-  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_SAINT_VENANT) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
+  // the transient element's control is the nodal current temperature field
+  if (phys->physics == FOLGB_TRANSIENT_THERMAL &&
+      (phys->control_layout != FOLGB_CONTROL_NODAL || !(phys->time_step > 0.0)))
+    return FOLGB_ERR_INVALID_ARGUMENT;
   if (phys->control_layout != FOLGB_CONTROL_NODAL && phys->control_layout != FOLGB_CONTROL_ELEMENT)
     return FOLGB_ERR_INVALID_ARGUMENT;
   if (phys->num_gp < 1 || phys->num_gp > 3) return FOLGB_ERR_INVALID_ARGUMENT;
-  ndof = phys->physics == FOLGB_THERMAL ? 1 : dim;
+  ndof = (phys->physics == FOLGB_THERMAL || phys->physics == FOLGB_TRANSIENT_THERMAL) ? 1 : dim;
   return FOLGB_OK;
 }
 
@@ -345,6 +352,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     for (int a = 0; a < nen; ++a) elem_bc[e] |= dmask[c32[(size_t)e * nen + a]] ? 1 : 0;
   if ((rc = upload(&p->d_conn, c32.data(), c32.size())) || (rc = upload(&p->d_xyz4, x4.data(), x4.size())) ||
       (rc = upload(&p->d_elem_bc, elem_bc.data(), elem_bc.size())) ||
+      (rc = upload(&p->d_k0, std::vector<float>(num_nodes, 1.f).data(), (size_t)num_nodes)) ||
       (rc = upload(&p->d_inc_ptr, inc_ptr.data(), inc_ptr.size())) ||
       (rc = upload(&p->d_inc_slot, inc_rec.data(), inc_rec.size())) ||
       (pad && (rc = upload(&p->d_inc_padded, inc_padded.data(), inc_padded.size()))) ||
@@ -364,7 +372,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
 extern "C" int folgb_plan_destroy(folgb_plan* p) {
   if (!p) return FOLGB_OK;
   void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_inc_padded, p->d_dmask, p->d_elem_bc,
-                  p->d_dval, p->d_gp,
+                  p->d_k0, p->d_dval, p->d_gp,
                   p->d_adj_ptr, p->d_adj, p->d_rowptr, p->d_colind, p->d_pair_row, p->d_pair_ptr,
                   p->d_pair_slot};
   for (void* q : ptrs)
@@ -390,6 +398,14 @@ extern "C" int folgb_plan_set_dirichlet_values(folgb_plan* p, const double* valu
   std::vector<float> dval((size_t)p->ndof * p->N, 0.f);
   for (size_t i = 0; i < p->dir_dofs.size(); ++i) dval[p->dir_dofs[i]] = (float)(load_increment * values[i]);
   FOLGB_CUDA_TRY(cudaMemcpy(p->d_dval, dval.data(), dval.size() * sizeof(float), cudaMemcpyHostToDevice));
+  return FOLGB_OK;
+}
+
+extern "C" int folgb_plan_set_nodal_field(folgb_plan* p, const double* values) {
+  if (!p || !values) return FOLGB_ERR_INVALID_ARGUMENT;
+  std::vector<float> v(p->N);
+  for (int64_t n = 0; n < p->N; ++n) v[n] = (float)values[n];
+  FOLGB_CUDA_TRY(cudaMemcpy(p->d_k0, v.data(), v.size() * sizeof(float), cudaMemcpyHostToDevice));
   return FOLGB_OK;
 }
 

@@ -209,7 +209,14 @@ class FiniteElementLoss:
         p.beta = float(getattr(self, "_beta", 0.0))
         p.c = float(getattr(self, "_c", 1.0))
         p.loss_exponent = float(self.loss_function_exponent)
+        p.rho_cp = float(getattr(self, "_rho_cp", 1.0))
+        p.time_step = float(getattr(self, "_dt", 1.0))
+        p.material_beta = float(getattr(self, "_mbeta", 0.0))
         return p
+
+    def _configure_plan(self, plan: "Plan") -> "Plan":
+        """Per-plan data beyond the physics struct (overridden where needed)."""
+        return plan
 
     def Initialize(self, reinitialize=False) -> None:
         if self.initialized and not reinitialize:
@@ -232,15 +239,16 @@ class FiniteElementLoss:
         conn = np.asarray(self.fe_mesh.GetElementsNodes(self.element_type), dtype=np.int64)
         xyz = np.asarray(self.fe_mesh.GetNodesCoordinates(), dtype=np.float64)
         self._conn, self._xyz = conn, xyz
-        self._plan = Plan(self._physics_struct(), conn, xyz, self.dirichlet_indices, self.dirichlet_values, False)
+        self._plan = self._configure_plan(Plan(self._physics_struct(), conn, xyz, self.dirichlet_indices,
+                                               self.dirichlet_values, False))
         self._csr_plan = None
         self._status = _torch().zeros(1, dtype=_torch().int32, device="cuda")
         self.initialized = True
 
     def _get_csr_plan(self) -> Plan:
         if self._csr_plan is None:
-            self._csr_plan = Plan(self._physics_struct(), self._conn, self._xyz, self.dirichlet_indices,
-                                  self.dirichlet_values, True)
+            self._csr_plan = self._configure_plan(Plan(self._physics_struct(), self._conn, self._xyz,
+                                                       self.dirichlet_indices, self.dirichlet_values, True))
         return self._csr_plan
 
     def Finalize(self) -> None:
@@ -549,3 +557,78 @@ class SaintVenantMechanicalLoss2DQuad(SaintVenantMechanicalLoss):
         loss_settings.setdefault("num_gp", 2)
         super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["Ux", "Uy"], element_type="quad"),
                          fe_mesh)
+
+
+class TransientThermalLoss(ThermalLoss):
+    """transient_thermal.py:16-172: implicit-Euler step of nonlinear heat
+    conduction.  The control is the CURRENT nodal temperature field, the dofs
+    the NEXT one; material_dict gives rho, cp, beta and the nodal conductivity
+    k0 (default ones), time_integration_dict the time step, loss_settings "c"
+    the exponent of K = k0 (1 + beta T^c).  Energy (the loss) is
+    1/2 T.Se(T).T + rho cp/(2 dt) |T - T_current|^2 per element, with its true
+    gradient; the residual (Me + dt Se) T - Me T_current and the tangent
+    Me + dt Se_dR follow transient_thermal.py:64-78."""
+    physics = capi.TRANSIENT_THERMAL
+
+    def Initialize(self, reinitialize=False) -> None:
+        if self.initialized and not reinitialize:
+            return
+        mat = {"rho": 1.0, "cp": 1.0, "beta": 0.0, **self.loss_settings.get("material_dict", {})}
+        ti = {"method": "implicit-euler", "time_step": None, **self.loss_settings.get("time_integration_dict", {})}
+        if ti["time_step"] is None:
+            raise ValueError("time step should be provided in the time_integration_dict ")
+        n = self.fe_mesh.GetNumberOfNodes()
+        k0 = np.asarray(mat.get("k0", np.ones(n)), dtype=np.float64).reshape(-1)
+        if k0.shape != (n,):
+            raise ValueError(f"provided k0({k0.shape}) in the material_dict does not match the mesh with {n} nodes !")
+        self._k0 = np.ascontiguousarray(k0)
+        self._rho_cp = float(mat["rho"]) * float(mat["cp"])
+        self._dt = float(ti["time_step"])
+        self._mbeta = float(mat["beta"])
+        self.loss_settings["control_layout"] = "nodal"
+        super().Initialize(reinitialize)
+        self._beta = 0.0
+
+    def _configure_plan(self, plan):
+        capi.check("folgb_plan_set_nodal_field", plan.lib.folgb_plan_set_nodal_field(plan.handle,
+                                                                                    self._k0.ctypes.data))
+        return plan
+
+    def ComputeElement(self, xyze, Te_c, Te_n, Ke):
+        """(energy, residual, tangent) of one element (transient_thermal.py:43-78)."""
+        nen = _NEN[self.element_type]
+        settings = dict(self.loss_settings)
+        settings["material_dict"] = {**settings.get("material_dict", {}),
+                                     "k0": np.asarray(Ke, dtype=np.float64).reshape(nen)}
+        xyze = np.asarray(xyze, dtype=np.float64)
+        mesh = Mesh("element", "element.mem")
+        mesh.node_ids = np.arange(nen)
+        mesh.nodes_coordinates = xyze
+        mesh.elements_nodes = {self.element_type: np.arange(nen)[None]}
+        settings["dirichlet_bc_dict"] = {d: {} for d in self.dofs}
+        settings["loss_function_exponent"] = 1.0
+        one = type(self)(self._name + "_element", settings, mesh)
+        one.Initialize()
+        tc = np.asarray(Te_c, dtype=np.float64).reshape(-1)
+        tn = np.asarray(Te_n, dtype=np.float64).reshape(-1)
+        jac, res = one.ComputeJacobianMatrixAndResidualVector(tc, tn)
+        en = one.ComputeTotalEnergy(tc, tn)
+        return float(en.item()), res.double().cpu().numpy(), jac.todense()
+
+
+class TransientThermalLoss3DTetra(TransientThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["T"], element_type="tetra"), fe_mesh)
+
+
+class TransientThermalLoss3DHexa(TransientThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=3, ordered_dofs=["T"], element_type="hexahedron"),
+                         fe_mesh)
+
+
+class TransientThermalLoss2DQuad(TransientThermalLoss):
+    def __init__(self, name, loss_settings, fe_mesh):
+        loss_settings.setdefault("num_gp", 2)
+        super().__init__(name, _with(loss_settings, compute_dims=2, ordered_dofs=["T"], element_type="quad"), fe_mesh)

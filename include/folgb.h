@@ -47,7 +47,10 @@ enum {
   FOLGB_THERMAL = 0,  /* thermal.py:28-49                 */
   FOLGB_ELASTIC = 1,  /* mechanical.py:98-117             */
   FOLGB_NEOHOOKE = 2, /* mechanical_neohooke_AD.py:254-293 */
-  FOLGB_SAINT_VENANT = 3 /* mechanical_saint_venant.py:263-296 */
+  FOLGB_SAINT_VENANT = 3, /* mechanical_saint_venant.py:263-296 */
+  FOLGB_TRANSIENT_THERMAL = 4 /* transient_thermal.py:43-78: implicit Euler;
+                                 the control is the current temperature
+                                 field, the dofs the next one */
 };
 /* control layout: nodal values gathered by connectivity (fe_loss.py:160), or
  * one value per element used as de = value * 1 (partition of unity). */
@@ -59,7 +62,8 @@ enum { FOLGB_SHEAR_REFERENCE = 0, FOLGB_SHEAR_CONSISTENT = 1 };
 
 typedef struct folgb_physics {
   int32_t element_type;   /* FOLGB_QUAD4 / HEX8 / TET4                         */
-  int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE / SAINT_VENANT */
+  int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE / SAINT_VENANT /
+                             TRANSIENT_THERMAL                                  */
   int32_t num_gp;         /* Gauss order 1..3 ("num_gp", fe_loss.py:68-83)     */
   int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
   int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */
@@ -72,6 +76,10 @@ typedef struct folgb_physics {
   double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */
   double beta, c;         /* thermal conductivity nonlinearity (thermal.py:22) */
   double loss_exponent;   /* loss_function_exponent (fe_loss.py:117-120)       */
+  /* transient thermal only (transient_thermal.py:20-41): rho * cp, the time
+   * step, and material_dict "beta" (K = k0 (1 + material_beta T^c), c above);
+   * the nodal k0 field is set with folgb_plan_set_nodal_field (default 1) */
+  double rho_cp, time_step, material_beta;
 } folgb_physics;
 
 typedef struct folgb_plan folgb_plan;
@@ -100,6 +108,11 @@ int folgb_plan_info(const folgb_plan* plan, int64_t* ndof_per_node, int64_t* tot
  * load_increment (ApplyDirichletBCOnDofVector, fe_loss.py:186-189). values is a
  * HOST array in the order given to folgb_plan_create. */
 int folgb_plan_set_dirichlet_values(folgb_plan* plan, const double* values, double load_increment);
+
+/* Sets the plan's nodal material field (HOST, num_nodes doubles): the
+ * transient-thermal conductivity k0 (material_dict "k0",
+ * transient_thermal.py:24-33).  Other physics ignore it. */
+int folgb_plan_set_nodal_field(folgb_plan* plan, const double* values);
 
 /* Operation ids for folgb_workspace_bytes. */
 enum { FOLGB_OP_LOSS_ADJOINT = 0, FOLGB_OP_ASSEMBLE = 1, FOLGB_OP_PCG = 2,

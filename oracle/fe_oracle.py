@@ -433,6 +433,64 @@ def neohooke_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None,
     return energy, re, Ke, fcons, dEn
 
 
+def transient_thermal_element(etype, X, Tc, Tn, k0, num_gp=2, rho_cp=1.0, dt=1.0, beta=0.0, c=1.0,
+                              want_tangent=True):
+    """Implicit-Euler transient thermal element (transient_thermal.py:43-78).
+
+    Tc: current nodal temperatures (the control), Tn: next (the unknowns), k0:
+    nodal conductivity field.  The element's gradient operator is the
+    reference's B = J^-1 dN/dxi^T (transient_thermal.py:57-59), i.e. the
+    transpose of J^-1 where ShapeFunctionsGlobalGradients uses J^-T; the two
+    agree when J is symmetric, and the golden vectors follow this one.
+    Per Gauss point K = (N.k0)(1 + beta T_n^c),
+    Se = sum w detJ K dN dN^T, Me = sum w detJ rho cp N N^T.  Returns
+    (energy, re, Ke, dEnergy/dTn, dEnergy/dTc) with
+      energy = 1/2 Tn.Se(Tn).Tn + sum w detJ rho cp /(2 dt) (T_n - T_c)^2,
+      re = (Me + dt Se) Tn - Me Tc,  Ke = Me + dt Se_dR,
+      Se_dR = sum w detJ (dK/dT N (x) (grad T . grad N) + K dN dN^T)
+    (as written at :64 this is the transpose of d re / d Tn when beta != 0);
+    the energy has no stop-gradient, so dEnergy/dTn includes dK/dT."""
+    X, Tc, Tn, squeeze = _as_batch(X, Tc, Tn)
+    k0 = np.atleast_2d(np.asarray(k0))
+    nen, dim = ELEMENTS[etype]
+    pts, wts = gauss_rule(etype, num_gp)
+    E = X.shape[0]
+    dt_ = np.result_type(X, Tc, Tn, k0)
+    Se = np.zeros((E, nen, nen), dtype=dt_)
+    Me = np.zeros((E, nen, nen), dtype=dt_)
+    SdR = np.zeros((E, nen, nen), dtype=dt_)
+    tterm = np.zeros(E, dtype=dt_)
+    dEn = np.zeros((E, nen), dtype=dt_)
+    dEc = np.zeros((E, nen), dtype=dt_)
+    for xi, w in zip(pts, wts):
+        Nv = shape_values(etype, xi)
+        J = jacobian(etype, X, xi)
+        detJ = _det(J)
+        dNdx = np.einsum("ejk,ak->eaj", _inv(J), shape_local_grads(etype, xi))  # B^T of the reference
+        wd = w * detJ
+        Tq_n, Tq_c, kq = Tn @ Nv, Tc @ Nv, k0 @ Nv
+        K = kq * (1.0 + beta * Tq_n ** c)
+        dKdT = kq * beta * c * Tq_n ** (c - 1.0)
+        gT = np.einsum("ea,eaj->ej", Tn, dNdx)
+        GG = np.einsum("eaj,ebj->eab", dNdx, dNdx)
+        Se += (wd * K)[:, None, None] * GG
+        Me += (rho_cp * wd)[:, None, None] * np.outer(Nv, Nv)[None]
+        diff = Tq_n - Tq_c
+        tterm += rho_cp * 0.5 / dt * wd * diff ** 2
+        gTN = np.einsum("ej,ebj->eb", gT, dNdx)
+        SdR += wd[:, None, None] * (dKdT[:, None, None] * Nv[None, :, None] * gTN[:, None, :]
+                                    + K[:, None, None] * GG)
+        dEn += wd[:, None] * (K[:, None] * gTN + 0.5 * (dKdT * np.einsum("ej,ej->e", gT, gT))[:, None] * Nv[None]
+                              + (rho_cp / dt * diff)[:, None] * Nv[None])
+        dEc -= (wd * rho_cp / dt * diff)[:, None] * Nv[None]
+    energy = 0.5 * np.einsum("ea,eab,eb->e", Tn, Se, Tn) + tterm
+    re = np.einsum("eab,eb->ea", Me + dt * Se, Tn) - np.einsum("eab,eb->ea", Me, Tc)
+    Ke = Me + dt * SdR
+    if squeeze:
+        return energy[0], re[0], Ke[0], dEn[0], dEc[0]
+    return energy, re, Ke, dEn, dEc
+
+
 def saint_venant_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None, want_tangent=True):
     """Saint-Venant-Kirchhoff element (mechanical_saint_venant.py:263-296 with
     constitutive_material_models/saint_venant.py:13-31).
@@ -526,7 +584,7 @@ def square_mesh(L, N):
 # ----------------------------------------------------------------------------
 
 PHYSICS_NDOF = {"thermal": lambda dim: 1, "elastic": lambda dim: dim, "neohooke": lambda dim: dim,
-                "saint_venant": lambda dim: dim}
+                "saint_venant": lambda dim: dim, "transient_thermal": lambda dim: 1}
 
 
 class FELossOracle:
@@ -540,7 +598,8 @@ class FELossOracle:
 
     def __init__(self, etype, physics, xyz, conn, dirichlet=None, node_sets=None,
                  num_gp=None, young=1.0, nu=0.3, body_force=None, beta=0.0, c=1.0,
-                 exponent=1.0, shear_mode="reference", control_layout="nodal"):
+                 exponent=1.0, shear_mode="reference", control_layout="nodal",
+                 rho_cp=1.0, time_step=1.0, material_beta=0.0, k0=None):
         self.etype, self.physics = etype, physics
         self.nen, self.dim = ELEMENTS[etype]
         self.ndof = PHYSICS_NDOF[physics](self.dim)
@@ -553,6 +612,10 @@ class FELossOracle:
         self.exponent = exponent
         self.shear_mode = shear_mode
         self.control_layout = control_layout
+        # transient thermal (transient_thermal.py:20-41): the control is the
+        # current temperature field, k0 a nodal conductivity field
+        self.rho_cp, self.time_step, self.material_beta = rho_cp, time_step, material_beta
+        self.k0 = np.ones(len(xyz)) if k0 is None else np.asarray(k0, dtype=np.float64)
         self.total_dofs = self.ndof * self.num_nodes
         # __CreateDofsDict (fe_loss.py:34-55)
         idx, val = [], []
@@ -593,6 +656,10 @@ class FELossOracle:
             return en, re, Ke, re, dEn
         if self.physics == "saint_venant":
             return saint_venant_element(self.etype, X, de, ue, self.num_gp, self.nu, self.body_force, want_tangent)
+        if self.physics == "transient_thermal":
+            en, re, Ke, dEn, dEc = transient_thermal_element(self.etype, X, de, ue, self.k0[self.conn], self.num_gp,
+                                                             self.rho_cp, self.time_step, self.material_beta, self.c)
+            return en, re, Ke, dEn, dEc
         en, re, Ke, fcons, dEn = neohooke_element(self.etype, X, de, ue, self.num_gp, self.nu,
                                                   self.body_force, self.shear_mode, want_tangent)
         return en, re, Ke, fcons, dEn

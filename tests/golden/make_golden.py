@@ -131,12 +131,30 @@ def sensitivity_test(ref_root):
     return out
 
 
+def transient_thermal_tests(ref_root):
+    """Implicit-Euler transient thermal element (test_nonlinear_transient_thermal.py):
+    T_current = 1, T_next = 0, k0 = 1, rho = cp = 1, beta = 1.5, c = 1, dt = 0.005."""
+    rel = "tests/unit/test_nonlinear_transient_thermal.py"
+    fns = _arrays_by_function(os.path.join(ref_root, rel))
+    out = {}
+    for fn, key in (("test_tetra", "tet4"), ("test_hexa", "hex8")):
+        arrs = fns[fn]
+        coords = arrs[0]
+        mats = [a for a in arrs if a[1].ndim == 2 and a[1].shape[0] == a[1].shape[1] and a[1].shape[0] > 3]
+        vecs = [a for a in arrs if a[1].ndim == 1 and a[1].size > 3]
+        out[key] = {"xyz": _entry(rel, *coords), "stiffness": _entry(rel, *mats[0]),
+                    "residual": _entry(rel, *vecs[0])}
+    out.update({"rho": 1.0, "cp": 1.0, "beta": 1.5, "c": 1.0, "time_step": 0.005, "rtol": 1e-5, "atol": 1e-10})
+    return out
+
+
 def main(ref_root):
     fixtures = {
         "mechanical_linear.json": element_tests(ref_root, "tests/unit/test_mechanical_loss.py"),
         "neohooke_ad.json": element_tests(ref_root, "tests/unit/test_neo_hooke_mechanical_loss_AD.py"),
         "geometries.json": geometry_tests(ref_root),
         "sensitivity_quad4.json": sensitivity_test(ref_root),
+        "transient_thermal.json": transient_thermal_tests(ref_root),
     }
     for name, obj in fixtures.items():
         with open(os.path.join(HERE, name), "w") as f:

@@ -91,3 +91,17 @@ def test_sensitivity_golden():
     np.testing.assert_allclose(rhs, arr(S["rhs"]), **tol)
     np.testing.assert_allclose(R.nodal_control_derivatives(K, u, adj), arr(S["control_derivatives"]), **tol)
     np.testing.assert_allclose(R.nodal_shape_derivatives(K, u, adj), arr(S["shape_derivatives"]), **tol)
+
+
+@pytest.mark.parametrize("etype", ["tet4", "hex8"])
+def test_transient_thermal_element_golden(etype):
+    """tests/unit/test_nonlinear_transient_thermal.py: ComputeElement with
+    T_current = 1, T_next = 0, k0 = 1 (rho = cp = 1, beta = 1.5, dt = 0.005)."""
+    G = golden("transient_thermal.json")
+    g = G[etype]
+    nen = fo.ELEMENTS[etype][0]
+    en, re, K, dEn, dEc = fo.transient_thermal_element(etype, arr(g["xyz"]), np.ones(nen), np.zeros(nen), np.ones(nen),
+                                                       NGP[etype], G["rho"] * G["cp"], G["time_step"], G["beta"],
+                                                       G["c"])
+    np.testing.assert_allclose(K, arr(g["stiffness"]), rtol=G["rtol"], atol=G["atol"])
+    np.testing.assert_allclose(re, arr(g["residual"]), rtol=G["rtol"], atol=G["atol"])

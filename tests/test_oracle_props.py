@@ -131,3 +131,28 @@ def test_saint_venant_element_consistency(etype):
     np.testing.assert_allclose(K, dR, rtol=1e-10, atol=1e-12)
     dE_de = fo._complex_step(lambda d: fo.saint_venant_element(etype, X, d, ue, None, 0.3, bf, False)[0], de)
     np.testing.assert_allclose(dEn, dE_de, rtol=1e-10, atol=1e-12)
+
+
+@pytest.mark.parametrize("etype", ["tet4", "hex8", "quad4"])
+@pytest.mark.parametrize("beta,c", [(0.0, 1.0), (1.5, 1.0), (0.7, 2.0)])
+def test_transient_thermal_consistency(etype, beta, c):
+    """Transient thermal element: dEnergy/dTn and dEnergy/dTc are the
+    derivatives of the energy value, and the tangent is (d residual / d Tn)^T."""
+    rng = np.random.default_rng(11)
+    nen, dim = fo.ELEMENTS[etype]
+    X = {"quad4": np.array([[0.0, 0.0, 0.0], [1.1, 0.1, 0.0], [1.0, 0.9, 0.0], [0.1, 1.2, 0.0]]),
+         "tet4": np.array([[0.0, 0.0, 0.0], [1.0, 0.1, 0.0], [0.1, 1.0, 0.1], [0.0, 0.2, 1.1]]),
+         "hex8": np.array(fo._HEX_SIGNS) * 0.5 + 0.5 + 0.05 * rng.standard_normal((8, 3))}[etype]
+    Tc, Tn, k0 = rng.random(nen), 0.5 + rng.random(nen), 0.5 + rng.random(nen)
+    args = (None, 2 if etype != "tet4" else 1, 1.3, 0.01, beta, c)
+
+    def f(tc, tn):
+        return fo.transient_thermal_element(etype, X, tc, tn, k0, *args[1:])
+    en, re, K, dEn, dEc = f(Tc, Tn)
+    np.testing.assert_allclose(dEn, fo._complex_step(lambda v: f(Tc, v)[0], Tn), rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(dEc, fo._complex_step(lambda v: f(v, Tn)[0], Tc), rtol=1e-10, atol=1e-12)
+    # the reference's tangent writes the conductivity-derivative term as
+    # N_a (grad T . grad N_b) (transient_thermal.py:64), the transpose of
+    # d r_a / d T_b; Me and the conductivity term are symmetric, so the whole
+    # matrix is the transpose of the exact Jacobian (equal when beta = 0)
+    np.testing.assert_allclose(K, fo._complex_step(lambda v: f(Tc, v)[1], Tn).T, rtol=1e-10, atol=1e-12)
