@@ -433,6 +433,113 @@ def neohooke_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None,
     return energy, re, Ke, fcons, dEn
 
 
+# --- Neo-Hookean with a volumetric-isochoric split (non-AD variant) ------------
+# fol/loss_functions/mechanical_neohooke.py:243-275 with
+# fol/constitutive_material_models/neo_hooke.py:14-59 (2-D), 64-111 (3-D).
+
+def bulk_shear(e, nu):
+    """kappa, mu from the Young's modulus field at a Gauss point
+    (mechanical_neohooke.py:254-255; the same 3-D bulk modulus in 2-D)."""
+    return e / (3.0 * (1.0 - 2.0 * nu)), e / (2.0 * (1.0 + nu))
+
+
+def nh_split_energy_stress(C, kappa, mu):
+    """psi = kappa/4 (J^2 - 2 lnJ - 1) + mu/2 (J^(-2/d) I1 - d) in d = 2 or 3
+    dimensions (neo_hooke.py:35-38, 87-90) and S = 2 dpsi/dC,
+      S = kappa/2 (J^2 - 1) C^-1 + mu J^(-2/d) (I - I1/d C^-1)
+    (neo_hooke.py:41-45, 93-97: J p C^-1 + J^(-2/d) P:(mu I)).  Returns psi, S,
+    the directional derivative dS(dC) (the reference's C_vol + C_iso,
+    neo_hooke.py:47-56, 99-108, is 2 dS/dC), dpsi/dkappa and dpsi/dmu."""
+    d = C.shape[-1]
+    detC = _det(C)
+    lnJ = 0.5 * np.log(detC)
+    Ci = _inv(C)
+    I1 = np.trace(C, axis1=-2, axis2=-1)
+    eye = np.eye(d)
+    k_ = kappa[..., None, None]
+    mu_ = mu[..., None, None]
+    a = np.exp(-2.0 / d * lnJ)                  # J^(-2/d)
+    dpsi_dk = 0.25 * (detC - 2.0 * lnJ - 1.0)
+    dpsi_dmu = 0.5 * (a * I1 - d)
+    psi = kappa * dpsi_dk + mu * dpsi_dmu
+    iso = eye - (I1 / d)[..., None, None] * Ci
+    S = 0.5 * k_ * (detC - 1.0)[..., None, None] * Ci + mu_ * a[..., None, None] * iso
+
+    def dS(dC):
+        trCidC = np.einsum("...ij,...ji->...", Ci, dC)
+        dCi = -Ci @ dC @ Ci
+        ddet = detC * trCidC
+        da = -(1.0 / d) * a * trCidC
+        dI1 = np.trace(dC, axis1=-2, axis2=-1)
+        diso = -((dI1 / d)[..., None, None] * Ci + (I1 / d)[..., None, None] * dCi)
+        return (0.5 * k_ * (ddet[..., None, None] * Ci + (detC - 1.0)[..., None, None] * dCi)
+                + mu_ * (da[..., None, None] * iso + a[..., None, None] * diso))
+
+    return psi, S, dS, dpsi_dk, dpsi_dmu
+
+
+def neohooke_split_element(etype, X, de, ue, num_gp=None, nu=0.3, body_force=None, want_tangent=True):
+    """Neo-Hookean element of mechanical_neohooke.py:243-275.
+
+    Per Gauss point kappa, mu from the interpolated Young's modulus
+    (:253-255), F = I + H, psi and S of nh_split_energy_stress.  Returns
+    (energy, re, Ke, fint, dEnergy/dde) with energy = sum_gp w detJ psi (:266),
+    fint = sum_gp w detJ B^T S_voigt (:265, = d energy / d ue), re = fint - Fe
+    (:275) and Ke = B^T C_voigt B + the geometric stiffness (:262-263,
+    = d re / d ue: the material model's tangent is consistent with its stress).
+    """
+    X, de, ue, squeeze = _as_batch(X, de, ue)
+    nen, d = ELEMENTS[etype]
+    if num_gp is None:
+        num_gp = 1 if etype == "tet4" else 2
+    V = _V3 if d == 3 else _V2
+    b = np.zeros(d) if body_force is None else np.asarray(body_force, dtype=np.float64).ravel()[:d]
+    pts, wts = gauss_rule(etype, num_gp)
+    E = X.shape[0]
+    dt = np.result_type(X, de, ue)
+    nd = d * nen
+    energy = np.zeros(E, dtype=dt)
+    fint = np.zeros((E, nd), dtype=dt)
+    Fe = np.zeros((E, nd), dtype=dt)
+    Ke = np.zeros((E, nd, nd), dtype=dt) if want_tangent else None
+    dEn = np.zeros((E, nen), dtype=dt)
+    U = ue.reshape(E, nen, d)
+    k1, mu1 = bulk_shear(1.0, nu)
+    for xi, w in zip(pts, wts):
+        Nv = shape_values(etype, xi)
+        dNdx, detJ = global_grads(etype, X, xi)
+        wd = w * detJ
+        kappa, mu = bulk_shear(de @ Nv, nu)
+        F = np.eye(d) + np.einsum("eai,eaj->eij", U, dNdx)
+        C = np.einsum("eki,ekj->eij", F, F)
+        psi, S, dS, dpsi_dk, dpsi_dmu = nh_split_energy_stress(C, kappa, mu)
+        B = nl_B(F, dNdx)
+        Sv = np.stack([S[:, p, q] for p, q in V], axis=1)
+        fint += wd[:, None] * np.einsum("evi,ev->ei", B, Sv)
+        energy += wd * psi
+        Fe += wd[:, None] * (N_matrix(Nv, d).T @ b)[None]
+        dEn += (wd * (k1 * dpsi_dk + mu1 * dpsi_dmu))[:, None] * Nv[None]
+        if want_tangent:
+            G = np.einsum("eap,epq,ebq->eab", dNdx, S, dNdx)
+            Kg = np.zeros((E, nd, nd), dtype=dt)
+            for k in range(d):
+                Kg[:, k::d, k::d] = G
+            Km = np.zeros((E, nd, nd), dtype=dt)
+            for bnode in range(nen):
+                for l in range(d):
+                    dF = np.zeros((E, d, d), dtype=dt)
+                    dF[:, l, :] = dNdx[:, bnode, :]
+                    dC = np.einsum("eki,ekj->eij", dF, F) + np.einsum("eki,ekj->eij", F, dF)
+                    dSt = dS(dC)
+                    dSv = np.stack([dSt[:, p, q] for p, q in V], axis=1)
+                    Km[:, :, d * bnode + l] = np.einsum("evi,ev->ei", B, dSv)
+            Ke += wd[:, None, None] * (Km + Kg)
+    re = fint - Fe
+    if squeeze:
+        return energy[0], re[0], (Ke[0] if want_tangent else None), fint[0], dEn[0]
+    return energy, re, Ke, fint, dEn
+
+
 def transient_thermal_element(etype, X, Tc, Tn, k0, num_gp=2, rho_cp=1.0, dt=1.0, beta=0.0, c=1.0,
                               want_tangent=True):
     """Implicit-Euler transient thermal element (transient_thermal.py:43-78).
@@ -584,7 +691,8 @@ def square_mesh(L, N):
 # ----------------------------------------------------------------------------
 
 PHYSICS_NDOF = {"thermal": lambda dim: 1, "elastic": lambda dim: dim, "neohooke": lambda dim: dim,
-                "saint_venant": lambda dim: dim, "transient_thermal": lambda dim: 1}
+                "saint_venant": lambda dim: dim, "transient_thermal": lambda dim: 1,
+                "neohooke_split": lambda dim: dim}
 
 
 class FELossOracle:
@@ -656,6 +764,8 @@ class FELossOracle:
             return en, re, Ke, re, dEn
         if self.physics == "saint_venant":
             return saint_venant_element(self.etype, X, de, ue, self.num_gp, self.nu, self.body_force, want_tangent)
+        if self.physics == "neohooke_split":
+            return neohooke_split_element(self.etype, X, de, ue, self.num_gp, self.nu, self.body_force, want_tangent)
         if self.physics == "transient_thermal":
             en, re, Ke, dEn, dEc = transient_thermal_element(self.etype, X, de, ue, self.k0[self.conn], self.num_gp,
                                                              self.rho_cp, self.time_step, self.material_beta, self.c)

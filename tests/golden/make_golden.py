@@ -152,6 +152,7 @@ def main(ref_root):
     fixtures = {
         "mechanical_linear.json": element_tests(ref_root, "tests/unit/test_mechanical_loss.py"),
         "neohooke_ad.json": element_tests(ref_root, "tests/unit/test_neo_hooke_mechanical_loss_AD.py"),
+        "neohooke.json": element_tests(ref_root, "tests/unit/test_neo_hooke_mechanical_loss.py"),
         "geometries.json": geometry_tests(ref_root),
         "sensitivity_quad4.json": sensitivity_test(ref_root),
         "transient_thermal.json": transient_thermal_tests(ref_root),

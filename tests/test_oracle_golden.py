@@ -47,6 +47,20 @@ def test_neohooke_element_golden(etype):
     np.testing.assert_allclose(re, arr(g["residual"]), rtol=1e-5, atol=1e-6)
 
 
+@pytest.mark.parametrize("etype", ["tet4", "hex8", "quad4"])
+def test_neohooke_split_element_golden(etype):
+    """tests/unit/test_neo_hooke_mechanical_loss.py (the non-AD element of
+    mechanical_neohooke.py): K_e = B^T C B + geometric stiffness, r_e, at u = 1."""
+    g = golden("neohooke.json")[etype]
+    nen, dim = fo.ELEMENTS[etype]
+    en, re, K, fint, dE = fo.neohooke_split_element(etype, arr(g["xyz"]), np.ones(nen), np.ones(nen * dim),
+                                                    NGP[etype], g["poisson_ratio"], arr(g["body_force"]).ravel())
+    np.testing.assert_allclose(K, arr(g["stiffness"]), rtol=g["rtol"], atol=g["atol"])
+    np.testing.assert_allclose(re, arr(g["residual"]).ravel(), rtol=g["rtol"], atol=g["atol"])
+    # u = 1 is a rigid translation: stress-free, so r_e = -F_e
+    assert abs(en) < 1e-12 and np.abs(fint).max() < 1e-12
+
+
 @pytest.mark.parametrize("etype", ["quad4", "tet4", "hex8"])
 @pytest.mark.parametrize("order", [1, 2, 3])
 def test_geometry_golden(etype, order):

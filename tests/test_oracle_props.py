@@ -110,9 +110,12 @@ def test_newton_neohooke_converges():
 
 
 @pytest.mark.parametrize("etype", ["tet4", "hex8", "quad4"])
-def test_saint_venant_element_consistency(etype):
-    """Saint-Venant element: internal force = d energy / d u and tangent =
-    d residual / d u (complex step), energy control derivative = d energy / d e."""
+@pytest.mark.parametrize("element", ["saint_venant_element", "neohooke_split_element"])
+def test_hyperelastic_element_consistency(etype, element):
+    """Saint-Venant and split neo-Hooke elements: internal force = d energy / d u
+    and tangent = d residual / d u (complex step), energy control derivative =
+    d energy / d e."""
+    elem = getattr(fo, element)
     rng = np.random.default_rng(9)
     nen, dim = fo.ELEMENTS[etype]
     if etype == "quad4":
@@ -124,12 +127,12 @@ def test_saint_venant_element_consistency(etype):
     de = 0.5 + rng.random(nen)
     ue = 0.1 * rng.standard_normal(nen * dim)
     bf = np.array([0.3, -0.2, 0.1])
-    en, re, K, fint, dEn = fo.saint_venant_element(etype, X, de, ue, None, 0.3, bf)
-    dE_du = fo._complex_step(lambda v: fo.saint_venant_element(etype, X, de, v, None, 0.3, bf, False)[0], ue)
+    en, re, K, fint, dEn = elem(etype, X, de, ue, None, 0.3, bf)
+    dE_du = fo._complex_step(lambda v: elem(etype, X, de, v, None, 0.3, bf, False)[0], ue)
     np.testing.assert_allclose(fint, dE_du, rtol=1e-10, atol=1e-12)
-    dR = fo._complex_step(lambda v: fo.saint_venant_element(etype, X, de, v, None, 0.3, bf, False)[1], ue)
+    dR = fo._complex_step(lambda v: elem(etype, X, de, v, None, 0.3, bf, False)[1], ue)
     np.testing.assert_allclose(K, dR, rtol=1e-10, atol=1e-12)
-    dE_de = fo._complex_step(lambda d: fo.saint_venant_element(etype, X, d, ue, None, 0.3, bf, False)[0], de)
+    dE_de = fo._complex_step(lambda d: elem(etype, X, d, ue, None, 0.3, bf, False)[0], de)
     np.testing.assert_allclose(dEn, dE_de, rtol=1e-10, atol=1e-12)
 
 
