@@ -3,8 +3,9 @@
 The package keeps the reference's FiniteElementLoss / Solver API
 (fol/loss_functions, fol/solvers) and runs every numerical step in the CUDA
 kernels of libfolgb.so (C ABI: include/folgb.h).  Loss classes live in
-``folax_gb300.loss``, solvers in ``folax_gb300.solvers``, the many-instance
-path in ``folax_gb300.batched``.
+``folax_gb300.loss`` (the split neo-Hooke family of the reference's
+mechanical_neohooke.py in ``folax_gb300.mechanical_neohooke``), solvers in
+``folax_gb300.solvers``, the many-instance path in ``folax_gb300.batched``.
 """
 from .mesh import Mesh, create_2D_square_mesh, create_3D_box_mesh, split_hex_to_tets  # noqa: F401
 

@@ -29,7 +29,7 @@ STATUS_NAMES = {
 }
 
 QUAD4, HEX8, TET4 = 0, 1, 2
-THERMAL, ELASTIC, NEOHOOKE, SAINT_VENANT, TRANSIENT_THERMAL = 0, 1, 2, 3, 4
+THERMAL, ELASTIC, NEOHOOKE, SAINT_VENANT, TRANSIENT_THERMAL, NEOHOOKE_SPLIT = 0, 1, 2, 3, 4, 5
 CONTROL_NODAL, CONTROL_ELEMENT = 0, 1
 SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
 OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4

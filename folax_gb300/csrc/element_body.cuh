@@ -8,6 +8,9 @@
 //   thermal element                 fol/loss_functions/thermal.py:28-49
 //   linear elastic element          fol/loss_functions/mechanical.py:98-117
 //   Neo-Hookean (AD) element        fol/loss_functions/mechanical_neohooke_AD.py:254-293
+//   split Neo-Hookean element       fol/loss_functions/mechanical_neohooke.py:243-275
+//   Saint-Venant-Kirchhoff element  fol/loss_functions/mechanical_saint_venant.py:263-296
+//   transient thermal element       fol/loss_functions/transient_thermal.py:43-78
 //   batch loss                      fol/loss_functions/fe_loss.py:250-262
 #pragma once
 
@@ -24,22 +27,25 @@ struct Tag {
 
 template <class F>
 int dispatch(int et, int ph, F&& f) {
-  switch (et * 5 + ph) {
+  switch (et * 6 + ph) {
     case 0: return f(Tag<FOLGB_QUAD4, FOLGB_THERMAL>{});
     case 1: return f(Tag<FOLGB_QUAD4, FOLGB_ELASTIC>{});
     case 2: return f(Tag<FOLGB_QUAD4, FOLGB_NEOHOOKE>{});
     case 3: return f(Tag<FOLGB_QUAD4, FOLGB_SAINT_VENANT>{});
     case 4: return f(Tag<FOLGB_QUAD4, FOLGB_TRANSIENT_THERMAL>{});
-    case 5: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
-    case 6: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
-    case 7: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
-    case 8: return f(Tag<FOLGB_HEX8, FOLGB_SAINT_VENANT>{});
-    case 9: return f(Tag<FOLGB_HEX8, FOLGB_TRANSIENT_THERMAL>{});
-    case 10: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
-    case 11: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
-    case 12: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
-    case 13: return f(Tag<FOLGB_TET4, FOLGB_SAINT_VENANT>{});
-    case 14: return f(Tag<FOLGB_TET4, FOLGB_TRANSIENT_THERMAL>{});
+    case 5: return f(Tag<FOLGB_QUAD4, FOLGB_NEOHOOKE_SPLIT>{});
+    case 6: return f(Tag<FOLGB_HEX8, FOLGB_THERMAL>{});
+    case 7: return f(Tag<FOLGB_HEX8, FOLGB_ELASTIC>{});
+    case 8: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE>{});
+    case 9: return f(Tag<FOLGB_HEX8, FOLGB_SAINT_VENANT>{});
+    case 10: return f(Tag<FOLGB_HEX8, FOLGB_TRANSIENT_THERMAL>{});
+    case 11: return f(Tag<FOLGB_HEX8, FOLGB_NEOHOOKE_SPLIT>{});
+    case 12: return f(Tag<FOLGB_TET4, FOLGB_THERMAL>{});
+    case 13: return f(Tag<FOLGB_TET4, FOLGB_ELASTIC>{});
+    case 14: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE>{});
+    case 15: return f(Tag<FOLGB_TET4, FOLGB_SAINT_VENANT>{});
+    case 16: return f(Tag<FOLGB_TET4, FOLGB_TRANSIENT_THERMAL>{});
+    case 17: return f(Tag<FOLGB_TET4, FOLGB_NEOHOOKE_SPLIT>{});
   }
   return FOLGB_ERR_INVALID_ARGUMENT;
 }
@@ -307,6 +313,48 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
           } else {
             g[a] = fmaf(wd, rc * diff * gp.N[q][a] + mt.dt * Kc * gn, g[a]);
           }
+        }
+      } else if constexpr (PH == FOLGB_NEOHOOKE_SPLIT) {
+        float H[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+            H[i][j] = s;
+          }
+        NHSState<DIM> st;
+        nh_split_state<DIM>(H, mt.kap_f * egp, mt.mu_f * egp, st);
+        float P[DIM][DIM];  // first Piola-Kirchhoff stress F S
+#pragma unroll
+        for (int k = 0; k < DIM; ++k)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) {
+            float s = 0.f;
+#pragma unroll
+            for (int p = 0; p < DIM; ++p) s = fmaf(st.F[k][p], st.S[p][j], s);
+            P[k][j] = s;
+          }
+        energy = fmaf(wd, st.psi, energy);
+        const float dpsi_de = st.dpsi_dk * mt.kap_f + st.dpsi_dmu * mt.mu_f;
+#pragma unroll
+        for (int a = 0; a < NEN; ++a) {
+#pragma unroll
+          for (int k = 0; k < DIM; ++k) {
+            float s = 0.f;
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
+            g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
+          }
+          gd[a] = fmaf(wd * dpsi_de, gp.N[q][a], gd[a]);
+        }
+        if (MODE == MODE_RESIDUAL && mt.has_bf) {
+#pragma unroll
+          for (int a = 0; a < NEN; ++a)
+#pragma unroll
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
         }
       } else if constexpr (PH == FOLGB_SAINT_VENANT) {
         float H[DIM][DIM];

@@ -200,7 +200,7 @@ struct MatRec {
   static constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM;
   static constexpr int NV = Voigt<DIM>::NV;
   static constexpr int GEO = NEN * DIM + 3;  // dNdx, wd, coef, sedw
-  static constexpr int EXTRA = (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT) ? (2 * DIM * DIM + NV * NV)
+  static constexpr int EXTRA = is_hyperelastic(PH) ? (2 * DIM * DIM + NV * NV)
                                : (PH == FOLGB_TRANSIENT_THERMAL ? NEN + 2 + DIM : 0);
   static constexpr int SIZE = GEO + EXTRA;
   static constexpr int O_WD = NEN * DIM, O_COEF = O_WD + 1, O_SED = O_WD + 2;
@@ -274,7 +274,7 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       egp = __ldg(ctrl + e);
     }
     rec[R::O_WD] = wd;
-    const bool need_u = (PH == FOLGB_NEOHOOKE) || (PH == FOLGB_SAINT_VENANT) || (PH == FOLGB_TRANSIENT_THERMAL) ||
+    const bool need_u = is_hyperelastic(PH) || (PH == FOLGB_TRANSIENT_THERMAL) ||
                         (MMODE == MAT_PLAIN) ||
                         (PH == FOLGB_THERMAL && mt.beta != 0.f);
     float ue[ND];
@@ -348,6 +348,45 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       rec[R::O_DK] = kq * mt.mbeta * mt.c * powf(Tn, mt.c - 1.f);
 #pragma unroll
       for (int j = 0; j < DIM; ++j) rec[R::O_GT + j] = gT[j];
+    } else if constexpr (PH == FOLGB_NEOHOOKE_SPLIT) {
+      float H[DIM][DIM];
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          float s = 0.f;
+#pragma unroll
+          for (int a = 0; a < NEN; ++a) s = fmaf(ue[a * DIM + i], dNdx[a][j], s);
+          H[i][j] = s;
+        }
+      const float kappa = mt.kap_f * egp, mu = mt.mu_f * egp;
+      NHSState<DIM> st;
+      nh_split_state<DIM>(H, kappa, mu, st);
+      rec[R::O_COEF] = wd;
+      rec[R::O_SED] = 0.f;
+#pragma unroll
+      for (int i = 0; i < DIM; ++i)
+#pragma unroll
+        for (int j = 0; j < DIM; ++j) {
+          rec[R::O_F + i * DIM + j] = st.F[i][j];
+          rec[R::O_M + i * DIM + j] = st.S[i][j];
+        }
+      // Voigt tangent dS_v / dC_w (the layout of the other hyperelastic models)
+#pragma unroll
+      for (int w = 0; w < NV; ++w) {
+        float dC[DIM][DIM];
+#pragma unroll
+        for (int i = 0; i < DIM; ++i)
+#pragma unroll
+          for (int j = 0; j < DIM; ++j) dC[i][j] = 0.f;
+        const int pw = Voigt<DIM>::p(w), qw = Voigt<DIM>::q(w);
+        dC[pw][qw] = 1.f;
+        dC[qw][pw] = 1.f;
+        float dS[DIM][DIM];
+        nh_split_dS<DIM>(st, kappa, mu, dC, dS);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) rec[R::O_HM + v * NV + w] = dS[Voigt<DIM>::p(v)][Voigt<DIM>::q(v)];
+      }
     } else if constexpr (PH == FOLGB_SAINT_VENANT) {
       float H[DIM][DIM];
 #pragma unroll
@@ -929,8 +968,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
                                         void* stream) {
   int rc = check_loss_args(p, B, control, dofs, losses);
   if (rc) return rc;
-  if (p->physics == FOLGB_NEOHOOKE || p->physics == FOLGB_SAINT_VENANT ||
-      p->physics == FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (is_hyperelastic(p->physics) || p->physics == FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
   LossWS w;
   size_t need = layout_loss(p, B, true, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
@@ -968,7 +1006,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
   rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
-    if constexpr (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT || PH == FOLGB_TRANSIENT_THERMAL) {
+    if constexpr (is_hyperelastic(PH) || PH == FOLGB_TRANSIENT_THERMAL) {
       return (int)FOLGB_ERR_INVALID_ARGUMENT;
     } else {
       int r = launch_matrix<ET, PH, MAT_PLAIN>(M, B, npts, s);

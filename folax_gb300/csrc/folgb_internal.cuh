@@ -48,7 +48,13 @@ struct MatConst {
   int has_bf;
   int shear_ref;        // 1: reference (doubled) shear for the FE residual/tangent
   float rho_cp, dt, mbeta;  // transient thermal: rho cp, time step, material beta
+  float kap_f;          // split neo-Hooke: kappa = kap_f * e_gp, mu = mu_f * e_gp
 };
+
+// Hyperelastic physics: residual B(F)^T S, tangent B^T C B + geometric stiffness.
+constexpr bool is_hyperelastic(int ph) {
+  return ph == FOLGB_NEOHOOKE || ph == FOLGB_SAINT_VENANT || ph == FOLGB_NEOHOOKE_SPLIT;
+}
 
 }  // namespace folgb
 
@@ -385,6 +391,191 @@ __device__ __forceinline__ void nh_dS(const NHState<D>& st, float mu, float lam,
         dS[i][j] += mu * (da * ((i == j ? 1.f : 0.f) - t * st.Ci[i][j]) -
                           st.a * (dI1 * (1.f / 3.f) * st.Ci[i][j] + t * dCi[i][j]));
   }
+}
+
+// x - log(1 + x) without the cancellation of the direct form near x = 0:
+// x^2 sum_{k=2..11} (-1)^k x^(k-2) / k for |x| < 1/8 (truncation below
+// 3e-9 relative), the direct form beyond (relative error ~ 2 eps / |x|).
+__device__ __forceinline__ float x_minus_log1p(float x) {
+  if (fabsf(x) < 0.125f) {
+    float h = -1.f / 11.f;
+#pragma unroll
+    for (int k = 10; k >= 2; --k) h = fmaf(h, x, ((k & 1) ? -1.f : 1.f) / (float)k);
+    return x * x * h;
+  }
+  return x - log1pf(x);
+}
+
+// exp(y) - 1 - y, the same way: y^2 sum_{k=2..11} y^(k-2) / k! for |y| < 1/8.
+__device__ __forceinline__ float expm1_minus_x(float y) {
+  if (fabsf(y) < 0.125f) {
+    float h = 1.f / 39916800.f;  // 1/11!
+    float f = 39916800.f;
+#pragma unroll
+    for (int k = 10; k >= 2; --k) {
+      f /= (float)(k + 1);
+      h = fmaf(h, y, 1.f / f);
+    }
+    return y * y * h;
+  }
+  return expm1f(y) - y;
+}
+
+// Neo-Hookean material with a volumetric-isochoric split at one Gauss point
+// (fol/constitutive_material_models/neo_hooke.py:14-59 in 2-D, 64-111 in 3-D;
+// used by fol/loss_functions/mechanical_neohooke.py:243-275), d = D:
+//   psi = kappa/4 (J^2 - 2 lnJ - 1) + mu/2 (J^(-2/d) I1 - d)
+//   S   = kappa/2 (J^2 - 1) C^-1 + mu J^(-2/d) (I - I1/d C^-1)
+// The energy is second order in H = grad u, and the direct forms lose it to
+// fp32 cancellation of first-order terms at small strains.  So, with
+// J - 1 = tr H + m2(H) + det H (invariant expansion of det(I + H)) and
+// tr E = tr H + |H|^2 / 2:
+//   J^2 - 2 lnJ - 1       = (J-1)^2 + 2 ((J-1) - log1p(J-1))
+//   J^(-2/d) I1 - d        = 2 (tr E - (J-1)) + 2 ((J-1) - log1p(J-1))
+//                            + d (e^y - 1 - y) + 2 tr E (e^y - 1),  y = -2/d lnJ
+//   I - I1/d C^-1          = 2 C^-1 dev(E)
+// where tr E - (J-1) = |H|^2 / 2 - m2 - det H needs no first-order term.
+// dpsi_dk and dpsi_dmu are the energy per unit kappa and mu.
+template <int D>
+struct NHSState {
+  float F[D][D];
+  float Ci[D][D];
+  float S[D][D];
+  float detCm1, a, I1, psi, dpsi_dk, dpsi_dmu;
+};
+
+template <int D>
+__device__ __forceinline__ void nh_split_state(const float (&H)[D][D], float kappa, float mu, NHSState<D>& st) {
+  float E[D][D];
+  float hh = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(H[k][i], H[k][j], s);
+      E[i][j] = 0.5f * (H[i][j] + H[j][i] + s);
+      st.F[i][j] = H[i][j] + (i == j ? 1.f : 0.f);
+      hh = fmaf(H[i][j], H[i][j], hh);
+    }
+  float trE = 0.f, trH = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    trE += E[i][i];
+    trH += H[i][i];
+  }
+  float q;  // tr E - (J - 1), second order
+  if constexpr (D == 3) {
+    const float m2 = H[0][0] * H[1][1] - H[0][1] * H[1][0] + H[0][0] * H[2][2] - H[0][2] * H[2][0] +
+                     H[1][1] * H[2][2] - H[1][2] * H[2][1];
+    const float dH = H[0][0] * (H[1][1] * H[2][2] - H[1][2] * H[2][1]) -
+                     H[0][1] * (H[1][0] * H[2][2] - H[1][2] * H[2][0]) +
+                     H[0][2] * (H[1][0] * H[2][1] - H[1][1] * H[2][0]);
+    q = 0.5f * hh - m2 - dH;
+    st.detCm1 = trH + m2 + dH;  // J - 1 for now
+  } else {
+    const float dH = H[0][0] * H[1][1] - H[0][1] * H[1][0];
+    q = 0.5f * hh - dH;
+    st.detCm1 = trH + dH;
+  }
+  const float Jm1 = st.detCm1;
+  const float lnJ = log1pf(Jm1);
+  const float J = 1.f + Jm1;
+  const float rdet = 1.f / (J * J);
+  float C[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) C[i][j] = 2.f * E[i][j] + (i == j ? 1.f : 0.f);
+  if constexpr (D == 3) {
+    st.Ci[0][0] = (C[1][1] * C[2][2] - C[1][2] * C[2][1]) * rdet;
+    st.Ci[0][1] = (C[0][2] * C[2][1] - C[0][1] * C[2][2]) * rdet;
+    st.Ci[0][2] = (C[0][1] * C[1][2] - C[0][2] * C[1][1]) * rdet;
+    st.Ci[1][1] = (C[0][0] * C[2][2] - C[0][2] * C[2][0]) * rdet;
+    st.Ci[1][2] = (C[0][2] * C[1][0] - C[0][0] * C[1][2]) * rdet;
+    st.Ci[2][2] = (C[0][0] * C[1][1] - C[0][1] * C[1][0]) * rdet;
+    st.Ci[1][0] = st.Ci[0][1];
+    st.Ci[2][0] = st.Ci[0][2];
+    st.Ci[2][1] = st.Ci[1][2];
+  } else {
+    st.Ci[0][0] = C[1][1] * rdet;
+    st.Ci[1][1] = C[0][0] * rdet;
+    st.Ci[0][1] = -C[0][1] * rdet;
+    st.Ci[1][0] = st.Ci[0][1];
+  }
+  const float y = (-2.f / (float)D) * lnJ;
+  const float am1 = expm1f(y);
+  const float a = 1.f + am1;
+  const float xl = x_minus_log1p(Jm1);
+  const float iso = 2.f * q + 2.f * xl + (float)D * expm1_minus_x(y) + 2.f * trE * am1;  // J^(-2/d) I1 - d
+  const float vol = fmaf(Jm1, Jm1, 2.f * xl);                                              // J^2 - 2 lnJ - 1
+  st.detCm1 = Jm1 * (2.f + Jm1);                                                           // J^2 - 1
+  st.dpsi_dk = 0.25f * vol;
+  st.dpsi_dmu = 0.5f * iso;
+  st.psi = kappa * st.dpsi_dk + mu * st.dpsi_dmu;
+  st.a = a;
+  st.I1 = (float)D + 2.f * trE;
+  float dev[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) dev[i][j] = E[i][j] - (i == j ? trE * (1.f / (float)D) : 0.f);
+  const float pv = 0.5f * kappa * st.detCm1;
+  const float ma2 = 2.f * mu * a;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(st.Ci[i][k], dev[k][j], s);
+      st.S[i][j] = fmaf(pv, st.Ci[i][j], ma2 * s);
+    }
+}
+
+// Directional derivative dS along a symmetric dC (half the reference's
+// C_vol + C_iso tangent, neo_hooke.py:47-56, 99-108, applied to dC).
+template <int D>
+__device__ __forceinline__ void nh_split_dS(const NHSState<D>& st, float kappa, float mu, const float (&dC)[D][D],
+                                            float (&dS)[D][D]) {
+  float CidC[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(st.Ci[i][k], dC[k][j], s);
+      CidC[i][j] = s;
+    }
+  float tr = 0.f, dI1 = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    tr += CidC[i][i];
+    dI1 += dC[i][i];
+  }
+  float dCi[D][D];
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      float s = 0.f;
+#pragma unroll
+      for (int k = 0; k < D; ++k) s = fmaf(CidC[i][k], st.Ci[k][j], s);
+      dCi[i][j] = -s;
+    }
+  const float rd = 1.f / (float)D;
+  const float ddet = (1.f + st.detCm1) * tr;
+  const float da = -rd * st.a * tr;
+  const float t = st.I1 * rd;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j)
+      dS[i][j] = 0.5f * kappa * (ddet * st.Ci[i][j] + st.detCm1 * dCi[i][j]) +
+                 mu * (da * ((i == j ? 1.f : 0.f) - t * st.Ci[i][j]) -
+                       st.a * (dI1 * rd * st.Ci[i][j] + t * dCi[i][j]));
 }
 
 // Voigt index pairs: 3-D [xx,yy,zz,yz,xz,xy], 2-D [xx,yy,xy]

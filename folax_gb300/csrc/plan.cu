@@ -145,6 +145,9 @@ int fill_material(const folgb_physics& p, int dim, MatConst& m) {
   }
   m.mu_f = (float)(1.0 / (2.0 * (1.0 + nu)));
   m.lam_f = (float)(nu / ((1.0 + nu) * (1.0 - 2.0 * nu)));
+  // bulk modulus per unit Young's modulus, the 3-D one in 2-D as well
+  // (mechanical_neohooke.py:254)
+  m.kap_f = (float)(1.0 / (3.0 * (1.0 - 2.0 * nu)));
   m.beta = (float)p.beta;
   m.c = (float)p.c;
   for (int i = 0; i < 3; ++i) m.bf[i] = (float)p.body_force[i];
@@ -261,7 +264,7 @@ int check_physics(const folgb_physics* phys, int& nen, int& dim, int& ndof) {
     case FOLGB_TET4: nen = 4; dim = 3; break;
     default: return FOLGB_ERR_INVALID_ARGUMENT;
   }
-  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (phys->physics < FOLGB_THERMAL || phys->physics > FOLGB_NEOHOOKE_SPLIT) return FOLGB_ERR_INVALID_ARGUMENT;
   // the transient element's control is the nodal current temperature field
   if (phys->physics == FOLGB_TRANSIENT_THERMAL &&
       (phys->control_layout != FOLGB_CONTROL_NODAL || !(phys->time_step > 0.0)))

@@ -371,8 +371,7 @@ extern "C" int folgb_response(const folgb_plan* p, int32_t num_monomials, const 
   if (!p || !control || !dofs || num_monomials < 0 || num_monomials > kMaxMonomials ||
       (num_monomials > 0 && !monomials))
     return FOLGB_ERR_INVALID_ARGUMENT;
-  if (p->physics == FOLGB_NEOHOOKE || p->physics == FOLGB_SAINT_VENANT ||
-      p->physics == FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (is_hyperelastic(p->physics) || p->physics == FOLGB_TRANSIENT_THERMAL) return FOLGB_ERR_INVALID_ARGUMENT;
   if ((dcontrol || dxyz) && !adjoint) return FOLGB_ERR_INVALID_ARGUMENT;
   RespWS w;
   const size_t need = layout_response(p, workspace, workspace_bytes, &w);
@@ -405,7 +404,7 @@ extern "C" int folgb_response(const folgb_plan* p, int32_t num_monomials, const 
   if (value) FOLGB_CUDA_TRY(cudaMemsetAsync(w.counter, 0, sizeof(unsigned), s));
   int rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
-    if constexpr (PH == FOLGB_NEOHOOKE || PH == FOLGB_SAINT_VENANT || PH == FOLGB_TRANSIENT_THERMAL) {
+    if constexpr (is_hyperelastic(PH) || PH == FOLGB_TRANSIENT_THERMAL) {
       return FOLGB_ERR_INVALID_ARGUMENT;
     } else {
       k_response<ET, PH><<<response_blocks(p), 128, 0, s>>>(A, p->d_gp);

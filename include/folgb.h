@@ -11,7 +11,8 @@
  *
  * Reference interfaces replaced (paths inside the folax project):
  *   fol/loss_functions/fe_loss.py           FiniteElementLoss
- *   fol/loss_functions/thermal.py, mechanical.py, mechanical_neohooke_AD.py
+ *   fol/loss_functions/thermal.py, mechanical.py, mechanical_neohooke_AD.py,
+ *   mechanical_neohooke.py, mechanical_saint_venant.py, transient_thermal.py
  *   fol/solvers/fe_solver.py                FiniteElementSolver.LinearSolve
  *   fol/loss_functions/ffi_functions/kr_small_displacement_element.cc
  *                                           (XLA FFI handler precedent)
@@ -48,9 +49,12 @@ enum {
   FOLGB_ELASTIC = 1,  /* mechanical.py:98-117             */
   FOLGB_NEOHOOKE = 2, /* mechanical_neohooke_AD.py:254-293 */
   FOLGB_SAINT_VENANT = 3, /* mechanical_saint_venant.py:263-296 */
-  FOLGB_TRANSIENT_THERMAL = 4 /* transient_thermal.py:43-78: implicit Euler;
-                                 the control is the current temperature
-                                 field, the dofs the next one */
+  FOLGB_TRANSIENT_THERMAL = 4, /* transient_thermal.py:43-78: implicit Euler;
+                                  the control is the current temperature
+                                  field, the dofs the next one */
+  FOLGB_NEOHOOKE_SPLIT = 5 /* mechanical_neohooke.py:243-275: neo-Hooke with a
+                              volumetric-isochoric split, kappa and mu from
+                              the Young's modulus control */
 };
 /* control layout: nodal values gathered by connectivity (fe_loss.py:160), or
  * one value per element used as de = value * 1 (partition of unity). */
@@ -63,7 +67,7 @@ enum { FOLGB_SHEAR_REFERENCE = 0, FOLGB_SHEAR_CONSISTENT = 1 };
 typedef struct folgb_physics {
   int32_t element_type;   /* FOLGB_QUAD4 / HEX8 / TET4                         */
   int32_t physics;        /* FOLGB_THERMAL / ELASTIC / NEOHOOKE / SAINT_VENANT /
-                             TRANSIENT_THERMAL                                  */
+                             TRANSIENT_THERMAL / NEOHOOKE_SPLIT                 */
   int32_t num_gp;         /* Gauss order 1..3 ("num_gp", fe_loss.py:68-83)     */
   int32_t control_layout; /* FOLGB_CONTROL_NODAL / ELEMENT                     */
   int32_t shear_mode;     /* FOLGB_SHEAR_REFERENCE / CONSISTENT                */

@@ -35,6 +35,7 @@ def bc_dict(etype, physics, nonzero=True):
 
 def gpu_loss(etype, physics, m, settings):
     from folax_gb300 import loss as L
+    from folax_gb300 import mechanical_neohooke as NH
     cls = {("quad4", "thermal"): L.ThermalLoss2DQuad, ("hex8", "thermal"): L.ThermalLoss3DHexa,
            ("tet4", "thermal"): L.ThermalLoss3DTetra, ("quad4", "elastic"): L.MechanicalLoss2DQuad,
            ("hex8", "elastic"): L.MechanicalLoss3DHexa, ("tet4", "elastic"): L.MechanicalLoss3DTetra,
@@ -42,7 +43,10 @@ def gpu_loss(etype, physics, m, settings):
            ("tet4", "neohooke"): L.NeoHookeMechanicalLoss3DTetra,
            ("quad4", "saint_venant"): L.SaintVenantMechanicalLoss2DQuad,
            ("hex8", "saint_venant"): L.SaintVenantMechanicalLoss3DHexa,
-           ("tet4", "saint_venant"): L.SaintVenantMechanicalLoss3DTetra}[(etype, physics)]
+           ("tet4", "saint_venant"): L.SaintVenantMechanicalLoss3DTetra,
+           ("quad4", "neohooke_split"): NH.NeoHookeMechanicalLoss2DQuad,
+           ("hex8", "neohooke_split"): NH.NeoHookeMechanicalLoss3DHexa,
+           ("tet4", "neohooke_split"): NH.NeoHookeMechanicalLoss3DTetra}[(etype, physics)]
     loss = cls("loss", dict(settings), m)
     loss.Initialize()
     return loss
