@@ -20,12 +20,14 @@ ERR_CUDA = 5
 ERR_WORKSPACE = 6
 ERR_NO_PATTERN = 7
 ERR_TOO_LARGE = 8
+ERR_TIMEOUT = 9
 
 STATUS_NAMES = {
     OK: "ok", ERR_INVALID_ARGUMENT: "invalid argument", ERR_NONPOSITIVE_DETJ: "non-positive detJ",
     ERR_NAN: "non-finite value", ERR_NOT_CONVERGED: "not converged", ERR_CUDA: "CUDA error",
     ERR_WORKSPACE: "workspace too small", ERR_NO_PATTERN: "plan has no CSR pattern",
     ERR_TOO_LARGE: "problem larger than the fixed scratch",
+    ERR_TIMEOUT: "a bounded device-side wait gave up",
 }
 
 QUAD4, HEX8, TET4 = 0, 1, 2

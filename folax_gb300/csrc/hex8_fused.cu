@@ -142,24 +142,16 @@ __device__ __forceinline__ float2 det_inv_pair(const float2 (&J)[3][3], float2 (
 //          per SM) through __launch_bounds__, or REGS for the
 //          k_hex8_elastic_regs wrapper: each SM sub-partition holds 16,384
 //          registers, so 96 registers give 5 resident warps per partition
-//          (20 per SM) and 80 give 6 (24 per SM), at the price of spills.
+//          (20 per SM) and 80 give 6 (24 per SM), at the price of spills;
+//   TMA:   the persistent k_hex8_elastic_tma below (connectivity streamed
+//          into shared memory by bulk copies), 4 or 5 blocks per SM.
+// One element: gathers, the 8 Gauss points, the adjoint, the records.
+// nodes[] are the element's node ids in the reference's local order.
 template <int CL, int MODE, bool BF, int ACC>
-__device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
-  __shared__ float wsum[32];
-  __shared__ unsigned wcount;
-  pdl_launch_dependents();  // the gather may start its independent loads during this kernel's tail
-  if (MODE == MODE_LOSS) {
-    if (threadIdx.x == 0) wcount = 0u;
-    __syncthreads();
-  }
-  const int b = blockIdx.y;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  float energy = 0.f;
-  int bad = 0;
-  if (e < A.E) {
+__device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b, const int64_t e,
+                                                  const int (&nodes)[8], float& energy, int& bad) {
+  {
     constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
-    int nodes[8];
-    load_nodes<8>(A.conn, e, nodes);
     const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
     const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
     const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
@@ -429,8 +421,121 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
     if (MODE == MODE_LOSS && CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
       A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
   }
+}
+
+// One element per thread.
+template <int CL, int MODE, bool BF, int ACC>
+__device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  pdl_launch_dependents();  // the gather may start its independent loads during this kernel's tail
+  if (MODE == MODE_LOSS) {
+    if (threadIdx.x == 0) wcount = 0u;
+    __syncthreads();
+  }
+  const int b = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float energy = 0.f;
+  int bad = 0;
+  if (e < A.E) {
+    int nodes[8];
+    load_nodes<8>(A.conn, e, nodes);
+    hex8_elastic_elem<CL, MODE, BF, ACC>(A, b, e, nodes, energy, bad);
+  }
   if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount);
   else report_bad_warp(bad, A.status);
+}
+
+// Persistent variant with the connectivity streamed by the TMA engine.  Each
+// warp owns a fixed, strided sequence of 32-element tiles (tiles gw, gw + W,
+// ... for global warp gw of W) and keeps kTmaStages of them in flight: lane 0
+// issues one bulk copy per tile (the tile's 32 connectivity rows, 1 KB) into
+// the warp's stage buffer in shared memory, completing on that stage's
+// mbarrier.  A tile's node gathers therefore start as soon as its rows have
+// landed, with no dependent global load in front of them, and the rows of
+// the next tiles arrive while this one computes.  The fixed tile order keeps
+// every energy sum in a fixed order.  Every mbarrier wait is bounded: a copy
+// that never lands sets FOLGB_ERR_TIMEOUT in the status word and the warp
+// stops after waiting (bounded) for its other copies in flight.
+constexpr int kTmaStages = 3;
+constexpr int kTmaWarps = 4;  // 128 threads per block
+
+template <int CL, int MODE, bool BF, int ACC>
+__device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  __shared__ __align__(128) int4 rows[kTmaWarps][kTmaStages][64];  // 32 elements x 8 node ids
+  __shared__ __align__(8) uint64_t bar[kTmaWarps][kTmaStages];
+  pdl_launch_dependents();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) wcount = 0u;
+  if (lane == 0) {
+#pragma unroll
+    for (int st = 0; st < kTmaStages; ++st) mbar_init(&bar[warp][st], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();  // wcount and the barriers are initialised
+  const int b = blockIdx.y;
+  // element counts fit in int: folgb_plan_create bounds E * nen^2 by INT32_MAX
+  const int E = (int)A.E, ntiles = (E + 31) >> 5;
+  const int gw = blockIdx.x * kTmaWarps + warp, W = gridDim.x * kTmaWarps;
+  auto issue = [&](int t, int st) {
+    const int n = E - t * 32;
+    const unsigned bytes = (unsigned)((n < 32 ? n : 32) * 32);  // whole rows: a multiple of 16
+    mbar_arrive_expect_tx(&bar[warp][st], bytes);
+    bulk_copy_g2s(&rows[warp][st][0], A.conn + (int64_t)t * 256, bytes, &bar[warp][st]);
+  };
+  if (lane == 0) {
+#pragma unroll
+    for (int st = 0; st < kTmaStages; ++st)
+      if (gw + st * W < ntiles) issue(gw + st * W, st);
+  }
+  float energy = 0.f;
+  int bad = 0;
+  int st = 0;
+  unsigned parity = 0u;
+  int t = gw;
+  bool timed_out = false;
+  for (; t < ntiles; t += W) {
+    if (!__all_sync(0xffffffffu, mbar_wait_bounded(&bar[warp][st], parity))) {
+      timed_out = true;
+      break;
+    }
+    const int e = t * 32 + lane;
+    if (e < E) {
+      const int4 p = rows[warp][st][2 * lane], q = rows[warp][st][2 * lane + 1];
+      const int nodes[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
+      hex8_elastic_elem<CL, MODE, BF, ACC>(A, b, e, nodes, energy, bad);
+    }
+    __syncwarp();  // every lane has used its rows of this stage
+    if (lane == 0 && t + kTmaStages * W < ntiles) {
+      fence_proxy_async_smem();
+      issue(t + kTmaStages * W, st);
+    }
+    if (++st == kTmaStages) {
+      st = 0;
+      parity ^= 1u;
+    }
+  }
+  if (timed_out && lane == 0) {
+    // copies still in flight target this block's shared memory: wait for
+    // them (bounded) before leaving
+    for (int j = 0; j < kTmaStages; ++j) {
+      if (t + j * W < ntiles) mbar_wait_bounded(&bar[warp][st], parity);
+      if (++st == kTmaStages) {
+        st = 0;
+        parity ^= 1u;
+      }
+    }
+    if (A.status) atomicOr(A.status, 1 << FOLGB_ERR_TIMEOUT);
+  }
+  if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount);
+  else report_bad_warp(bad, A.status);
+}
+
+template <int CL, int MODE, bool BF, int ACC, int MINB>
+__global__ void __launch_bounds__(kTmaWarps * 32, MINB) k_hex8_elastic_tma(const VecArgs A) {
+  hex8_elastic_tma_body<CL, MODE, BF, ACC>(A);
 }
 
 template <int CL, int MODE, bool BF, int ACC, int BLOCK>
@@ -457,6 +562,33 @@ static void launch_variant_regs(const VecArgs& A, dim3 grid, bool bf, cudaStream
   else k_hex8_elastic_regs<CL, MODE, false, ACC, REGS><<<g2, 128, 0, s>>>(A);
 }
 
+// Persistent grid: as many blocks as fit on the GPU at once, at most one
+// 4-warp block per 4 tiles.
+// (resident blocks per SM queried once per kernel instantiation)
+template <class K>
+static unsigned persistent_blocks(K kernel, int64_t E) {
+  static int per_sm = 0;
+  if (per_sm == 0) {
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kTmaWarps * 32, 0) != cudaSuccess || n < 1) n = 1;
+    per_sm = n;
+  }
+  const int64_t want = (((E + 31) >> 5) + kTmaWarps - 1) / kTmaWarps;
+  const int64_t cap = (int64_t)per_sm * num_sms();
+  return (unsigned)(want < cap ? want : cap);
+}
+
+template <int CL, int MODE, int ACC, int MINB>
+static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
+  if (bf) {
+    auto k = k_hex8_elastic_tma<CL, MODE, true, ACC, MINB>;
+    k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
+  } else {
+    auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB>;
+    k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
+  }
+}
+
 template <int CL, int MODE>
 static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cudaStream_t s) {
   switch (variant) {
@@ -472,12 +604,15 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
     case 9: launch_variant_regs<CL, MODE, 1, 80>(A, grid, bf, s); break;
     case 10: launch_variant<CL, MODE, 2, 256>(A, grid, bf, s); break;
     case 11: launch_variant<CL, MODE, 2, 128>(A, grid, bf, s); break;
-    default: launch_variant_regs<CL, MODE, 2, 96>(A, grid, bf, s); break;
+    case 12: launch_variant_regs<CL, MODE, 2, 96>(A, grid, bf, s); break;
+    case 13: launch_variant_tma<CL, MODE, 2, 4>(A, grid, bf, s); break;
+    case 14: launch_variant_tma<CL, MODE, 2, 5>(A, grid, bf, s); break;
+    default: launch_variant_tma<CL, MODE, 0, 5>(A, grid, bf, s); break;
   }
 }
 
 // Number of sum-factorised variants the autotuner may choose from.
-constexpr int kHex8Variants = 13;
+constexpr int kHex8Variants = 16;
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's

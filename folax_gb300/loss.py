@@ -29,13 +29,16 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 13
+HEX8_VARIANTS = 16
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
                       "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
                       "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
                       "128 thr, 80 regs, point sums", "128 thr, 80 regs, dual coefficients",
                       "256 thr, paired points (f32x2)", "128 thr, paired points (f32x2)",
-                      "128 thr, 96 regs, paired points (f32x2)"]
+                      "128 thr, 96 regs, paired points (f32x2)",
+                      "persistent, TMA-staged rows, paired points (f32x2)",
+                      "persistent, TMA-staged rows, 96 regs, paired points (f32x2)",
+                      "persistent, TMA-staged rows, 96 regs, point sums"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 
@@ -273,11 +276,11 @@ class FiniteElementLoss:
         return int(self._status.item())
 
     def CheckDeviceStatus(self):
-        """Raise FolgbError if a kernel flagged a non-positive detJ or a
-        non-finite value, then clear the flags."""
+        """Raise FolgbError if a kernel flagged a non-positive detJ, a
+        non-finite value or a device wait that gave up, then clear the flags."""
         st = self.GetDeviceStatus()
         self._status.zero_()
-        for code in (capi.ERR_NONPOSITIVE_DETJ, capi.ERR_NAN):
+        for code in (capi.ERR_NONPOSITIVE_DETJ, capi.ERR_NAN, capi.ERR_TIMEOUT):
             if (st >> code) & 1:
                 raise capi.FolgbError("FE kernel", code)
 

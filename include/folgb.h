@@ -38,7 +38,8 @@ enum {
   FOLGB_ERR_CUDA = 5,             /* a CUDA runtime call failed              */
   FOLGB_ERR_WORKSPACE = 6,        /* workspace NULL or smaller than required */
   FOLGB_ERR_NO_PATTERN = 7,       /* plan built without the CSR tables       */
-  FOLGB_ERR_TOO_LARGE = 8         /* problem exceeds a fixed-size scratch    */
+  FOLGB_ERR_TOO_LARGE = 8,        /* problem exceeds a fixed-size scratch    */
+  FOLGB_ERR_TIMEOUT = 9           /* a bounded device-side wait gave up      */
 };
 
 /* element types (fol/geometries/__init__.py:18-21) */
@@ -74,7 +75,7 @@ typedef struct folgb_physics {
   int32_t kernel_variant; /* 0: fastest kernel for the element (sum-factorised
                              hex8 2x2x2 elasticity, variant set by
                              folgb_autotune); 1: the generic Gauss loop;
-                             2 + v: sum-factorised variant v (0..12) */
+                             2 + v: sum-factorised variant v (0..15) */
   double young_modulus;   /* material_dict young_modulus (elastic D scale)     */
   double poisson_ratio;   /* material_dict poisson_ratio                       */
   double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */

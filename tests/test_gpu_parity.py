@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import arr, golden
+from folax_gb300.mesh import create_3D_box_mesh
 from gpu_cases import bc_dict, gpu_loss, make_mesh, oracle_loss, rel_fro
 from oracle import fe_oracle as fo
 
@@ -93,7 +94,7 @@ def test_hex8_sum_factorised_matches_generic_and_oracle(cuda, layout, bf):
     assert rel_fro(Rf.cpu().numpy(), Ro) < TOL
 
 
-@pytest.mark.parametrize("variant", list(range(13)))
+@pytest.mark.parametrize("variant", list(range(16)))
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 def test_hex8_every_variant_matches_oracle(cuda, variant, layout):
     """Each autotuner candidate (block size x accumulation scheme) is exact."""
@@ -110,6 +111,29 @@ def test_hex8_every_variant_matches_oracle(cuda, variant, layout):
         assert rel_fro(x.cpu().numpy(), z) < TOL
 
 
+@pytest.mark.parametrize("tma,twin", [(13, 11), (15, 6)])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_tma_variant_equals_its_per_thread_twin(cuda, tma, twin, layout):
+    """The persistent TMA-staged kernel runs the same element code as its
+    one-element-per-thread twin: on a 100^3 mesh (about 10 tiles per warp, so
+    every stage buffer is refilled and its barrier phase flips several times)
+    both gradients are bit-identical and the losses (summed in another block
+    grouping) agree to 1e-6."""
+    m = create_3D_box_mesh(100, 100, 100)
+    s = _settings("hex8", "elastic", layout, 1.0, [0.2, 0.0, -0.1])
+    a_loss = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": tma})
+    b_loss = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": twin})
+    rng = np.random.default_rng(29)
+    ctrl = 0.5 + rng.random((2, a_loss.GetNumberOfControls()))
+    u = 0.003 * rng.standard_normal((2, a_loss.GetTotalNumberOfDOFs()))
+    a = a_loss.ComputeBatchLossAndGrad(ctrl, u)
+    b = b_loss.ComputeBatchLossAndGrad(ctrl, u)
+    a_loss.CheckDeviceStatus()
+    assert rel_fro(a[2].cpu().numpy(), b[2].cpu().numpy()) < 1e-6
+    assert np.array_equal(a[3].cpu().numpy(), b[3].cpu().numpy())
+    assert np.array_equal(a[4].cpu().numpy(), b[4].cpu().numpy())
+
+
 def test_autotune_keeps_results_exact(cuda):
     m = make_mesh("hex8", 6, seed=25)
     s = _settings("hex8", "elastic", "element")
@@ -118,7 +142,7 @@ def test_autotune_keeps_results_exact(cuda):
     ctrl = 0.5 + rng.random((1, gl.GetNumberOfControls()))
     u = 0.01 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
     info = gl.Autotune(ctrl, u, repeats=2)
-    assert 0 <= info["chosen"] < 13 and len(info["ms"]) == 13 and min(info["ms"]) > 0
+    assert 0 <= info["chosen"] < 16 and len(info["ms"]) == 16 and min(info["ms"]) > 0
     a = gl.ComputeBatchLossAndGrad(ctrl, u)
     o = ol.batch_loss_and_grads(ctrl, u)
     for x, z in zip(a[2:], o[2:]):
