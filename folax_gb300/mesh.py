@@ -12,10 +12,97 @@ seeded, structured meshes in the reference's node/element orderings:
 * split_hex_to_tets: a conforming 6-tetrahedron split of every hexahedron,
   oriented to positive Jacobian (fol/mesh_input_output/mesh.py:123-142 swaps
   nodes 0 and 1 of negatively oriented elements; this split never needs it).
+
+``Mesh.Initialize`` reads Kratos ``.mdpa`` files (mesh.py:93-110, 196-242):
+nodes, element blocks (the Kratos geometry name mapped to the element type
+key, mesh.py:15-37) and the nodes of each SubModelPart as a node set.  The
+other formats the reference reads go through meshio (mesh.py:74-91), which is
+not available here; they raise.
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
+
+# Kratos geometry names -> element type keys (the type names mesh.py:15-37 uses)
+MDPA_ELEMENT_TYPES = {
+    "Line2D2": "line", "Line3D2": "line", "Triangle2D3": "triangle", "Triangle3D3": "triangle",
+    "Quadrilateral2D4": "quad", "Quadrilateral3D4": "quad", "Tetrahedra3D4": "tetra", "Hexahedra3D8": "hexahedron",
+    "Prism3D6": "wedge", "Line2D3": "line3", "Triangle2D6": "triangle6", "Triangle3D6": "triangle6",
+    "Quadrilateral2D9": "quad9", "Quadrilateral3D9": "quad9", "Tetrahedra3D10": "tetra10",
+    "Hexahedra3D27": "hexahedron27", "Point2D": "vertex", "Point3D": "vertex", "Quadrilateral2D8": "quad8",
+    "Quadrilateral3D8": "quad8", "Hexahedra3D20": "hexahedron20",
+}
+
+
+def _mdpa_element_type(block_header: str):
+    """Element type of a 'Begin Elements <name>' block: the first Kratos
+    geometry name contained in <name> (mesh.py:199-206 matches by substring)."""
+    name = block_header[len("Begin Elements"):].strip()
+    for key, etype in MDPA_ELEMENT_TYPES.items():
+        if key in name:
+            return etype
+    return None
+
+
+def read_mdpa(path: str, scale_factor: float = 1.0):
+    """Parses a Kratos .mdpa file.  Returns (coordinates [N, 3],
+    {element type: connectivity [E, nen]}, {SubModelPart name: node indices}).
+    Node ids are mapped to 0-based row indices in file order (for the usual
+    ids 1..N this is id - 1, as mesh.py:208-215 and 232-238 assume)."""
+    coords, ids = [], []
+    blocks: dict = {}
+    sets: dict = {}
+    with open(path, "r") as f:
+        lines = iter(f)
+        for raw in lines:
+            line = raw.strip()
+            if line.startswith("Begin Nodes"):
+                for raw in lines:
+                    t = raw.split()
+                    if t and t[0] == "End":
+                        break
+                    if t:
+                        ids.append(int(t[0]))
+                        coords.append([float(t[1]), float(t[2]), float(t[3])])
+            elif line.startswith("Begin Elements"):
+                etype = _mdpa_element_type(line)
+                rows = []
+                for raw in lines:
+                    t = raw.split()
+                    if t and t[0] == "End":
+                        break
+                    if t:
+                        rows.append([int(v) for v in t[2:]])  # element id, property id, node ids
+                blocks.setdefault(etype, []).extend(rows)
+            elif line.split()[:2] == ["Begin", "SubModelPart"]:
+                # the part's own node list; nested parts are skipped
+                name = line[len("Begin SubModelPart"):].strip()
+                depth, node_ids = 1, None
+                for raw in lines:
+                    t = raw.split()
+                    if t[:2] == ["Begin", "SubModelPart"]:
+                        depth += 1
+                    elif t[:2] == ["End", "SubModelPart"]:
+                        depth -= 1
+                        if depth == 0:
+                            break
+                    elif t[:2] == ["Begin", "SubModelPartNodes"] and depth == 1:
+                        node_ids = []
+                        for raw2 in lines:
+                            t2 = raw2.split()
+                            if t2[:1] == ["End"]:
+                                break
+                            if t2:
+                                node_ids.append(int(t2[0]))
+                if node_ids is not None:
+                    sets[name] = node_ids
+    index = {nid: k for k, nid in enumerate(ids)}
+    xyz = scale_factor * np.asarray(coords, dtype=np.float64).reshape(-1, 3)
+    conn = {et: np.asarray([[index[n] for n in row] for row in rows], dtype=np.int64) for et, rows in blocks.items()}
+    node_sets = {name: np.asarray([index[n] for n in nl], dtype=np.int64) for name, nl in sets.items()}
+    return xyz, conn, node_sets
 
 ELEMENT_NODES = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
@@ -23,10 +110,13 @@ ELEMENT_NODES = {"quad": 4, "hexahedron": 8, "tetra": 4}
 class Mesh:
     """In-memory FE mesh (node coordinates, element connectivity, node sets)."""
 
-    def __init__(self, io_name: str = "mesh", file_name: str = "mesh.mem", case_dir: str = "."):
+    def __init__(self, io_name: str = "mesh", file_name: str = "mesh.mem", case_dir: str = ".",
+                 scale_factor: float = 1.0):
         self._name = io_name
         self.file_name = file_name
+        self.mesh_format = file_name.split(sep=".")[1] if "." in file_name else ""
         self.case_dir = case_dir
+        self.scale_factor = scale_factor
         self.node_ids = np.zeros(0, dtype=np.int64)
         self.nodes_coordinates = np.zeros((0, 3))
         self.elements_nodes: dict[str, np.ndarray] = {}
@@ -38,8 +128,20 @@ class Mesh:
         return self._name
 
     def Initialize(self) -> None:
+        """Reads the mesh file (mesh.py:64-121) unless the mesh was built in
+        memory ('.mem'), then orients the elements."""
         if self.is_initialized:
             return
+        if self.mesh_format == "mdpa":
+            xyz, conn, sets = read_mdpa(os.path.join(self.case_dir, self.file_name), self.scale_factor)
+            self.nodes_coordinates = xyz
+            self.node_ids = np.arange(len(xyz))
+            self.elements_nodes = conn
+            self.node_sets = sets
+            self.element_sets = {}
+        elif self.mesh_format not in ("mem", ""):
+            raise NotImplementedError(f"reading .{self.mesh_format} meshes needs meshio, which is not available; "
+                                      "use .mdpa or build the mesh in memory")
         self.CheckAndOrientElements()
         self.is_initialized = True
 
@@ -47,6 +149,8 @@ class Mesh:
         """Swap nodes 0 and 1 of elements whose Jacobian determinant at the
         first Gauss point is negative (mesh.py:123-142)."""
         for etype, conn in self.elements_nodes.items():
+            if etype not in ELEMENT_NODES:
+                continue
             det = element_jacobian_det(etype, self.nodes_coordinates, conn)
             neg = det < 0
             if np.any(neg):

@@ -148,8 +148,28 @@ def transient_thermal_tests(ref_root):
     return out
 
 
+def mesh_io_tests(ref_root):
+    """The .mdpa fixture of tests/unit/test_mesh_io.py (copied next to this
+    script) and the counts that test asserts for it (read as text)."""
+    import re
+    import shutil
+    rel = "tests/unit/test_mesh_io.py"
+    text = open(os.path.join(ref_root, rel)).read()
+    src = lambda m: f"{rel}:{text.count(chr(10), 0, m.start()) + 1}"  # noqa: E731
+    out = {"file": "coarse_sphere.mdpa", "node_sets": {}}
+    m = re.search(r"self\.mdpa_io\.GetNumberOfNodes\(\),\s*(\d+)", text)
+    out["num_nodes"] = {"value": int(m.group(1)), "src": src(m)}
+    m = re.search(r'self\.mdpa_io\.GetNumberOfElements\("(\w+)"\),\s*(\d+)', text)
+    out["num_elements"] = {"type": m.group(1), "value": int(m.group(2)), "src": src(m)}
+    for m in re.finditer(r'len\(self\.mdpa_io\.GetNodeSet\("(\w+)"\)\),\s*(\d+)', text):
+        out["node_sets"][m.group(1)] = {"value": int(m.group(2)), "src": src(m)}
+    shutil.copyfile(os.path.join(ref_root, "tests/meshes/coarse_sphere.mdpa"), os.path.join(HERE, "coarse_sphere.mdpa"))
+    return out
+
+
 def main(ref_root):
     fixtures = {
+        "mesh_io.json": mesh_io_tests(ref_root),
         "mechanical_linear.json": element_tests(ref_root, "tests/unit/test_mechanical_loss.py"),
         "neohooke_ad.json": element_tests(ref_root, "tests/unit/test_neo_hooke_mechanical_loss_AD.py"),
         "neohooke.json": element_tests(ref_root, "tests/unit/test_neo_hooke_mechanical_loss.py"),
