@@ -356,11 +356,11 @@ class FiniteElementLoss:
         dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda")
         ws = self._plan.workspace(capi.OP_LOSS_ADJOINT, B)
         chosen = C.c_int32()
-        times = (C.c_float * 16)()
+        times = (C.c_float * HEX8_VARIANTS)()
         rc = self._plan.lib.folgb_autotune(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1],
                                            capi.ptr(U), U.shape[1], capi.ptr(losses), capi.ptr(du), capi.ptr(dp),
                                            capi.ptr(ws), ws.numel(), repeats, capi.stream_handle(), C.byref(chosen),
-                                           C.cast(times, C.c_void_p), 16)
+                                           C.cast(times, C.c_void_p), HEX8_VARIANTS)
         capi.check("folgb_autotune", rc)
         tunable = (self.element_type == "hexahedron" and self.physics == capi.ELASTIC and self.num_gp == 2
                    and self.loss_settings.get("kernel_variant", "auto") == "auto")
