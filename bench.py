@@ -43,14 +43,19 @@ FLUSH_BYTES = 512 * 1024 * 1024
 # grad u (72 FMA), stress (~20), B^T sigma (72 FMA), energy and dE (~25):
 # 4 x 72 x 2 + 75 = 651 flops, x 8 points = 5,208 flops; plus gathers ~0.
 FLOPS_PER_ELEMENT = 5208.0
-# DRAM bytes (read + write) of one k_hex8_elastic launch on the 64^3 workload,
-# from an ncu capture (dram__bytes_read.sum + dram__bytes_write.sum of the
-# autotuned variant, 128 threads / 96 registers): 17,498,624 + 108,544.  Other
-# mesh sizes report null.
-NCU_TRAFFIC_BYTES = {64: 17_607_168}
-# Warp instructions of the same launch (smsp__inst_executed.sum): the kernel's
-# real limit is instruction issue (4 warp instructions per clock per SM).
-NCU_WARP_INSTRUCTIONS = {64: 16_144_605}
+# ncu figures of one launch of the fused element kernel on the 64^3 workload,
+# per kernel variant (the autotuner's index): DRAM bytes read + written
+# (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
+# (smsp__inst_executed.sum; the kernel's real limit is instruction issue, 4
+# warp instructions per clock per SM).  Variants without a capture report null.
+#   6:  k_hex8_elastic_regs, 128 threads / 96 registers, point sums
+#   13: k_hex8_elastic_tma, persistent, TMA-staged rows, paired points
+NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16_144_605},
+                    13: {"traffic": 17_585_152 + 17_664, "warp_instructions": 12_610_462}}}
+
+
+def ncu_figure(n, variant, key):
+    return NCU_FIGURES.get(n, {}).get(variant, {}).get(key)
 
 
 def parse():
@@ -66,7 +71,7 @@ def parse():
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     ap.add_argument("--hex8-variant", type=int, default=None,
-                    help="force one hex8 kernel variant (0-12) instead of autotuning (profiling runs)")
+                    help="force one hex8 kernel variant (0-15) instead of autotuning (profiling runs)")
     ap.add_argument("--extras", default="small,pcg,batched,neohooke",
                     help="comma list of the extra measurements to run (small, pcg, batched, neohooke)")
     return ap.parse_args()
@@ -146,10 +151,10 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
-def issue_roofline(n, elem_ms, clk, peaks):
+def issue_roofline(n, variant, elem_ms, clk, peaks):
     """Instruction-issue roofline of the element kernel: ncu's warp-instruction
     count over 152 SMs x 4 issue slots per clock at the sampled SM clock."""
-    wi = NCU_WARP_INSTRUCTIONS.get(n)
+    wi = ncu_figure(n, variant, "warp_instructions")
     if wi is None:
         return None
     mhz = (clk or {}).get("sm_mhz") or (peaks or {}).get("sm_max_mhz", 2070.0)
@@ -666,16 +671,17 @@ def main():
                                          "variants": HEX8_VARIANT_NAMES}},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                              "frac": achieved / hbm,
-                             "traffic": NCU_TRAFFIC_BYTES.get(args.n),
+                             "traffic": ncu_figure(args.n, tune["chosen"], "traffic"),
                              "traffic_unit": "bytes per launch (ncu dram read + write)",
                              "algorithmic_bytes": alg_bytes,
-                             "kernel": "k_hex8_elastic (sum-factorised hex8 2x2x2)",
+                             "kernel": "sum-factorised hex8 2x2x2 element kernel, variant %d (%s)"
+                                       % (tune["chosen"], HEX8_VARIANT_NAMES[tune["chosen"]]),
                              "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
                              "fp32": {"achieved_tflops": fp32_achieved, "nominal_peak_tflops": fp32_peak,
                                       "frac": fp32_achieved / fp32_peak,
                                       "flops_per_element": FLOPS_PER_ELEMENT,
                                       "note": "naive-algorithm flop count; the sum-factorised kernel executes fewer"},
-                             "issue": issue_roofline(args.n, elem_ms, clk, peaks)},
+                             "issue": issue_roofline(args.n, tune["chosen"], elem_ms, clk, peaks)},
                 "e2e": {"value": B * nE / (ms_e2e * 1e-3) / 1e6, "unit": "M elements/s", "ms_per_step": ms_e2e,
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
