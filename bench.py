@@ -606,16 +606,13 @@ def main():
     out_du = torch.empty_like(u_pin).pin_memory()
     out_dc = torch.empty_like(c_pin).pin_memory()
     out_l = torch.empty(1).pin_memory()
-    u_dev = torch.empty_like(u)
-    c_dev = torch.empty_like(ctrl)
 
     def e2e_step():
-        u_dev.copy_(u_pin, non_blocking=True)
-        c_dev.copy_(c_pin, non_blocking=True)
-        _, _, losses, du, dc = loss.ComputeBatchLossAndGrad(c_dev, u_dev)
-        out_l.copy_(losses, non_blocking=True)
-        out_du.copy_(du, non_blocking=True)
-        out_dc.copy_(dc, non_blocking=True)
+        # the public API with pinned host buffers: the dofs are copied in, the
+        # element controls read in place, the gradients stored straight into
+        # the host result buffers by the kernels, the loss copied out; each
+        # step's timed region ends when all of it has reached host memory
+        loss.ComputeBatchLossAndGrad(c_pin, u_pin, out=(out_l, out_du, out_dc))
 
     for _ in range(3):
         e2e_step()

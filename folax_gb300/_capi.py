@@ -74,6 +74,8 @@ PROTOTYPES = {
     "folgb_loss_adjoint_plain": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_loss_adjoint_noalloc": (C.c_int, [vp, i32, vp, i64, vp, i64, i32, vp, vp, vp, vp, vp]),
     "folgb_autotune": (C.c_int, [vp, i32, vp, i64, vp, i64, vp, vp, vp, vp, sz, i32, vp, C.POINTER(i32), vp, i32]),
+    "folgb_autotune_flushed": (C.c_int, [vp, i32, vp, i64, vp, i64, vp, vp, vp, vp, sz, i32, vp, C.POINTER(i32), vp,
+                                         i32, vp, sz]),
     "folgb_csr_pattern": (C.c_int, [vp, vp, vp, vp]),
     "folgb_assemble": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_pcg": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),

@@ -1115,11 +1115,15 @@ int hex8_variant_count();
 
 // Times every kernel variant of the plan's loss + adjoint path on the given
 // inputs (2 warm-up and `repeats` timed calls each, CUDA events on the stream)
-// and keeps the fastest in the plan.  Synchronises the stream.
-extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control, int64_t control_stride,
-                              const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
-                              float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
-                              void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants) {
+// and keeps the fastest in the plan.  With a flush buffer, each timed call is
+// preceded (outside its events) by a write of the whole buffer, so the calls
+// start with the mesh tables and inputs out of L2, as they do in a training
+// step.  Synchronises the stream.
+static int autotune_impl(folgb_plan* p, int32_t batch, const float* control, int64_t control_stride,
+                         const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                         float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
+                         void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants,
+                         void* flush, size_t flush_bytes) {
   if (!p || !chosen) return FOLGB_ERR_INVALID_ARGUMENT;
   const bool tunable = p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && p->phys.num_gp == 2 &&
                        p->phys.kernel_variant == 0;  // a forced variant is not retuned
@@ -1138,14 +1142,19 @@ extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control
     for (int k = 0; k < 2 && rc == FOLGB_OK; ++k)
       rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
                               dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
-    cudaEventRecord(a, s);
-    for (int k = 0; k < repeats && rc == FOLGB_OK; ++k)
-      rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
-                              dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
-    cudaEventRecord(b, s);
-    if (cudaEventSynchronize(b) != cudaSuccess) rc = FOLGB_ERR_CUDA;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, a, b);
+    for (int k = 0; k < repeats && rc == FOLGB_OK; ++k) {
+      if (flush && flush_bytes && cudaMemsetAsync(flush, k & 0xff, flush_bytes, s) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+      cudaEventRecord(a, s);
+      if (rc == FOLGB_OK)
+        rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
+                                dloss_dcontrol, nullptr, workspace, workspace_bytes, stream);
+      cudaEventRecord(b, s);
+      if (cudaEventSynchronize(b) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+      float one = 0.f;
+      cudaEventElapsedTime(&one, a, b);
+      ms += one;
+    }
     ms /= repeats;
     if (ms_per_variant && v < max_variants) ms_per_variant[v] = ms;
     if (tunable && (v == 0 || ms < best_ms)) {
@@ -1158,4 +1167,23 @@ extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control
   p->hex8_variant = best;
   *chosen = best;
   return rc;
+}
+
+extern "C" int folgb_autotune(folgb_plan* p, int32_t batch, const float* control, int64_t control_stride,
+                              const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                              float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
+                              void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants) {
+  return autotune_impl(p, batch, control, control_stride, dofs, dofs_stride, losses, dloss_ddofs, dloss_dcontrol,
+                       workspace, workspace_bytes, repeats, stream, chosen, ms_per_variant, max_variants, nullptr, 0);
+}
+
+extern "C" int folgb_autotune_flushed(folgb_plan* p, int32_t batch, const float* control, int64_t control_stride,
+                                      const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                                      float* dloss_dcontrol, void* workspace, size_t workspace_bytes,
+                                      int32_t repeats, void* stream, int32_t* chosen, float* ms_per_variant,
+                                      int32_t max_variants, void* flush_buffer, size_t flush_bytes) {
+  if (!flush_buffer || !flush_bytes) return FOLGB_ERR_INVALID_ARGUMENT;
+  return autotune_impl(p, batch, control, control_stride, dofs, dofs_stride, losses, dloss_ddofs, dloss_dcontrol,
+                       workspace, workspace_bytes, repeats, stream, chosen, ms_per_variant, max_variants,
+                       flush_buffer, flush_bytes);
 }

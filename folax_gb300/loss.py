@@ -53,6 +53,8 @@ def _dev(x, dtype=None):
     if isinstance(x, torch.Tensor):
         if x.is_cuda and x.dtype == dtype and x.is_contiguous():
             return x  # already usable: no conversion call on the hot path
+        if x.device.type == "cpu" and x.is_pinned() and x.dtype == dtype and x.is_contiguous():
+            return x.to(device="cuda", non_blocking=True)  # stream-ordered copy from pinned memory
         return x.to(device="cuda", dtype=dtype).contiguous()
     return torch.as_tensor(np.asarray(x), dtype=dtype, device="cuda").contiguous()
 
@@ -319,20 +321,54 @@ class FiniteElementLoss:
             raise ValueError("batch_params must have 1 or batch rows")
         return P, U, B
 
-    def ComputeBatchLossAndGrad(self, batch_params, batch_dofs, grads: bool = True, plain: bool = False):
+    def ComputeBatchLossAndGrad(self, batch_params, batch_dofs, grads: bool = True, plain: bool = False,
+                                out=None):
         """Fused FE loss + adjoint (fe_loss.py:250-262 and its reverse pass).
 
         Returns (mean, (min, max, mean), per-instance losses, dLoss/d dofs,
-        dLoss/d params); the gradients are None when grads is False."""
+        dLoss/d params); the gradients are None when grads is False.
+
+        Host buffers: out = (losses [B], dLoss/d dofs [B, dofs],
+        dLoss/d params [B, controls]) gives the result buffers, float32 and
+        contiguous, on the GPU or in pinned host memory.  The kernels store the
+        gradients straight into pinned host buffers over the host link (no
+        separate device-to-host copy) and the per-instance losses follow with
+        one small copy; like torch's non_blocking copies, host results are
+        complete once the current stream has finished (mean / min / max stay
+        on the GPU).  Pinned host inputs: the dofs are copied to the GPU on the
+        current stream; element-layout controls (read once per element) are
+        read by the kernel straight from pinned host memory."""
         torch = _torch()
-        P, U, B = self._batched(batch_params, batch_dofs)
+        direct_ctrl = (isinstance(batch_params, torch.Tensor) and batch_params.device.type == "cpu"
+                       and batch_params.is_pinned() and batch_params.dtype == torch.float32
+                       and batch_params.is_contiguous() and self._plan.phys.control_layout == capi.CONTROL_ELEMENT
+                       and not self.parametric_boundary_learning)
+        U = _dev(batch_dofs)
+        U = U.reshape(-1, self.total_number_of_dofs) if U.dim() != 2 else U
+        if direct_ctrl:
+            P, B = batch_params.reshape(-1, self.GetNumberOfControls()), U.shape[0]
+            if P.shape[0] not in (1, B):
+                raise ValueError("batch_params must have 1 or batch rows")
+        else:
+            P, U, B = self._batched(batch_params, U)
         apply_bc = 1
         if self.parametric_boundary_learning:
             U = self.GetFullDofVector(P, U)
             apply_bc = 0
-        losses = torch.empty(B, dtype=torch.float32, device="cuda")
-        du = torch.empty_like(U) if grads else None
-        dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if grads else None
+        out_losses = None
+        if out is not None:
+            out_losses, du, dp = out
+            want = [(out_losses, (B,)), (du, (B, U.shape[1])), (dp, (B, P.shape[1]))]
+            for t, shape in want:
+                if (t.dtype != torch.float32 or not t.is_contiguous() or t.numel() != int(np.prod(shape))
+                        or not (t.is_cuda or t.is_pinned())):
+                    raise ValueError(f"out buffers must be float32, contiguous, of {shape} elements, "
+                                     "on the GPU or in pinned host memory")
+            losses = out_losses if out_losses.is_cuda else torch.empty(B, dtype=torch.float32, device="cuda")
+        else:
+            losses = torch.empty(B, dtype=torch.float32, device="cuda")
+            du = torch.empty_like(U) if grads else None
+            dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if grads else None
         op = capi.OP_PLAIN if plain else capi.OP_LOSS_ADJOINT
         ws = self._plan.workspace(op, B)
         fn = self._plan.lib.folgb_loss_adjoint_plain if plain else self._plan.lib.folgb_loss_adjoint
@@ -340,15 +376,22 @@ class FiniteElementLoss:
                 apply_bc, capi.ptr(losses), capi.ptr(du), capi.ptr(dp), capi.ptr(self._status), capi.ptr(ws),
                 ws.numel(), capi.stream_handle())
         capi.check("folgb_loss_adjoint_plain" if plain else "folgb_loss_adjoint", rc)
+        if out_losses is not None and out_losses is not losses:
+            out_losses.copy_(losses, non_blocking=True)
+        ret_losses = losses if out_losses is None else out_losses
         if B == 1:  # views, no extra kernels
             mean = losses[0]
-            return mean, (mean, mean, mean), losses, du, dp
+            return mean, (mean, mean, mean), ret_losses, du, dp
         mean = losses.mean()
-        return mean, (losses.min(), losses.max(), mean), losses, du, dp
+        return mean, (losses.min(), losses.max(), mean), ret_losses, du, dp
 
-    def Autotune(self, batch_params, batch_dofs, repeats: int = 5):
-        """Time the plan's kernel variants on these inputs and keep the fastest
-        (folgb_autotune).  Returns {"chosen": v, "ms": [per-variant times]}."""
+    def Autotune(self, batch_params, batch_dofs, repeats: int = 5, cold_l2: bool = True):
+        """Time the plan's kernel variants on these inputs and keep the fastest.
+        cold_l2: every timed call starts with the L2 cache flushed (a
+        temporary 256 MiB device buffer is overwritten before it,
+        folgb_autotune_flushed), as inside a training step; otherwise the calls
+        run back to back (folgb_autotune).  Returns {"chosen": v, "ms":
+        [per-variant times]}."""
         torch = _torch()
         P, U, B = self._batched(batch_params, batch_dofs)
         losses = torch.empty(B, dtype=torch.float32, device="cuda")
@@ -357,11 +400,17 @@ class FiniteElementLoss:
         ws = self._plan.workspace(capi.OP_LOSS_ADJOINT, B)
         chosen = C.c_int32()
         times = (C.c_float * HEX8_VARIANTS)()
-        rc = self._plan.lib.folgb_autotune(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1],
-                                           capi.ptr(U), U.shape[1], capi.ptr(losses), capi.ptr(du), capi.ptr(dp),
-                                           capi.ptr(ws), ws.numel(), repeats, capi.stream_handle(), C.byref(chosen),
-                                           C.cast(times, C.c_void_p), HEX8_VARIANTS)
-        capi.check("folgb_autotune", rc)
+        args = (self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1], capi.ptr(U), U.shape[1],
+                capi.ptr(losses), capi.ptr(du), capi.ptr(dp), capi.ptr(ws), ws.numel(), repeats,
+                capi.stream_handle(), C.byref(chosen), C.cast(times, C.c_void_p), HEX8_VARIANTS)
+        if cold_l2:
+            flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+            rc = self._plan.lib.folgb_autotune_flushed(*args, capi.ptr(flush), flush.numel())
+            del flush
+            capi.check("folgb_autotune_flushed", rc)
+        else:
+            rc = self._plan.lib.folgb_autotune(*args)
+            capi.check("folgb_autotune", rc)
         tunable = (self.element_type == "hexahedron" and self.physics == capi.ELASTIC and self.num_gp == 2
                    and self.loss_settings.get("kernel_variant", "auto") == "auto")
         n = HEX8_VARIANTS if tunable else 1

@@ -188,6 +188,17 @@ int folgb_autotune(folgb_plan* plan, int32_t batch, const float* control, int64_
                    float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
                    void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants);
 
+/* folgb_autotune with the L2 cold before every timed call, as it is inside a
+ * training step where other work runs between loss evaluations: the caller's
+ * device buffer flush_buffer (flush_bytes, larger than the L2 cache, e.g.
+ * 256 MiB on GB300) is overwritten before each timed call, outside its timing.
+ * No counterpart in the reference. */
+int folgb_autotune_flushed(folgb_plan* plan, int32_t batch, const float* control, int64_t control_stride,
+                           const float* dofs, int64_t dofs_stride, float* losses, float* dloss_ddofs,
+                           float* dloss_dcontrol, void* workspace, size_t workspace_bytes, int32_t repeats,
+                           void* stream, int32_t* chosen, float* ms_per_variant, int32_t max_variants,
+                           void* flush_buffer, size_t flush_bytes);
+
 /* Copies the plan's CSR pattern (canonical: sorted column indices, one entry
  * per connected dof pair, the pattern scipy.sparse.csr_array builds from the
  * reference's BCOO, fe_solver.py:71-72) into device arrays indptr[rows+1],

@@ -134,6 +134,32 @@ def test_tma_variant_equals_its_per_thread_twin(cuda, tma, twin, layout):
     assert np.array_equal(a[4].cpu().numpy(), b[4].cpu().numpy())
 
 
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+@pytest.mark.parametrize("B", [1, 3])
+def test_pinned_host_buffers_equal_device_buffers(cuda, layout, B):
+    """Pinned host inputs (element controls read by the kernel in place) and
+    result buffers (the kernels store straight into host memory) give
+    bit-identical results to device buffers."""
+    torch = cuda
+    m = make_mesh("hex8", 6, seed=36, jitter=0.1)
+    s = _settings("hex8", "elastic", layout, 1.0)
+    gl = gpu_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(37)
+    ctrl = (0.5 + rng.random((B, gl.GetNumberOfControls()))).astype(np.float32)
+    u = (0.01 * rng.standard_normal((B, gl.GetTotalNumberOfDOFs()))).astype(np.float32)
+    a = gl.ComputeBatchLossAndGrad(torch.from_numpy(ctrl).cuda(), torch.from_numpy(u).cuda())
+    out = (torch.empty(B).pin_memory(), torch.empty(B, u.shape[1]).pin_memory(),
+           torch.empty(B, ctrl.shape[1]).pin_memory())
+    h = gl.ComputeBatchLossAndGrad(torch.from_numpy(ctrl).pin_memory(), torch.from_numpy(u).pin_memory(), out=out)
+    torch.cuda.synchronize()  # host results are complete once the stream has finished
+    assert np.array_equal(a[0].cpu().numpy(), h[0].cpu().numpy())
+    for x, y, o in zip(a[2:], h[2:], out):
+        assert y.data_ptr() == o.data_ptr() and not y.is_cuda
+        assert np.array_equal(x.cpu().numpy(), y.numpy())
+    with pytest.raises(ValueError):
+        gl.ComputeBatchLossAndGrad(ctrl, u, out=(torch.empty(B), out[1], out[2]))  # pageable: refused
+
+
 def test_autotune_keeps_results_exact(cuda):
     m = make_mesh("hex8", 6, seed=25)
     s = _settings("hex8", "elastic", "element")
@@ -141,7 +167,9 @@ def test_autotune_keeps_results_exact(cuda):
     rng = np.random.default_rng(26)
     ctrl = 0.5 + rng.random((1, gl.GetNumberOfControls()))
     u = 0.01 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
-    info = gl.Autotune(ctrl, u, repeats=2)
+    warm = gl.Autotune(ctrl, u, repeats=2, cold_l2=False)  # back-to-back calls
+    assert 0 <= warm["chosen"] < 16 and len(warm["ms"]) == 16 and min(warm["ms"]) > 0
+    info = gl.Autotune(ctrl, u, repeats=2)  # every timed call after an L2 flush
     assert 0 <= info["chosen"] < 16 and len(info["ms"]) == 16 and min(info["ms"]) > 0
     a = gl.ComputeBatchLossAndGrad(ctrl, u)
     o = ol.batch_loss_and_grads(ctrl, u)
