@@ -72,8 +72,8 @@ def parse():
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     ap.add_argument("--hex8-variant", type=int, default=None,
                     help="force one hex8 kernel variant (0-15) instead of autotuning (profiling runs)")
-    ap.add_argument("--extras", default="small,pcg,batched,neohooke",
-                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke)")
+    ap.add_argument("--extras", default="small,pcg,batched,neohooke,newton",
+                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke, newton)")
     return ap.parse_args()
 
 
@@ -462,8 +462,58 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
     h = solver.history[-1] if solver.history else {}
     out["newton"] = {"mesh": f"{newton_n}^3 hex split into {len(m2.elements_nodes['tetra'])} tets",
                      "dofs": l2.GetTotalNumberOfDOFs(), "ms_per_newton_iteration": t_newton * 1e3,
-                     "linear": h.get("linear") or solver.last_linear_info, "residual_norm": h.get("res_norm"),
+                     "solve": "device-resident (one CUDA graph: assembly + fp64-vector BiCGSTAB loop)",
+                     "newton_info": solver.last_newton_info, "residual_norm": h.get("res_norm"),
                      "error": err}
+    return out
+
+
+def extra_newton(args, n=10, seed=7, steps=5):
+    """A whole nonlinear solve, Saint-Venant-Kirchhoff hex8 on an n^3 box
+    (two-phase nodal Young's modulus, bottom fixed, top stretched by 0.1 in
+    4 load steps): the device-resident Newton solve (one CUDA graph) against
+    the host-driven Newton loop, wall time per solve with the result on the
+    device."""
+    import torch
+    from folax_gb300 import fields
+    from folax_gb300.loss import SaintVenantMechanicalLoss3DHexa
+    from folax_gb300.mesh import create_3D_box_mesh
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    mesh = create_3D_box_mesh(n, n, n)
+    settings = {"dirichlet_bc_dict": {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.1}},
+                "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3}}
+    loss = SaintVenantMechanicalLoss3DHexa("svk", dict(settings), mesh)
+    loss.Initialize()
+    Ee = fields.two_phase_voxels(n, seed)
+    ctrl = np.zeros(mesh.GetNumberOfNodes())
+    cnt = np.zeros(mesh.GetNumberOfNodes())
+    conn = mesh.elements_nodes["hexahedron"]
+    np.add.at(ctrl, conn, Ee[:, None])
+    np.add.at(cnt, conn, 1.0)
+    ctrl = (ctrl / cnt).astype(np.float32)
+    out = {"mesh": f"{n}^3 hex8, Saint-Venant-Kirchhoff", "dofs": loss.GetTotalNumberOfDOFs()}
+    for resident in (True, False):
+        solver = FiniteElementNonLinearResidualBasedSolver("nl", loss, {
+            "linear_solver_settings": {"solver": "JAX-bicgstab", "tol": 1e-8, "maxiter": 5000},
+            "nonlinear_solver_settings": {"load_incr": 4, "maxiter": 10, "abs_tol": 1e-6, "rel_tol": 1e-7,
+                                          "device_resident": resident}})
+        solver.Initialize()
+        u0 = np.zeros(loss.GetTotalNumberOfDOFs(), dtype=np.float32)
+        for _ in range(2):
+            solver.Solve(ctrl, u0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            x = solver.Solve(ctrl, u0)
+        torch.cuda.synchronize()
+        ms = (time.perf_counter() - t0) / steps * 1e3
+        key = "device_resident" if resident else "host_loop"
+        out[key] = {"ms_per_solve": ms, "newton_iterations": len(solver.history),
+                    "final_res_norm": solver.history[-1]["res_norm"] if solver.history else None}
+        if resident:
+            out[key]["krylov_iterations"] = (solver.last_newton_info or {}).get("krylov_iterations")
+        out[key + "_solution_norm"] = float(torch.linalg.vector_norm(x.double()).item())
+    out["speedup_device_resident"] = out["host_loop"]["ms_per_solve"] / out["device_resident"]["ms_per_solve"]
     return out
 
 
@@ -639,7 +689,8 @@ def main():
         for key, name, fn in (("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
                               ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
                               ("batched", "batched_quad4_512", lambda: extra_batched(args)),
-                              ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args))):
+                              ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args)),
+                              ("newton", "newton_svk_hex8_10", lambda: extra_newton(args))):
             if key not in wanted:
                 continue
             try:

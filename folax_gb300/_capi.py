@@ -59,6 +59,17 @@ class Physics(C.Structure):
     ]
 
 
+class NewtonSettings(C.Structure):
+    _fields_ = [("load_steps", C.c_int32), ("max_iterations", C.c_int32), ("abs_tol", C.c_double),
+                ("rel_tol", C.c_double), ("krylov_method", C.c_int32), ("vector_bits", C.c_int32),
+                ("krylov_rtol", C.c_double), ("krylov_maxiter", C.c_int32), ("check_every", C.c_int32)]
+
+
+class NewtonInfo(C.Structure):
+    _fields_ = [("newton_iterations", C.c_int32), ("krylov_iterations", C.c_int64), ("last_res_norm", C.c_double),
+                ("last_delta_norm", C.c_double), ("krylov_failures", C.c_int32), ("status", C.c_int32)]
+
+
 vp = C.c_void_p
 i32, i64, f32, f64, sz = C.c_int32, C.c_int64, C.c_float, C.c_double, C.c_size_t
 
@@ -83,6 +94,8 @@ PROTOTYPES = {
     "folgb_krylov": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz,
                                vp]),
     "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
+    "folgb_newton_workspace_bytes": (sz, [vp, C.POINTER(NewtonSettings)]),
+    "folgb_newton": (C.c_int, [vp, vp, vp, C.POINTER(NewtonSettings), C.POINTER(NewtonInfo), vp, vp, vp, sz, vp]),
     "folgb_adam_step": (C.c_int, [vp, vp, vp, vp, i64, vp, f32, f32, f32, f32, vp]),
     "folgb_batch_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), i32, vp, vp, vp, vp, vp, vp, i64, i32]),
     "folgb_batch_plan_destroy": (C.c_int, [vp]),

@@ -605,6 +605,10 @@ __global__ void k_krylov_continue(KScalars* sc, cudaGraphConditionalHandle loop,
   cudaGraphSetConditional(loop, sc->done ? 0u : 1u);
 }
 
+__global__ void k_arm_conditional(cudaGraphConditionalHandle h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(h, 1u);
+}
+
 template <int NDOF>
 static int group_width(int maxdeg) {
   int g = 1;
@@ -959,10 +963,15 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
   return false;
 }
 
+// capture_sc != NULL: s is being captured into a graph (the device-resident
+// Newton solve); the solve is enqueued as init + one WHILE node over
+// [K iterations, true residual, loop control] + the fp32 copy of x, with no
+// host synchronisation, and *capture_sc receives the solver's device scalars.
 template <class VT>
 static int krylov_solve(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
                         float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
-                        double* rel_residual, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+                        double* rel_residual, void* workspace, size_t workspace_bytes, cudaStream_t s,
+                        KScalars** capture_sc = nullptr) {
   if (!p || !vals || !dinv || !rhs || !x || maxiter <= 0 || !(rtol >= 0.0)) return FOLGB_ERR_INVALID_ARGUMENT;
   if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
   KWork<VT> w;
@@ -1030,13 +1039,7 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
       // once; the host reads the scalars at the end only.  Not while tracing
       // (the events would be captured) or while the caller's stream is being
       // captured itself; any graph API failure falls back to the host loop.
-      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-      bool resident = !trace_active() && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
-                      cap == cudaStreamCaptureStatusNone;
-      // small systems: the whole solve in one cluster launch (fp32 vectors:
-      // with fp64 vectors the per-nonzero fp64 arithmetic of a few SMs is
-      // slower than the all-SM multi-kernel path)
-      if (resident && n <= kClusterMaxDofs && sizeof(VT) == sizeof(float)) {
+      auto cluster_args = [&]() {
         ClusterArgs<VT> ca;
         ca.N = p->N;
         ca.adj_ptr = p->d_adj_ptr;
@@ -1058,6 +1061,65 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         ca.sc = w.sc;
         ca.rtol = rtol;
         ca.maxiter = maxiter;
+        return ca;
+      };
+      if (capture_sc) {
+        // small fp32 systems: the whole solve is one cluster launch here too
+        if (n <= kClusterMaxDofs && sizeof(VT) == sizeof(float) &&
+            launch_cluster_solver<NDOF, G, VT>(solver, cluster_args(), s)) {
+          *capture_sc = w.sc;
+          return (int)FOLGB_OK;
+        }
+        cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
+        cudaGraph_t graph = nullptr;
+        const cudaGraphNode_t* deps = nullptr;
+        size_t ndeps = 0;
+        FOLGB_CUDA_TRY(cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+        if (cst != cudaStreamCaptureStatusActive) return (int)FOLGB_ERR_INVALID_ARGUMENT;
+        cudaGraphConditionalHandle loop{};
+        FOLGB_CUDA_TRY(cudaGraphConditionalHandleCreate(&loop, graph, 1u, cudaGraphCondAssignDefault));
+        // the default value is assigned only when the top-level graph is
+        // launched: re-arm the loop each time the enclosing body runs
+        k_arm_conditional<<<1, 32, 0, s>>>(loop);
+        FOLGB_LAUNCH_CHECK();
+        FOLGB_CUDA_TRY(cudaStreamGetCaptureInfo(s, &cst, nullptr, &graph, &deps, nullptr, &ndeps));
+        cudaGraphNodeParams np{};
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = loop;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        FOLGB_CUDA_TRY(cudaGraphAddNode(&node, graph, deps, nullptr, ndeps, &np));
+        FOLGB_CUDA_TRY(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+        cudaStream_t cs = nullptr;
+        FOLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+        int crc = FOLGB_OK;
+        if (cudaStreamBeginCaptureToGraph(cs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+          crc = FOLGB_ERR_CUDA;
+        } else {
+          chunk(K, cs);
+          true_residual(cs);
+          k_krylov_continue<<<1, 32, 0, cs>>>(w.sc, loop, maxiter, max_rounds);
+          const bool launched_ok = cudaGetLastError() == cudaSuccess;
+          cudaGraph_t body_out = nullptr;
+          if (cudaStreamEndCapture(cs, &body_out) != cudaSuccess || !launched_ok) crc = FOLGB_ERR_CUDA;
+        }
+        cudaStreamDestroy(cs);
+        if (crc) return crc;
+        k_to_float<<<vb, 256, 0, s>>>(n, w.x, x);
+        FOLGB_LAUNCH_CHECK();
+        *capture_sc = w.sc;
+        return (int)FOLGB_OK;
+      }
+      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+      bool resident = !trace_active() && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
+                      cap == cudaStreamCaptureStatusNone;
+      // small systems: the whole solve in one cluster launch (fp32 vectors:
+      // with fp64 vectors the per-nonzero fp64 arithmetic of a few SMs is
+      // slower than the all-SM multi-kernel path)
+      if (resident && n <= kClusterMaxDofs && sizeof(VT) == sizeof(float)) {
+        ClusterArgs<VT> ca = cluster_args();
         if (launch_cluster_solver<NDOF, G, VT>(solver, ca, s)) {
           FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
           FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
@@ -1134,7 +1196,7 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
       return (int)FOLGB_OK;
     });
   });
-  if (rc) return rc;
+  if (rc || capture_sc) return rc;
   if (iterations) *iterations = host.iters;
   if (rel_residual) *rel_residual = host.bnorm2 > 0 ? std::sqrt(host.rnorm2 / host.bnorm2) : 0.0;
   if (host.done == 3) return FOLGB_ERR_NAN;
@@ -1202,4 +1264,237 @@ extern "C" int folgb_adam_step(float* params, const float* grads, float* m, floa
   k_step_inc<<<1, 1, 0, s>>>(step);
   FOLGB_LAUNCH_CHECK();
   return FOLGB_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Device-resident Newton-Raphson with load stepping
+// (fol/solvers/fe_nonlinear_residual_based_solver.py:76-170).  The whole solve
+// is one CUDA graph: a WHILE node whose body is one Newton iteration
+// [load-scaled Dirichlet values at the start of a load step, residual and
+// CSR tangent assembly, |r| and rhs = -r, the Krylov solve (a nested WHILE
+// node), |du|, the convergence test, u += du], launched once; the host reads
+// the Newton state when the graph has finished.  Convergence as the
+// reference: |r| < abs_tol or |du| < rel_tol or the iteration cap, the
+// converged iteration's update not applied; a non-finite |r| stops the solve.
+// ---------------------------------------------------------------------------
+namespace folgb {
+
+struct NState {
+  double rn2, dn2, abs2, rel2;
+  long long krylov_total;
+  int step, it, steps, maxit, done, status, newton_total, apply, krylov_fail;
+};
+
+constexpr int kNewtonBlocks = 1024;
+
+__global__ void k_newton_bc(int64_t N, int ndof, const unsigned char* __restrict__ dmask,
+                            const float* __restrict__ dval, float* __restrict__ u, const NState* st) {
+  if (st->it != 0 || st->done) return;  // only at the start of a load step
+  const double frac = (double)(st->step + 1) / (double)st->steps;
+  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < N; n += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned m = dmask[n];
+    for (int c = 0; c < ndof; ++c)
+      if ((m >> c) & 1u) u[(int64_t)ndof * n + c] = (float)(frac * (double)dval[(int64_t)ndof * n + c]);
+  }
+}
+
+// rhs = -r (when neg) and the fp64 squared norm of v into *out, fixed order
+__global__ void k_newton_norm(int64_t n, const float* __restrict__ v, float* __restrict__ neg, double* part,
+                              unsigned* counter, double* out) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float x = v[i];
+    if (neg) neg[i] = -x;
+    acc += (double)x * (double)x;
+  }
+  const double s = block_sum_d(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (!last_block(counter)) return;
+  const double tot = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *out = tot;
+    *counter = 0u;
+  }
+}
+
+// hist[k] = (load step, iteration, |r|, |du|) of Newton iteration k
+__global__ void k_newton_control(NState* st, const KScalars* sc, cudaGraphConditionalHandle loop, double* hist,
+                                 int hist_cap) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = st->newton_total;
+  if (k < hist_cap) {
+    hist[4 * k] = st->step + 1;
+    hist[4 * k + 1] = st->it + 1;
+    hist[4 * k + 2] = sqrt(st->rn2);
+    hist[4 * k + 3] = sqrt(st->dn2);
+  }
+  st->newton_total = k + 1;
+  st->krylov_total += sc->iters;
+  if (sc->done == 3 || sc->done == 4) st->krylov_fail += 1;
+  st->it += 1;
+  st->apply = 0;
+  if (!isfinite(st->rn2)) {
+    st->status = FOLGB_ERR_NAN;
+    st->done = 1;
+  } else if (st->rn2 < st->abs2 || st->dn2 < st->rel2 || st->it >= st->maxit) {
+    st->step += 1;
+    st->it = 0;
+    if (st->step >= st->steps) st->done = 1;
+  } else {
+    st->apply = 1;
+  }
+  // every body execution is one Newton iteration: at most steps * maxit
+  if (st->newton_total >= st->steps * st->maxit) st->done = 1;
+  cudaGraphSetConditional(loop, st->done ? 0u : 1u);
+}
+
+__global__ void k_newton_update(int64_t n, float* __restrict__ u, const float* __restrict__ du, const NState* st) {
+  if (!st->apply) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    u[i] += du[i];
+}
+
+struct NewtonWS {
+  void* asm_ws;
+  size_t asm_bytes;
+  void* kry_ws;
+  size_t kry_bytes;
+  float *r, *rhs, *du, *vals, *dinv;
+  NState* st;
+  double* part;
+  unsigned* counter;
+  double* hist;
+};
+
+static size_t layout_newton(const folgb_plan* p, int vector_bits, int hist_cap, void* base, size_t cap,
+                            NewtonWS* w) {
+  Bump bp(base, cap);
+  const size_t n = (size_t)p->ndof * p->N;
+  NewtonWS t;
+  t.asm_bytes = folgb_workspace_bytes(p, FOLGB_OP_ASSEMBLE, 1);
+  t.asm_ws = bp.take<char>(t.asm_bytes);
+  t.kry_bytes = vector_bits == 64 ? krylov64_workspace_bytes(p) : pcg_workspace_bytes(p);
+  t.kry_ws = bp.take<char>(t.kry_bytes);
+  t.r = bp.take<float>(n);
+  t.rhs = bp.take<float>(n);
+  t.du = bp.take<float>(n);
+  t.vals = bp.take<float>((size_t)p->nnz);
+  t.dinv = bp.take<float>(n);
+  t.st = bp.take<NState>(1);
+  t.part = bp.take<double>(kNewtonBlocks);
+  t.counter = bp.take<unsigned>(2);
+  t.hist = bp.take<double>((size_t)4 * hist_cap);
+  if (w) *w = t;
+  return align_up(bp.off);
+}
+
+}  // namespace folgb
+
+extern "C" size_t folgb_newton_workspace_bytes(const folgb_plan* p, const folgb_newton_settings* s) {
+  if (!p || !s || !p->has_csr || s->load_steps <= 0 || s->max_iterations <= 0) return 0;
+  return layout_newton(p, s->vector_bits, s->load_steps * s->max_iterations, nullptr, 0, nullptr);
+}
+
+extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* dofs, const folgb_newton_settings* s,
+                            folgb_newton_info* info, double* history, int32_t* device_status, void* workspace,
+                            size_t workspace_bytes, void* stream) {
+  if (!p || !control || !dofs || !s) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
+  if (s->load_steps <= 0 || s->max_iterations <= 0 || s->krylov_maxiter <= 0 || !(s->krylov_rtol >= 0.0) ||
+      !(s->abs_tol >= 0.0) || !(s->rel_tol >= 0.0) || (s->vector_bits != 32 && s->vector_bits != 64) ||
+      (s->krylov_method != FOLGB_KRYLOV_CG && s->krylov_method != FOLGB_KRYLOV_BICGSTAB))
+    return FOLGB_ERR_INVALID_ARGUMENT;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  FOLGB_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+  // the solve synchronises at its end; kernel tracing would record host events
+  if (cap != cudaStreamCaptureStatusNone || trace_active()) return FOLGB_ERR_INVALID_ARGUMENT;
+  const int hist_cap = s->load_steps * s->max_iterations;
+  NewtonWS w;
+  const size_t need = layout_newton(p, s->vector_bits, hist_cap, workspace, workspace_bytes, &w);
+  if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
+  const int64_t n = (int64_t)p->ndof * p->N;
+  const int solver = s->krylov_method == FOLGB_KRYLOV_CG ? SOLVER_CG : SOLVER_BICGSTAB;
+  int vb = (int)((n + 255) / 256);
+  if (vb > kNewtonBlocks) vb = kNewtonBlocks;
+  int nb = (int)((p->N + 255) / 256);
+  if (nb > kNewtonBlocks) nb = kNewtonBlocks;
+
+  NState init{};
+  init.abs2 = s->abs_tol * s->abs_tol;
+  init.rel2 = s->rel_tol * s->rel_tol;
+  init.steps = s->load_steps;
+  init.maxit = s->max_iterations;
+  init.status = FOLGB_OK;
+
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = nullptr;
+  int rc = FOLGB_OK;
+  cudaGraphConditionalHandle loop{};
+  cudaGraphNodeParams np{};
+  if (cudaGraphCreate(&g, 0) != cudaSuccess || cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault) != cudaSuccess) {
+    rc = FOLGB_ERR_CUDA;
+  } else {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = loop;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess ||
+        cudaStreamBeginCaptureToGraph(cs, np.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                      cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      rc = FOLGB_ERR_CUDA;
+  }
+  if (rc == FOLGB_OK) {
+    KScalars* ksc = nullptr;
+    k_newton_bc<<<nb, 256, 0, cs>>>(p->N, p->ndof, p->d_dmask, p->d_dval, dofs, w.st);
+    rc = folgb_assemble(p, control, dofs, 0, w.r, w.vals, w.dinv, device_status, w.asm_ws, w.asm_bytes, cs);
+    if (rc == FOLGB_OK) {
+      k_newton_norm<<<vb, 256, 0, cs>>>(n, w.r, w.rhs, w.part, w.counter, &w.st->rn2);
+      rc = s->vector_bits == 64
+               ? krylov_solve<double>(p, solver, w.vals, w.dinv, w.rhs, w.du, s->krylov_rtol, s->krylov_maxiter,
+                                      s->check_every, nullptr, nullptr, w.kry_ws, w.kry_bytes, cs, &ksc)
+               : krylov_solve<float>(p, solver, w.vals, w.dinv, w.rhs, w.du, s->krylov_rtol, s->krylov_maxiter,
+                                     s->check_every, nullptr, nullptr, w.kry_ws, w.kry_bytes, cs, &ksc);
+    }
+    if (rc == FOLGB_OK) {
+      k_newton_norm<<<vb, 256, 0, cs>>>(n, w.du, nullptr, w.part, w.counter + 1, &w.st->dn2);
+      k_newton_control<<<1, 32, 0, cs>>>(w.st, ksc, loop, w.hist, hist_cap);
+      k_newton_update<<<vb, 256, 0, cs>>>(n, dofs, w.du, w.st);
+      if (cudaGetLastError() != cudaSuccess) rc = FOLGB_ERR_CUDA;
+    }
+    cudaGraph_t body_out = nullptr;
+    if (cudaStreamEndCapture(cs, &body_out) != cudaSuccess && rc == FOLGB_OK) rc = FOLGB_ERR_CUDA;
+  }
+  if (rc == FOLGB_OK && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+  NState fin{};
+  if (rc == FOLGB_OK) {
+    if (cudaMemsetAsync(w.counter, 0, 2 * sizeof(unsigned), st) != cudaSuccess ||
+        cudaMemcpyAsync(w.st, &init, sizeof(NState), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaGraphLaunch(exec, st) != cudaSuccess ||
+        cudaMemcpyAsync(&fin, w.st, sizeof(NState), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        (history && cudaMemcpyAsync(history, w.hist, sizeof(double) * 4 * hist_cap, cudaMemcpyDeviceToHost, st) !=
+                        cudaSuccess) ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      rc = FOLGB_ERR_CUDA;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (g) cudaGraphDestroy(g);
+  if (cs) cudaStreamDestroy(cs);
+  if (rc != FOLGB_OK) {
+    cudaGetLastError();
+    return rc;
+  }
+  if (info) {
+    info->newton_iterations = fin.newton_total;
+    info->krylov_iterations = fin.krylov_total;
+    info->last_res_norm = fin.newton_total > 0 ? std::sqrt(fin.rn2) : 0.0;
+    info->last_delta_norm = fin.newton_total > 0 ? std::sqrt(fin.dn2) : 0.0;
+    info->krylov_failures = fin.krylov_fail;
+    info->status = fin.status;
+  }
+  return fin.status;
 }

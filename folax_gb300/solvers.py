@@ -146,12 +146,18 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
 
     Convergence: |r|_2 < abs_tol or |dx|_2 < rel_tol or maxiter (the
     converged step's update is not applied, as in the reference).  Norms are
-    fp64 reductions on the device; one host read per Newton iteration."""
+    fp64 reductions on the device.  nonlinear_solver_settings
+    "device_resident" (default True): the whole solve, load steps, Newton
+    iterations and Krylov iterations, runs as one CUDA graph (folgb_newton)
+    with no host synchronisation until it ends; False: a host loop with one
+    host read per Newton iteration."""
 
     def __init__(self, fe_solver_name, fe_loss_function, fe_solver_settings: dict = {}, history_plot_settings: dict = {}):
         super().__init__(fe_solver_name, fe_loss_function, fe_solver_settings)
-        self.nonlinear_solver_settings = {"rel_tol": 1e-8, "abs_tol": 1e-8, "maxiter": 20, "load_incr": 5}
+        self.nonlinear_solver_settings = {"rel_tol": 1e-8, "abs_tol": 1e-8, "maxiter": 20, "load_incr": 5,
+                                          "device_resident": True}
         self.history = []
+        self.last_newton_info = None
 
     def Initialize(self) -> None:
         super().Initialize()
@@ -159,10 +165,45 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
             self.nonlinear_solver_settings = UpdateDefaultDict(self.nonlinear_solver_settings,
                                                                self.fe_solver_settings["nonlinear_solver_settings"])
 
+    def _solve_device_resident(self, current_control_vars, current_dofs):
+        torch = _torch()
+        loss = self.fe_loss_function
+        s = self.nonlinear_solver_settings
+        ls = self.linear_solver_settings
+        plan = loss._get_csr_plan()
+        st = capi.NewtonSettings()
+        st.load_steps, st.max_iterations = int(s["load_incr"]), int(s["maxiter"])
+        st.abs_tol, st.rel_tol = float(s["abs_tol"]), float(s["rel_tol"])
+        st.krylov_method = capi.KRYLOV_CG if self.LinearSolve == self.PCGLinearSolver else capi.KRYLOV_BICGSTAB
+        st.vector_bits = self._vector_bits()
+        st.krylov_rtol, st.krylov_maxiter = float(ls["tol"]), int(ls["maxiter"])
+        st.check_every = int(ls.get("check_every", 32))
+        nbytes = plan.lib.folgb_newton_workspace_bytes(plan.handle, C.byref(st))
+        ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+        u = _dev(current_dofs).clone().reshape(-1)
+        ctrl = _dev(current_control_vars).reshape(-1)
+        info = capi.NewtonInfo()
+        hist = np.zeros((st.load_steps * st.max_iterations, 4))
+        rc = plan.lib.folgb_newton(plan.handle, capi.ptr(ctrl), capi.ptr(u), C.byref(st), C.byref(info),
+                                   hist.ctypes.data, capi.ptr(loss._status), capi.ptr(ws), nbytes,
+                                   capi.stream_handle())
+        self.last_newton_info = {"newton_iterations": info.newton_iterations,
+                                 "krylov_iterations": info.krylov_iterations,
+                                 "res_norm": info.last_res_norm, "delta_norm": info.last_delta_norm,
+                                 "krylov_failures": info.krylov_failures, "status": info.status}
+        self.history = [{"load_step": int(h[0]), "iteration": int(h[1]), "res_norm": float(h[2]),
+                         "delta_dofs_norm": float(h[3])} for h in hist[:info.newton_iterations]]
+        if rc == capi.ERR_NAN:
+            raise ValueError("Residual norm contains NaN values.")
+        capi.check("folgb_newton", rc)
+        return u
+
     def Solve(self, current_control_vars, current_dofs):
         torch = _torch()
         loss = self.fe_loss_function
         s = self.nonlinear_solver_settings
+        if s.get("device_resident", True):
+            return self._solve_device_resident(current_control_vars, current_dofs)
         u = _dev(current_dofs).clone()
         n_steps = int(s["load_incr"])
         self.history = []

@@ -252,6 +252,44 @@ int folgb_krylov(const folgb_plan* plan, int32_t method, int32_t vector_bits,
                  double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
                  double* rel_residual, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ---- device-resident Newton-Raphson with load stepping --------------------
+ * FiniteElementNonLinearResidualBasedSolver.Solve
+ * (fol/solvers/fe_nonlinear_residual_based_solver.py:76-170) as ONE CUDA
+ * graph launched once: a WHILE node over Newton iterations, each [the
+ * load-scaled Dirichlet values written into dofs at the start of a load step
+ * (ApplyDirichletBCOnDofVector, fe_loss.py:186-189, with the plan's Dirichlet
+ * values), residual + CSR tangent assembly (folgb_assemble), |r| and
+ * rhs = -r, the Krylov solve of folgb_krylov (itself a nested WHILE node),
+ * |du|, the convergence test, dofs += du].  Convergence as the reference:
+ * |r| < abs_tol or |du| < rel_tol or max_iterations, the converged
+ * iteration's update not applied; a non-finite |r| stops the solve with
+ * FOLGB_ERR_NAN (the reference raises, :122-136).  Norms are fp64.  No host
+ * synchronisation until the end; the call then waits for the stream. */
+typedef struct folgb_newton_settings {
+  int32_t load_steps;       /* nonlinear_solver_settings "load_incr"  */
+  int32_t max_iterations;   /* "maxiter" per load step                */
+  double abs_tol, rel_tol;  /* "abs_tol" on |r|, "rel_tol" on |du|    */
+  int32_t krylov_method;    /* FOLGB_KRYLOV_CG / FOLGB_KRYLOV_BICGSTAB */
+  int32_t vector_bits;      /* 32 or 64 (folgb_krylov)                */
+  double krylov_rtol;       /* linear_solver_settings "tol"           */
+  int32_t krylov_maxiter, check_every;
+} folgb_newton_settings;
+typedef struct folgb_newton_info {
+  int32_t newton_iterations;   /* over all load steps                 */
+  int64_t krylov_iterations;   /* sum over the Newton iterations      */
+  double last_res_norm, last_delta_norm;
+  int32_t krylov_failures;     /* linear solves that ended non-finite / broke down */
+  int32_t status;              /* FOLGB_OK or FOLGB_ERR_NAN           */
+} folgb_newton_info;
+size_t folgb_newton_workspace_bytes(const folgb_plan* plan, const folgb_newton_settings* settings);
+/* dofs [total_dofs] (device): the initial guess in, the solution out.
+ * history (HOST, may be NULL): 4 doubles per Newton iteration, at most
+ * load_steps * max_iterations rows: (load step, iteration, |r|, |du|).
+ * Needs a plan with the CSR tables; the caller's stream must not be capturing. */
+int folgb_newton(const folgb_plan* plan, const float* control, float* dofs, const folgb_newton_settings* settings,
+                 folgb_newton_info* info, double* history, int32_t* device_status, void* workspace,
+                 size_t workspace_bytes, void* stream);
+
 /* y = A x on the plan's CSR (FP32). */
 int folgb_spmv(const folgb_plan* plan, const float* csr_values, const float* x, float* y,
                void* stream);

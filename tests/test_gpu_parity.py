@@ -462,6 +462,59 @@ def test_device_resident_krylov_loop_matches_host_loop(cuda, solver_name):
     assert torch.equal(x_dev, x_host)
 
 
+@pytest.mark.parametrize("etype,physics,n,solver_name,bits", [("hex8", "saint_venant", 14, "JAX-bicgstab", "fp32"),
+                                                               ("tet4", "neohooke_split", 4, "JAX-bicgstab", "fp64"),
+                                                               ("quad4", "neohooke", 8, "JAX-bicgstab", "fp64"),
+                                                               ("hex8", "elastic", 14, "GB300-pcg", "fp32")])
+def test_device_resident_newton_matches_host_loop(cuda, etype, physics, n, solver_name, bits):
+    """The whole Newton solve as one CUDA graph (WHILE over Newton iterations,
+    a nested WHILE over Krylov iterations, no host synchronisation until it
+    ends) against the host-driven Newton loop: the same iteration sequence
+    and residual history, and the same root within the Krylov tolerance.  14^3
+    hex8 (10,125 dofs) runs the host loop's linear solves in the
+    single-cluster solver, so the Krylov arithmetic differs; 4^3 tets and the
+    fp64-vector solves share it."""
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    m = make_mesh(etype, n, seed=63)
+    s = _settings(etype, physics, "nodal")
+    gl = gpu_loss(etype, physics, m, s)
+    ctrl = 0.5 + np.random.default_rng(64).random(gl.GetNumberOfControls())
+    out = {}
+    for resident in (True, False):
+        solver = FiniteElementNonLinearResidualBasedSolver("nl", gl, {
+            "linear_solver_settings": {"solver": solver_name, "tol": 1e-10, "maxiter": 5000, "vector_precision": bits},
+            "nonlinear_solver_settings": {"load_incr": 2, "maxiter": 8, "abs_tol": 1e-7, "rel_tol": 1e-8,
+                                          "device_resident": resident}})
+        solver.Initialize()
+        x = solver.Solve(ctrl, np.zeros(gl.GetTotalNumberOfDOFs())).double().cpu().numpy()
+        out[resident] = (x, [(h["load_step"], h["iteration"], h["res_norm"]) for h in solver.history])
+    (xd, hd), (xh, hh) = out[True], out[False]
+    assert [h[:2] for h in hd] == [h[:2] for h in hh]
+    np.testing.assert_allclose([h[2] for h in hd], [h[2] for h in hh], rtol=1e-3, atol=1e-9)
+    assert rel_fro(xd, xh) < 1e-6
+
+
+def test_device_resident_newton_reports_nan(cuda):
+    """A NaN in the control makes |r| non-finite: the device-resident solve
+    stops and raises like the reference's host check."""
+    from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
+    m = make_mesh("hex8", 3, seed=65)
+    s = _settings("hex8", "elastic", "nodal")
+    gl = gpu_loss("hex8", "elastic", m, s)
+    ctrl = np.ones(gl.GetNumberOfControls())
+    ctrl[5] = np.nan
+    solver = FiniteElementNonLinearResidualBasedSolver("nl", gl, {"nonlinear_solver_settings": {"load_incr": 2}})
+    solver.Initialize()
+    with pytest.raises(ValueError):
+        solver.Solve(ctrl, np.zeros(gl.GetTotalNumberOfDOFs()))
+    assert solver.last_newton_info["newton_iterations"] == 1
+    gl._status.zero_()  # the assembly also raised the NaN status bit
+    # the context is still usable
+    x = FiniteElementNonLinearResidualBasedSolver("nl2", gl, {"nonlinear_solver_settings": {"load_incr": 1}})
+    x.Initialize()
+    assert np.isfinite(x.Solve(np.ones(gl.GetNumberOfControls()), np.zeros(gl.GetTotalNumberOfDOFs())).cpu().numpy()).all()
+
+
 @pytest.mark.parametrize("solver_name,etype,physics,n", [("GB300-pcg", "hex8", "elastic", 8),
                                                         ("GB300-pcg", "quad4", "thermal", 50),
                                                         ("JAX-bicgstab", "tet4", "elastic", 6),
