@@ -71,7 +71,7 @@ def parse():
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
     ap.add_argument("--hex8-variant", type=int, default=None,
-                    help="force one hex8 kernel variant (0-15) instead of autotuning (profiling runs)")
+                    help="force one hex8 kernel variant (0-17) instead of autotuning (profiling runs)")
     ap.add_argument("--extras", default="small,pcg,batched,neohooke,newton",
                     help="comma list of the extra measurements to run (small, pcg, batched, neohooke, newton)")
     return ap.parse_args()

@@ -460,7 +460,18 @@ __device__ __forceinline__ void hex8_elastic_body(const VecArgs& A) {
 constexpr int kTmaStages = 3;
 constexpr int kTmaWarps = 4;  // 128 threads per block
 
-template <int CL, int MODE, bool BF, int ACC>
+//
+// PF (prefetch): when the next tile's rows have already landed (a
+// non-blocking mbarrier test), each lane prefetches its next element's node
+// coordinates and dofs into L1 (PF 1) or L2 (PF 2) before computing the
+// current element, so the next tile's gathers hit the cache.
+template <int PF>
+__device__ __forceinline__ void prefetch_node(const void* p) {
+  if constexpr (PF == 1) asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+  else asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+}
+
+template <int CL, int MODE, bool BF, int ACC, int PF = 0>
 __device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
@@ -502,6 +513,22 @@ __device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
       break;
     }
     const int e = t * 32 + lane;
+    if constexpr (PF > 0) {
+      const int sn = st + 1 == kTmaStages ? 0 : st + 1;
+      const unsigned pn = sn == 0 ? parity ^ 1u : parity;
+      const int en = (t + W) * 32 + lane;
+      // the next tile's rows, only once they have landed (never waits)
+      if (t + W < ntiles && en < E && mbar_test_wait(&bar[warp][sn], pn)) {
+        const int4 p = rows[warp][sn][2 * lane], q = rows[warp][sn][2 * lane + 1];
+        const int nn[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
+        const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+#pragma unroll
+        for (int a = 0; a < 8; ++a) {
+          prefetch_node<PF>(A.xyz4 + nn[a]);
+          prefetch_node<PF>(dofs + 3 * (int64_t)nn[a]);
+        }
+      }
+    }
     if (e < E) {
       const int4 p = rows[warp][st][2 * lane], q = rows[warp][st][2 * lane + 1];
       const int nodes[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
@@ -533,9 +560,9 @@ __device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
   else report_bad_warp(bad, A.status);
 }
 
-template <int CL, int MODE, bool BF, int ACC, int MINB>
+template <int CL, int MODE, bool BF, int ACC, int MINB, int PF>
 __global__ void __launch_bounds__(kTmaWarps * 32, MINB) k_hex8_elastic_tma(const VecArgs A) {
-  hex8_elastic_tma_body<CL, MODE, BF, ACC>(A);
+  hex8_elastic_tma_body<CL, MODE, BF, ACC, PF>(A);
 }
 
 template <int CL, int MODE, bool BF, int ACC, int BLOCK>
@@ -578,13 +605,13 @@ static unsigned persistent_blocks(K kernel, int64_t E) {
   return (unsigned)(want < cap ? want : cap);
 }
 
-template <int CL, int MODE, int ACC, int MINB>
+template <int CL, int MODE, int ACC, int MINB, int PF = 0>
 static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
   if (bf) {
-    auto k = k_hex8_elastic_tma<CL, MODE, true, ACC, MINB>;
+    auto k = k_hex8_elastic_tma<CL, MODE, true, ACC, MINB, PF>;
     k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
   } else {
-    auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB>;
+    auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB, PF>;
     k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
   }
 }
@@ -607,12 +634,14 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
     case 12: launch_variant_regs<CL, MODE, 2, 96>(A, grid, bf, s); break;
     case 13: launch_variant_tma<CL, MODE, 2, 4>(A, grid, bf, s); break;
     case 14: launch_variant_tma<CL, MODE, 2, 5>(A, grid, bf, s); break;
-    default: launch_variant_tma<CL, MODE, 0, 5>(A, grid, bf, s); break;
+    case 15: launch_variant_tma<CL, MODE, 0, 5>(A, grid, bf, s); break;
+    case 16: launch_variant_tma<CL, MODE, 2, 4, 1>(A, grid, bf, s); break;
+    default: launch_variant_tma<CL, MODE, 2, 4, 2>(A, grid, bf, s); break;
   }
 }
 
 // Number of sum-factorised variants the autotuner may choose from.
-constexpr int kHex8Variants = 16;
+constexpr int kHex8Variants = 18;
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's

@@ -29,7 +29,7 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 16
+HEX8_VARIANTS = 18
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
                       "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
                       "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
@@ -38,7 +38,9 @@ HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, du
                       "128 thr, 96 regs, paired points (f32x2)",
                       "persistent, TMA-staged rows, paired points (f32x2)",
                       "persistent, TMA-staged rows, 96 regs, paired points (f32x2)",
-                      "persistent, TMA-staged rows, 96 regs, point sums"]
+                      "persistent, TMA-staged rows, 96 regs, point sums",
+                      "persistent, TMA-staged rows, next tile's nodes prefetched to L1, paired points (f32x2)",
+                      "persistent, TMA-staged rows, next tile's nodes prefetched to L2, paired points (f32x2)"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 

@@ -75,7 +75,7 @@ typedef struct folgb_physics {
   int32_t kernel_variant; /* 0: fastest kernel for the element (sum-factorised
                              hex8 2x2x2 elasticity, variant set by
                              folgb_autotune); 1: the generic Gauss loop;
-                             2 + v: sum-factorised variant v (0..15) */
+                             2 + v: sum-factorised variant v (0..17) */
   double young_modulus;   /* material_dict young_modulus (elastic D scale)     */
   double poisson_ratio;   /* material_dict poisson_ratio                       */
   double body_force[3];   /* loss_settings "body_foce" (mechanical.py:27)      */
