@@ -94,3 +94,30 @@ extern "C" int folgb_trace_read(int32_t kernel_id, int64_t* n_launches, double* 
   if (ms) *ms = total_ms[kernel_id];
   return FOLGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Self-test of the bounded mbarrier wait that the TMA-staged kernels use:
+// one thread initialises a barrier in shared memory, announces 16 bytes of
+// transactions that no copy will ever deliver, and waits with
+// mbar_wait_bounded.  The wait gives up after its poll limit, the kernel
+// records FOLGB_ERR_TIMEOUT in the status word and returns; nothing else is
+// pending on the barrier, so the block exits cleanly and the context stays
+// usable.
+// ---------------------------------------------------------------------------
+namespace folgb {
+__global__ void k_selftest_bounded_wait(int* status) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x != 0) return;
+  mbar_init(&bar, 1);
+  fence_mbar_init();
+  mbar_arrive_expect_tx(&bar, 16u);
+  if (!mbar_wait_bounded(&bar, 0u)) atomicOr(status, 1 << FOLGB_ERR_TIMEOUT);
+}
+}  // namespace folgb
+
+extern "C" int folgb_selftest_bounded_wait(int32_t* device_status, void* stream) {
+  if (!device_status) return FOLGB_ERR_INVALID_ARGUMENT;
+  folgb::k_selftest_bounded_wait<<<1, 32, 0, (cudaStream_t)stream>>>(device_status);
+  FOLGB_LAUNCH_CHECK();
+  return FOLGB_OK;
+}

@@ -395,6 +395,13 @@ enum {
   FOLGB_KERNEL_PCG_SPMV = 6, FOLGB_KERNEL_PCG_UPDATE = 7, FOLGB_KERNEL_BATCH_LOSS = 8,
   FOLGB_KERNEL_HEX8_FUSED = 9
 };
+/* Self-test of the bounded device-side wait (no counterpart in the
+ * reference): launches one block that waits on a shared-memory mbarrier whose
+ * announced copy never comes; the wait gives up after its poll limit (well
+ * under a second) and ORs 1 << FOLGB_ERR_TIMEOUT into device_status (device
+ * int).  Shows that a lost copy cannot hang a kernel. */
+int folgb_selftest_bounded_wait(int32_t* device_status, void* stream);
+
 int folgb_trace_enable(int32_t on);
 int folgb_trace_reset(void);
 int folgb_trace_read(int32_t kernel_id, int64_t* launches, double* total_ms);

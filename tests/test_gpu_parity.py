@@ -300,6 +300,27 @@ def test_newton_neohooke_matches_oracle(cuda):
     assert cuda.linalg.vector_norm(du) < 1e-3 * cuda.linalg.vector_norm(du0)
 
 
+def test_bounded_wait_gives_up_and_reports(cuda):
+    """A TMA-stage wait whose copy never comes (an mbarrier with announced
+    bytes and no copy) gives up after its poll limit: the status word gets
+    FOLGB_ERR_TIMEOUT and the context stays usable."""
+    import time
+    from folax_gb300 import _capi
+    torch = cuda
+    lib = _capi.load()
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    t0 = time.perf_counter()
+    assert lib.folgb_selftest_bounded_wait(_capi.ptr(status), _capi.stream_handle()) == 0
+    torch.cuda.synchronize()
+    assert time.perf_counter() - t0 < 30.0
+    assert int(status.item()) == 1 << _capi.ERR_TIMEOUT
+    m = make_mesh("hex8", 3, seed=66)
+    gl = gpu_loss("hex8", "elastic", m, _settings("hex8", "elastic"))
+    _, _, losses, _, _ = gl.ComputeBatchLossAndGrad(np.ones((1, gl.GetNumberOfControls())),
+                                                    np.zeros((1, gl.GetTotalNumberOfDOFs())))
+    assert np.isfinite(losses.cpu().numpy()).all()
+
+
 def test_inverted_element_and_nan_are_reported(cuda):
     """Host-made faults: an inverted element raises the detJ status bit, a NaN
     in u the NaN bit; the context stays usable."""
