@@ -166,6 +166,18 @@ def issue_roofline(n, variant, elem_ms, clk, peaks):
             "frac": bound_us / (elem_ms * 1e3), "sm_mhz": mhz}
 
 
+def max_over_ranks(x: float) -> float:
+    """The largest x over all ranks of the default process group (the
+    whole-job time is the slowest rank's); CUDA tensors under NCCL, host
+    tensors under gloo."""
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def measured_peaks():
     try:
         return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -630,9 +642,7 @@ def main():
     torch.cuda.synchronize()
     barrier()
     if world > 1:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        ms = max_over_ranks(ms)
     value = world * B * nE / (ms * 1e-3) / 1e6
 
     # dominant kernel: tracing events around the element kernel

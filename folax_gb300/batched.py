@@ -149,6 +149,25 @@ class AdamState:
         capi.check("folgb_adam_step", rc)
 
 
+def shard_instances(element_counts, world_size: int):
+    """Instances of a batch spread over world_size ranks (one GPU each) by
+    element count: largest instance first onto the least-loaded rank (ties to
+    the lower rank), so every rank gets about the same number of elements.
+    Instances are independent, so the ranks exchange nothing on the data
+    path; only the scalar loss mean needs one reduction.  Returns one
+    ascending index array per rank; deterministic."""
+    counts = np.asarray(element_counts, dtype=np.int64)
+    if world_size < 1:
+        raise ValueError("world_size must be >= 1")
+    load = np.zeros(world_size, dtype=np.int64)
+    parts = [[] for _ in range(world_size)]
+    for i in sorted(range(len(counts)), key=lambda k: (-counts[k], k)):
+        r = int(np.argmin(load))  # first minimum: the lowest rank among ties
+        parts[r].append(i)
+        load[r] += counts[i]
+    return [np.asarray(sorted(p), dtype=np.int64) for p in parts]
+
+
 def capture_step(fn, warmup: int = 3):
     """Record fn() (device work only, fixed buffers) as a CUDA graph; returns
     (graph, result of the captured call).  Replaying the graph repeats the work."""
