@@ -80,6 +80,7 @@ struct VecArgs {
   float* scale;       // [B]
   float exponent, inv_batch;
   int* status;
+  int stream_rec = 0;  // 1: records larger than L2; store them evict-first (__stcs)
 };
 
 __device__ __forceinline__ void load_gp_table(GPTable& dst, const GPTable* src) {
@@ -451,13 +452,29 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
     if (!isfinite(energy)) bad |= 2;
     // one record per (element, node), local-node-major ([b][a][e]): ndof
     // vector components, then the nodal control sensitivity when present
+    // One vector store per record (the record widths are 1, 2 or 4 floats,
+    // padding zeroed); evict-first when the records do not fit in L2, so they
+    // do not push the node data out of it.
     const bool nodal_gde = (MODE == MODE_LOSS) && A.ctrl_layout == FOLGB_CONTROL_NODAL;
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
-      float* rec = A.g + (((int64_t)b * NEN + a) * A.E + e) * A.rec;
+      float v[4] = {0.f, 0.f, 0.f, 0.f};
 #pragma unroll
-      for (int c = 0; c < NDOF; ++c) rec[c] = g[a * NDOF + c];
-      if (nodal_gde) rec[NDOF] = gd[a];
+      for (int c = 0; c < NDOF; ++c) v[c] = g[a * NDOF + c];
+      if (nodal_gde) v[NDOF < 4 ? NDOF : 3] = gd[a];
+      float* rec = A.g + (((int64_t)b * NEN + a) * A.E + e) * A.rec;
+      if (A.rec == 4) {
+        const float4 t = make_float4(v[0], v[1], v[2], v[3]);
+        if (A.stream_rec) __stcs(reinterpret_cast<float4*>(rec), t);
+        else *reinterpret_cast<float4*>(rec) = t;
+      } else if (A.rec == 2) {
+        const float2 t = make_float2(v[0], v[1]);
+        if (A.stream_rec) __stcs(reinterpret_cast<float2*>(rec), t);
+        else *reinterpret_cast<float2*>(rec) = t;
+      } else {
+        if (A.stream_rec) __stcs(rec, v[0]);
+        else rec[0] = v[0];
+      }
     }
     if (MODE == MODE_LOSS) {
       if (!nodal_gde && A.dctrl_elem) {
@@ -488,12 +505,14 @@ __device__ __forceinline__ void report_bad_warp(int bad, int* status) {
 // in block order.  The order of every sum is fixed, whichever warp or block
 // finishes last.  wcount must be zeroed before any warp can post.
 __device__ __forceinline__ void finish_loss_warp(float energy, int bad, const VecArgs& A, int b, float* wsum,
-                                                 unsigned* wcount) {
+                                                 unsigned* wcount, int blk = -1, int nblk_arg = -1) {
   report_bad_warp(bad, A.status);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) energy += __shfl_xor_sync(0xffffffffu, energy, o);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const int nblk = gridDim.x;
+  // the block's index among the instance's blocks (default: blockIdx.x of gridDim.x)
+  const int nblk = nblk_arg >= 0 ? nblk_arg : (int)gridDim.x;
+  const int bi = blk >= 0 ? blk : (int)blockIdx.x;
   int last = 0;
   if (lane == 0) {
     wsum[warp] = energy;
@@ -507,7 +526,7 @@ __device__ __forceinline__ void finish_loss_warp(float energy, int bad, const Ve
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
   last = 0;
   if (lane == 0) {
-    A.partials[(int64_t)b * nblk + blockIdx.x] = v;
+    A.partials[(int64_t)b * nblk + bi] = v;
     __threadfence();
     last = atomicAdd(A.counters + b, 1u) == (unsigned)nblk - 1;
   }

@@ -20,23 +20,28 @@ namespace folgb {
 
 // One thread per element: gather, Gauss-point loop, element energy, element
 // energy gradient (LOSS) or element residual (RESIDUAL).
-template <int ET, int PH, int MODE>
+// IFAST (batches): the grid is (instances, element blocks), so the blocks of
+// all instances for one element range are dispatched together and share the
+// connectivity and coordinate loads in L2 instead of each instance sweeping
+// the whole mesh.
+template <int ET, int PH, int MODE, bool IFAST = false>
 __global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
   __shared__ GPTable gp;
-  __shared__ float red[32];
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
   pdl_launch_dependents();
   load_gp_table(gp, A.gp);
+  if (threadIdx.x == 0) wcount = 0u;
   __syncthreads();
-  const int b = blockIdx.y;
-  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = IFAST ? blockIdx.x : blockIdx.y;
+  const int blk = IFAST ? blockIdx.y : blockIdx.x, nblk = IFAST ? gridDim.y : gridDim.x;
+  const int64_t e = (int64_t)blk * blockDim.x + threadIdx.x;
   float energy = 0.f;
   int bad = 0;
   if (e < A.E) elem_vector_body<ET, PH, MODE>(A, gp, b, e, energy, bad);
-  report_bad(bad, A.status);
-  if (MODE == MODE_LOSS) {
-    float be = block_sum(energy, red);
-    finish_loss(be, A, b, red);
-  }
+  // warp-level epilogues: no block barrier after the element work
+  if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount, blk, nblk);
+  else report_bad_warp(bad, A.status);
 }
 
 
@@ -107,13 +112,16 @@ __device__ __forceinline__ void sum_slots(const float* __restrict__ g, const int
 }
 
 // PAD = 4 or 8: padded slot table; PAD = 0: CSR slot list in chunks of 8.
-template <int NDOF, int REC, bool GDE, int PAD>
+// IFAST (batches): grid (instances, node blocks), the instances of one node
+// range dispatched together so they share the incidence loads in L2.
+template <int NDOF, int REC, bool GDE, int PAD, bool IFAST = false>
 __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
-  const int b = blockIdx.y;
+  const int b = IFAST ? blockIdx.x : blockIdx.y;
+  const int blk = IFAST ? blockIdx.y : blockIdx.x, nblk = IFAST ? gridDim.y : gridDim.x;
   const float* g = A.g + (int64_t)b * A.E * A.nen * REC;
-  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t stride = (int64_t)nblk * blockDim.x;
   float scb = 1.f;
-  for (int64_t n = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; n < A.N; n += stride) {
+  for (int64_t n = (int64_t)blk * blockDim.x + threadIdx.x; n < A.N; n += stride) {
     float acc[NDOF];
 #pragma unroll
     for (int c = 0; c < NDOF; ++c) acc[c] = 0.f;
@@ -155,7 +163,7 @@ __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
   if (A.rescale_elem && A.dctrl_elem) {
     pdl_wait_primary();
     if (A.scale) scb = A.scale[b];
-    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < A.E; e += stride)
+    for (int64_t e = (int64_t)blk * blockDim.x + threadIdx.x; e < A.E; e += stride)
       A.dctrl_elem[(int64_t)b * A.E + e] *= A.elem_inst ? A.scale[__ldg(A.elem_inst + e)] : scb;
   }
 }
@@ -827,12 +835,14 @@ int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_
   int blocks = (int)((work + 255) / 256);
   int cap = num_sms() * 8;
   if (blocks > cap) blocks = cap;
-  dim3 grid((unsigned)blocks, (unsigned)B);
+  const bool ifast = B > 1;  // blocks <= num_sms * 8 < 65536
+  dim3 grid = ifast ? dim3((unsigned)B, (unsigned)blocks) : dim3((unsigned)blocks, (unsigned)B);
   auto go = [&](auto nd, auto rc_, auto gde) -> int {
     constexpr int NDOF = decltype(nd)::value, REC = decltype(rc_)::value;
     constexpr bool GDE = decltype(gde)::value;
-    auto kernel = p->inc_pad == 4 ? k_node_gather<NDOF, REC, GDE, 4>
-                  : (p->inc_pad == 8 ? k_node_gather<NDOF, REC, GDE, 8> : k_node_gather<NDOF, REC, GDE, 0>);
+    auto kernel = p->inc_pad == 4 ? (ifast ? k_node_gather<NDOF, REC, GDE, 4, true> : k_node_gather<NDOF, REC, GDE, 4>)
+                  : (p->inc_pad == 8 ? (ifast ? k_node_gather<NDOF, REC, GDE, 8, true> : k_node_gather<NDOF, REC, GDE, 8>)
+                                     : (ifast ? k_node_gather<NDOF, REC, GDE, 0, true> : k_node_gather<NDOF, REC, GDE, 0>));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
     cfg.blockDim = dim3(256);
@@ -899,6 +909,9 @@ static VecArgs make_vec_args(const folgb_plan* p, int B, const float* control, i
   A.exponent = (float)p->phys.loss_exponent;
   A.inv_batch = 1.f / (float)B;
   A.status = status;
+  // records far larger than L2 are written evict-first (they are read back
+  // from HBM by the gather in any case)
+  A.stream_rec = (size_t)B * p->E * p->nen * w.rec * sizeof(float) > ((size_t)96 << 20) ? 1 : 0;
   return A;
 }
 
@@ -945,7 +958,10 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
       constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
       trace_begin(KID_ELEM_LOSS, s);
-      k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
+      if (grid.y > 1 && grid.x <= 65535u)
+        k_elem_vector<ET, PH, MODE_LOSS, true><<<dim3(grid.y, grid.x), 256, 0, s>>>(A);
+      else
+        k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
       trace_end(KID_ELEM_LOSS, s);
       FOLGB_LAUNCH_CHECK();
       return FOLGB_OK;
