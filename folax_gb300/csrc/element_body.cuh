@@ -180,7 +180,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int k = 0; k < DIM; ++k) {
           float s = 0.f;
 #pragma unroll
-          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], gp.dN[q][a][k], s);
+          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], dN_at<ET>(gp, q, a, k), s);
           J[i][k] = s;
         }
       float Ji[DIM][DIM];
@@ -197,7 +197,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int j = 0; j < DIM; ++j) {
           float s = 0.f;
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], kTransposedInverse ? Ji[j][k] : Ji[k][j], s);
+          for (int k = 0; k < DIM; ++k) s = fmaf(dN_at<ET>(gp, q, a, k), kTransposedInverse ? Ji[j][k] : Ji[k][j], s);
           dNdx[a][j] = s;
         }
       float egp;

@@ -254,7 +254,7 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
       for (int k = 0; k < DIM; ++k) {
         float s = 0.f;
 #pragma unroll
-        for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], gp.dN[q][a][k], s);
+        for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], dN_at<ET>(gp, q, a, k), s);
         J[i][k] = s;
       }
     float Ji[DIM][DIM];
@@ -270,7 +270,7 @@ __global__ void __launch_bounds__(256) k_elem_matrix(const MatArgs A) {
 #pragma unroll
         // the transient thermal element uses J^-1 dN/dxi^T (transient_thermal.py:57-59)
         for (int k = 0; k < DIM; ++k)
-          s = fmaf(gp.dN[q][a][k], PH == FOLGB_TRANSIENT_THERMAL ? Ji[j][k] : Ji[k][j], s);
+          s = fmaf(dN_at<ET>(gp, q, a, k), PH == FOLGB_TRANSIENT_THERMAL ? Ji[j][k] : Ji[k][j], s);
         dNdx[a][j] = s;
         rec[a * DIM + j] = s;
       }

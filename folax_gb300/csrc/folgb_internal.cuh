@@ -205,6 +205,16 @@ template <> struct ElemT<FOLGB_QUAD4> { static constexpr int NEN = 4, DIM = 2; }
 template <> struct ElemT<FOLGB_HEX8>  { static constexpr int NEN = 8, DIM = 3; };
 template <> struct ElemT<FOLGB_TET4>  { static constexpr int NEN = 4, DIM = 3; };
 
+// Reference derivatives dN_a/dxi_k at Gauss point q.  The linear tetrahedron
+// (N = 1 - xi - eta - zeta, xi, eta, zeta; tetrahedra_3d_4.py:48-60) has the
+// same gradients at every point: compile-time constants, so its Jacobian and
+// dN/dx fold to differences and copies (the same values as the table's).
+template <int ET>
+__device__ __forceinline__ float dN_at(const GPTable& gp, int q, int a, int k) {
+  if constexpr (ET == FOLGB_TET4) return a == 0 ? -1.f : (a - 1 == k ? 1.f : 0.f);
+  else return gp.dN[q][a][k];
+}
+
 template <int PH, int DIM> struct NdofT {
   static constexpr int V = (PH == FOLGB_THERMAL || PH == FOLGB_TRANSIENT_THERMAL) ? 1 : DIM;
 };

@@ -131,7 +131,7 @@ __global__ void __launch_bounds__(128) k_response(const RespArgs A, const GPTabl
         for (int k = 0; k < DIM; ++k) {
           float s = 0.f;
 #pragma unroll
-          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], gp.dN[q][a][k], s);
+          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], dN_at<ET>(gp, q, a, k), s);
           J[i][k] = s;
         }
       float Ji[DIM][DIM];
@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(128) k_response(const RespArgs A, const GPTabl
         for (int j = 0; j < DIM; ++j) {
           float s = 0.f;
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) s = fmaf(gp.dN[q][a][k], Ji[k][j], s);
+          for (int k = 0; k < DIM; ++k) s = fmaf(dN_at<ET>(gp, q, a, k), Ji[k][j], s);
           G[a][j] = s;
         }
       float dq = d_elem;
