@@ -40,7 +40,7 @@ struct BatchArgs {
   int I;
 };
 
-template <int ET, int PH>
+template <int ET, int PH, int NP = 0>
 __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const BatchArgs T) {
   __shared__ GPTable gp;
   __shared__ float red[32];
@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const Batch
     const int cnt = T.tile_count[t];
     float energy = 0.f;
     for (int k = threadIdx.x; k < cnt; k += blockDim.x)
-      elem_vector_body<ET, PH, MODE_LOSS>(A, gp, 0, e0 + k, energy, bad);
+      elem_vector_body<ET, PH, MODE_LOSS, NP>(A, gp, 0, e0 + k, energy, bad);
     float be = block_sum(energy, red);
     if (threadIdx.x == 0) A.partials[t] = be;
   }
@@ -226,7 +226,9 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
   int rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
     constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
     trace_begin(KID_BATCH_LOSS, s);
-    k_batch_loss<ET, PH><<<(unsigned)grid, 256, 0, s>>>(A, T);
+    with_const_gp<ET>(p, [&](auto np) {
+      k_batch_loss<ET, PH, decltype(np)::value><<<(unsigned)grid, 256, 0, s>>>(A, T);
+    });
     trace_end(KID_BATCH_LOSS, s);
     FOLGB_LAUNCH_CHECK();
     return (int)FOLGB_OK;

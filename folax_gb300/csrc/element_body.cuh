@@ -15,6 +15,7 @@
 #pragma once
 
 #include <cmath>
+#include <type_traits>
 
 #include "folgb_internal.cuh"
 
@@ -51,6 +52,19 @@ int dispatch(int et, int ph, F&& f) {
 }
 
 enum { MODE_LOSS = 0, MODE_RESIDUAL = 1 };
+
+// Calls f(std::integral_constant<int, NP>) with the plan's compile-time Gauss
+// rule (const_gp_points), instantiating only the rules element type ET has.
+template <int ET, class F>
+void with_const_gp(const folgb_plan* p, F&& f) {
+  const int np = const_gp_points(p->etype, p->phys.num_gp);
+  if constexpr (ET == FOLGB_QUAD4) {
+    if (np == 4) return f(std::integral_constant<int, 4>{});
+  } else if constexpr (ET == FOLGB_TET4) {
+    if (np == 1) return f(std::integral_constant<int, 1>{});
+  }
+  f(std::integral_constant<int, 0>{});
+}
 
 struct VecArgs {
   int64_t E, N;
@@ -133,8 +147,9 @@ __device__ __forceinline__ void finish_loss(float block_energy, const VecArgs& A
   }
 }
 
-// Per-element body shared by the single-mesh and the batched kernels.
-template <int ET, int PH, int MODE>
+// Per-element body shared by the single-mesh and the batched kernels.  NP > 0:
+// the Gauss rule is the compile-time one of GPc (unrolled point loop).
+template <int ET, int PH, int MODE, int NP = 0>
 __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable& gp, const int b, const int64_t e,
                                                  float& energy, int& bad) {
   constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM, NDOF = NdofT<PH, DIM>::V;
@@ -171,8 +186,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
 #pragma unroll
     for (int a = 0; a < NEN; ++a) gd[a] = 0.f;
     const MatConst& mt = A.mat;
-#pragma unroll 1
-    for (int q = 0; q < gp.npts; ++q) {
+    auto point = [&](const int q) {
       float J[DIM][DIM];
 #pragma unroll
       for (int i = 0; i < DIM; ++i)
@@ -180,13 +194,13 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int k = 0; k < DIM; ++k) {
           float s = 0.f;
 #pragma unroll
-          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], dN_at<ET>(gp, q, a, k), s);
+          for (int a = 0; a < NEN; ++a) s = fmaf(X[a][i], dN_at<ET, NP>(gp, q, a, k), s);
           J[i][k] = s;
         }
       float Ji[DIM][DIM];
       float det = det_inv<DIM>(J, Ji);
       bad |= !(det > 0.f);
-      const float wd = gp.w[q] * det;
+      const float wd = gp_w<ET, NP>(gp, q) * det;
       // dN/dx = dN/dxi J^-1; the transient thermal element uses J^-1 dN/dxi^T
       // instead (transient_thermal.py:57-59), the same for symmetric J
       constexpr bool kTransposedInverse = PH == FOLGB_TRANSIENT_THERMAL;
@@ -197,14 +211,14 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int j = 0; j < DIM; ++j) {
           float s = 0.f;
 #pragma unroll
-          for (int k = 0; k < DIM; ++k) s = fmaf(dN_at<ET>(gp, q, a, k), kTransposedInverse ? Ji[j][k] : Ji[k][j], s);
+          for (int k = 0; k < DIM; ++k) s = fmaf(dN_at<ET, NP>(gp, q, a, k), kTransposedInverse ? Ji[j][k] : Ji[k][j], s);
           dNdx[a][j] = s;
         }
       float egp;
       if (A.ctrl_layout == FOLGB_CONTROL_NODAL) {
         egp = 0.f;
 #pragma unroll
-        for (int a = 0; a < NEN; ++a) egp = fmaf(gp.N[q][a], de[a], egp);
+        for (int a = 0; a < NEN; ++a) egp = fmaf(gp_N<ET, NP>(gp, q, a), de[a], egp);
       } else {
         egp = eval;
       }
@@ -214,7 +228,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int j = 0; j < DIM; ++j) gT[j] = 0.f;
 #pragma unroll
         for (int a = 0; a < NEN; ++a) {
-          Tg = fmaf(gp.N[q][a], ue[a], Tg);
+          Tg = fmaf(gp_N<ET, NP>(gp, q, a), ue[a], Tg);
 #pragma unroll
           for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
         }
@@ -231,7 +245,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
 #pragma unroll
           for (int j = 0; j < DIM; ++j) s = fmaf(dNdx[a][j], gT[j], s);
           g[a] = fmaf(kw, s, g[a]);
-          gd[a] = fmaf(wd * gf * gg, gp.N[q][a], gd[a]);
+          gd[a] = fmaf(wd * gf * gg, gp_N<ET, NP>(gp, q, a), gd[a]);
         }
       } else if constexpr (PH == FOLGB_ELASTIC) {
         float H[DIM][DIM];
@@ -272,14 +286,14 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
             for (int j = 0; j < DIM; ++j) s = fmaf(sig[i][j], dNdx[a][j], s);
             g[a * DIM + i] = fmaf(wd, s, g[a * DIM + i]);
           }
-          gd[a] = fmaf(wd * sed, gp.N[q][a], gd[a]);
+          gd[a] = fmaf(wd * sed, gp_N<ET, NP>(gp, q, a), gd[a]);
         }
         if (mt.has_bf) {
 #pragma unroll
           for (int a = 0; a < NEN; ++a)
 #pragma unroll
             for (int i = 0; i < DIM; ++i) {
-              float f = wd * gp.N[q][a] * mt.bf[i];
+              float f = wd * gp_N<ET, NP>(gp, q, a) * mt.bf[i];
               g[a * DIM + i] -= f;
               energy = fmaf(-f, ue[a * DIM + i], energy);
             }
@@ -291,8 +305,8 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
         for (int j = 0; j < DIM; ++j) gT[j] = 0.f;
 #pragma unroll
         for (int a = 0; a < NEN; ++a) {
-          Tn = fmaf(gp.N[q][a], ue[a], Tn);
-          kq = fmaf(gp.N[q][a], ke[a], kq);
+          Tn = fmaf(gp_N<ET, NP>(gp, q, a), ue[a], Tn);
+          kq = fmaf(gp_N<ET, NP>(gp, q, a), ke[a], kq);
 #pragma unroll
           for (int j = 0; j < DIM; ++j) gT[j] = fmaf(ue[a], dNdx[a][j], gT[j]);
         }
@@ -309,10 +323,10 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
 #pragma unroll
           for (int j = 0; j < DIM; ++j) gn = fmaf(dNdx[a][j], gT[j], gn);
           if (MODE == MODE_LOSS) {
-            g[a] = fmaf(wd, Kc * gn + (0.5f * dKdT * gg + rc / mt.dt * diff) * gp.N[q][a], g[a]);
-            gd[a] = fmaf(-wd * rc / mt.dt * diff, gp.N[q][a], gd[a]);
+            g[a] = fmaf(wd, Kc * gn + (0.5f * dKdT * gg + rc / mt.dt * diff) * gp_N<ET, NP>(gp, q, a), g[a]);
+            gd[a] = fmaf(-wd * rc / mt.dt * diff, gp_N<ET, NP>(gp, q, a), gd[a]);
           } else {
-            g[a] = fmaf(wd, rc * diff * gp.N[q][a] + mt.dt * Kc * gn, g[a]);
+            g[a] = fmaf(wd, rc * diff * gp_N<ET, NP>(gp, q, a) + mt.dt * Kc * gn, g[a]);
           }
         }
       } else if constexpr (PH == FOLGB_NEOHOOKE_SPLIT) {
@@ -349,13 +363,13 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
             for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
             g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
           }
-          gd[a] = fmaf(wd * dpsi_de, gp.N[q][a], gd[a]);
+          gd[a] = fmaf(wd * dpsi_de, gp_N<ET, NP>(gp, q, a), gd[a]);
         }
         if (MODE == MODE_RESIDUAL && mt.has_bf) {
 #pragma unroll
           for (int a = 0; a < NEN; ++a)
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp_N<ET, NP>(gp, q, a) * mt.bf[i];
         }
       } else if constexpr (PH == FOLGB_SAINT_VENANT) {
         float H[DIM][DIM];
@@ -390,13 +404,13 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
             for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
             g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
           }
-          gd[a] = fmaf(wd * st.dpsi_de, gp.N[q][a], gd[a]);
+          gd[a] = fmaf(wd * st.dpsi_de, gp_N<ET, NP>(gp, q, a), gd[a]);
         }
         if (MODE == MODE_RESIDUAL && mt.has_bf) {
 #pragma unroll
           for (int a = 0; a < NEN; ++a)
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp_N<ET, NP>(gp, q, a) * mt.bf[i];
         }
       } else {  // neo-Hooke
         float H[DIM][DIM];
@@ -439,15 +453,22 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
             for (int j = 0; j < DIM; ++j) s = fmaf(P[k][j], dNdx[a][j], s);
             g[a * DIM + k] = fmaf(wd, s, g[a * DIM + k]);
           }
-          gd[a] = fmaf(wd * dpsi_de, gp.N[q][a], gd[a]);
+          gd[a] = fmaf(wd * dpsi_de, gp_N<ET, NP>(gp, q, a), gd[a]);
         }
         if (MODE == MODE_RESIDUAL && mt.has_bf) {
 #pragma unroll
           for (int a = 0; a < NEN; ++a)
 #pragma unroll
-            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp.N[q][a] * mt.bf[i];
+            for (int i = 0; i < DIM; ++i) g[a * DIM + i] -= wd * gp_N<ET, NP>(gp, q, a) * mt.bf[i];
         }
       }
+    };
+    if constexpr (NP > 0) {
+#pragma unroll
+      for (int q = 0; q < NP; ++q) point(q);
+    } else {
+#pragma unroll 1
+      for (int q = 0; q < gp.npts; ++q) point(q);
     }
     if (!isfinite(energy)) bad |= 2;
     // one record per (element, node), local-node-major ([b][a][e]): ndof

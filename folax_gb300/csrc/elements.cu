@@ -24,7 +24,7 @@ namespace folgb {
 // all instances for one element range are dispatched together and share the
 // connectivity and coordinate loads in L2 instead of each instance sweeping
 // the whole mesh.
-template <int ET, int PH, int MODE, bool IFAST = false>
+template <int ET, int PH, int MODE, bool IFAST = false, int NP = 0>
 __global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
   __shared__ GPTable gp;
   __shared__ float wsum[32];
@@ -38,7 +38,7 @@ __global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
   const int64_t e = (int64_t)blk * blockDim.x + threadIdx.x;
   float energy = 0.f;
   int bad = 0;
-  if (e < A.E) elem_vector_body<ET, PH, MODE>(A, gp, b, e, energy, bad);
+  if (e < A.E) elem_vector_body<ET, PH, MODE, NP>(A, gp, b, e, energy, bad);
   // warp-level epilogues: no block barrier after the element work
   if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount, blk, nblk);
   else report_bad_warp(bad, A.status);
@@ -958,10 +958,13 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
       constexpr int ET = decltype(tag)::ET, PH = decltype(tag)::PH;
       trace_begin(KID_ELEM_LOSS, s);
-      if (grid.y > 1 && grid.x <= 65535u)
-        k_elem_vector<ET, PH, MODE_LOSS, true><<<dim3(grid.y, grid.x), 256, 0, s>>>(A);
-      else
-        k_elem_vector<ET, PH, MODE_LOSS><<<grid, 256, 0, s>>>(A);
+      with_const_gp<ET>(p, [&](auto np) {
+        constexpr int NP = decltype(np)::value;
+        if (grid.y > 1 && grid.x <= 65535u)
+          k_elem_vector<ET, PH, MODE_LOSS, true, NP><<<dim3(grid.y, grid.x), 256, 0, s>>>(A);
+        else
+          k_elem_vector<ET, PH, MODE_LOSS, false, NP><<<grid, 256, 0, s>>>(A);
+      });
       trace_end(KID_ELEM_LOSS, s);
       FOLGB_LAUNCH_CHECK();
       return FOLGB_OK;
@@ -1086,7 +1089,9 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
     if (residual) {
       if (!(p->phys.kernel_variant != 1 && launch_hex8_fast(p, A, grid, MODE_RESIDUAL, s))) {
         trace_begin(KID_ELEM_RESIDUAL, s);
-        k_elem_vector<ET, PH, MODE_RESIDUAL><<<grid, 256, 0, s>>>(A);
+        with_const_gp<ET>(p, [&](auto np) {
+          k_elem_vector<ET, PH, MODE_RESIDUAL, false, decltype(np)::value><<<grid, 256, 0, s>>>(A);
+        });
         trace_end(KID_ELEM_RESIDUAL, s);
       }
       FOLGB_LAUNCH_CHECK();

@@ -209,10 +209,54 @@ template <> struct ElemT<FOLGB_TET4>  { static constexpr int NEN = 4, DIM = 3; }
 // (N = 1 - xi - eta - zeta, xi, eta, zeta; tetrahedra_3d_4.py:48-60) has the
 // same gradients at every point: compile-time constants, so its Jacobian and
 // dN/dx fold to differences and copies (the same values as the table's).
-template <int ET>
+// Compile-time Gauss rules for the small common cases (NP points; NP = 0:
+// the plan's table at run time): quad4 with the 2x2 rule (NP 4) and tet4
+// with the 1-point rule (NP 1), in the reference's point order
+// (quadrilateral_2d_4.py:22-31, tetrahedra_3d_4.py:16-20) and with the table's
+// values (computed in double, rounded to float), so loops over them unroll
+// into constants.
+template <int ET, int NP> struct GPc;
+template <> struct GPc<FOLGB_QUAD4, 4> {
+  static constexpr double g = 0.57735026918962576451;  // 1/sqrt(3)
+  __device__ static constexpr double sx(int a) { return (a == 1 || a == 2) ? 1.0 : -1.0; }
+  __device__ static constexpr double sy(int a) { return a >= 2 ? 1.0 : -1.0; }
+  __device__ static constexpr float w(int) { return 1.f; }
+  __device__ static constexpr float N(int q, int a) {
+    return (float)(0.25 * (1.0 + sx(a) * (sx(q) * g)) * (1.0 + sy(a) * (sy(q) * g)));
+  }
+  __device__ static constexpr float dN(int q, int a, int k) {
+    return k == 0 ? (float)(0.25 * sx(a) * (1.0 + sy(a) * (sy(q) * g)))
+                  : (k == 1 ? (float)(0.25 * sy(a) * (1.0 + sx(a) * (sx(q) * g))) : 0.f);
+  }
+};
+template <> struct GPc<FOLGB_TET4, 1> {
+  __device__ static constexpr float w(int) { return (float)(1.0 / 6.0); }
+  __device__ static constexpr float N(int, int) { return 0.25f; }
+  __device__ static constexpr float dN(int, int a, int k) { return a == 0 ? -1.f : (a - 1 == k ? 1.f : 0.f); }
+};
+
+template <int ET, int NP = 0>
 __device__ __forceinline__ float dN_at(const GPTable& gp, int q, int a, int k) {
-  if constexpr (ET == FOLGB_TET4) return a == 0 ? -1.f : (a - 1 == k ? 1.f : 0.f);
+  if constexpr (NP > 0) return GPc<ET, NP>::dN(q, a, k);
+  else if constexpr (ET == FOLGB_TET4) return a == 0 ? -1.f : (a - 1 == k ? 1.f : 0.f);
   else return gp.dN[q][a][k];
+}
+template <int ET, int NP = 0>
+__device__ __forceinline__ float gp_w(const GPTable& gp, int q) {
+  if constexpr (NP > 0) return GPc<ET, NP>::w(q);
+  else return gp.w[q];
+}
+template <int ET, int NP = 0>
+__device__ __forceinline__ float gp_N(const GPTable& gp, int q, int a) {
+  if constexpr (NP > 0) return GPc<ET, NP>::N(q, a);
+  else return gp.N[q][a];
+}
+
+// The compile-time rule a plan can use (0: none).
+inline int const_gp_points(int etype, int num_gp) {
+  if (etype == FOLGB_QUAD4 && num_gp == 2) return 4;
+  if (etype == FOLGB_TET4 && num_gp == 1) return 1;
+  return 0;
 }
 
 template <int PH, int DIM> struct NdofT {
