@@ -52,6 +52,12 @@ struct KWork {
 };
 
 constexpr int kVecBlocks = 1024;
+// The PCG SpMV with fp32 vectors fits in 64 registers without spilling: 4
+// blocks of 256 threads per SM (32 warps) keep more loads in flight than the
+// 3 blocks an unconstrained build gives.  fp64 vectors, and the BiCGSTAB and
+// true-residual kernels, would spill under that cap.
+template <class VT>
+constexpr int kSpmvMinBlocks = sizeof(VT) == sizeof(float) ? 4 : 1;
 constexpr double kReplaceDrop2 = 1e-6;  // replace when |r|^2 <= 1e-6 |r_true|^2
 constexpr int kMaxBreakdowns = 8;       // consecutive breakdown restarts before giving up
 constexpr double kDiverge2 = 1e12;      // stop when |r_true|^2 > 1e12 |b|^2 (diverged)
@@ -339,7 +345,7 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
 }
 
 template <int NDOF, int G, class VT>
-__global__ void __launch_bounds__(256) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
+__global__ void __launch_bounds__(256, kSpmvMinBlocks<VT>) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                   const int* __restrict__ adj, int maxdeg,
                                                   const float* __restrict__ vals, const VT* __restrict__ z,
                                                   const VT* __restrict__ pold, VT* __restrict__ pnew,
