@@ -395,7 +395,35 @@ __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __re
   const double alpha = sc->alpha;
   const VT af = (VT)alpha;
   VT rz = VT(0), rr = VT(0);  // per-thread partials over a few entries
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+  // four independent entries per trip: their loads are in flight together
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  for (; i + 3 * stride < n; i += 4 * stride) {
+    double xv[4];
+    VT pv[4], qv[4], rv[4];
+    float dv[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t j = i + k * stride;
+      xv[k] = x[j];
+      pv[k] = p[j];
+      qv[k] = q[j];
+      rv[k] = r[j];
+      dv[k] = dinv[j];
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int64_t j = i + k * stride;
+      x[j] = fma(alpha, (double)pv[k], xv[k]);
+      const VT ri = vfma(-af, qv[k], rv[k]);
+      r[j] = ri;
+      const VT zi = (VT)dv[k] * ri;
+      z[j] = zi;
+      rz = vfma(ri, zi, rz);
+      rr = vfma(ri, ri, rr);
+    }
+  }
+  for (; i < n; i += stride) {
     x[i] = fma(alpha, (double)p[i], x[i]);
     const VT ri = vfma(-af, q[i], r[i]);
     r[i] = ri;
@@ -987,6 +1015,10 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
   const int64_t n = (int64_t)p->ndof * p->N;
   int vb = (int)((n + 255) / 256);
   if (vb > kVecBlocks) vb = kVecBlocks;
+  // the PCG update: 2 blocks per SM, 4 entries per thread per trip (few
+  // blocks keep the last-block-done counter, one atomic per block, cheap)
+  int ub = (int)((n + 1023) / 1024);
+  if (ub > 2 * num_sms()) ub = 2 * num_sms();
   FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, 8 * sizeof(unsigned), s));
   if (solver == SOLVER_CG)
     k_pcg_init<VT><<<vb, 256, 0, s>>>(n, rhs, dinv, w.x, w.r, w.z, w.p0, w.part, w.counters, w.sc, rtol, maxiter);
@@ -1010,7 +1042,7 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
                                                      w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, cs);
             trace_begin(KID_PCG_UPDATE, cs);
-            k_pcg_update<VT><<<vb, 256, 0, cs>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
+            k_pcg_update<VT><<<ub, 256, 0, cs>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_UPDATE, cs);
             std::swap(pa, pb);
           } else {
