@@ -562,3 +562,28 @@ def test_cluster_solver_matches_direct_solve(cuda, solver_name, etype, physics, 
     assert torch.equal(x1, x2)
     A, Ro = ol.csr(ctrl, u)
     assert rel_fro(x1.cpu().numpy(), fo.direct_solve(A, -Ro)) < 1e-5
+
+
+@pytest.mark.parametrize("etype,n", [("quad4", 6), ("tet4", 2), ("hex8", 3)])
+@pytest.mark.parametrize("order", [1, 2, 3])
+@pytest.mark.parametrize("physics", ["thermal", "elastic"])
+def test_every_gauss_order_matches_oracle(cuda, etype, n, order, physics):
+    """Gauss orders 1-3 (fe_loss.py:68-83): the compile-time rules (quad4 2x2,
+    tet4 1-point) and the run-time tables give the oracle's loss, gradients,
+    residual and tangent, batched and single."""
+    m = make_mesh(etype, n, seed=40 + order)
+    s = {**_settings(etype, physics, "nodal"), "num_gp": order}
+    gl, ol = gpu_loss(etype, physics, m, s), oracle_loss(etype, physics, m, s)
+    rng = np.random.default_rng(50 + order)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = (0.05 / n) * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    o = ol.batch_loss_and_grads(ctrl, u)
+    gl.CheckDeviceStatus()
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+    uf = ol.full_dof_vector(u[0])
+    jac, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl[0], uf)
+    A, Ro = ol.csr(ctrl[0], uf)
+    assert rel_fro(jac.data.cpu().numpy(), A.data) < TOL
+    assert rel_fro(R.cpu().numpy(), Ro) < TOL
