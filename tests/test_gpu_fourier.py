@@ -33,22 +33,37 @@ def _xyz(mesh):
     return X
 
 
-@pytest.mark.parametrize("etype,n,scale", [("hex8", 12, (0.0, 1.0)), ("quad4", 40, (-0.5, 1.5)),
-                                           ("tet4", 6, (0.0, 1.0))])
-def test_fourier_forward_and_vjp_match_oracle(cuda, etype, n, scale):
+# more than four frequencies on an axis: several 4 x 4 x 4 tiles of the
+# frequency grid, with partly empty edge tiles
+WIDE = {"x_freqs": np.arange(0, 6), "y_freqs": np.array([1, 3]), "z_freqs": np.array([0, 1, 2, 3, 5]),
+        "beta": 4.0, "min": 0.1, "max": 1.0}
+# more than 64 tiles: the forward kernels read the coefficients in plain order
+MANY = {"x_freqs": np.arange(0, 17), "y_freqs": np.arange(0, 17), "z_freqs": np.arange(0, 13),
+        "beta": 4.0, "min": 0.1, "max": 1.0}
+
+
+@pytest.mark.parametrize("etype,n,scale,settings", [("hex8", 12, (0.0, 1.0), SETTINGS),
+                                                    ("quad4", 40, (-0.5, 1.5), SETTINGS),
+                                                    ("tet4", 6, (0.0, 1.0), SETTINGS),
+                                                    ("hex8", 12, (0.0, 1.0), WIDE),
+                                                    ("quad4", 40, (-0.5, 1.5), WIDE),
+                                                    ("hex8", 8, (0.0, 1.0), MANY)])
+def test_fourier_forward_and_vjp_match_oracle(cuda, etype, n, scale, settings):
     torch = cuda
     m = make_mesh(etype, n, seed=41)
-    fc = _control(m, scale=scale)
-    freqs = fo.fourier_frequencies(SETTINGS["x_freqs"], SETTINGS["y_freqs"], SETTINGS["z_freqs"])
+    fc = _control(m, settings=settings, scale=scale)
+    freqs = fo.fourier_frequencies(settings["x_freqs"], settings["y_freqs"], settings["z_freqs"])
     rng = np.random.default_rng(42)
-    c = 0.5 * rng.standard_normal((3, fc.GetNumberOfVariables()))
+    F = fc.GetNumberOfVariables()
+    # K's spread kept near one for big bases, so the sigmoid is not saturated
+    c = 0.5 * min(1.0, np.sqrt(64 / F)) * rng.standard_normal((3, F))
     vals = fc.ComputeBatchControlledVariables(c)
-    ref = fo.fourier_control_values(c, freqs, _xyz(m), **_oracle_kw(scale=scale))
+    ref = fo.fourier_control_values(c, freqs, _xyz(m), **_oracle_kw(settings, scale=scale))
     assert rel_fro(vals.cpu().numpy(), ref) < TOL
     assert rel_fro(fc.ComputeControlledVariables(c[1]).cpu().numpy(), ref[1]) < TOL
     dv = rng.standard_normal((3, fc.GetNumberOfControlledVariables()))
     g = fc.ComputeBatchControlledVariablesVJP(c, dv)
-    gref = fo.fourier_control_vjp(c, dv, freqs, _xyz(m), **_oracle_kw(scale=scale))
+    gref = fo.fourier_control_vjp(c, dv, freqs, _xyz(m), **_oracle_kw(settings, scale=scale))
     assert rel_fro(g.cpu().numpy(), gref) < TOL
     # deterministic: the same launch twice gives the same bits
     assert torch.equal(g, fc.ComputeBatchControlledVariablesVJP(c, dv))
