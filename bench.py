@@ -73,10 +73,12 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-soak", action="store_true", help="skip the one-second clock soak (profiling runs)")
     ap.add_argument("--no-extras", action="store_true", help="skip the PCG / batched / neo-Hooke measurements")
+    ap.add_argument("--only-extras", action="store_true",
+                    help="run only the --extras measurements and print them (profiling runs; no bench line)")
     ap.add_argument("--hex8-variant", type=int, default=None,
                     help="force one hex8 kernel variant (0-17) instead of autotuning (profiling runs)")
-    ap.add_argument("--extras", default="small,pcg,batched,neohooke,newton",
-                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke, newton)")
+    ap.add_argument("--extras", default="small,pcg,batched,neohooke,newton,fourier",
+                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke, newton, fourier)")
     return ap.parse_args()
 
 
@@ -484,6 +486,51 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
     return out
 
 
+def extra_fourier(args, n=64, batch=4, freqs=4, seed=2024):
+    """FOL training step with a Fourier-parametrised Young's modulus on the
+    64^3 hex8 workload (fourier_control.py:24-59 in front of fe_loss.py:250-262):
+    coefficients -> nodal E -> fused loss + adjoint -> dL/dcoefficients ->
+    Adam on the coefficients, batch 4, 4 x 4 x 4 frequencies, one CUDA graph
+    (L2 flushed before every timed step); and the control's VJP alone."""
+    import torch
+    from folax_gb300.batched import AdamState, capture_step
+    from folax_gb300.fields import FourierControl
+    from folax_gb300.loss import MechanicalLoss3DHexa
+    mesh, settings, _, u_h = workload(n, seed)
+    settings = dict(settings, control_layout="nodal")
+    loss = MechanicalLoss3DHexa("fourier", settings, mesh)
+    loss.Initialize()
+    fr = np.arange(1, freqs + 1)
+    fc = FourierControl("E", {"x_freqs": fr, "y_freqs": fr, "z_freqs": fr, "beta": 20.0, "min": 0.1, "max": 1.0},
+                        mesh)
+    fc.Initialize()
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    coeffs = torch.rand((batch, fc.GetNumberOfVariables()), device="cuda", generator=gen)
+    u = loss.ApplyDirichletBCOnDofVector(torch.tensor(u_h, device="cuda")).reshape(1, -1).repeat(batch, 1)
+    adam = AdamState(coeffs, lr=1e-3)
+
+    def step():
+        E = fc.ComputeBatchControlledVariables(coeffs)
+        _, _, losses, du, dE = loss.ComputeBatchLossAndGrad(E, u)
+        dc = fc.ComputeBatchControlledVariablesVJP(coeffs, dE)
+        adam.update(coeffs, dc)
+        return losses, dc
+
+    g, _ = capture_step(step, warmup=3)
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device="cuda")
+    steps = 20
+    ms_step = _events_ms(torch, g.replay, steps, flush)
+    E0 = fc.ComputeBatchControlledVariables(coeffs)
+    dv = torch.ones_like(E0)
+    ms_vjp = _events_ms(torch, lambda: fc.ComputeBatchControlledVariablesVJP(coeffs, dv), steps, flush)
+    ms_fwd = _events_ms(torch, lambda: fc.ComputeBatchControlledVariables(coeffs), steps, flush)
+    nE = n ** 3
+    return {"mesh": f"{n}^3 hex8", "instances": batch, "coefficients": fc.GetNumberOfVariables(),
+            "graph_ms_per_step": ms_step, "melem_s": batch * nE / (ms_step * 1e-3) / 1e6,
+            "control_forward_ms": ms_fwd, "control_vjp_ms": ms_vjp,
+            "step": "Fourier control forward + fused loss/adjoint + control VJP + Adam, one CUDA graph, L2 flushed"}
+
+
 def extra_newton(args, n=10, seed=7, steps=5):
     """A whole nonlinear solve, Saint-Venant-Kirchhoff hex8 on an n^3 box
     (two-phase nodal Young's modulus, bottom fixed, top stretched by 0.1 in
@@ -568,6 +615,27 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_extras(args, loss, ctrl):
+    """The extra measurements named by --extras; a failed one is reported, not hidden."""
+    import torch
+    extras = {}
+    wanted = set(args.extras.split(","))
+    for key, name, fn in (("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
+                          ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
+                          ("batched", "batched_quad4_512", lambda: extra_batched(args)),
+                          ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args)),
+                          ("newton", "newton_svk_hex8_10", lambda: extra_newton(args)),
+                          ("fourier", "fourier_hex8_64_batch4", lambda: extra_fourier(args))):
+        if key not in wanted:
+            continue
+        try:
+            extras[name] = fn()
+        except Exception as exc:  # noqa: BLE001
+            extras[name] = {"error": f"{type(exc).__name__}: {exc}"}
+        torch.cuda.empty_cache()
+    return extras
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -598,6 +666,9 @@ def main():
     lib = _capi.load()
     ctrl = torch.from_numpy(E_h).cuda()[None]
     u = torch.from_numpy(u_h).cuda()[None]
+    if args.only_extras:  # profiling runs: the extra workloads alone
+        print(json.dumps({"extras": run_extras(args, loss, ctrl)}))
+        return
     flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     nE = args.n ** 3
     B = 1
@@ -696,22 +767,7 @@ def main():
     fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
     fp32_achieved = FLOPS_PER_ELEMENT * nE / (elem_ms * 1e-3) / 1e12
 
-    extras = None
-    if rank == 0 and not args.no_extras:
-        extras = {}
-        wanted = set(args.extras.split(","))
-        for key, name, fn in (("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
-                              ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
-                              ("batched", "batched_quad4_512", lambda: extra_batched(args)),
-                              ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args)),
-                              ("newton", "newton_svk_hex8_10", lambda: extra_newton(args))):
-            if key not in wanted:
-                continue
-            try:
-                extras[name] = fn()
-            except Exception as exc:  # report, do not hide, a failed extra
-                extras[name] = {"error": f"{type(exc).__name__}: {exc}"}
-            torch.cuda.empty_cache()
+    extras = run_extras(args, loss, ctrl) if rank == 0 and not args.no_extras else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_port(args.n, args.seed)
