@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const Batch
   __shared__ GPTable gp;
   __shared__ float red[32];
   __shared__ bool last;
-  load_gp_table(gp, A.gp);
+  if constexpr (NP == 0) load_gp_table(gp, A.gp);  // a compile-time rule needs no table
   __syncthreads();
   int bad = 0;
   for (int64_t t = blockIdx.x; t < T.ntiles; t += gridDim.x) {

@@ -23,22 +23,27 @@ namespace folgb {
 // IFAST (batches): the grid is (instances, element blocks), so the blocks of
 // all instances for one element range are dispatched together and share the
 // connectivity and coordinate loads in L2 instead of each instance sweeping
-// the whole mesh.
+// the whole mesh.  A block takes `tiles` consecutive ranges of blockDim.x
+// elements (big batches: fewer, longer-lived blocks keep the SMs fuller than
+// many short ones).  With a compile-time Gauss rule (NP > 0) the table in
+// shared memory is not used and not loaded.
 template <int ET, int PH, int MODE, bool IFAST = false, int NP = 0>
-__global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A) {
+__global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A, const int tiles) {
   __shared__ GPTable gp;
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   pdl_launch_dependents();
-  load_gp_table(gp, A.gp);
+  if constexpr (NP == 0) load_gp_table(gp, A.gp);
   if (threadIdx.x == 0) wcount = 0u;
   __syncthreads();
   const int b = IFAST ? blockIdx.x : blockIdx.y;
   const int blk = IFAST ? blockIdx.y : blockIdx.x, nblk = IFAST ? gridDim.y : gridDim.x;
-  const int64_t e = (int64_t)blk * blockDim.x + threadIdx.x;
   float energy = 0.f;
   int bad = 0;
-  if (e < A.E) elem_vector_body<ET, PH, MODE, NP>(A, gp, b, e, energy, bad);
+  for (int k = 0; k < tiles; ++k) {
+    const int64_t e = ((int64_t)blk * tiles + k) * blockDim.x + threadIdx.x;
+    if (e < A.E) elem_vector_body<ET, PH, MODE, NP>(A, gp, b, e, energy, bad);
+  }
   // warp-level epilogues: no block barrier after the element work
   if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount, blk, nblk);
   else report_bad_warp(bad, A.status);
@@ -750,6 +755,13 @@ struct LossWS {
 };
 
 static int loss_blocks(const folgb_plan* p) { return (int)((p->E + 255) / 256); }
+// element ranges per block of k_elem_vector: up to 4 while the launch keeps
+// at least 8 waves of 4 blocks per SM
+static int elem_tiles(int64_t nb, int B) {
+  int t = 1;
+  while (t < 4 && ((nb + 2 * t - 1) / (2 * t)) * B >= (int64_t)32 * num_sms()) t *= 2;
+  return t;
+}
 // partial-sum slots: enough for the smallest element-kernel block (64 threads)
 static int loss_partial_slots(const folgb_plan* p) { return (int)((p->E + 63) / 64); }
 
@@ -960,10 +972,12 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
       trace_begin(KID_ELEM_LOSS, s);
       with_const_gp<ET>(p, [&](auto np) {
         constexpr int NP = decltype(np)::value;
-        if (grid.y > 1 && grid.x <= 65535u)
-          k_elem_vector<ET, PH, MODE_LOSS, true, NP><<<dim3(grid.y, grid.x), 256, 0, s>>>(A);
+        const int tiles = elem_tiles(grid.x, (int)grid.y);
+        const unsigned nb = (unsigned)((grid.x + tiles - 1) / tiles);
+        if (grid.y > 1 && nb <= 65535u)
+          k_elem_vector<ET, PH, MODE_LOSS, true, NP><<<dim3(grid.y, nb), 256, 0, s>>>(A, tiles);
         else
-          k_elem_vector<ET, PH, MODE_LOSS, false, NP><<<grid, 256, 0, s>>>(A);
+          k_elem_vector<ET, PH, MODE_LOSS, false, NP><<<dim3(nb, grid.y), 256, 0, s>>>(A, tiles);
       });
       trace_end(KID_ELEM_LOSS, s);
       FOLGB_LAUNCH_CHECK();
@@ -1090,7 +1104,7 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
       if (!(p->phys.kernel_variant != 1 && launch_hex8_fast(p, A, grid, MODE_RESIDUAL, s))) {
         trace_begin(KID_ELEM_RESIDUAL, s);
         with_const_gp<ET>(p, [&](auto np) {
-          k_elem_vector<ET, PH, MODE_RESIDUAL, false, decltype(np)::value><<<grid, 256, 0, s>>>(A);
+          k_elem_vector<ET, PH, MODE_RESIDUAL, false, decltype(np)::value><<<grid, 256, 0, s>>>(A, 1);
         });
         trace_end(KID_ELEM_RESIDUAL, s);
       }

@@ -52,3 +52,20 @@ def test_large_generic_cases_match_c_oracle(cuda, etype, physics, n, layout):
     ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
     u = (0.05 / n) * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
     _compare(gl, cl, ctrl, u)
+
+
+# Batches big enough that each block of the generic element kernel takes
+# several element ranges: tet4 24^3 split (82,944 tets, 324 ranges of 256) at
+# batch 32 gives 2 ranges per block, quad4 256^2 (256 ranges) at batch 80
+# gives 4, on a 152-SM GPU (at least 8 waves of 4 blocks per SM either way).
+@pytest.mark.parametrize("etype,physics,n,batch", [("tet4", "elastic", 24, 32), ("quad4", "thermal", 256, 80)])
+def test_multi_range_blocks_match_c_oracle(cuda, etype, physics, n, batch):
+    m = make_mesh(etype, n, seed=33)
+    from gpu_cases import bc_dict
+    s = {"dirichlet_bc_dict": bc_dict(etype, physics), "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
+         "control_layout": "element"}
+    gl, cl = gpu_loss(etype, physics, m, s), c_oracle_loss(etype, physics, m, s)
+    rng = np.random.default_rng(34)
+    ctrl = 0.5 + rng.random((batch, gl.GetNumberOfControls()))
+    u = (0.05 / n) * rng.standard_normal((batch, gl.GetTotalNumberOfDOFs()))
+    _compare(gl, cl, ctrl, u)
