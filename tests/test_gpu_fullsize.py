@@ -56,9 +56,11 @@ def test_large_generic_cases_match_c_oracle(cuda, etype, physics, n, layout):
 
 # Batches big enough that each block of the generic element kernel takes
 # several element ranges: tet4 24^3 split (82,944 tets, 324 ranges of 256) at
-# batch 32 gives 2 ranges per block, quad4 256^2 (256 ranges) at batch 80
-# gives 4, on a 152-SM GPU (at least 8 waves of 4 blocks per SM either way).
-@pytest.mark.parametrize("etype,physics,n,batch", [("tet4", "elastic", 24, 32), ("quad4", "thermal", 256, 80)])
+# batch 32 gives 2 ranges per block; quad4 256^2 (256 ranges) at batch 80,
+# 160 and 320 gives 4, 8 and 16, on a 152-SM GPU (at least 8 waves of 4
+# blocks per SM each time).
+@pytest.mark.parametrize("etype,physics,n,batch", [("tet4", "elastic", 24, 32), ("quad4", "thermal", 256, 80),
+                                                   ("quad4", "thermal", 256, 160), ("quad4", "elastic", 256, 320)])
 def test_multi_range_blocks_match_c_oracle(cuda, etype, physics, n, batch):
     m = make_mesh(etype, n, seed=33)
     from gpu_cases import bc_dict
