@@ -16,6 +16,8 @@
 //
 // Node order (hexahedra_3d_8.py:79-87) -> lexicographic (xi fastest):
 //   lex = [0, 1, 3, 2, 4, 5, 7, 6]   (node 2 is (+,+,-), node 3 is (-,+,-), ...)
+#include <type_traits>
+
 #include "element_body.cuh"
 
 namespace folgb {
@@ -217,23 +219,61 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
         for (int k = 0; k < 3; ++k)
 #pragma unroll
           for (int t = 0; t < 4; ++t) S[i][k][t] = 0.f;
+      // Affine element (a parallelepiped, e.g. every cell of a structured box
+      // mesh): the 12 reference derivatives of each coordinate are equal, so J
+      // is the same at all 8 points and its inverse is formed once.  The
+      // points then see exactly the J, J^-1 and detJ of the general path (the
+      // same operations on the same values): the results are bit-identical.
+      bool affine = true;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int k = 1; k < 4; ++k)
+          affine &= (DX[i].dxi[k] == DX[i].dxi[0]) & (DX[i].deta[k] == DX[i].deta[0]) &
+                    (DX[i].dzeta[k] == DX[i].dzeta[0]);
+      auto pairs = [&](auto aff) {
+        constexpr bool AFF = decltype(aff)::value;
+        float2 JiA[3][3], wdA;
+        if constexpr (AFF) {
+          float2 J[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            J[i][0] = f2(DX[i].dxi[0]);
+            J[i][1] = f2(DX[i].deta[0]);
+            J[i][2] = f2(DX[i].dzeta[0]);
+          }
+          wdA = det_inv_pair(J, JiA);
+          bad |= !(wdA.x > 0.f);
+        }
 #pragma unroll
       for (int pr = 0; pr < 4; ++pr) {
         const int ty = pr & 1, tz = pr >> 1;
         const int ix = ty + 2 * tz;
-        float2 J[3][3], Gm[3][3];
+        float2 Gm[3][3];
 #pragma unroll
         for (int i = 0; i < 3; ++i) {
-          J[i][0] = f2(DX[i].dxi[ix]);
-          J[i][1] = make_float2(DX[i].deta[2 * tz], DX[i].deta[2 * tz + 1]);
-          J[i][2] = make_float2(DX[i].dzeta[2 * ty], DX[i].dzeta[2 * ty + 1]);
           Gm[i][0] = f2(DU[i].dxi[ix]);
           Gm[i][1] = make_float2(DU[i].deta[2 * tz], DU[i].deta[2 * tz + 1]);
           Gm[i][2] = make_float2(DU[i].dzeta[2 * ty], DU[i].dzeta[2 * ty + 1]);
         }
-        float2 Ji[3][3];
-        const float2 wd = det_inv_pair(J, Ji);  // Gauss weight 1
-        bad |= !(wd.x > 0.f) | !(wd.y > 0.f);
+        float2 Ji[3][3], wd;
+        if constexpr (AFF) {
+#pragma unroll
+          for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Ji[i][j] = JiA[i][j];
+          wd = wdA;
+        } else {
+          float2 J[3][3];
+#pragma unroll
+          for (int i = 0; i < 3; ++i) {
+            J[i][0] = f2(DX[i].dxi[ix]);
+            J[i][1] = make_float2(DX[i].deta[2 * tz], DX[i].deta[2 * tz + 1]);
+            J[i][2] = make_float2(DX[i].dzeta[2 * ty], DX[i].dzeta[2 * ty + 1]);
+          }
+          wd = det_inv_pair(J, Ji);  // Gauss weight 1
+          bad |= !(wd.x > 0.f) | !(wd.y > 0.f);
+        }
         if constexpr (BF) {
           wdet[2 * pr] = wd.x;
           wdet[2 * pr + 1] = wd.y;
@@ -279,6 +319,9 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
           S[i][2][2 * ty + 1] += t2.y;
         }
       }
+      };
+      if (affine) pairs(std::true_type{});
+      else pairs(std::false_type{});
       energy += en2.x + en2.y;
       sedsum += sed2sum.x + sed2sum.y;
     } else {

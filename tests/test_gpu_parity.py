@@ -94,11 +94,28 @@ def test_hex8_sum_factorised_matches_generic_and_oracle(cuda, layout, bf):
     assert rel_fro(Rf.cpu().numpy(), Ro) < TOL
 
 
+def _hex8_mesh(kind):
+    """jittered: every element distorted; box: every element a cube (the
+    affine path of the paired kernels); mixed: cubes where x < 0.5, distorted
+    elsewhere, so warps hold both kinds."""
+    if kind == "jittered":
+        return make_mesh("hex8", 4, seed=23, jitter=0.15)
+    m = make_mesh("hex8", 4, seed=23, jitter=0.0)
+    if kind == "mixed":
+        rng = np.random.default_rng(25)
+        X = m.nodes_coordinates
+        moved = X[:, 0] > 0.6
+        X[moved] += (0.15 / 4) * rng.standard_normal((int(moved.sum()), 3))
+    return m
+
+
 @pytest.mark.parametrize("variant", list(range(18)))
 @pytest.mark.parametrize("layout", ["nodal", "element"])
-def test_hex8_every_variant_matches_oracle(cuda, variant, layout):
-    """Each autotuner candidate (block size x accumulation scheme) is exact."""
-    m = make_mesh("hex8", 4, seed=23, jitter=0.15)
+@pytest.mark.parametrize("mesh_kind", ["jittered", "box", "mixed"])
+def test_hex8_every_variant_matches_oracle(cuda, variant, layout, mesh_kind):
+    """Each autotuner candidate (block size x accumulation scheme) is exact,
+    on distorted, affine and mixed meshes."""
+    m = _hex8_mesh(mesh_kind)
     s = _settings("hex8", "elastic", layout, 1.0, [0.2, 0.0, -0.1])
     gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
     ol = oracle_loss("hex8", "elastic", m, s)
