@@ -183,11 +183,12 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
       for (int L = 0; L < 8; ++L) ub[L] = U[0][L] * A.mat.bf[0] + U[1][L] * A.mat.bf[1] + U[2][L] * A.mat.bf[2];
     }
     // reference derivatives of the geometry and of the displacement
-    Deriv12 DX[3], DU[3];
+    // (ACC 2 forms the coordinate derivatives only for non-affine elements)
+    Deriv12 DX[ACC == 2 ? 1 : 3], DU[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
       wht8(X[i]);
-      deriv12(X[i], DX[i]);
+      if constexpr (ACC != 2) deriv12(X[i], DX[i]);
       wht8(U[i]);
       deriv12(U[i], DU[i]);
     }
@@ -220,30 +221,34 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
 #pragma unroll
           for (int t = 0; t < 4; ++t) S[i][k][t] = 0.f;
       // Affine element (a parallelepiped, e.g. every cell of a structured box
-      // mesh): the 12 reference derivatives of each coordinate are equal, so J
-      // is the same at all 8 points and its inverse is formed once.  The
-      // points then see exactly the J, J^-1 and detJ of the general path (the
-      // same operations on the same values): the results are bit-identical.
+      // mesh): the coordinates' Hadamard coefficients of xi eta, xi zeta,
+      // eta zeta and xi eta zeta are zero, so deriv12 would give every point
+      // the same reference derivatives (s h1, s h2, s h4: the butterflies add
+      // and subtract zeros) and J is the same at all 8 points.  J^-1 and detJ
+      // are then formed once from those values; the points see exactly the J,
+      // J^-1 and detJ of the general path, so the results are bit-identical.
       bool affine = true;
 #pragma unroll
       for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int k = 1; k < 4; ++k)
-          affine &= (DX[i].dxi[k] == DX[i].dxi[0]) & (DX[i].deta[k] == DX[i].deta[0]) &
-                    (DX[i].dzeta[k] == DX[i].dzeta[0]);
+        affine &= (X[i][3] == 0.f) & (X[i][5] == 0.f) & (X[i][6] == 0.f) & (X[i][7] == 0.f);
       auto pairs = [&](auto aff) {
         constexpr bool AFF = decltype(aff)::value;
         float2 JiA[3][3], wdA;
+        Deriv12 DXg[AFF ? 1 : 3];
         if constexpr (AFF) {
+          constexpr float s8 = 0.125f;
           float2 J[3][3];
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            J[i][0] = f2(DX[i].dxi[0]);
-            J[i][1] = f2(DX[i].deta[0]);
-            J[i][2] = f2(DX[i].dzeta[0]);
+            J[i][0] = f2(s8 * X[i][1]);
+            J[i][1] = f2(s8 * X[i][2]);
+            J[i][2] = f2(s8 * X[i][4]);
           }
           wdA = det_inv_pair(J, JiA);
           bad |= !(wdA.x > 0.f);
+        } else {
+#pragma unroll
+          for (int i = 0; i < 3; ++i) deriv12(X[i], DXg[i]);
         }
 #pragma unroll
       for (int pr = 0; pr < 4; ++pr) {
@@ -267,9 +272,9 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
           float2 J[3][3];
 #pragma unroll
           for (int i = 0; i < 3; ++i) {
-            J[i][0] = f2(DX[i].dxi[ix]);
-            J[i][1] = make_float2(DX[i].deta[2 * tz], DX[i].deta[2 * tz + 1]);
-            J[i][2] = make_float2(DX[i].dzeta[2 * ty], DX[i].dzeta[2 * ty + 1]);
+            J[i][0] = f2(DXg[i].dxi[ix]);
+            J[i][1] = make_float2(DXg[i].deta[2 * tz], DXg[i].deta[2 * tz + 1]);
+            J[i][2] = make_float2(DXg[i].dzeta[2 * ty], DXg[i].dzeta[2 * ty + 1]);
           }
           wd = det_inv_pair(J, Ji);  // Gauss weight 1
           bad |= !(wd.x > 0.f) | !(wd.y > 0.f);
