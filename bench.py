@@ -50,11 +50,13 @@ FLOPS_PER_ELEMENT = 5208.0
 # warp instructions per clock per SM).  Variants without a capture report null.
 #   6:  k_hex8_elastic_regs, 128 threads / 96 registers, point sums
 #   13: k_hex8_elastic_tma, persistent, TMA-staged rows, paired points
-#   16: the same with the next tile's nodes prefetched to L1 (ncu's printed
-#       precision: 17.59 MB read, 11.26 KB written)
+#   16, 17: the same with the next tile's nodes prefetched to L1 / L2
+# (13, 16, 17 with the affine-element path; ncu's printed precision for the
+# DRAM bytes: 17.60 MB read, a few KB written)
 NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16_144_605},
-                    13: {"traffic": 17_585_152 + 17_664, "warp_instructions": 12_610_462},
-                    16: {"traffic": 17_590_000 + 11_260, "warp_instructions": 13_000_454}}}
+                    13: {"traffic": 17_600_000 + 4_860, "warp_instructions": 10_652_202},
+                    16: {"traffic": 17_600_000 + 9_470, "warp_instructions": 10_954_635},
+                    17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421}}}
 
 
 def ncu_figure(n, variant, key):
