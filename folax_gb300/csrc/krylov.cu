@@ -688,17 +688,53 @@ static int spmv_blocks(const folgb_plan* p, int G) {
   return (int)(blocks < cap ? blocks : cap);
 }
 
+// One Adam update (optax.adam): the bias corrections enter as the reciprocals
+// of 1 - beta^t, formed once per launch.
+struct AdamCoef {
+  float lr, b1, b2, eps, rb1, rb2;
+};
+
+__device__ __forceinline__ void adam_one(const AdamCoef& c, float& x, float g, float& m, float& v) {
+  m = fmaf(c.b1, m, (1.f - c.b1) * g);
+  v = fmaf(c.b2, v, (1.f - c.b2) * g * g);
+  x -= c.lr * (m * c.rb1) / (sqrtf(v * c.rb2) + c.eps);
+}
+
+// 16-byte loads and stores when all four arrays are 16-byte aligned (four
+// parameters per trip), plain ones otherwise and for the last n mod 4.
 __global__ void k_adam(float* __restrict__ x, const float* __restrict__ g, float* __restrict__ m, float* __restrict__ v,
                        int64_t n, const int* step, float lr, float b1, float b2, float eps) {
   const int t = *step + 1;
-  const float bc1 = 1.f - powf(b1, (float)t), bc2 = 1.f - powf(b2, (float)t);
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const float gi = g[i];
-    const float mi = fmaf(b1, m[i], (1.f - b1) * gi);
-    const float vi = fmaf(b2, v[i], (1.f - b2) * gi * gi);
+  const AdamCoef c{lr, b1, b2, eps, 1.f / (1.f - powf(b1, (float)t)), 1.f / (1.f - powf(b2, (float)t))};
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+  const bool vec = ((reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(g) | reinterpret_cast<uintptr_t>(m) |
+                     reinterpret_cast<uintptr_t>(v)) & 15u) == 0;
+  int64_t done = 0;
+  if (vec) {
+    const int64_t n4 = n >> 2;
+    float4* x4 = reinterpret_cast<float4*>(x);
+    const float4* g4 = reinterpret_cast<const float4*>(g);
+    float4* m4 = reinterpret_cast<float4*>(m);
+    float4* v4 = reinterpret_cast<float4*>(v);
+    for (int64_t i = tid; i < n4; i += stride) {
+      float4 xv = x4[i], mv = m4[i], vv = v4[i];
+      const float4 gv = g4[i];
+      adam_one(c, xv.x, gv.x, mv.x, vv.x);
+      adam_one(c, xv.y, gv.y, mv.y, vv.y);
+      adam_one(c, xv.z, gv.z, mv.z, vv.z);
+      adam_one(c, xv.w, gv.w, mv.w, vv.w);
+      x4[i] = xv;
+      m4[i] = mv;
+      v4[i] = vv;
+    }
+    done = n4 << 2;
+  }
+  for (int64_t i = done + tid; i < n; i += stride) {
+    float xi = x[i], mi = m[i], vi = v[i];
+    adam_one(c, xi, g[i], mi, vi);
+    x[i] = xi;
     m[i] = mi;
     v[i] = vi;
-    x[i] -= lr * (mi / bc1) / (sqrtf(vi / bc2) + eps);
   }
 }
 
@@ -1295,7 +1331,8 @@ extern "C" int folgb_adam_step(float* params, const float* grads, float* m, floa
   if (!params || !grads || !m || !v || !step || n < 0) return FOLGB_ERR_INVALID_ARGUMENT;
   if (n == 0) return FOLGB_OK;
   cudaStream_t s = (cudaStream_t)stream;
-  int blocks = (int)((n + 255) / 256);
+  int blocks = (int)((n / 4 + 255) / 256);
+  if (blocks < 1) blocks = 1;
   int cap = num_sms() * 8;
   if (blocks > cap) blocks = cap;
   k_adam<<<blocks, 256, 0, s>>>(params, grads, m, v, n, step, lr, beta1, beta2, eps);

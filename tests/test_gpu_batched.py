@@ -48,18 +48,22 @@ def test_batched_matches_per_instance_launches(cuda, layout, exponent):
     assert abs(float(mean) - losses.mean()) <= 1e-6 * abs(losses.mean())
 
 
-def test_adam_matches_reference_update(cuda):
+@pytest.mark.parametrize("n,offset", [(1000, 0), (1003, 0), (1000, 1)])
+def test_adam_matches_reference_update(cuda, n, offset):
+    """16-byte path (n a multiple of 4, aligned), its scalar tail (n = 1003)
+    and the plain path (parameters starting 4 bytes into an allocation)."""
     torch = cuda
     from folax_gb300.batched import AdamState
     rng = np.random.default_rng(3)
-    x0 = rng.standard_normal(1000).astype(np.float32)
-    x = torch.tensor(x0, device="cuda")
+    x0 = rng.standard_normal(n).astype(np.float32)
+    x = torch.zeros(n + offset, device="cuda")[offset:]
+    x.copy_(torch.tensor(x0, device="cuda"))
     st = AdamState(x, lr=1e-2)
     m = np.zeros_like(x0, dtype=np.float64)
     v = np.zeros_like(m)
     xr = x0.astype(np.float64)
     for t in range(1, 4):
-        g = rng.standard_normal(1000).astype(np.float32)
+        g = rng.standard_normal(n).astype(np.float32)
         st.update(x, torch.tensor(g, device="cuda"))
         m = 0.9 * m + 0.1 * g
         v = 0.999 * v + 0.001 * g.astype(np.float64) ** 2
