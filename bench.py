@@ -368,7 +368,8 @@ def extra_small_thermal(args, n=50, seed=5):
 def extra_batched(args, n_inst=512, seed=11):
     """C3: 512 quad4 thermal instances, side n ~ U{16..128}, own Fourier
     conductivity each: fused loss + adjoint + Adam on the nodal field as one
-    CUDA graph, against the same step as per-instance launches."""
+    CUDA graph (elements per tile chosen by the autotuner), against the same
+    step as per-instance launches."""
     import torch
     from folax_gb300 import fields
     from folax_gb300.batched import AdamState, BatchedFELoss, capture_step
@@ -386,6 +387,7 @@ def extra_batched(args, n_inst=512, seed=11):
         for i, m in enumerate(meshes)]), dtype=torch.float32, device="cuda")
     T = torch.rand(bl.total_dofs, device="cuda", generator=torch.Generator(device="cuda").manual_seed(seed))
     out = (torch.empty(n_inst, device="cuda"), torch.empty_like(T), torch.empty_like(ctrl))
+    tune = bl.Autotune(ctrl, T, repeats=5)  # elements per tile of the launch
     adam = AdamState(T, lr=1e-3)
 
     def step():
@@ -420,6 +422,8 @@ def extra_batched(args, n_inst=512, seed=11):
     ms_per = (time.perf_counter() - t0) * 1e3 / per_steps
     E = bl.num_elements
     return {"instances": n_inst, "elements": E, "nodes": bl.num_nodes, "plan_s": t_plan,
+            "autotune": {"elements_per_tile": tune["chosen"],
+                         "ms_per_tile_size": dict(zip(map(str, BatchedFELoss.BATCH_TILES), tune["ms"]))},
             "graph_ms_per_step": ms_graph, "graph_melem_s": E / (ms_graph * 1e-3) / 1e6,
             "per_instance_ms_per_step": ms_per, "per_instance_melem_s": E / (ms_per * 1e-3) / 1e6,
             "speedup_batched_vs_per_instance": ms_per / ms_graph,

@@ -101,6 +101,8 @@ PROTOTYPES = {
     "folgb_batch_plan_destroy": (C.c_int, [vp]),
     "folgb_batch_workspace_bytes": (sz, [vp]),
     "folgb_batch_loss_adjoint": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, vp]),
+    "folgb_batch_autotune": (C.c_int, [vp, vp, vp, i32, vp, vp, vp, vp, vp, sz, i32, vp, sz, vp, C.POINTER(i32), vp,
+                                       i32]),
     "folgb_response_workspace_bytes": (sz, [vp]),
     "folgb_response": (C.c_int, [vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, sz, vp]),
     "folgb_fourier_create": (C.c_int, [C.POINTER(vp), vp, i32, vp, i32, vp, i32, vp, i64, f64, f64, f64, f64, f64]),

@@ -7,7 +7,8 @@ plan with per-instance offset tables (include/folgb.h:
 folgb_batch_plan_create) so a single persistent kernel evaluates every
 instance's loss and adjoint, and ``AdamState`` applies the optimiser update
 (optax.adam semantics, deep_network.py:100,141) on the device.
-``capture_step`` records loss + adjoint + update as one CUDA graph.
+``capture_step`` records loss + adjoint + update as one CUDA graph;
+``BatchedFELoss.Autotune`` picks the elements per tile of the launch.
 """
 from __future__ import annotations
 
@@ -39,6 +40,7 @@ class BatchedFELoss:
         self.element_type, self.physics_name = element_type, physics
         self.settings = settings
         self.meshes = meshes
+        self.elements_per_tile = int(elements_per_tile)
         ndof = _NDOF[(element_type, physics)]
         self.ndof = ndof
         dofnames = ["T"] if ndof == 1 else ["Ux", "Uy", "Uz"][:ndof]
@@ -121,6 +123,33 @@ class BatchedFELoss:
                                                capi.ptr(self.workspace), self.workspace.numel(), capi.stream_handle())
         capi.check("folgb_batch_loss_adjoint", rc)
         return losses.mean(), losses, du, dc
+
+    BATCH_TILES = (256, 512, 1024, 2048, 4096)
+
+    def Autotune(self, control, dofs, repeats: int = 5, cold_l2: bool = True):
+        """Times the batched launch with each tile size of BATCH_TILES
+        (elements per tile) on these inputs and keeps the fastest in the plan
+        (folgb_batch_autotune); cold_l2: a temporary 256 MiB device buffer is
+        overwritten before every timed call, as inside a training step.
+        Returns {"chosen": elements per tile, "ms": [per-size times]}."""
+        torch = _torch()
+        ctrl = _dev(control).reshape(-1)
+        u = _dev(dofs).reshape(-1)
+        losses = torch.empty(self.num_instances, dtype=torch.float32, device="cuda")
+        du, dc = torch.empty_like(u), torch.empty_like(ctrl)
+        flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda") if cold_l2 else None
+        chosen = C.c_int32()
+        times = (C.c_float * len(self.BATCH_TILES))()
+        rc = self.lib.folgb_batch_autotune(self.handle, capi.ptr(ctrl), capi.ptr(u), 1, capi.ptr(losses), capi.ptr(du),
+                                           capi.ptr(dc), capi.ptr(self.status), capi.ptr(self.workspace),
+                                           self.workspace.numel(), int(repeats),
+                                           capi.ptr(flush) if flush is not None else None,
+                                           flush.numel() if flush is not None else 0, capi.stream_handle(),
+                                           C.byref(chosen), C.cast(times, C.c_void_p), len(self.BATCH_TILES))
+        del flush
+        capi.check("folgb_batch_autotune", rc)
+        self.elements_per_tile = chosen.value
+        return {"chosen": chosen.value, "ms": [times[i] for i in range(len(self.BATCH_TILES))]}
 
     def __del__(self):
         try:

@@ -21,7 +21,9 @@ struct folgb_batch_plan {
   folgb_plan* mesh = nullptr;
   int32_t I = 0;
   int64_t ntiles = 0;
+  int64_t max_tiles = 0;  // tiles at the smallest tile size the autotuner tries
   int tile = 0;
+  std::vector<int64_t> eoff;  // host copy of the instance element offsets
   int64_t* d_tile_start = nullptr;
   int* d_tile_count = nullptr;
   int* d_tile_off = nullptr;   // [I+1] tile range of each instance
@@ -40,13 +42,18 @@ struct BatchArgs {
   int I;
 };
 
+// Each warp writes its own energy partial of every tile it works on
+// (partials[t][warp]), so a tile needs no block barrier; the last block sums
+// an instance's partials in (tile, warp) order.
+constexpr int kBatchWarps = 8;  // 256 threads
+
 template <int ET, int PH, int NP = 0>
-__global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const BatchArgs T) {
+__global__ void __launch_bounds__(kBatchWarps * 32) k_batch_loss(const VecArgs A, const BatchArgs T) {
   __shared__ GPTable gp;
-  __shared__ float red[32];
   __shared__ bool last;
   if constexpr (NP == 0) load_gp_table(gp, A.gp);  // a compile-time rule needs no table
   __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   int bad = 0;
   for (int64_t t = blockIdx.x; t < T.ntiles; t += gridDim.x) {
     const int64_t e0 = T.tile_start[t];
@@ -54,12 +61,13 @@ __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const Batch
     float energy = 0.f;
     for (int k = threadIdx.x; k < cnt; k += blockDim.x)
       elem_vector_body<ET, PH, MODE_LOSS, NP>(A, gp, 0, e0 + k, energy, bad);
-    float be = block_sum(energy, red);
-    if (threadIdx.x == 0) A.partials[t] = be;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) energy += __shfl_xor_sync(0xffffffffu, energy, o);
+    if (lane == 0) A.partials[t * kBatchWarps + warp] = energy;
   }
-  report_bad(bad, A.status);
+  __threadfence();  // this warp's partials are visible before the block is counted
+  report_bad(bad, A.status);  // a block barrier
   if (threadIdx.x == 0) {
-    __threadfence();
     unsigned prev = atomicAdd(A.counters, 1u);
     last = (prev == gridDim.x - 1);
   }
@@ -70,7 +78,9 @@ __global__ void __launch_bounds__(256) k_batch_loss(const VecArgs A, const Batch
   const float p = A.exponent;
   for (int i = threadIdx.x; i < T.I; i += blockDim.x) {
     float L = 0.f;
-    for (int t = T.tile_off[i]; t < T.tile_off[i + 1]; ++t) L += pv[t];
+    for (int t = T.tile_off[i]; t < T.tile_off[i + 1]; ++t)
+#pragma unroll
+      for (int w = 0; w < kBatchWarps; ++w) L += pv[t * kBatchWarps + w];
     const float Lp = (p == 1.f) ? L : powf(L, p);
     A.losses[i] = Lp;
     A.scale[i] = (p == 1.f) ? A.inv_batch : p * powf(L, p - 1.f) * A.inv_batch;
@@ -93,7 +103,7 @@ static size_t layout_batch(const folgb_batch_plan* bp, void* base, size_t cap, B
   BatchWS t;
   t.rec = loss_record(p);
   t.g = b.take<float>((size_t)p->E * p->nen * t.rec);
-  t.partials = b.take<float>((size_t)bp->ntiles);
+  t.partials = b.take<float>((size_t)std::max(bp->ntiles, bp->max_tiles) * kBatchWarps);
   t.counters = b.take<unsigned>(1);
   t.scale = b.take<float>((size_t)bp->I);
   if (w) *w = t;
@@ -104,6 +114,43 @@ template <class T>
 static int upload_vec(T** dst, const std::vector<T>& v) {
   FOLGB_CUDA_TRY(cudaMalloc((void**)dst, std::max<size_t>(1, v.size()) * sizeof(T)));
   if (!v.empty()) FOLGB_CUDA_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return FOLGB_OK;
+}
+
+// tile sizes the autotuner tries (elements per tile, every tile inside one instance)
+constexpr int kBatchTiles[] = {256, 512, 1024, 2048, 4096};
+constexpr int kBatchTileCount = 5;
+
+static int64_t count_tiles(const std::vector<int64_t>& eoff, int tile) {
+  int64_t n = 0;
+  for (size_t i = 0; i + 1 < eoff.size(); ++i) n += (eoff[i + 1] - eoff[i] + tile - 1) / tile;
+  return n;
+}
+
+// (re)builds the tile tables of the plan for `tile` elements per tile
+static int build_tiles(folgb_batch_plan* bp, int tile) {
+  std::vector<int64_t> tstart;
+  std::vector<int> tcount, toff(bp->I + 1, 0);
+  for (int i = 0; i < bp->I; ++i) {
+    toff[i] = (int)tstart.size();
+    for (int64_t e = bp->eoff[i]; e < bp->eoff[i + 1]; e += tile) {
+      tstart.push_back(e);
+      tcount.push_back((int)std::min<int64_t>(tile, bp->eoff[i + 1] - e));
+    }
+  }
+  toff[bp->I] = (int)tstart.size();
+  void* old[] = {bp->d_tile_start, bp->d_tile_count, bp->d_tile_off};
+  for (void* q : old)
+    if (q) cudaFree(q);
+  bp->d_tile_start = nullptr;
+  bp->d_tile_count = nullptr;
+  bp->d_tile_off = nullptr;
+  bp->tile = tile;
+  bp->ntiles = (int64_t)tstart.size();
+  int rc;
+  if ((rc = upload_vec(&bp->d_tile_start, tstart)) || (rc = upload_vec(&bp->d_tile_count, tcount)) ||
+      (rc = upload_vec(&bp->d_tile_off, toff)))
+    return rc;
   return FOLGB_OK;
 }
 
@@ -151,24 +198,16 @@ extern "C" int folgb_batch_plan_create(folgb_batch_plan** out, const folgb_physi
     delete bp;
     return rc;
   }
-  int tile = elements_per_tile > 0 ? elements_per_tile : 1024;
+  const int tile = elements_per_tile > 0 ? elements_per_tile : 1024;
   bp->I = I;
-  bp->tile = tile;
-  std::vector<int64_t> tstart;
-  std::vector<int> tcount, toff(I + 1, 0), node_inst(N), elem_inst(E);
+  bp->eoff.assign(eoff, eoff + I + 1);
+  bp->max_tiles = std::max(count_tiles(bp->eoff, kBatchTiles[0]), count_tiles(bp->eoff, tile));
+  std::vector<int> node_inst(N), elem_inst(E);
   for (int i = 0; i < I; ++i) {
-    toff[i] = (int)tstart.size();
-    for (int64_t e = eoff[i]; e < eoff[i + 1]; e += tile) {
-      tstart.push_back(e);
-      tcount.push_back((int)std::min<int64_t>(tile, eoff[i + 1] - e));
-    }
     for (int64_t n = noff[i]; n < noff[i + 1]; ++n) node_inst[n] = i;
     for (int64_t e = eoff[i]; e < eoff[i + 1]; ++e) elem_inst[e] = i;
   }
-  toff[I] = (int)tstart.size();
-  bp->ntiles = (int64_t)tstart.size();
-  if ((rc = upload_vec(&bp->d_tile_start, tstart)) || (rc = upload_vec(&bp->d_tile_count, tcount)) ||
-      (rc = upload_vec(&bp->d_tile_off, toff)) || (rc = upload_vec(&bp->d_node_inst, node_inst)) ||
+  if ((rc = build_tiles(bp, tile)) || (rc = upload_vec(&bp->d_node_inst, node_inst)) ||
       (rc = upload_vec(&bp->d_elem_inst, elem_inst))) {
     folgb_batch_plan_destroy(bp);
     return rc;
@@ -239,5 +278,74 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
                        elem_ctrl ? nullptr : dloss_dcontrol, 0, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, bp->d_node_inst, bp->d_elem_inst);
   }
+  return rc;
+}
+
+// Times the batched loss + adjoint with each tile size of kBatchTiles (2
+// warm-up and `repeats` timed calls each, CUDA events on the stream, the
+// flush buffer, if given, overwritten before every timed call outside its
+// events) and keeps the fastest tile size in the plan.  Synchronises the
+// stream; the tile tables are rebuilt between candidates, so no other work
+// may use the plan meanwhile.
+extern "C" int folgb_batch_autotune(folgb_batch_plan* bp, const float* control, const float* dofs,
+                                    int32_t apply_dirichlet, float* losses, float* dloss_ddofs,
+                                    float* dloss_dcontrol, int32_t* device_status, void* workspace,
+                                    size_t workspace_bytes, int32_t repeats, void* flush_buffer, size_t flush_bytes,
+                                    void* stream, int32_t* chosen_tile, float* ms_per_candidate,
+                                    int32_t max_candidates) {
+  if (!bp || !chosen_tile || !control || !dofs || !losses) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (!workspace || workspace_bytes < layout_batch(bp, nullptr, 0, nullptr)) return FOLGB_ERR_WORKSPACE;
+  if (repeats < 1) repeats = 1;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FOLGB_CUDA_TRY(cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return FOLGB_ERR_CUDA;
+  }
+  const int start_tile = bp->tile;
+  int rc = FOLGB_OK, best = -1;
+  float best_ms = 0.f;
+  auto call = [&]() {
+    return folgb_batch_loss_adjoint(bp, control, dofs, apply_dirichlet, losses, dloss_ddofs, dloss_dcontrol,
+                                    device_status, workspace, workspace_bytes, stream);
+  };
+  for (int c = 0; c < kBatchTileCount && !rc; ++c) {
+    if (cudaStreamSynchronize(s) != cudaSuccess) {
+      rc = FOLGB_ERR_CUDA;
+      break;
+    }
+    if ((rc = build_tiles(bp, kBatchTiles[c]))) break;
+    for (int w = 0; w < 2 && !rc; ++w) rc = call();
+    float total = 0.f;
+    for (int r = 0; r < repeats && !rc; ++r) {
+      if (flush_buffer && flush_bytes && cudaMemsetAsync(flush_buffer, r & 0xff, flush_bytes, s) != cudaSuccess) {
+        rc = FOLGB_ERR_CUDA;
+        break;
+      }
+      if (cudaEventRecord(e0, s) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+      if (!rc) rc = call();
+      if (!rc && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess))
+        rc = FOLGB_ERR_CUDA;
+      float ms = 0.f;
+      if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+      total += ms;
+    }
+    if (rc) break;
+    const float ms = total / (float)repeats;
+    if (ms_per_candidate && c < max_candidates) ms_per_candidate[c] = ms;
+    if (best < 0 || ms < best_ms) {
+      best = c;
+      best_ms = ms;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // keep the fastest (or, after a failure, the tile size the plan had)
+  if (cudaStreamSynchronize(s) != cudaSuccess && !rc) rc = FOLGB_ERR_CUDA;
+  const int keep = (!rc && best >= 0) ? kBatchTiles[best] : start_tile;
+  const int rc2 = build_tiles(bp, keep);
+  if (!rc) rc = rc2;
+  if (!rc) *chosen_tile = keep;
   return rc;
 }

@@ -327,6 +327,21 @@ int folgb_batch_loss_adjoint(const folgb_batch_plan* plan, const float* control,
                              float* dloss_ddofs, float* dloss_dcontrol, int32_t* device_status,
                              void* workspace, size_t workspace_bytes, void* stream);
 
+/* Autotuner of the batched launch: times folgb_batch_loss_adjoint with 256,
+ * 512, 1024, 2048 and 4096 elements per tile on the caller's inputs (2
+ * warm-up and `repeats` timed calls each; flush_buffer, if not NULL, is
+ * overwritten before every timed call, outside its timing) and keeps the
+ * fastest in the plan: *chosen_tile, and ms_per_candidate[k] for the first
+ * max_candidates sizes.  The workspace is that of folgb_batch_workspace_bytes
+ * (it covers every tile size).  Synchronises the stream.  No counterpart in
+ * the reference. */
+int folgb_batch_autotune(folgb_batch_plan* plan, const float* control, const float* dofs,
+                         int32_t apply_dirichlet, float* losses, float* dloss_ddofs,
+                         float* dloss_dcontrol, int32_t* device_status, void* workspace,
+                         size_t workspace_bytes, int32_t repeats, void* flush_buffer, size_t flush_bytes,
+                         void* stream, int32_t* chosen_tile, float* ms_per_candidate,
+                         int32_t max_candidates);
+
 /* ---- adjoint sensitivities of an integral response ------------------------
  * FiniteElementResponse (fol/responses/fe_response.py:17-526) for thermal and
  * linear-elastic plans: J = sum_e sum_gp w detJ f(d_gp, u_gp) with d_gp, u_gp

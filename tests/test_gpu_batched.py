@@ -107,3 +107,33 @@ def test_graph_captured_step_replays_exactly(cuda):
     torch.cuda.synchronize()
     assert int(st.step.item()) == 5
     assert torch.equal(T, eager)
+
+
+def test_batch_autotune_keeps_a_tile_size_and_the_results(cuda):
+    """The batched autotuner picks one of its tile sizes, leaves the plan on
+    it, and the results stay those of the per-instance launches: gradients
+    bit-identical to the untuned plan (the tile size does not enter them),
+    losses within 1e-6 (summed in another grouping)."""
+    torch = cuda
+    from folax_gb300.batched import BatchedFELoss
+    sizes = [40, 90, 17, 64, 128, 33]
+    meshes = _instances(sizes, seed=7)
+    settings = {"dirichlet_bc_dict": {"T": {"left": 1.0, "right": 0.0}}, "control_layout": "element", "num_gp": 2}
+    bl = BatchedFELoss("quad", "thermal", meshes, settings, elements_per_tile=64)
+    rng = np.random.default_rng(8)
+    ctrl = torch.tensor(0.1 + rng.random(bl.num_elements), dtype=torch.float32, device="cuda")
+    u = torch.tensor(rng.random(bl.total_dofs), dtype=torch.float32, device="cuda")
+    _, l0, du0, dc0 = bl.ComputeLossAndGrad(ctrl, u)
+    l0, du0, dc0 = l0.clone(), du0.clone(), dc0.clone()
+    res = bl.Autotune(ctrl, u, repeats=2, cold_l2=False)
+    assert res["chosen"] in BatchedFELoss.BATCH_TILES and bl.elements_per_tile == res["chosen"]
+    assert len(res["ms"]) == len(BatchedFELoss.BATCH_TILES) and all(t > 0 for t in res["ms"])
+    _, l1, du1, dc1 = bl.ComputeLossAndGrad(ctrl, u)
+    assert torch.equal(du0, du1) and torch.equal(dc0, dc1)
+    assert rel_fro(l1.cpu().numpy(), l0.cpu().numpy()) < 1e-6
+    for i, m in enumerate(meshes):
+        single = gpu_loss("quad4", "thermal", m, dict(settings))
+        c0, c1 = bl.control_offsets[i], bl.control_offsets[i + 1]
+        a, b = bl.dof_offsets[i], bl.dof_offsets[i + 1]
+        _, _, li, _, _ = single.ComputeBatchLossAndGrad(ctrl[c0:c1][None], u[a:b][None])
+        assert rel_fro(l1[i].cpu().numpy(), li.cpu().numpy()[0]) < TOL
