@@ -637,12 +637,12 @@ static void launch_variant_regs(const VecArgs& A, dim3 grid, bool bf, cudaStream
   else k_hex8_elastic_regs<CL, MODE, false, ACC, REGS><<<g2, 128, 0, s>>>(A);
 }
 
-// Persistent grid: as many blocks as fit on the GPU at once, at most one
-// 4-warp block per 4 tiles.
-// (resident blocks per SM queried once per kernel instantiation)
+// Persistent grid: as many blocks as fit on the GPU at once (the resident
+// blocks per SM of `kernel`, queried once per kernel instantiation: per_sm is
+// that instantiation's own cache, x the SMs), at most one 4-warp block per 4
+// tiles.
 template <class K>
-static unsigned persistent_blocks(K kernel, int64_t E) {
-  static int per_sm = 0;
+static unsigned persistent_blocks(K kernel, int64_t E, int& per_sm) {
   if (per_sm == 0) {
     int n = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kTmaWarps * 32, 0) != cudaSuccess || n < 1) n = 1;
@@ -655,12 +655,13 @@ static unsigned persistent_blocks(K kernel, int64_t E) {
 
 template <int CL, int MODE, int ACC, int MINB, int PF = 0>
 static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
+  static int per_sm_bf = 0, per_sm = 0;  // one occupancy figure per kernel instantiation
   if (bf) {
     auto k = k_hex8_elastic_tma<CL, MODE, true, ACC, MINB, PF>;
-    k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
+    k<<<dim3(persistent_blocks(k, A.E, per_sm_bf), grid.y), kTmaWarps * 32, 0, s>>>(A);
   } else {
     auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB, PF>;
-    k<<<dim3(persistent_blocks(k, A.E), grid.y), kTmaWarps * 32, 0, s>>>(A);
+    k<<<dim3(persistent_blocks(k, A.E, per_sm), grid.y), kTmaWarps * 32, 0, s>>>(A);
   }
 }
 

@@ -4,6 +4,7 @@ import numpy as np
 import pytest
 
 from conftest import arr, golden
+from folax_gb300.loss import HEX8_VARIANTS
 from folax_gb300.mesh import create_3D_box_mesh
 from gpu_cases import bc_dict, gpu_loss, make_mesh, oracle_loss, rel_fro
 from oracle import fe_oracle as fo
@@ -109,7 +110,7 @@ def _hex8_mesh(kind):
     return m
 
 
-@pytest.mark.parametrize("variant", list(range(18)))
+@pytest.mark.parametrize("variant", list(range(HEX8_VARIANTS)))
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 @pytest.mark.parametrize("mesh_kind", ["jittered", "box", "mixed"])
 def test_hex8_every_variant_matches_oracle(cuda, variant, layout, mesh_kind):
@@ -185,9 +186,10 @@ def test_autotune_keeps_results_exact(cuda):
     ctrl = 0.5 + rng.random((1, gl.GetNumberOfControls()))
     u = 0.01 * rng.standard_normal((1, gl.GetTotalNumberOfDOFs()))
     warm = gl.Autotune(ctrl, u, repeats=2, cold_l2=False)  # back-to-back calls
-    assert 0 <= warm["chosen"] < 18 and len(warm["ms"]) == 18 and min(warm["ms"]) > 0
+    nv = HEX8_VARIANTS
+    assert 0 <= warm["chosen"] < nv and len(warm["ms"]) == nv and min(warm["ms"]) > 0
     info = gl.Autotune(ctrl, u, repeats=2)  # every timed call after an L2 flush
-    assert 0 <= info["chosen"] < 18 and len(info["ms"]) == 18 and min(info["ms"]) > 0
+    assert 0 <= info["chosen"] < nv and len(info["ms"]) == nv and min(info["ms"]) > 0
     a = gl.ComputeBatchLossAndGrad(ctrl, u)
     o = ol.batch_loss_and_grads(ctrl, u)
     for x, z in zip(a[2:], o[2:]):
