@@ -89,4 +89,10 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1
     line = json.loads(lines[0])
     assert line["impl"] == "reference" and line["n_gpus"] == 2 and line["value"] > 0
-    assert line["e2e"]["h2d_bytes_per_step"] == 0
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["value"] == line["value"]
+    # the same metric, unit and workload as the GPU arm's line
+    assert line["metric"].startswith("M elements/s") and line["unit"] == "M elements/s"
+    assert line["higher_is_better"] is True and line["steps"] == 1 and line["warmup"] == 0
+    assert line["config"]["workload"].startswith("hex8 linear-elastic fused loss+adjoint, 64^3")
+    cb = line["cpu_baseline"]
+    assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == line["value"] and cb["sample"]
