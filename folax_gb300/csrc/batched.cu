@@ -226,6 +226,8 @@ extern "C" int folgb_batch_loss_adjoint(const folgb_batch_plan* bp, const float*
                                         float* dloss_dcontrol, int32_t* device_status, void* workspace,
                                         size_t workspace_bytes, void* stream) {
   if (!bp || !control || !dofs || !losses) return FOLGB_ERR_INVALID_ARGUMENT;
+  // a tile table that could not be (re)built leaves the plan unusable
+  if (!bp->d_tile_start || !bp->d_tile_count || !bp->d_tile_off) return FOLGB_ERR_CUDA;
   const folgb_plan* p = bp->mesh;
   BatchWS w;
   size_t need = layout_batch(bp, workspace, workspace_bytes, &w);
