@@ -97,3 +97,20 @@ def test_oracle_fourier_control_vjp_matches_central_differences():
             fd = (np.sum(dv[b] * fo.fourier_control_values(cp[b], freqs, X, **kw)[0])
                   - np.sum(dv[b] * fo.fourier_control_values(cm[b], freqs, X, **kw)[0])) / (2 * h)
             assert abs(fd - g[b, q]) < 1e-7 * max(1.0, abs(fd))
+
+
+def test_python_mirrors_of_library_constants():
+    """The host's variant count, variant names and batched tile sizes are the
+    ones the CUDA sources define (kHex8Variants, kBatchTiles)."""
+    import os
+    import re
+    from conftest import ROOT
+    from folax_gb300.batched import BatchedFELoss
+    from folax_gb300.loss import HEX8_VARIANT_NAMES, HEX8_VARIANTS
+    csrc = os.path.join(ROOT, "folax_gb300", "csrc")
+    hex8 = open(os.path.join(csrc, "hex8_fused.cu")).read()
+    assert int(re.search(r"constexpr int kHex8Variants = (\d+);", hex8).group(1)) == HEX8_VARIANTS
+    assert len(HEX8_VARIANT_NAMES) == HEX8_VARIANTS
+    batched = open(os.path.join(csrc, "batched.cu")).read()
+    tiles = re.search(r"constexpr int kBatchTiles\[\] = \{([^}]*)\};", batched).group(1)
+    assert tuple(int(t) for t in tiles.split(",")) == BatchedFELoss.BATCH_TILES
