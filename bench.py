@@ -79,25 +79,15 @@ def parse():
                     help="run only the --extras measurements and print them (profiling runs; no bench line)")
     ap.add_argument("--hex8-variant", type=int, default=None,
                     help="force one hex8 kernel variant (0-17) instead of autotuning (profiling runs)")
-    ap.add_argument("--extras", default="small,pcg,batched,neohooke,newton,fourier",
-                    help="comma list of the extra measurements to run (small, pcg, batched, neohooke, newton, fourier)")
+    ap.add_argument("--extras", default="jittered,small,pcg,batched,neohooke,newton,fourier",
+                    help="comma list of the extra measurements to run (jittered, small, pcg, batched, neohooke, "
+                         "newton, fourier)")
     return ap.parse_args()
 
 
-def workload(n, seed):
-    from folax_gb300 import fields
-    from folax_gb300.mesh import create_3D_box_mesh
-    mesh = create_3D_box_mesh(n, n, n)
-    E = fields.two_phase_voxels(n, seed, sigma=3.0, high=1.0, low=0.1)
-    rng = np.random.default_rng(seed + 1)
-    u = np.zeros((mesh.GetNumberOfNodes(), 3))
-    u[:, 2] = 0.05 * mesh.nodes_coordinates[:, 2]
-    u += 0.01 * rng.standard_normal(u.shape)
-    settings = {"dirichlet_bc_dict": {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0},
-                                      "Uz": {"bottom": 0.0, "top": 0.05}},
-                "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
-                "control_layout": "element", "num_gp": 2}
-    return mesh, settings, E.astype(np.float32), u.ravel().astype(np.float32)
+def workload(n, seed, jitter=0.0):
+    from folax_gb300 import workloads
+    return workloads.hex8_elastic(n, seed, jitter)
 
 
 def workload_config(n, B):
@@ -256,6 +246,24 @@ def _cpu_baseline_numpy(n_sample=12, seed=7, reason=""):
                       f"{reps} repetitions, {dt * 1e3:.1f} ms each. {reason}"}
 
 
+# GPU results kept for the CPU leg's checks against the FP64 oracle
+_CPU_CHECKS = {}
+
+
+def cpu_check_pcg():
+    """FP64 Jacobi-CG (C oracle, rtol 1e-12, every host core) of the system
+    the GPU PCG solved: the GPU solution's relative error against it."""
+    if "pcg" not in _CPU_CHECKS:
+        return None
+    from oracle import c_oracle
+    indptr, indices, vals, r, dx = _CPU_CHECKS.pop("pcg")
+    t0 = time.perf_counter()
+    x, it, rel = c_oracle.pcg(indptr, indices, vals, -r, rtol=1e-12, threads=_host_threads())
+    return {"error_vs_fp64_cg": float(np.linalg.norm(dx - x) / np.linalg.norm(x)), "fp64_cg_iterations": it,
+            "fp64_cg_relative_residual": rel, "fp64_cg_s": time.perf_counter() - t0,
+            "check": "FP64 Jacobi-CG of the same assembled fp32 system on the host (C oracle)"}
+
+
 def _events_ms(torch, fn, steps, flush=None):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
     for a, b in ev:
@@ -297,10 +305,13 @@ def extra_pcg(args, loss, ctrl):
     lib.folgb_trace_enable(0)
     info = solver.last_linear_info
     it = max(1, info["iterations"])
-    # true residual of the returned solution, fp64 on the host
+    # true residual of the returned fp32 solution, fp64 on the host (the
+    # solver's own figure is that of its fp64 iterate)
     A = jac.to_scipy()
-    res = np.linalg.norm(A @ dx.double().cpu().numpy() + r.double().cpu().numpy()) / np.linalg.norm(
-        r.double().cpu().numpy())
+    dx_h, r_h = dx.double().cpu().numpy(), r.double().cpu().numpy()
+    res = np.linalg.norm(A @ dx_h + r_h) / np.linalg.norm(r_h)
+    # kept for the CPU leg, which checks dx against an FP64 CG of this system
+    _CPU_CHECKS["pcg"] = (A.indptr, A.indices, A.data, r_h, dx_h)
     plan = jac.plan
     N = plan.num_nodes
     nnz = plan.nnz
@@ -322,8 +333,11 @@ def extra_pcg(args, loss, ctrl):
             "pcg_launches": [n_s.value, n_u.value], "spmv_ms": spmv_ms,
             "spmv_gbs": spmv_bytes / (spmv_ms * 1e-3) / 1e9,
             "spmv_hbm_frac": spmv_bytes / (spmv_ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
-            "true_relative_residual": float(res),
-            "note": "Jacobi-PCG, fp32 matrix/vectors, fp64 dots, norms and iterate, reliable updates; "
+            "iterate_relative_residual": info["relative_residual"],
+            "returned_fp32_relative_residual": float(res),
+            "note": "Jacobi-PCG, fp32 matrix/vectors, fp64 dots, norms and iterate, reliable updates; the solver "
+                    "stops on the fp64 iterate's true residual (iterate_relative_residual); the solution it "
+                    "returns is that iterate rounded to fp32 (returned_fp32_relative_residual); "
                     "wall time includes one host flag read per 64 iterations"}
 
 
@@ -334,14 +348,11 @@ def extra_small_thermal(args, n=50, seed=5):
     vectors, fp64 dots and iterate: the single-cluster solver), as a linear FE
     solve (fe_linear_residual_based_solver.py:15-22) through the public API."""
     import torch
-    from folax_gb300 import fields
+    from folax_gb300 import workloads
     from folax_gb300.loss import ThermalLoss2DQuad
-    from folax_gb300.mesh import create_2D_square_mesh
     from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
-    m = create_2D_square_mesh(1.0, n + 1)
-    k = fields.fourier_conductivity(fields.element_centroids(m.nodes_coordinates, m.elements_nodes["quad"]), seed)
-    loss = ThermalLoss2DQuad("c0", {"dirichlet_bc_dict": {"T": {"left": 1.0, "right": 0.0}},
-                                    "control_layout": "element", "num_gp": 2}, m)
+    m, settings, k = workloads.square_thermal(n, seed)
+    loss = ThermalLoss2DQuad("c0", settings, m)
     loss.Initialize()
     solver = FiniteElementLinearResidualBasedSolver("c0", loss, {"linear_solver_settings": {
         "solver": "GB300-pcg", "tol": 1e-10, "maxiter": 20000, "vector_precision": "fp32"}})
@@ -371,20 +382,14 @@ def extra_batched(args, n_inst=512, seed=11):
     CUDA graph (elements per tile chosen by the autotuner), against the same
     step as per-instance launches."""
     import torch
-    from folax_gb300 import fields
+    from folax_gb300 import workloads
     from folax_gb300.batched import AdamState, BatchedFELoss, capture_step
     from folax_gb300.loss import ThermalLoss2DQuad
-    from folax_gb300.mesh import create_2D_square_mesh
-    rng = np.random.default_rng(seed)
-    sizes = rng.integers(16, 129, n_inst)
-    meshes = [create_2D_square_mesh(1.0, int(n) + 1) for n in sizes]
-    settings = {"dirichlet_bc_dict": {"T": {"left": 1.0, "right": 0.0}}, "control_layout": "element", "num_gp": 2}
+    meshes, settings, ks = workloads.thermal_instances(n_inst, seed)
     t0 = time.perf_counter()
     bl = BatchedFELoss("quad", "thermal", meshes, settings, elements_per_tile=1024)
     t_plan = time.perf_counter() - t0
-    ctrl = torch.tensor(np.concatenate([fields.fourier_conductivity(
-        fields.element_centroids(m.nodes_coordinates, m.elements_nodes["quad"]), seed + i)
-        for i, m in enumerate(meshes)]), dtype=torch.float32, device="cuda")
+    ctrl = torch.tensor(np.concatenate(ks), dtype=torch.float32, device="cuda")
     T = torch.rand(bl.total_dofs, device="cuda", generator=torch.Generator(device="cuda").manual_seed(seed))
     out = (torch.empty(n_inst, device="cuda"), torch.empty_like(T), torch.empty_like(ctrl))
     tune = bl.Autotune(ctrl, T, repeats=5)  # elements per tile of the launch
@@ -397,7 +402,8 @@ def extra_batched(args, n_inst=512, seed=11):
     g, _ = capture_step(step, warmup=3)
     steps = 20
     ms_graph = _events_ms(torch, g.replay, steps)
-    # per-instance launches: the same work, one loss object and launch set per instance
+    # per-instance launches: the same work, one loss object and launch set
+    # (element kernel + gather + Adam) per instance
     per = []
     offs_c, offs_d = bl.control_offsets, bl.dof_offsets
     for i, m in enumerate(meshes):
@@ -420,15 +426,24 @@ def extra_batched(args, n_inst=512, seed=11):
         per_step()
     torch.cuda.synchronize()
     ms_per = (time.perf_counter() - t0) * 1e3 / per_steps
+    # the same per-instance launch sets captured as one CUDA graph: no host
+    # dispatch, only the per-instance launches themselves
+    g_per, _ = capture_step(per_step, warmup=1)
+    ms_per_graph = _events_ms(torch, g_per.replay, 5)
     E = bl.num_elements
     return {"instances": n_inst, "elements": E, "nodes": bl.num_nodes, "plan_s": t_plan,
             "autotune": {"elements_per_tile": tune["chosen"],
                          "ms_per_tile_size": dict(zip(map(str, BatchedFELoss.BATCH_TILES), tune["ms"]))},
             "graph_ms_per_step": ms_graph, "graph_melem_s": E / (ms_graph * 1e-3) / 1e6,
-            "per_instance_ms_per_step": ms_per, "per_instance_melem_s": E / (ms_per * 1e-3) / 1e6,
-            "speedup_batched_vs_per_instance": ms_per / ms_graph,
+            "per_instance_graph_ms_per_step": ms_per_graph,
+            "per_instance_graph_melem_s": E / (ms_per_graph * 1e-3) / 1e6,
+            "per_instance_eager_ms_per_step": ms_per, "per_instance_eager_melem_s": E / (ms_per * 1e-3) / 1e6,
+            "speedup_batched_vs_per_instance": ms_per_graph / ms_graph,
+            "speedup_batched_vs_per_instance_eager": ms_per / ms_graph,
             "step": "fused loss + adjoint (one persistent launch + gather) + Adam on the nodal field, one CUDA graph",
-            "per_instance_step": "the same, one eager launch set per instance (wall clock)"}
+            "per_instance_step": "the same work as one launch set (element kernel, gather, Adam) per instance; "
+                                 "graph: all 512 launch sets captured as one CUDA graph (the speed-up denominator); "
+                                 "eager: the same from the Python API (wall clock)"}
 
 
 def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
@@ -441,24 +456,15 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
     and a full undamped Newton solve from u = 0 inverts elements beyond ~6^3,
     so one iteration is timed."""
     import torch
-    from folax_gb300 import fields
+    from folax_gb300 import fields, workloads
     from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
     from folax_gb300.mesh import create_3D_box_mesh, split_hex_to_tets
     from folax_gb300.solvers import FiniteElementNonLinearResidualBasedSolver
-    bc = {"Ux": {"bottom": 0.0}, "Uy": {"bottom": 0.0}, "Uz": {"bottom": 0.0, "top": 0.05}}
-    mesh = split_hex_to_tets(create_3D_box_mesh(n, n, n))
-    Ev = fields.two_phase_voxels(n, seed)
-    E_t = np.repeat(Ev, 6).astype(np.float32)
-    settings = {"dirichlet_bc_dict": bc, "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
-                "control_layout": "element"}
+    mesh, settings, E_b, u_b = workloads.neohooke_tets(n, batch, seed)
     loss = NeoHookeMechanicalLoss3DTetra("nh", settings, mesh)
     loss.Initialize()
-    rng = np.random.default_rng(seed)
-    u = np.zeros((batch, mesh.GetNumberOfNodes(), 3), dtype=np.float32)
-    u[:, :, 2] = 0.05 * mesh.nodes_coordinates[None, :, 2]
-    u += (0.002 * rng.standard_normal(u.shape)).astype(np.float32)
-    U = torch.tensor(u.reshape(batch, -1), device="cuda")
-    Cb = torch.tensor(np.repeat(E_t[None], batch, 0), device="cuda")
+    U = torch.tensor(u_b, device="cuda")
+    Cb = torch.tensor(E_b, device="cuda")
     for _ in range(3):
         loss.ComputeBatchLossAndGrad(Cb, U)
     torch.cuda.synchronize()
@@ -490,6 +496,49 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=12):
                      "newton_info": solver.last_newton_info, "residual_norm": h.get("res_norm"),
                      "error": err}
     return out
+
+
+def fp32_peak(torch, lib):
+    """Measured FP32 peak of this GPU: the library's FMA-chain probe
+    (folgb_fp32_peak_probe: 8 blocks of 256 threads per SM, 8 independent
+    packed-pair FMA chains per thread), timed with CUDA events.  Changes no
+    GPU setting.  Returns (TFLOP/s, ms per launch)."""
+    import ctypes as C
+    from folax_gb300 import _capi
+    sink = torch.zeros(1, device="cuda")
+    flops = C.c_double()
+
+    def run():
+        _capi.check("folgb_fp32_peak_probe", lib.folgb_fp32_peak_probe(_capi.ptr(sink), 8, 4096, C.byref(flops),
+                                                                       _capi.stream_handle()))
+
+    for _ in range(3):
+        run()
+    ms = _events_ms(torch, run, 10)
+    return flops.value / (ms * 1e-3) / 1e12, ms
+
+
+def extra_jittered(args):
+    """The headline step (fused loss + adjoint, 64^3 hex8, graph replay, L2
+    flushed) on a mesh whose interior nodes are moved by N(0, (0.1 h)^2): no
+    element is a parallelepiped, so the element kernel takes its general
+    (non-affine) path at every Gauss point."""
+    import torch
+    from folax_gb300.batched import capture_step
+    from folax_gb300.loss import MechanicalLoss3DHexa
+    mesh, settings, E_h, u_h = workload(args.n, args.seed, jitter=0.1)
+    loss = MechanicalLoss3DHexa("jittered", settings, mesh)
+    loss.Initialize()
+    ctrl = torch.from_numpy(E_h).cuda()[None]
+    u = torch.from_numpy(u_h).cuda()[None]
+    tune = loss.Autotune(ctrl, u, repeats=3)
+    g, _ = capture_step(lambda: loss.ComputeBatchLossAndGrad(ctrl, u), warmup=3)
+    flush = torch.empty(FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    ms = _events_ms(torch, g.replay, 20, flush)
+    nE = args.n ** 3
+    return {"mesh": f"{args.n}^3 hex8, interior nodes jittered by N(0, (0.1 h)^2)", "ms_per_step": ms,
+            "melem_s": nE / (ms * 1e-3) / 1e6, "chosen_variant": tune["chosen"],
+            "timing": "CUDA-graph replay of the fused step, L2 flushed before every step"}
 
 
 def extra_fourier(args, n=64, batch=4, freqs=4, seed=2024):
@@ -626,7 +675,8 @@ def run_extras(args, loss, ctrl):
     import torch
     extras = {}
     wanted = set(args.extras.split(","))
-    for key, name, fn in (("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
+    for key, name, fn in (("jittered", "jittered_hex8_64", lambda: extra_jittered(args)),
+                          ("small", "plain_small_quad4_thermal_50", lambda: extra_small_thermal(args)),
                           ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
                           ("batched", "batched_quad4_512", lambda: extra_batched(args)),
                           ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args)),
@@ -761,22 +811,48 @@ def main():
     h2d = u_pin.numel() * 4 + c_pin.numel() * 4
     d2h = out_du.numel() * 4 + out_dc.numel() * 4 + 4
 
-    # roofline of the element kernel (algorithmic bytes per launch):
-    # conn 32 B + control 4 B + dLoss/dE 4 B per element; coordinates 12 B and
-    # dofs 12 B per node (each node read once)
+    # roofline of the element kernel.  Bytes: conn 32 B + control 4 B +
+    # dLoss/dE 4 B per element; coordinates 12 B and dofs 12 B per node (each
+    # node read once).  Flops: the FP32 operations the kernel variant executes
+    # per launch (ncu's fadd + fmul + 2 x ffma thread-instruction counts,
+    # packed pairs counted twice), over the FP32 peak measured here.
     N = (args.n + 1) ** 3
     alg_bytes = nE * (32 + 4 + 4) + N * (12 + 12)
-    achieved = alg_bytes / (elem_ms * 1e-3) / 1e9
+    achieved_gbs = alg_bytes / (elem_ms * 1e-3) / 1e9
     peaks = measured_peaks()
     hbm = (peaks or {}).get("hbm_gbs", 6800.0)
-    sm_max = (peaks or {}).get("sm_max_mhz", 2070.0)
-    fp32_peak = 152 * 128 * 2 * sm_max * 1e6 / 1e12
-    fp32_achieved = FLOPS_PER_ELEMENT * nE / (elem_ms * 1e-3) / 1e12
+    fp32_tflops, fp32_probe_ms = fp32_peak(torch, lib)
+    flops_launch = ncu_figure(args.n, tune["chosen"], "fp32_flops")
+    flops_src = "ncu-counted FP32 operations of this kernel variant"
+    if flops_launch is None:
+        flops_launch = FLOPS_PER_ELEMENT * nE
+        flops_src = "naive per-element count (no ncu figure for this variant)"
+    fp32_achieved = flops_launch / (elem_ms * 1e-3) / 1e12
+    issue = issue_roofline(args.n, tune["chosen"], elem_ms, clk, peaks) or {}
+    roofline = {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_tflops, "unit": "TFLOP/s",
+                "frac": fp32_achieved / fp32_tflops,
+                "traffic": ncu_figure(args.n, tune["chosen"], "traffic"),
+                "traffic_unit": "bytes per launch (ncu dram read + write)",
+                "flops_per_launch": flops_launch, "flops_source": flops_src,
+                "naive_flops_per_element": FLOPS_PER_ELEMENT,
+                "peak_source": "measured in this run: folgb_fp32_peak_probe (FFMA2 chains on every SM), "
+                               f"{fp32_probe_ms:.3f} ms per probe launch",
+                "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm, "hbm_frac": achieved_gbs / hbm,
+                "hbm_peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                "algorithmic_bytes": alg_bytes,
+                "issue_frac": issue.get("frac"), "issue_bound_us": issue.get("issue_bound_us"),
+                "warp_instructions": issue.get("warp_instructions"),
+                "kernel_us": elem_ms * 1e3,
+                "kernel": "hex8 2x2x2 element kernel, variant %d (%s)"
+                          % (tune["chosen"], HEX8_VARIANT_NAMES[tune["chosen"]])}
 
     extras = run_extras(args, loss, ctrl) if rank == 0 and not args.no_extras else None
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline_port(args.n, args.seed)
+        chk = cpu_check_pcg()
+        if chk is not None and extras and isinstance(extras.get("pcg_hex8_64"), dict):
+            extras["pcg_hex8_64"].update(chk)
     if rank == 0:
         line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
                 "value": value, "unit": "M elements/s", "n_gpus": world, "steps": args.steps,
@@ -793,19 +869,7 @@ def main():
                 "kernels": {"elem_loss_ms": elem_ms, "gather_ms": gather_ms,
                             "autotune": {"chosen_variant": tune["chosen"], "ms_per_variant": tune["ms"],
                                          "variants": HEX8_VARIANT_NAMES}},
-                "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                             "frac": achieved / hbm,
-                             "traffic": ncu_figure(args.n, tune["chosen"], "traffic"),
-                             "traffic_unit": "bytes per launch (ncu dram read + write)",
-                             "algorithmic_bytes": alg_bytes,
-                             "kernel": "sum-factorised hex8 2x2x2 element kernel, variant %d (%s)"
-                                       % (tune["chosen"], HEX8_VARIANT_NAMES[tune["chosen"]]),
-                             "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
-                             "fp32": {"achieved_tflops": fp32_achieved, "nominal_peak_tflops": fp32_peak,
-                                      "frac": fp32_achieved / fp32_peak,
-                                      "flops_per_element": FLOPS_PER_ELEMENT,
-                                      "note": "naive-algorithm flop count; the sum-factorised kernel executes fewer"},
-                             "issue": issue_roofline(args.n, tune["chosen"], elem_ms, clk, peaks)},
+                "roofline": roofline,
                 "e2e": {"value": B * nE / (ms_e2e * 1e-3) / 1e6, "unit": "M elements/s", "ms_per_step": ms_e2e,
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,

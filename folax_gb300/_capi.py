@@ -111,6 +111,7 @@ PROTOTYPES = {
     "folgb_fourier_workspace_bytes": (sz, [vp, i32]),
     "folgb_fourier_backward": (C.c_int, [vp, i32, vp, vp, vp, vp, sz, vp]),
     "folgb_selftest_bounded_wait": (C.c_int, [vp, vp]),
+    "folgb_fp32_peak_probe": (C.c_int, [vp, i32, i32, C.POINTER(f64), vp]),
     "folgb_trace_enable": (C.c_int, [i32]),
     "folgb_trace_reset": (C.c_int, []),
     "folgb_trace_read": (C.c_int, [i32, C.POINTER(i64), C.POINTER(f64)]),

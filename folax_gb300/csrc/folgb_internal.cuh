@@ -128,6 +128,9 @@ struct Bump {
 
 int num_sms();
 
+// Looks up the no-alloc scratch array on the current device (noalloc.cu).
+void noalloc_prepare_current_device();
+
 // Element-result records: one per (instance, element, node), [b][a][e],
 // padded to 1, 2 or 4 floats so the gather reads them with one vector load.
 // Components [0, ndof) hold the vector; component ndof the nodal control

@@ -16,6 +16,7 @@
 //
 // Node order (hexahedra_3d_8.py:79-87) -> lexicographic (xi fastest):
 //   lex = [0, 1, 3, 2, 4, 5, 7, 6]   (node 2 is (+,+,-), node 3 is (-,+,-), ...)
+#include <atomic>
 #include <type_traits>
 
 #include "element_body.cuh"
@@ -637,17 +638,27 @@ static void launch_variant_regs(const VecArgs& A, dim3 grid, bool bf, cudaStream
   else k_hex8_elastic_regs<CL, MODE, false, ACC, REGS><<<g2, 128, 0, s>>>(A);
 }
 
-// Persistent grid: as many blocks as fit on the GPU at once (the resident
-// blocks per SM of `kernel`, queried once per kernel instantiation: per_sm is
-// that instantiation's own cache, x the SMs), at most one 4-warp block per 4
-// tiles.
+// Resident blocks per SM of `kernel` on the current device, queried once per
+// (kernel instantiation, device): cache[dev] is that instantiation's own
+// table (0 = not queried yet; racing threads store the same value).
+constexpr int kOccDevices = 64;
 template <class K>
-static unsigned persistent_blocks(K kernel, int64_t E, int& per_sm) {
-  if (per_sm == 0) {
-    int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, kTmaWarps * 32, 0) != cudaSuccess || n < 1) n = 1;
-    per_sm = n;
+static int blocks_per_sm(K kernel, int threads, size_t smem, std::atomic<int> (&cache)[kOccDevices]) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kOccDevices) dev = 0;
+  int n = cache[dev].load(std::memory_order_relaxed);
+  if (n == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem) != cudaSuccess || n < 1) n = 1;
+    cache[dev].store(n, std::memory_order_relaxed);
   }
+  return n;
+}
+
+// Persistent grid: as many blocks as fit on the GPU at once, at most one
+// 4-warp block per 4 tiles.
+template <class K>
+static unsigned persistent_blocks(K kernel, int64_t E, std::atomic<int> (&cache)[kOccDevices]) {
+  const int per_sm = blocks_per_sm(kernel, kTmaWarps * 32, 0, cache);
   const int64_t want = (((E + 31) >> 5) + kTmaWarps - 1) / kTmaWarps;
   const int64_t cap = (int64_t)per_sm * num_sms();
   return (unsigned)(want < cap ? want : cap);
@@ -655,13 +666,13 @@ static unsigned persistent_blocks(K kernel, int64_t E, int& per_sm) {
 
 template <int CL, int MODE, int ACC, int MINB, int PF = 0>
 static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_t s) {
-  static int per_sm_bf = 0, per_sm = 0;  // one occupancy figure per kernel instantiation
+  static std::atomic<int> occ_bf[kOccDevices], occ[kOccDevices];  // per kernel instantiation and device
   if (bf) {
     auto k = k_hex8_elastic_tma<CL, MODE, true, ACC, MINB, PF>;
-    k<<<dim3(persistent_blocks(k, A.E, per_sm_bf), grid.y), kTmaWarps * 32, 0, s>>>(A);
+    k<<<dim3(persistent_blocks(k, A.E, occ_bf), grid.y), kTmaWarps * 32, 0, s>>>(A);
   } else {
     auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB, PF>;
-    k<<<dim3(persistent_blocks(k, A.E, per_sm), grid.y), kTmaWarps * 32, 0, s>>>(A);
+    k<<<dim3(persistent_blocks(k, A.E, occ), grid.y), kTmaWarps * 32, 0, s>>>(A);
   }
 }
 

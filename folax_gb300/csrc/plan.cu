@@ -4,6 +4,7 @@
 // index work the reference redoes inside every jit call (element Jacobian
 // indices, fe_loss.py:178-184, and the BCOO -> CSR conversion of
 // fol/solvers/fe_solver.py:71-72).
+#include <atomic>
 #include <algorithm>
 #include <array>
 #include <cmath>
@@ -16,13 +17,17 @@ using namespace folgb;
 
 namespace folgb {
 
+// SM count of the current device, cached per device ordinal (racing threads
+// store the same value).
 int num_sms() {
-  static int sms = 0;
+  constexpr int kDevs = 64;
+  static std::atomic<int> cache[kDevs];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kDevs) dev = 0;
+  int sms = cache[dev].load(std::memory_order_relaxed);
   if (sms == 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 1;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0) sms = 1;
+    cache[dev].store(sms, std::memory_order_relaxed);
   }
   return sms;
 }
@@ -368,6 +373,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     folgb_plan_destroy(p);
     return rc;
   }
+  noalloc_prepare_current_device();
   *out = p;
   return FOLGB_OK;
 }

@@ -121,3 +121,42 @@ extern "C" int folgb_selftest_bounded_wait(int32_t* device_status, void* stream)
   FOLGB_LAUNCH_CHECK();
   return FOLGB_OK;
 }
+
+// ---------------------------------------------------------------------------
+// FP32 throughput probe (no counterpart in the reference): a grid of
+// independent fused multiply-add chains over every SM, for measuring the FP32
+// peak a roofline is reported against.  Each thread runs 8 chains of packed
+// fp32 pairs (FFMA2: two IEEE fp32 fused multiply-adds per instruction);
+// x <- x * b + c with |b| < 1 stays finite for any iteration count.  The
+// result is stored only if it equals a value it never reaches, so the work
+// cannot be removed and nothing is written.
+// ---------------------------------------------------------------------------
+namespace folgb {
+constexpr int kPeakThreads = 256, kPeakChains = 8;
+__global__ void __launch_bounds__(kPeakThreads) k_fp32_peak(float* sink, int iters, float b0, float c0) {
+  float2 acc[kPeakChains];
+#pragma unroll
+  for (int k = 0; k < kPeakChains; ++k) acc[k] = make_float2(1e-3f * threadIdx.x + k, 0.5f * k);
+  const float2 b = make_float2(b0, b0), c = make_float2(c0, c0);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < kPeakChains; ++k) acc[k] = __ffma2_rn(acc[k], b, c);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < kPeakChains; ++k) s += acc[k].x + acc[k].y;
+  if (s == -1234.5f) sink[0] = s;
+}
+}  // namespace folgb
+
+extern "C" int folgb_fp32_peak_probe(float* sink, int32_t blocks_per_sm, int32_t iterations,
+                                     double* flops_per_launch, void* stream) {
+  if (!sink || blocks_per_sm <= 0 || blocks_per_sm > 64 || iterations <= 0) return FOLGB_ERR_INVALID_ARGUMENT;
+  const int64_t blocks = (int64_t)blocks_per_sm * num_sms();
+  folgb::k_fp32_peak<<<(unsigned)blocks, folgb::kPeakThreads, 0, (cudaStream_t)stream>>>(sink, iterations, 0.999f,
+                                                                                          1e-3f);
+  FOLGB_LAUNCH_CHECK();
+  if (flops_per_launch)
+    *flops_per_launch = (double)blocks * folgb::kPeakThreads * iterations * folgb::kPeakChains * 2.0 * 2.0;
+  return FOLGB_OK;
+}

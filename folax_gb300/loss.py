@@ -16,6 +16,12 @@ Differences a caller can see:
   connectivity as the reference does.
 * ComputeJacobianMatrixAndResidualVector returns a CSRJacobian (canonical CSR,
   the pattern scipy.sparse.csr_array builds from the reference's BCOO).
+* The kernels report a non-positive detJ, a non-finite value or a device wait
+  that gave up through a status word on the GPU.  A wait that gave up makes
+  every output of that call invalid.  loss_settings["check_device_status"] =
+  True reads the word after every call (one stream synchronisation) and
+  raises FolgbError before any result is returned; otherwise call
+  CheckDeviceStatus() where a check is wanted.
 """
 from __future__ import annotations
 
@@ -250,6 +256,7 @@ class FiniteElementLoss:
                                                self.dirichlet_values, False))
         self._csr_plan = None
         self._status = _torch().zeros(1, dtype=_torch().int32, device="cuda")
+        self._strict_status = bool(s.get("check_device_status", False))
         self.initialized = True
 
     def _get_csr_plan(self) -> Plan:
@@ -378,6 +385,8 @@ class FiniteElementLoss:
                 apply_bc, capi.ptr(losses), capi.ptr(du), capi.ptr(dp), capi.ptr(self._status), capi.ptr(ws),
                 ws.numel(), capi.stream_handle())
         capi.check("folgb_loss_adjoint_plain" if plain else "folgb_loss_adjoint", rc)
+        if self._strict_status:
+            self.CheckDeviceStatus()
         if out_losses is not None and out_losses is not losses:
             out_losses.copy_(losses, non_blocking=True)
         ret_losses = losses if out_losses is None else out_losses
@@ -454,6 +463,8 @@ class FiniteElementLoss:
                                      capi.ptr(residual), capi.ptr(data), capi.ptr(inv_diag), capi.ptr(self._status),
                                      capi.ptr(ws), ws.numel(), capi.stream_handle())
         capi.check("folgb_assemble", rc)
+        if self._strict_status:
+            self.CheckDeviceStatus()
         if not with_matrix:
             return None, residual
         indptr, indices = plan.pattern()

@@ -2,13 +2,15 @@
 
 Mirrors fol/solvers/solver.py:11-49, fe_solver.py:21-105,
 fe_linear_residual_based_solver.py:10-22 and
-fe_nonlinear_residual_based_solver.py:15-170.  The linear solve is the
-Jacobi-preconditioned CG of folgb_pcg (fp32 vectors, fp64 inner products and
-norms, x0 = 0) on the assembled CSR; the reference's BiCGSTAB / direct / PETSc
-choices ("JAX-bicgstab", "JAX-direct", "PETSc-*") all map to it.  With the
-row-only Dirichlet rule (fe_loss.py:191-207) the BC rows of the system are
-diag * dx = 0, so CG started from 0 never leaves the free-dof subspace and
-solves K_FF dx_F = -r_F exactly as a symmetric system.
+fe_nonlinear_residual_based_solver.py:15-170.  The linear solve runs on the
+assembled CSR with Jacobi preconditioning, fp64 inner products and norms and
+x0 = 0.  The solver name "GB300-pcg" selects CG (folgb_pcg / folgb_krylov);
+every other name, the reference's "JAX-bicgstab", "JAX-direct" and
+"PETSc-*" choices included, selects BiCGSTAB, which also handles the
+nonsymmetric and indefinite tangents the reference's default solver is used
+for.  With the row-only Dirichlet rule (fe_loss.py:191-207) the BC rows of the
+system are diag * dx = 0, so a Krylov solve started from 0 never leaves the
+free-dof subspace: for CG it solves K_FF dx_F = -r_F as a symmetric system.
 """
 from __future__ import annotations
 

@@ -41,6 +41,11 @@ enum {
   FOLGB_ERR_TOO_LARGE = 8,        /* problem exceeds a fixed-size scratch    */
   FOLGB_ERR_TIMEOUT = 9           /* a bounded device-side wait gave up      */
 };
+/* Device status words (the device_status arguments) collect 1 << code for
+ * the codes found on the device.  1 << FOLGB_ERR_TIMEOUT means a kernel
+ * stopped early after a bounded wait gave up: every output of that launch
+ * (losses, gradients, records) is invalid and must not be used; callers that
+ * consume results without reading the status word accept that risk. */
 
 /* element types (fol/geometries/__init__.py:18-21) */
 enum { FOLGB_QUAD4 = 0, FOLGB_HEX8 = 1, FOLGB_TET4 = 2 };
@@ -161,15 +166,16 @@ int folgb_loss_adjoint_plain(const folgb_plan* plan, int32_t batch,
  * evaluate the loss (a framework custom call with no scratch-buffer slot, a
  * fixed memory budget, code running inside an allocator hook).  No
  * counterpart in the reference.  Same arguments and results as
- * folgb_loss_adjoint minus the workspace: the scratch is a fixed array inside
- * the library's device image, 48 MiB on every GPU that loads the library,
- * held until exit (enough for 64^3 hex8 elasticity, batch 1: the size
- * folgb_workspace_bytes(plan, FOLGB_OP_LOSS_ADJOINT, batch) reports must fit).
- * Larger problems return FOLGB_ERR_TOO_LARGE.  The array is shared
- * by all calls on a device, so calls that overlap on the GPU race; order them
- * on one stream.  The first call on each device looks up the array's address
- * (cudaGetSymbolAddress); make it before any stream capture.  Calls no
- * allocator. */
+ * folgb_loss_adjoint minus the workspace: the scratch is a fixed 48 MiB array
+ * inside the library's device image (enough for 64^3 hex8 elasticity, batch
+ * 1: the size folgb_workspace_bytes(plan, FOLGB_OP_LOSS_ADJOINT, batch)
+ * reports must fit).  Larger problems return FOLGB_ERR_TOO_LARGE.  The array
+ * is committed on a device when the first plan is created there
+ * (folgb_plan_create looks up its address), and held until exit; create
+ * plans before any stream capture.  A call made under another CUDA context
+ * than the one the address was found in (after cudaDeviceReset) looks it up
+ * again.  The array is shared by all calls on a device, so calls that overlap
+ * on the GPU race; order them on one stream.  Calls no allocator. */
 int folgb_loss_adjoint_noalloc(const folgb_plan* plan, int32_t batch,
                                const float* control, int64_t control_stride,
                                const float* dofs, int64_t dofs_stride, int32_t apply_dirichlet,
@@ -416,6 +422,15 @@ enum {
  * under a second) and ORs 1 << FOLGB_ERR_TIMEOUT into device_status (device
  * int).  Shows that a lost copy cannot hang a kernel. */
 int folgb_selftest_bounded_wait(int32_t* device_status, void* stream);
+
+/* FP32 throughput probe (no counterpart in the reference): launches
+ * blocks_per_sm x (SM count) blocks of 256 threads, each thread running
+ * `iterations` x 8 packed-pair fused multiply-adds (independent chains), on
+ * `stream`; *flops_per_launch gets the flop count (2 per FMA).  Time it with
+ * events on the stream to measure the GPU's FP32 peak.  sink: any device
+ * float (never written in practice). */
+int folgb_fp32_peak_probe(float* sink, int32_t blocks_per_sm, int32_t iterations, double* flops_per_launch,
+                          void* stream);
 
 int folgb_trace_enable(int32_t on);
 int folgb_trace_reset(void);

@@ -3,7 +3,10 @@
 TEST INFRASTRUCTURE ONLY: used by tests/ (pinned against the NumPy oracle) and
 by bench.py's CPU-baseline and reference legs.  ``CLossOracle`` mirrors
 ``FELossOracle.batch_loss_and_grads`` (fe_loss.py:250-262 plus its adjoint) for
-the thermal and small-strain elastic physics, FP64, OpenMP over elements.
+the thermal, small-strain elastic and neo-Hookean (AD) physics, FP64, OpenMP
+over elements; ``assemble_csr`` and ``pcg`` give the FP64 assembled system
+(fe_loss.py:264-318) and its Jacobi-CG solution (fe_solver.py:60-78) for the
+full-size solve checks.
 """
 from __future__ import annotations
 
@@ -15,7 +18,7 @@ from . import build_c
 from .fe_oracle import FELossOracle, gauss_rule
 
 _ET = {"quad4": 0, "hex8": 1, "tet4": 2}
-_PH = {"thermal": 0, "elastic": 1}
+_PH = {"thermal": 0, "elastic": 1, "neohooke": 2}
 _lib = None
 
 
@@ -28,6 +31,12 @@ def load():
         lib.feo_loss_adjoint.argtypes = [C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_double, C.c_double, P,
                                          C.c_double, C.c_double, C.c_int64, P, C.c_int64, P, P, P, P, P, P, P, P,
                                          P, P, P, P, C.c_int]
+        lib.feo_assemble_csr.restype = C.c_int
+        lib.feo_assemble_csr.argtypes = [C.c_int, C.c_int, C.c_int, P, P, C.c_int, C.c_double, C.c_double, P,
+                                         C.c_double, C.c_double, C.c_int64, P, C.c_int64, P, P, P, P, P, P, P, P,
+                                         C.c_int]
+        lib.feo_pcg.restype = C.c_int64
+        lib.feo_pcg.argtypes = [C.c_int64, P, P, P, P, P, C.c_double, C.c_int64, P, P, C.c_int]
         lib.feo_max_threads.restype = C.c_int
         lib.feo_max_threads.argtypes = []
         _lib = lib
@@ -38,14 +47,34 @@ def _p(a):
     return a.ctypes.data if a is not None else None
 
 
+def pcg(indptr, indices, values, b, rtol=1e-12, maxiter=100000, threads=0):
+    """FP64 Jacobi-preconditioned CG (x0 = 0) on a CSR matrix with int32
+    pattern; stops on the true residual.  Returns (x, iterations, relative
+    residual)."""
+    lib = load()
+    ip = np.ascontiguousarray(indptr, dtype=np.int32)
+    ix = np.ascontiguousarray(indices, dtype=np.int32)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    bb = np.ascontiguousarray(b, dtype=np.float64)
+    n = len(ip) - 1
+    x = np.empty(n)
+    work = np.empty(5 * n)
+    rel = C.c_double()
+    it = lib.feo_pcg(n, _p(ip), _p(ix), _p(v), _p(bb), _p(x), float(rtol), int(maxiter), C.byref(rel), _p(work),
+                     int(threads))
+    if it < 0:
+        raise ValueError("feo_pcg: bad arguments")
+    return x, int(it), rel.value
+
+
 class CLossOracle:
-    """Same constructor arguments as FELossOracle (thermal / elastic only)."""
+    """Same constructor arguments as FELossOracle (thermal / elastic / neo-Hooke)."""
 
     def __init__(self, *args, threads: int = 0, **kw):
         self.py = FELossOracle(*args, **kw)
         o = self.py
         if o.physics not in _PH:
-            raise ValueError(f"C oracle covers thermal and elastic, not {o.physics}")
+            raise ValueError(f"C oracle covers thermal, elastic and neohooke, not {o.physics}")
         self.lib = load()
         self.threads = int(threads)
         pts, wts = gauss_rule(o.etype, o.num_gp)
@@ -94,6 +123,26 @@ class CLossOracle:
         if rc == 1:
             raise ValueError("feo_loss_adjoint: bad arguments")
         return tot.value, du, dc, rc == 2
+
+    def assemble_csr(self, ctrl, u_full, indptr, indices):
+        """FP64 BC-applied residual and Jacobian values of one instance in the
+        given canonical CSR pattern (thermal / elastic); u_full has the
+        Dirichlet values set.  Returns (residual, values)."""
+        o = self.py
+        ctrl = np.ascontiguousarray(ctrl, dtype=np.float64)
+        u = np.ascontiguousarray(u_full, dtype=np.float64)
+        ip = np.ascontiguousarray(indptr, dtype=np.int32)
+        ix = np.ascontiguousarray(indices, dtype=np.int32)
+        res = np.empty(o.total_dofs)
+        vals = np.empty(len(ix))
+        layout = 1 if o.control_layout == "element" else 0
+        rc = self.lib.feo_assemble_csr(_ET[o.etype], _PH[o.physics], len(self.gw), _p(self.gp), _p(self.gw), layout,
+                                       o.young, o.nu, _p(self.bf), o.beta, o.c, len(self.conn), _p(self.conn),
+                                       o.num_nodes, _p(self.xyz), _p(self.dmask), _p(ctrl), _p(u), _p(ip), _p(ix),
+                                       _p(res), _p(vals), self.threads)
+        if rc == 1:
+            raise ValueError("feo_assemble_csr: bad arguments or an entry outside the pattern")
+        return res, vals
 
     def batch_loss_and_grads(self, batch_ctrl, batch_u):
         """Same returns as FELossOracle.batch_loss_and_grads."""

@@ -22,9 +22,25 @@
  * points and weights (oracle/fe_oracle.py:gauss_rule) so both oracles share
  * one point order.
  *
+ * Neo-Hookean (AD variant) loss: energy = sum_gp w detJ psi(C) with
+ *   3-D psi = mu/2 (J^-2/3 I1 - 3) - mu ln J + lam/2 ln^2 J
+ *   (fol/constitutive_material_models/neo_hooke.py:129-135), 2-D
+ *   psi = mu/2 (I1 - 2) - mu ln J + lam/2 ln^2 J (:178-181), mu and lam from the
+ *   interpolated control (mechanical_neohooke_AD.py:264-267); its adjoint is
+ *   the true energy gradient sum_gp w detJ (F S) dN/dx (what jax.grad of
+ *   mechanical_neohooke_AD.py:279-293 gives) and dpsi/d(control).
+ *
  * Element loop and nodal gather run under OpenMP; the nodal gather walks a
  * node -> (element, local node) incidence list in a fixed order and the total
- * is summed serially, so results do not depend on the thread count.
+ * is summed serially, so loss and adjoint do not depend on the thread count.
+ *
+ * Also here, for the solve checks: the BC-applied residual and Jacobian
+ * assembled in FP64 into a given canonical CSR pattern
+ * (fe_loss.py:191-207, 264-318; the row-only Dirichlet rule), and FP64
+ * Jacobi-preconditioned CG on a CSR matrix (fe_solver.py:60-78 with CG, x0 = 0).
+ * The assembly adds element entries with OpenMP atomics, so its values may
+ * differ from run to run in the last bits of FP64 (far below every tolerance
+ * they are used with).
  */
 #include <math.h>
 #include <stdint.h>
@@ -34,7 +50,7 @@
 #endif
 
 enum { FEO_QUAD4 = 0, FEO_HEX8 = 1, FEO_TET4 = 2 };
-enum { FEO_THERMAL = 0, FEO_ELASTIC = 1 };
+enum { FEO_THERMAL = 0, FEO_ELASTIC = 1, FEO_NEOHOOKE = 2 };
 enum { FEO_NODAL = 0, FEO_ELEMENT = 1 };
 
 #define MAXN 8
@@ -51,6 +67,7 @@ typedef struct {
   double D[6][6];
   double bf[3];
   double beta, c;
+  double mu1, lam1; /* neo-Hooke: mu, lambda for a unit control (mechanical_neohooke_AD.py:264-267) */
 } Spec;
 
 static void shape(const Spec* s, const double* xi, double* N, double dN[MAXN][3]) {
@@ -151,7 +168,7 @@ static void strain_B(const Spec* s, double G[MAXN][3], double B[6][MAXD]) {
  * Returns 0, or 1 when detJ <= 0 at some point. */
 static inline __attribute__((always_inline)) int element(const Spec* s, const double X[MAXN][3],
                                                          const double* de, const double* ue, double* energy,
-                                                         double* re, double* gde) {
+                                                         double* re, double* gde, double* Se_out) {
   const int nen = s->nen, nd = nen * s->ndof;
   double Se[MAXD][MAXD], Fe[MAXD];
   memset(Se, 0, sizeof(Se));
@@ -216,6 +233,101 @@ static inline __attribute__((always_inline)) int element(const Spec* s, const do
     en += ue[i] * t;
   }
   *energy = en;
+  if (Se_out)
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j) Se_out[i * nd + j] = Se[i][j];
+  return bad;
+}
+
+/* 3x3 / 2x2 determinant and inverse of a symmetric matrix C (d = 2 or 3). */
+static double inv_sym(int d, const double C[3][3], double Ci[3][3]) {
+  if (d == 2) {
+    const double det = C[0][0] * C[1][1] - C[0][1] * C[1][0];
+    Ci[0][0] = C[1][1] / det;
+    Ci[1][1] = C[0][0] / det;
+    Ci[0][1] = -C[0][1] / det;
+    Ci[1][0] = -C[1][0] / det;
+    return det;
+  }
+  const double c00 = C[1][1] * C[2][2] - C[1][2] * C[2][1];
+  const double c01 = C[1][2] * C[2][0] - C[1][0] * C[2][2];
+  const double c02 = C[1][0] * C[2][1] - C[1][1] * C[2][0];
+  const double det = C[0][0] * c00 + C[0][1] * c01 + C[0][2] * c02;
+  Ci[0][0] = c00 / det;
+  Ci[1][0] = c01 / det;
+  Ci[2][0] = c02 / det;
+  Ci[0][1] = (C[0][2] * C[2][1] - C[0][1] * C[2][2]) / det;
+  Ci[1][1] = (C[0][0] * C[2][2] - C[0][2] * C[2][0]) / det;
+  Ci[2][1] = (C[0][1] * C[2][0] - C[0][0] * C[2][1]) / det;
+  Ci[0][2] = (C[0][1] * C[1][2] - C[0][2] * C[1][1]) / det;
+  Ci[1][2] = (C[0][2] * C[1][0] - C[0][0] * C[1][2]) / det;
+  Ci[2][2] = (C[0][0] * C[1][1] - C[0][1] * C[1][0]) / det;
+  return det;
+}
+
+/* Neo-Hookean (AD variant) element: energy sum_gp w detJ psi, re = the
+ * energy gradient sum_gp w detJ (F S) dN/dx, gde[a] = d energy / d de[a]. */
+static int element_nh(const Spec* s, const double X[MAXN][3], const double* de, const double* ue, double* energy,
+                      double* re, double* gde) {
+  const int nen = s->nen, d = s->dim, nd = nen * d;
+  for (int i = 0; i < nd; ++i) re[i] = 0.0;
+  for (int a = 0; a < nen; ++a) gde[a] = 0.0;
+  double en = 0.0;
+  int bad = 0;
+  for (int q = 0; q < s->ngp; ++q) {
+    double N[MAXN], dN[MAXN][3], G[MAXN][3];
+    shape(s, s->gp + 3 * q, N, dN);
+    const double detJ = global_grads(s, X, dN, G);
+    if (!(detJ > 0.0)) bad = 1;
+    const double wd = s->gw[q] * detJ;
+    double egp = 0.0;
+    for (int a = 0; a < nen; ++a) egp += de[a] * N[a];
+    const double mu = s->mu1 * egp, lam = s->lam1 * egp;
+    double F[3][3] = {{0}}, C[3][3] = {{0}}, Ci[3][3], S[3][3], P[3][3];
+    for (int k = 0; k < d; ++k) {
+      F[k][k] = 1.0;
+      for (int j = 0; j < d; ++j)
+        for (int a = 0; a < nen; ++a) F[k][j] += ue[a * d + k] * G[a][j];
+    }
+    for (int i = 0; i < d; ++i)
+      for (int j = 0; j < d; ++j)
+        for (int k = 0; k < d; ++k) C[i][j] += F[k][i] * F[k][j];
+    const double detC = inv_sym(d, C, Ci);
+    const double lnJ = 0.5 * log(detC);
+    double I1 = 0.0;
+    for (int i = 0; i < d; ++i) I1 += C[i][i];
+    double psi, dpsi_dmu;
+    if (d == 3) {
+      const double aJ = exp(-2.0 / 3.0 * lnJ);
+      psi = 0.5 * mu * (aJ * I1 - 3.0) - mu * lnJ + 0.5 * lam * lnJ * lnJ;
+      dpsi_dmu = 0.5 * (aJ * I1 - 3.0) - lnJ;
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j)
+          S[i][j] = mu * aJ * ((i == j ? 1.0 : 0.0) - I1 / 3.0 * Ci[i][j]) + (lam * lnJ - mu) * Ci[i][j];
+    } else {
+      psi = 0.5 * mu * (I1 - 2.0) - mu * lnJ + 0.5 * lam * lnJ * lnJ;
+      dpsi_dmu = 0.5 * (I1 - 2.0) - lnJ;
+      for (int i = 0; i < 2; ++i)
+        for (int j = 0; j < 2; ++j) S[i][j] = mu * ((i == j ? 1.0 : 0.0) - Ci[i][j]) + lam * lnJ * Ci[i][j];
+    }
+    const double dpsi_dlam = 0.5 * lnJ * lnJ;
+    en += wd * psi;
+    for (int k = 0; k < d; ++k)
+      for (int j = 0; j < d; ++j) {
+        double t = 0.0;
+        for (int p = 0; p < d; ++p) t += F[k][p] * S[p][j];
+        P[k][j] = t;
+      }
+    for (int a = 0; a < nen; ++a) {
+      for (int k = 0; k < d; ++k) {
+        double t = 0.0;
+        for (int j = 0; j < d; ++j) t += P[k][j] * G[a][j];
+        re[a * d + k] += wd * t;
+      }
+      gde[a] += wd * (dpsi_dmu * s->mu1 + dpsi_dlam * s->lam1) * N[a];
+    }
+  }
+  *energy = en;
   return bad;
 }
 
@@ -231,7 +343,7 @@ static inline __attribute__((always_inline)) int element(const Spec* s, const do
     s.dim = DIM;                                                                                          \
     s.ndof = NDOF;                                                                                        \
     s.nv = NV;                                                                                            \
-    return element(&s, X, de, ue, en, re, gde);                                                           \
+    return element(&s, X, de, ue, en, re, gde, NULL);                                                     \
   }
 FEO_SPECIALISE(el_quad4_th, FEO_QUAD4, FEO_THERMAL, 4, 2, 1, 3)
 FEO_SPECIALISE(el_hex8_th, FEO_HEX8, FEO_THERMAL, 8, 3, 1, 6)
@@ -239,6 +351,21 @@ FEO_SPECIALISE(el_tet4_th, FEO_TET4, FEO_THERMAL, 4, 3, 1, 6)
 FEO_SPECIALISE(el_quad4_el, FEO_QUAD4, FEO_ELASTIC, 4, 2, 2, 3)
 FEO_SPECIALISE(el_hex8_el, FEO_HEX8, FEO_ELASTIC, 8, 3, 3, 6)
 FEO_SPECIALISE(el_tet4_el, FEO_TET4, FEO_ELASTIC, 4, 3, 3, 6)
+
+#define FEO_SPECIALISE_NH(NAME, ET, NEN, DIM, NV)                                                         \
+  static int NAME(const Spec* s0, const double X[MAXN][3], const double* de, const double* ue, double* en, \
+                  double* re, double* gde) {                                                              \
+    Spec s = *s0;                                                                                         \
+    s.et = ET;                                                                                            \
+    s.nen = NEN;                                                                                          \
+    s.dim = DIM;                                                                                          \
+    s.ndof = DIM;                                                                                         \
+    s.nv = NV;                                                                                            \
+    return element_nh(&s, X, de, ue, en, re, gde);                                                        \
+  }
+FEO_SPECIALISE_NH(el_quad4_nh, FEO_QUAD4, 4, 2, 3)
+FEO_SPECIALISE_NH(el_hex8_nh, FEO_HEX8, 8, 3, 6)
+FEO_SPECIALISE_NH(el_tet4_nh, FEO_TET4, 4, 3, 6)
 
 typedef int (*ElementFn)(const Spec*, const double[MAXN][3], const double*, const double*, double*, double*,
                          double*);
@@ -250,8 +377,10 @@ static int make_spec(Spec* s, int et, int ph, int ngp, const double* gp, const d
   s->ph = ph;
   s->nen = et == FEO_HEX8 ? 8 : 4;
   s->dim = et == FEO_QUAD4 ? 2 : 3;
-  if (et < 0 || et > 2 || ph < 0 || ph > 1 || ngp <= 0) return 1;
+  if (et < 0 || et > 2 || ph < 0 || ph > 2 || ngp <= 0) return 1;
   s->ndof = ph == FEO_THERMAL ? 1 : s->dim;
+  s->mu1 = 1.0 / (2.0 * (1.0 + nu));
+  s->lam1 = nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
   s->nv = s->dim == 2 ? 3 : 6;
   s->ngp = ngp;
   s->gp = gp;
@@ -291,7 +420,9 @@ int feo_loss_adjoint(int et, int ph, int ngp, const double* gp, const double* gw
   Spec s;
   if (make_spec(&s, et, ph, ngp, gp, gw, young, nu, bf, beta, c)) return 1;
   const int nen = s.nen, ndof = s.ndof, nd = nen * ndof;
-  static const ElementFn kFns[2][3] = {{el_quad4_th, el_hex8_th, el_tet4_th}, {el_quad4_el, el_hex8_el, el_tet4_el}};
+  static const ElementFn kFns[3][3] = {{el_quad4_th, el_hex8_th, el_tet4_th},
+                                       {el_quad4_el, el_hex8_el, el_tet4_el},
+                                       {el_quad4_nh, el_hex8_nh, el_tet4_nh}};
   const ElementFn fn = kFns[ph][et];
 #ifdef _OPENMP
   if (nthreads > 0) omp_set_num_threads(nthreads);
@@ -333,6 +464,163 @@ int feo_loss_adjoint(int et, int ph, int ngp, const double* gp, const double* gw
     }
   }
   return bad ? 2 : 0;
+}
+
+/* Position of column `col` in CSR row `row` (binary search of the sorted
+ * column indices), or -1. */
+static int64_t csr_find(const int32_t* rowptr, const int32_t* colind, int64_t row, int64_t col) {
+  int64_t lo = rowptr[row], hi = rowptr[row + 1] - 1;
+  while (lo <= hi) {
+    const int64_t mid = (lo + hi) >> 1;
+    if (colind[mid] < col) lo = mid + 1;
+    else if (colind[mid] > col) hi = mid - 1;
+    else return mid;
+  }
+  return -1;
+}
+
+/* ComputeJacobianMatrixAndResidualVector (fe_loss.py:264-318) in FP64 for the
+ * thermal and small-strain elastic elements: element residuals and matrices
+ * with the row-only Dirichlet rule (fe_loss.py:191-207: a Dirichlet row keeps
+ * only the element diagonal, its residual is zero), summed into the given
+ * canonical CSR pattern (rowptr[rows+1], sorted colind).  dmask (ndof*N): 1
+ * on Dirichlet dofs.  u: full dof vector.  Outputs residual (ndof*N) and
+ * values (nnz).  Returns 0, 1 for bad arguments or an entry outside the
+ * pattern, 2 when an element has detJ <= 0. */
+int feo_assemble_csr(int et, int ph, int ngp, const double* gp, const double* gw, int layout, double young,
+                     double nu, const double* bf, double beta, double c, int64_t E, const int64_t* conn, int64_t N,
+                     const double* xyz, const uint8_t* dmask, const double* ctrl, const double* u,
+                     const int32_t* rowptr, const int32_t* colind, double* residual, double* values, int nthreads) {
+  Spec s;
+  if (make_spec(&s, et, ph, ngp, gp, gw, young, nu, bf, beta, c) || ph == FEO_NEOHOOKE) return 1;
+  const int nen = s.nen, ndof = s.ndof, nd = nen * ndof;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  const int64_t ndofs = ndof * N;
+  memset(residual, 0, sizeof(double) * ndofs);
+  memset(values, 0, sizeof(double) * rowptr[ndofs]);
+  int bad = 0, miss = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad, miss)
+  for (int64_t e = 0; e < E; ++e) {
+    double X[MAXN][3], de[MAXN], ue[MAXD], re[MAXD], gde[MAXN], Se[MAXD * MAXD], en;
+    int64_t dof[MAXD];
+    for (int a = 0; a < nen; ++a) {
+      const int64_t n = conn[e * nen + a];
+      for (int k = 0; k < 3; ++k) X[a][k] = xyz[3 * n + k];
+      de[a] = layout == FEO_ELEMENT ? ctrl[e] : ctrl[n];
+      for (int cc = 0; cc < ndof; ++cc) {
+        dof[a * ndof + cc] = ndof * n + cc;
+        ue[a * ndof + cc] = u[ndof * n + cc];
+      }
+    }
+    bad |= element(&s, X, de, ue, &en, re, gde, Se);
+    for (int i = 0; i < nd; ++i) {
+      const int64_t r = dof[i];
+      const int keep_row = !dmask[r];
+      if (keep_row) {
+#pragma omp atomic
+        residual[r] += re[i];
+      }
+      for (int j = 0; j < nd; ++j) {
+        double v = Se[i * nd + j];
+        if (!keep_row) v = (i == j) ? v : 0.0;
+        if (v == 0.0 && !(i == j)) continue;
+        const int64_t pos = csr_find(rowptr, colind, r, dof[j]);
+        if (pos < 0) {
+          miss = 1;
+          continue;
+        }
+#pragma omp atomic
+        values[pos] += v;
+      }
+    }
+  }
+  if (miss) return 1;
+  return bad ? 2 : 0;
+}
+
+/* FP64 Jacobi-preconditioned CG with x0 = 0 on a CSR matrix (rows x rows,
+ * int32 pattern, double values): stops when the true residual
+ * ||b - A x|| <= rtol ||b|| (the recurrence residual is replaced by b - A x
+ * every 50 iterations and whenever it reaches the tolerance) or at maxiter.
+ * Writes x; returns the iteration count, -1 for bad arguments. */
+int64_t feo_pcg(int64_t rows, const int32_t* rowptr, const int32_t* colind, const double* values, const double* b,
+                double* x, double rtol, int64_t maxiter, double* rel_residual, double* work, int nthreads) {
+  if (rows <= 0 || !rowptr || !colind || !values || !b || !x || !work) return -1;
+#ifdef _OPENMP
+  if (nthreads > 0) omp_set_num_threads(nthreads);
+#else
+  (void)nthreads;
+#endif
+  double *r = work, *z = work + rows, *p = work + 2 * rows, *q = work + 3 * rows, *dinv = work + 4 * rows;
+  double bn = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : bn)
+  for (int64_t i = 0; i < rows; ++i) {
+    double d = 0.0;
+    for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k)
+      if (colind[k] == i) d = values[k];
+    dinv[i] = d != 0.0 ? 1.0 / d : 0.0;
+    x[i] = 0.0;
+    r[i] = b[i];
+    z[i] = dinv[i] * r[i];
+    p[i] = z[i];
+    bn += b[i] * b[i];
+  }
+  bn = sqrt(bn);
+  if (rel_residual) *rel_residual = 0.0;
+  if (bn == 0.0) return 0;
+  double rz = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rz)
+  for (int64_t i = 0; i < rows; ++i) rz += r[i] * z[i];
+  int64_t it = 0;
+  double rn = bn;
+  while (it < maxiter) {
+    ++it;
+    double pq = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : pq)
+    for (int64_t i = 0; i < rows; ++i) {
+      double t = 0.0;
+      for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) t += values[k] * p[colind[k]];
+      q[i] = t;
+      pq += p[i] * t;
+    }
+    const double alpha = rz / pq;
+    double rr = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rr)
+    for (int64_t i = 0; i < rows; ++i) {
+      x[i] += alpha * p[i];
+      r[i] -= alpha * q[i];
+      rr += r[i] * r[i];
+    }
+    /* the true residual b - A x every 50 iterations and before stopping */
+    if ((it % 50) == 0 || sqrt(rr) <= rtol * bn) {
+      rr = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rr)
+      for (int64_t i = 0; i < rows; ++i) {
+        double t = b[i];
+        for (int32_t k = rowptr[i]; k < rowptr[i + 1]; ++k) t -= values[k] * x[colind[k]];
+        r[i] = t;
+        rr += t * t;
+      }
+    }
+    rn = sqrt(rr);
+    if (rn <= rtol * bn) break;
+    double rz_new = 0.0;
+#pragma omp parallel for schedule(static) reduction(+ : rz_new)
+    for (int64_t i = 0; i < rows; ++i) {
+      z[i] = dinv[i] * r[i];
+      rz_new += r[i] * z[i];
+    }
+    const double beta_ = rz_new / rz;
+    rz = rz_new;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < rows; ++i) p[i] = z[i] + beta_ * p[i];
+  }
+  if (rel_residual) *rel_residual = rn / bn;
+  return it;
 }
 
 int feo_max_threads(void) {

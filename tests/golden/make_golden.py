@@ -7,7 +7,7 @@ file into this directory.  Each array records the ``file:line`` it came from.
 
 Run it where the reference checkout is present::
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <path of the folax checkout>
 
 The fixtures are committed; nothing at test time reads the reference.
 """
@@ -184,4 +184,6 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py <path of the folax checkout>")
+    main(sys.argv[1])

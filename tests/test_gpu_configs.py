@@ -1,0 +1,105 @@
+"""Parity at the configured sizes the benchmark reports, against FP64 oracles.
+
+* 64^3 hex8 two-phase elasticity, CSR assembly + Jacobi-PCG to rtol 1e-8:
+  the returned solution against an FP64 CG (C oracle, rtol 1e-12) of the same
+  assembled system (the solver's error, bound 1e-6), and against the FP64
+  solution of the FP64-assembled system (the whole fp32 pipeline).  The
+  second error is dominated by storing the matrix in fp32: it is compared
+  with the error of an FP64 solve whose only approximation is the FP64
+  matrix rounded to fp32.
+* 6-tet split of 64^3 (1,572,864 tets), neo-Hookean, batch 16: losses and
+  both gradients of two instances against the C oracle (1e-5).
+* 512 uneven quad4 thermal instances (the benchmark's seed): losses and both
+  gradients of every instance against the C oracle (1e-5).
+The FP64 oracle errors measured here are printed (pytest -s shows them)."""
+import numpy as np
+import pytest
+
+from gpu_cases import c_oracle_loss, gpu_loss, rel_fro
+from folax_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def test_c1_pcg_64cubed_solution_against_fp64(cuda):
+    torch = cuda
+    from folax_gb300.loss import MechanicalLoss3DHexa
+    from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
+    from oracle import c_oracle
+    mesh, settings, E, _ = workloads.hex8_elastic(64, 2024)
+    loss = MechanicalLoss3DHexa("c1", dict(settings), mesh)
+    loss.Initialize()
+    u0 = loss.ApplyDirichletBCOnDofVector(torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda"))
+    ctrl = torch.tensor(E, device="cuda")
+    jac, r = loss.ComputeJacobianMatrixAndResidualVector(ctrl, u0)
+    solver = FiniteElementLinearResidualBasedSolver("c1", loss, {"linear_solver_settings": {
+        "solver": "GB300-pcg", "tol": 1e-8, "maxiter": 20000, "check_every": 64}})
+    solver.Initialize()
+    dx = solver.LinearSolve(jac, r).double().cpu().numpy()
+    loss.CheckDeviceStatus()
+    assert solver.last_linear_info["status"] == 0
+    indptr, indices = jac.indptr.cpu().numpy(), jac.indices.cpu().numpy()
+    A32 = jac.data.double().cpu().numpy()
+    r32 = r.double().cpu().numpy()
+    # (a) the solver: FP64 CG of the same fp32 system
+    x_a, it_a, rel_a = c_oracle.pcg(indptr, indices, A32, -r32, rtol=1e-12)
+    assert rel_a <= 1e-12
+    err_solver = rel_fro(dx, x_a)
+    # (b) the pipeline: FP64 assembly + FP64 CG, and the fp32-rounding floor
+    cl = c_oracle_loss("hex8", "elastic", mesh, settings)
+    u_full = cl.py.full_dof_vector(np.zeros(cl.py.total_dofs))
+    R64, V64 = cl.assemble_csr(E.astype(np.float64), u_full, indptr, indices)
+    assert rel_fro(r32, R64) < TOL and rel_fro(A32, V64) < TOL
+    x_b, _, rel_b = c_oracle.pcg(indptr, indices, V64, -R64, rtol=1e-12)
+    assert rel_b <= 1e-12
+    V_rounded = V64.astype(np.float32).astype(np.float64)
+    x_c, _, _ = c_oracle.pcg(indptr, indices, V_rounded, -R64, rtol=1e-12)
+    err_pipeline = rel_fro(dx, x_b)
+    err_floor = rel_fro(x_c, x_b)
+    print(f"\nC1 64^3: PCG iterations {solver.last_linear_info['iterations']}, "
+          f"error vs FP64 CG of the same system {err_solver:.3e}, vs the FP64 pipeline {err_pipeline:.3e}, "
+          f"fp32-rounded FP64 matrix alone {err_floor:.3e}")
+    assert err_solver <= 1e-6
+    assert err_pipeline <= 2.0 * err_floor + 1e-6
+
+
+def test_c4_neohooke_64cubed_batch16_against_c_oracle(cuda):
+    from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
+    mesh, settings, E, U = workloads.neohooke_tets(64, 16, 2024)
+    loss = NeoHookeMechanicalLoss3DTetra("c4", dict(settings), mesh)
+    loss.Initialize()
+    _, _, losses, du, dE = loss.ComputeBatchLossAndGrad(E, U)
+    loss.CheckDeviceStatus()
+    losses, du, dE = losses.cpu().numpy(), du.cpu().numpy(), dE.cpu().numpy()
+    cl = c_oracle_loss("tet4", "neohooke", mesh, settings)
+    B = len(U)
+    for i in (0, 9):
+        tot, g, gc, bad = cl.loss_adjoint(E[i].astype(np.float64), cl.py.full_dof_vector(U[i].astype(np.float64)))
+        assert not bad
+        errs = (rel_fro(losses[i], tot), rel_fro(du[i] * B, g), rel_fro(dE[i] * B, gc))
+        print(f"\nC4 instance {i}: loss {errs[0]:.2e}, dL/du {errs[1]:.2e}, dL/dE {errs[2]:.2e}")
+        assert max(errs) < TOL, errs
+
+
+def test_c3_512_instances_against_c_oracle(cuda):
+    torch = cuda
+    from folax_gb300.batched import BatchedFELoss
+    meshes, settings, ks = workloads.thermal_instances(512, 11)
+    bl = BatchedFELoss("quad", "thermal", meshes, settings, elements_per_tile=2048)
+    ctrl = np.concatenate(ks)
+    T = torch.rand(bl.total_dofs, device="cuda", generator=torch.Generator(device="cuda").manual_seed(11))
+    _, losses, du, dc = bl.ComputeLossAndGrad(torch.tensor(ctrl, dtype=torch.float32, device="cuda"), T)
+    losses, du, dc, T = losses.cpu().numpy(), du.cpu().numpy(), dc.cpu().numpy(), T.cpu().numpy()
+    I = len(meshes)
+    worst = np.zeros(3)
+    for i, m in enumerate(meshes):
+        cl = c_oracle_loss("quad4", "thermal", m, settings)
+        a, b = bl.dof_offsets[i], bl.dof_offsets[i + 1]
+        c0, c1 = bl.control_offsets[i], bl.control_offsets[i + 1]
+        tot, g, gc, bad = cl.loss_adjoint(ks[i], cl.py.full_dof_vector(T[a:b].astype(np.float64)))
+        assert not bad
+        errs = np.array([rel_fro(losses[i], tot), rel_fro(du[a:b] * I, g), rel_fro(dc[c0:c1] * I, gc)])
+        worst = np.maximum(worst, errs)
+    print(f"\nC3 512 instances, worst over instances: loss {worst[0]:.2e}, dL/dT {worst[1]:.2e}, dL/dk {worst[2]:.2e}")
+    assert worst.max() < TOL, worst

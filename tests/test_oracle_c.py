@@ -3,7 +3,9 @@
 The NumPy oracle is pinned on the reference's golden vectors; these cases pin
 the C restatement to it on jittered meshes of every element type, both control
 layouts, body force, the loss exponent and the thermal nonlinearity, and check
-that the result does not depend on the OpenMP thread count."""
+that the result does not depend on the OpenMP thread count.  The FP64 CSR
+assembly is checked against the NumPy oracle's canonical CSR, the FP64 CG
+against a direct solve."""
 import numpy as np
 import pytest
 
@@ -31,7 +33,8 @@ def _pair(etype, physics, layout="nodal", exponent=1.0, bf=None, **extra):
 
 
 @pytest.mark.parametrize("etype,physics", [("quad4", "thermal"), ("hex8", "thermal"), ("tet4", "thermal"),
-                                           ("quad4", "elastic"), ("hex8", "elastic"), ("tet4", "elastic")])
+                                           ("quad4", "elastic"), ("hex8", "elastic"), ("tet4", "elastic"),
+                                           ("quad4", "neohooke"), ("hex8", "neohooke"), ("tet4", "neohooke")])
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 def test_c_oracle_matches_numpy(etype, physics, layout):
     L, Lc, ctrl, u = _pair(etype, physics, layout)
@@ -71,3 +74,27 @@ def test_c_oracle_thread_count_invariant():
     b = Lc.loss_adjoint(ctrl, uf)
     assert a[0] == b[0]
     assert np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
+
+
+@pytest.mark.parametrize("etype,physics", [("quad4", "thermal"), ("hex8", "elastic"), ("tet4", "elastic"),
+                                           ("hex8", "thermal"), ("quad4", "elastic")])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_c_oracle_csr_assembly_matches_numpy(etype, physics, layout):
+    L, Lc, ctrl, u = _pair(etype, physics, layout)
+    uf = L.full_dof_vector(u)
+    A, R = L.csr(ctrl, uf)
+    res, vals = Lc.assemble_csr(ctrl, uf, A.indptr, A.indices)
+    assert _rel(res, R) < 1e-12
+    assert _rel(vals, A.data) < 1e-12
+
+
+def test_c_oracle_pcg_matches_direct_solve():
+    import scipy.sparse.linalg as spla
+    from oracle import fe_oracle as fo
+    L, Lc, ctrl, u = _pair("hex8", "elastic", "element")
+    A, R = L.csr(ctrl, L.full_dof_vector(np.zeros_like(u)))
+    x_ref = fo.direct_solve(A, -R)
+    x, it, rel = c_oracle.pcg(A.indptr, A.indices, A.data, -R, rtol=1e-13)
+    assert it > 0 and rel <= 1e-13
+    assert _rel(x, x_ref) < 1e-10
+    assert np.linalg.norm(A @ x + R) <= 1.0001e-13 * np.linalg.norm(R)

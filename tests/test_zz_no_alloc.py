@@ -79,3 +79,40 @@ def test_noalloc_rejects_problems_larger_than_its_scratch(cuda):
     u = np.zeros((B, loss.GetTotalNumberOfDOFs()))
     rc, *_ = _call(torch, lib, loss, ctrl, u, noalloc=True)
     assert rc == _capi.ERR_TOO_LARGE
+
+
+def test_noalloc_limit_covers_64cubed_hex8_and_rejects_one_instance_more(cuda):
+    """The stated guarantee (64^3 hex8 elasticity, batch 1, fits the fixed
+    scratch) for both control layouts, and the boundary: the largest batch
+    that fits runs and matches the workspace entry point, one instance more
+    is refused before any work."""
+    from folax_gb300 import _capi
+    from folax_gb300.loss import MechanicalLoss3DHexa
+    from folax_gb300.mesh import create_3D_box_mesh
+    torch = cuda
+    lib = _capi.load()
+    limit = 48 << 20
+    m64 = create_3D_box_mesh(64, 64, 64)
+    for layout in ("element", "nodal"):
+        loss = MechanicalLoss3DHexa("l64", {"dirichlet_bc_dict": bc_dict("hex8", "elastic"),
+                                            "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3},
+                                            "control_layout": layout, "num_gp": 2}, m64)
+        loss.Initialize()
+        need = lib.folgb_workspace_bytes(loss._plan.handle, _capi.OP_LOSS_ADJOINT, 1)
+        assert 0 < need <= limit, (layout, need)
+        del loss
+    loss = _case("hex8", "elastic", 16, "element", seed=35)
+    ws = lambda b: lib.folgb_workspace_bytes(loss._plan.handle, _capi.OP_LOSS_ADJOINT, b)
+    B = 1
+    while ws(B + 1) <= limit:
+        B += 1
+    rng = np.random.default_rng(36)
+    ctrl = 0.5 + rng.random((1, loss.GetNumberOfControls()))
+    u = (0.03 / 16) * rng.standard_normal((B + 1, loss.GetTotalNumberOfDOFs()))
+    rc, *_ = _call(torch, lib, loss, ctrl, u, noalloc=True)
+    assert rc == _capi.ERR_TOO_LARGE
+    rc_n, st_n, *out_n = _call(torch, lib, loss, ctrl, u[:B], noalloc=True)
+    rc_w, st_w, *out_w = _call(torch, lib, loss, ctrl, u[:B], noalloc=False)
+    assert rc_n == _capi.OK and rc_w == _capi.OK and st_n == 0 and st_w == 0
+    for a, b in zip(out_n, out_w):
+        assert rel_fro(a, b) < TOL
