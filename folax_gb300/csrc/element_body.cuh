@@ -95,6 +95,10 @@ struct VecArgs {
   float exponent, inv_batch;
   int* status;
   int stream_rec = 0;  // 1: records larger than L2; store them evict-first (__stcs)
+  // tile-local kernels write the finished nodes' gradients themselves
+  float* out = nullptr;          // [B][out_stride] dLoss/d dofs
+  int64_t out_stride = 0;
+  float* dctrl_nodal = nullptr;  // [B][N] nodal control gradient (nodal layout)
 };
 
 __device__ __forceinline__ void load_gp_table(GPTable& dst, const GPTable* src) {
@@ -583,4 +587,5 @@ __device__ __forceinline__ void report_bad(int bad, int* status) {
 namespace folgb {
 // sum-factorised hex8 2x2x2 elasticity (hex8_fused.cu); returns 1 if launched
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s);
+int launch_tile_boundary(const folgb_plan* p, const VecArgs& A, int B, cudaStream_t s, int pdl);
 }  // namespace folgb

@@ -764,7 +764,11 @@ static int elem_tiles(int64_t nb, int B) {
   return t;
 }
 // partial-sum slots: enough for the smallest element-kernel block (64 threads)
-static int loss_partial_slots(const folgb_plan* p) { return (int)((p->E + 63) / 64); }
+// and for one per tile of the tile-local kernel
+static int loss_partial_slots(const folgb_plan* p) {
+  const int blocks = (int)((p->E + 63) / 64);
+  return blocks > p->tiles ? blocks : p->tiles;
+}
 
 // record width of the loss path: ndof components (+ the nodal control sensitivity)
 static int loss_rec(const folgb_plan* p) { return loss_record(p); }
@@ -773,7 +777,10 @@ static size_t layout_loss(const folgb_plan* p, int B, bool plain, void* base, si
   Bump bp(base, cap);
   const int64_t ND = (int64_t)p->nen * p->ndof;
   const int rec = loss_rec(p);
-  float* g = bp.take<float>((size_t)B * p->E * p->nen * rec);
+  // element records of the node gather, or the boundary partial records of
+  // the tile-local kernel (4 floats per slot): the same region serves both
+  const size_t recs = (size_t)B * p->E * p->nen * rec, parts = (size_t)B * p->tile_boundary_slots * 4;
+  float* g = bp.take<float>(recs > parts ? recs : parts);
   float* partials = bp.take<float>((size_t)B * loss_partial_slots(p));
   unsigned* counters = bp.take<unsigned>((size_t)B);
   float* scale = bp.take<float>((size_t)B);
@@ -964,8 +971,12 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
   VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
                             elem_ctrl ? dloss_dcontrol : nullptr, device_status);
+  A.out = dloss_ddofs;
+  A.out_stride = (int64_t)p->ndof * p->N;
+  A.dctrl_nodal = elem_ctrl ? nullptr : dloss_dcontrol;
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
-  if (p->phys.kernel_variant != 1 && launch_hex8_fast(p, A, grid, MODE_LOSS, s)) {
+  const int fast = p->phys.kernel_variant != 1 ? launch_hex8_fast(p, A, grid, MODE_LOSS, s) : 0;
+  if (fast) {
     FOLGB_LAUNCH_CHECK();
   } else {
     rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
@@ -986,7 +997,9 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     });
   }
   if (rc) return rc;
-  if (dloss_ddofs || dloss_dcontrol) {
+  if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
+    rc = launch_tile_boundary(p, A, B, s, trace_active() ? 0 : 1);
+  } else if (dloss_ddofs || dloss_dcontrol) {
     rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
                        elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr,

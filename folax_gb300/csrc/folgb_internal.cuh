@@ -80,6 +80,28 @@ struct folgb_plan {
   folgb::GPTable* d_gp = nullptr;
   std::vector<int64_t> dir_dofs;
   std::vector<double> dir_vals;
+  // Element tiles of the tile-local fused loss (tiles.cu): elements grouped
+  // into tiles of at most kTileElems elements and kTileNodes distinct nodes
+  // (Morton order of the centroids, closed greedily); per tile its elements,
+  // its distinct ("local") nodes, boundary ones first, and for each local
+  // node the shared-memory records that contribute to it.
+  int tiles = 0;                        // 0: no tile tables (other element types / physics)
+  int64_t tile_local_nodes = 0;         // K: local node slots over all tiles
+  int64_t tile_boundary_slots = 0;      // S: boundary local node slots (partial records per instance)
+  int64_t tile_boundary_nodes = 0;      // NB: nodes in 0 or more than 1 tile
+  int64_t tile_interior_nodes = 0;      // NI: nodes inside exactly one tile
+  int* d_tile_eptr = nullptr;           // [T+1] element range of each tile (tile order)
+  int* d_tile_nptr = nullptr;           // [T+1] local node range of each tile
+  int* d_tile_bptr = nullptr;           // [T+1] boundary slot range of each tile (its first local nodes)
+  int* d_t_elem = nullptr;              // [E] element ids in tile order
+  unsigned char* d_t_lconn = nullptr;   // [E][nen] local node ids, reference node order
+  unsigned short* d_tc_pos = nullptr;   // [E*nen] record position a*kTileElems + e_local, grouped by local node
+  int* d_tn_gid = nullptr;              // [K] global node id of each local node
+  unsigned short* d_tn_cend = nullptr;  // [K] end of the local node's records in tc_pos (tile-relative)
+  int* d_bn_node = nullptr;             // [NB] boundary nodes
+  int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
+  int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
+  int* d_in_node = nullptr;             // [NI] interior nodes (rescaled when the loss exponent is not 1)
   // CSR tables
   bool has_csr = false;
   int64_t P = 0, nnz = 0, rows = 0;
@@ -130,6 +152,12 @@ int num_sms();
 
 // Looks up the no-alloc scratch array on the current device (noalloc.cu).
 void noalloc_prepare_current_device();
+
+// Element tiles of the tile-local fused loss (tiles.cu).
+constexpr int kTileElems = 128;  // elements per tile at most (one thread each)
+constexpr int kTileNodes = 256;  // distinct nodes per tile at most (8-bit local ids)
+int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz);
+void free_tile_tables(folgb_plan* p);
 
 // Element-result records: one per (instance, element, node), [b][a][e],
 // padded to 1, 2 or 4 floats so the gather reads them with one vector load.

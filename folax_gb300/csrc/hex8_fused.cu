@@ -16,6 +16,7 @@
 //
 // Node order (hexahedra_3d_8.py:79-87) -> lexicographic (xi fastest):
 //   lex = [0, 1, 3, 2, 4, 5, 7, 6]   (node 2 is (+,+,-), node 3 is (-,+,-), ...)
+#include <algorithm>
 #include <atomic>
 #include <type_traits>
 
@@ -148,40 +149,24 @@ __device__ __forceinline__ float2 det_inv_pair(const float2 (&J)[3][3], float2 (
 //          (20 per SM) and 80 give 6 (24 per SM), at the price of spills;
 //   TMA:   the persistent k_hex8_elastic_tma below (connectivity streamed
 //          into shared memory by bulk copies), 4 or 5 blocks per SM.
-// One element: gathers, the 8 Gauss points, the adjoint, the records.
-// nodes[] are the element's node ids in the reference's local order.
-template <int CL, int MODE, bool BF, int ACC>
-__device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b, const int64_t e,
-                                                  const int (&nodes)[8], float& energy, int& bad) {
+// The element math on gathered values: X and U are the coordinates and
+// displacements at the 8 nodes in lexicographic order (LEX), egp the nodal
+// controls (CL nodal, lexicographic) or the element control (egp[0]).  Adds
+// the element energy to `energy`; g gets the residual (adjoint) per
+// lexicographic node, wsed the Gauss-point weights w detJ sed (nodal
+// controls), sedsum sum_q w detJ sed (element control); bad gets bit 0 for a
+// non-positive detJ.  X and U are overwritten (transformed in place).
+template <int CL, bool BF, int ACC>
+__device__ __forceinline__ void hex8_elastic_core(const MatConst& mt, float (&X)[3][8], float (&U)[3][8],
+                                                  float (&egp)[CL == FOLGB_CONTROL_NODAL ? 8 : 1], float& energy,
+                                                  float& sedsum, float (&wsed)[CL == FOLGB_CONTROL_NODAL ? 8 : 1],
+                                                  float (&g)[8][3], int& bad) {
   {
-    constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
-    const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
-    const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
-    const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
-    float X[3][8], U[3][8];
-    float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
-#pragma unroll
-    for (int L = 0; L < 8; ++L) {
-      const int n = nodes[LEX[L]];
-      const float4 x = __ldg(A.xyz4 + n);
-      X[0][L] = x.x;
-      X[1][L] = x.y;
-      X[2][L] = x.z;
-      const unsigned m = bc ? __ldg(A.dmask + n) : 0u;
-#pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        const int64_t d = 3 * (int64_t)n + c;
-        U[c][L] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
-      }
-      if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = __ldg(ctrl + n);
-    }
-    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
-    else egp[0] = __ldg(ctrl + e);
     float bfe = 0.f;  // u . b at the nodes, weighted below (body force only)
     float ub[BF ? 8 : 1];
     if constexpr (BF) {
 #pragma unroll
-      for (int L = 0; L < 8; ++L) ub[L] = U[0][L] * A.mat.bf[0] + U[1][L] * A.mat.bf[1] + U[2][L] * A.mat.bf[2];
+      for (int L = 0; L < 8; ++L) ub[L] = U[0][L] * mt.bf[0] + U[1][L] * mt.bf[1] + U[2][L] * mt.bf[2];
     }
     // reference derivatives of the geometry and of the displacement
     // (ACC 2 forms the coordinate derivatives only for non-affine elements)
@@ -207,10 +192,7 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
         for (int k = 0; k < 8; ++k) Dd[i][k] = 0.f;
       }
     }
-    float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
     float wdet[BF ? 8 : 1];
-    float sedsum = 0.f;
-    const MatConst& mt = A.mat;
     if constexpr (ACC == 2) {
       // Gauss points in pairs q = (0|1) + 2 ty + 4 tz: dxi is shared by the pair,
       // deta / dzeta and every per-point quantity are packed (t_xi = 0, 1)
@@ -402,7 +384,6 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
     }
     }  // ACC != 2
     // adjoint: per component, dual Hadamard coefficients then the transposed transform
-    float g[8][3];
     const float s = 0.125f, sg_ = 0.125f * kG, sg2 = 0.125f * kG2;
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -454,6 +435,42 @@ __device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b,
       }
       energy -= bfe;
     }
+  }
+}
+
+// One element: gathers, the 8 Gauss points, the adjoint, the records.
+// nodes[] are the element's node ids in the reference's local order.
+template <int CL, int MODE, bool BF, int ACC>
+__device__ __forceinline__ void hex8_elastic_elem(const VecArgs& A, const int b, const int64_t e,
+                                                  const int (&nodes)[8], float& energy, int& bad) {
+  {
+    constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
+    const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+    const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+    const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
+    float X[3][8], U[3][8];
+    float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+#pragma unroll
+    for (int L = 0; L < 8; ++L) {
+      const int n = nodes[LEX[L]];
+      const float4 x = __ldg(A.xyz4 + n);
+      X[0][L] = x.x;
+      X[1][L] = x.y;
+      X[2][L] = x.z;
+      const unsigned m = bc ? __ldg(A.dmask + n) : 0u;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int64_t d = 3 * (int64_t)n + c;
+        U[c][L] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+      }
+      if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = __ldg(ctrl + n);
+    }
+    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
+    else egp[0] = __ldg(ctrl + e);
+    float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+    float g[8][3];
+    float sedsum = 0.f;
+    hex8_elastic_core<CL, BF, ACC>(A.mat, X, U, egp, energy, sedsum, wsed, g, bad);
     if (!isfinite(energy)) bad |= 2;
     // 16-byte records, local-node-major ([b][a][e]): the 3 vector components
     // and the nodal control sensitivity (or padding); for each local node the
@@ -676,6 +693,222 @@ static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tile-local fused loss + adjoint (tiles.cu builds the tables).  One block of
+// kTileElems threads per (tile, instance):
+//   1. the tile's distinct nodes (coordinates, dofs with the Dirichlet values
+//      substituted, nodal controls) are loaded cooperatively into shared
+//      memory: one load of each node per tile instead of one per element;
+//   2. each thread evaluates one element from shared memory and stores its 8
+//      residual records (+ nodal control sensitivity) in shared memory,
+//      corner-major so a warp's stores are conflict-free;
+//   3. each local node sums its records in a fixed order; a node inside this
+//      tile only writes its gradient directly, a node on the tile boundary
+//      writes one partial record to global memory for k_tile_boundary.
+// The element's energy goes through the fixed-order block/tile reduction.
+// With a loss exponent other than 1 the gradients are written unscaled and
+// k_tile_boundary scales them once the loss is known.
+struct TileArgs {
+  int ntiles;
+  int64_t S;  // boundary slots per instance
+  const int* tile_eptr;
+  const int* tile_nptr;
+  const int* tile_bptr;
+  const int* t_elem;
+  const uint2* t_lconn;
+  const unsigned short* tc_pos;
+  const int* tn_gid;
+  const unsigned short* tn_cend;
+  const int* bn_node;
+  const int* bn_ptr;
+  const int* bn_slot;
+  const int* in_node;
+  int64_t nb_nodes, ni_nodes;
+};
+
+template <int CL, bool BF, int MINB>
+__global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const VecArgs A, const TileArgs T) {
+  __shared__ float4 sX[kTileNodes];
+  __shared__ float4 sU[kTileNodes];  // displacements, nodal control in w
+  __shared__ unsigned char sM[kTileNodes];
+  __shared__ float4 sR[8 * kTileElems];
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  pdl_launch_dependents();
+  const int tile = blockIdx.x, b = blockIdx.y;
+  const int e0 = __ldg(T.tile_eptr + tile), ne = __ldg(T.tile_eptr + tile + 1) - e0;
+  const int n0 = __ldg(T.tile_nptr + tile), nl = __ldg(T.tile_nptr + tile + 1) - n0;
+  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+  if (threadIdx.x == 0) wcount = 0u;
+  for (int k = threadIdx.x; k < nl; k += kTileElems) {
+    const int n = __ldg(T.tn_gid + n0 + k);
+    const float4 x = __ldg(A.xyz4 + n);
+    const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
+    float u[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t d = 3 * (int64_t)n + c;
+      u[c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+    }
+    sX[k] = x;
+    sU[k] = make_float4(u[0], u[1], u[2], CL == FOLGB_CONTROL_NODAL ? __ldg(ctrl + n) : 0.f);
+    sM[k] = (unsigned char)m;
+  }
+  __syncthreads();
+  float energy = 0.f;
+  int bad = 0;
+  const int t = threadIdx.x;
+  if (t < ne) {
+    constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
+    const int e = __ldg(T.t_elem + e0 + t);
+    const uint2 lc = __ldg(T.t_lconn + e0 + t);
+    const int loc[8] = {(int)(lc.x & 0xff), (int)((lc.x >> 8) & 0xff), (int)((lc.x >> 16) & 0xff), (int)(lc.x >> 24),
+                        (int)(lc.y & 0xff), (int)((lc.y >> 8) & 0xff), (int)((lc.y >> 16) & 0xff), (int)(lc.y >> 24)};
+    float X[3][8], U[3][8];
+    float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+#pragma unroll
+    for (int L = 0; L < 8; ++L) {
+      const int k = loc[LEX[L]];
+      const float4 x = sX[k], u = sU[k];
+      X[0][L] = x.x;
+      X[1][L] = x.y;
+      X[2][L] = x.z;
+      U[0][L] = u.x;
+      U[1][L] = u.y;
+      U[2][L] = u.z;
+      if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = u.w;
+    }
+    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
+    else egp[0] = __ldg(ctrl + e);
+    float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+    float g[8][3];
+    float sedsum = 0.f;
+    hex8_elastic_core<CL, BF, 2>(A.mat, X, U, egp, energy, sedsum, wsed, g, bad);
+    if (!isfinite(energy)) bad |= 2;
+    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(wsed);
+#pragma unroll
+    for (int L = 0; L < 8; ++L) {
+      float w = 0.f;
+      if constexpr (CL == FOLGB_CONTROL_NODAL) w = wsed[L];
+      sR[LEX[L] * kTileElems + t] = make_float4(g[L][0], g[L][1], g[L][2], w);
+    }
+    if (CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
+      A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
+  }
+  __syncthreads();
+  const int bbase = __ldg(T.tile_bptr + tile), nb = __ldg(T.tile_bptr + tile + 1) - bbase;
+  const float sc = (A.exponent == 1.f) ? A.inv_batch : 1.f;
+  const unsigned short* cp = T.tc_pos + (int64_t)e0 * 8;
+  float4* bpart = reinterpret_cast<float4*>(A.g) + (int64_t)b * T.S;
+  for (int k = threadIdx.x; k < nl; k += kTileElems) {
+    const int c0 = k == 0 ? 0 : (int)__ldg(T.tn_cend + n0 + k - 1), c1 = __ldg(T.tn_cend + n0 + k);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = c0; j < c1; ++j) {
+      const float4 r = sR[__ldg(cp + j)];
+      acc.x += r.x;
+      acc.y += r.y;
+      acc.z += r.z;
+      acc.w += r.w;
+    }
+    if (k < nb) {
+      bpart[bbase + k] = acc;
+    } else {
+      const int n = __ldg(T.tn_gid + n0 + k);
+      const unsigned m = sM[k];
+      if (A.out) {
+        float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
+        o[0] = (m & 1u) ? 0.f : sc * acc.x;
+        o[1] = (m & 2u) ? 0.f : sc * acc.y;
+        o[2] = (m & 4u) ? 0.f : sc * acc.z;
+      }
+      if (CL == FOLGB_CONTROL_NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = sc * acc.w;
+    }
+  }
+  finish_loss_warp(energy, bad, A, b, wsum, &wcount, tile, T.ntiles);
+}
+
+// The nodes on tile boundaries (and nodes of no element): the partial
+// records of their tiles summed in ascending tile order, scaled and written.
+// With a loss exponent other than 1 it also scales what the tile kernel wrote
+// unscaled (interior nodes, element control gradients).  Launched as a
+// programmatic dependent of the tile kernel.
+template <bool NODAL>
+__global__ void __launch_bounds__(256) k_tile_boundary(const VecArgs A, const TileArgs T, int rescale) {
+  const int b = blockIdx.y;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  const int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const float4* bpart = reinterpret_cast<const float4*>(A.g) + (int64_t)b * T.S;
+  pdl_wait_primary();
+  const float sc = (A.exponent == 1.f) ? A.inv_batch : A.scale[b];
+  for (int64_t i = i0; i < T.nb_nodes; i += stride) {
+    const int n = __ldg(T.bn_node + i);
+    const int s0 = __ldg(T.bn_ptr + i), s1 = __ldg(T.bn_ptr + i + 1);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = s0; j < s1; ++j) {
+      const float4 r = bpart[__ldg(T.bn_slot + j)];
+      acc.x += r.x;
+      acc.y += r.y;
+      acc.z += r.z;
+      acc.w += r.w;
+    }
+    if (A.out) {
+      const unsigned m = __ldg(A.dmask + n);
+      float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
+      o[0] = (m & 1u) ? 0.f : sc * acc.x;
+      o[1] = (m & 2u) ? 0.f : sc * acc.y;
+      o[2] = (m & 4u) ? 0.f : sc * acc.z;
+    }
+    if (NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = sc * acc.w;
+  }
+  if (!rescale) return;
+  for (int64_t i = i0; i < T.ni_nodes; i += stride) {
+    const int n = __ldg(T.in_node + i);
+    if (A.out) {
+      float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
+      o[0] *= sc;
+      o[1] *= sc;
+      o[2] *= sc;
+    }
+    if (NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] *= sc;
+  }
+  if (!NODAL && A.dctrl_elem)
+    for (int64_t e = i0; e < A.E; e += stride) A.dctrl_elem[(int64_t)b * A.E + e] *= sc;
+}
+
+static TileArgs tile_args(const folgb_plan* p) {
+  TileArgs T;
+  T.ntiles = p->tiles;
+  T.S = p->tile_boundary_slots;
+  T.tile_eptr = p->d_tile_eptr;
+  T.tile_nptr = p->d_tile_nptr;
+  T.tile_bptr = p->d_tile_bptr;
+  T.t_elem = p->d_t_elem;
+  T.t_lconn = reinterpret_cast<const uint2*>(p->d_t_lconn);
+  T.tc_pos = p->d_tc_pos;
+  T.tn_gid = p->d_tn_gid;
+  T.tn_cend = p->d_tn_cend;
+  T.bn_node = p->d_bn_node;
+  T.bn_ptr = p->d_bn_ptr;
+  T.bn_slot = p->d_bn_slot;
+  T.in_node = p->d_in_node;
+  T.nb_nodes = p->tile_boundary_nodes;
+  T.ni_nodes = p->tile_interior_nodes;
+  return T;
+}
+
+template <int CL, int MINB>
+static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, cudaStream_t s) {
+  const TileArgs T = tile_args(p);
+  dim3 grid((unsigned)p->tiles, (unsigned)B);
+  if (bf) k_hex8_elastic_tile<CL, true, MINB><<<grid, kTileElems, 0, s>>>(A, T);
+  else k_hex8_elastic_tile<CL, false, MINB><<<grid, kTileElems, 0, s>>>(A, T);
+}
+
+// Variants of the tile-local kernel: index - kHex8TileFirst -> blocks per SM
+// of its register budget (4: 128 registers, 5: 102).
+constexpr int kHex8TileFirst = 18;
+
 template <int CL, int MODE>
 static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cudaStream_t s) {
   switch (variant) {
@@ -700,19 +933,35 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
   }
 }
 
-// Number of sum-factorised variants the autotuner may choose from.
-constexpr int kHex8Variants = 18;
+// Number of sum-factorised variants the autotuner may choose from: 0..17
+// one element per thread with global records, 18..19 tile-local.
+constexpr int kHex8Variants = 20;
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's
 // block count is recomputed for the variant's block size; the caller's
 // partial-sum buffers are sized for the smallest block (64 threads).
+// Returns 2 when the tile-local kernel ran (the caller then finishes with
+// launch_tile_boundary instead of the node gather).  The residual path
+// (MODE_RESIDUAL, records for the node gather) runs variant 11 in place of a
+// tile-local variant.
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2) return 0;
-  const int variant = p->hex8_variant;
+  int variant = p->hex8_variant;
   const bool bf = p->mat.has_bf != 0;
+  const bool tile = variant >= kHex8TileFirst && p->tiles > 0;
+  if (variant >= kHex8TileFirst && (mode != MODE_LOSS || !tile)) variant = 11;
   trace_begin(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
-  if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
+  if (mode == MODE_LOSS && tile) {
+    const bool minb5 = variant == kHex8TileFirst + 1;
+    if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
+      if (minb5) launch_tile<FOLGB_CONTROL_NODAL, 5>(p, A, (int)grid.y, bf, s);
+      else launch_tile<FOLGB_CONTROL_NODAL, 4>(p, A, (int)grid.y, bf, s);
+    } else {
+      if (minb5) launch_tile<FOLGB_CONTROL_ELEMENT, 5>(p, A, (int)grid.y, bf, s);
+      else launch_tile<FOLGB_CONTROL_ELEMENT, 4>(p, A, (int)grid.y, bf, s);
+    }
+  } else if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
     if (mode == MODE_LOSS) launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_LOSS>(A, grid, bf, variant, s);
     else launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_RESIDUAL>(A, grid, bf, variant, s);
   } else {
@@ -720,7 +969,31 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
     else launch_cl_mode<FOLGB_CONTROL_ELEMENT, MODE_RESIDUAL>(A, grid, bf, variant, s);
   }
   trace_end(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
-  return 1;
+  return (mode == MODE_LOSS && tile) ? 2 : 1;
+}
+
+// Second launch of the tile-local path (the nodes shared by tiles), as a
+// programmatic dependent of the tile kernel when pdl != 0.
+int launch_tile_boundary(const folgb_plan* p, const VecArgs& A, int B, cudaStream_t s, int pdl) {
+  const TileArgs T = tile_args(p);
+  const int rescale = A.exponent != 1.f ? 1 : 0;
+  int64_t work = rescale ? std::max<int64_t>(std::max<int64_t>(T.nb_nodes, T.ni_nodes), A.E) : T.nb_nodes;
+  int blocks = (int)std::min<int64_t>((work + 255) / 256, (int64_t)num_sms() * 8);
+  if (blocks < 1) blocks = 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks, (unsigned)B);
+  cfg.blockDim = dim3(256);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  trace_begin(KID_GATHER, s);
+  if (p->ctrl_layout == FOLGB_CONTROL_NODAL) FOLGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_tile_boundary<true>, A, T, rescale));
+  else FOLGB_CUDA_TRY(cudaLaunchKernelEx(&cfg, k_tile_boundary<false>, A, T, rescale));
+  trace_end(KID_GATHER, s);
+  return FOLGB_OK;
 }
 
 int hex8_variant_count() { return kHex8Variants; }

@@ -373,6 +373,12 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     folgb_plan_destroy(p);
     return rc;
   }
+  // tile tables of the tile-local fused kernel (hex8 elasticity, 2x2x2 Gauss)
+  if (p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && phys->num_gp == 2 &&
+      (rc = build_tile_tables(p, c32, xyz))) {
+    folgb_plan_destroy(p);
+    return rc;
+  }
   noalloc_prepare_current_device();
   *out = p;
   return FOLGB_OK;
@@ -386,6 +392,7 @@ extern "C" int folgb_plan_destroy(folgb_plan* p) {
                   p->d_pair_slot};
   for (void* q : ptrs)
     if (q) cudaFree(q);
+  free_tile_tables(p);
   delete p;
   return FOLGB_OK;
 }

@@ -35,7 +35,7 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 18
+HEX8_VARIANTS = 20
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
                       "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
                       "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
@@ -46,7 +46,9 @@ HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, du
                       "persistent, TMA-staged rows, 96 regs, paired points (f32x2)",
                       "persistent, TMA-staged rows, 96 regs, point sums",
                       "persistent, TMA-staged rows, next tile's nodes prefetched to L1, paired points (f32x2)",
-                      "persistent, TMA-staged rows, next tile's nodes prefetched to L2, paired points (f32x2)"]
+                      "persistent, TMA-staged rows, next tile's nodes prefetched to L2, paired points (f32x2)",
+                      "tile-local: nodes staged and residuals summed in shared memory, paired points (f32x2)",
+                      "tile-local, 96 regs, paired points (f32x2)"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 

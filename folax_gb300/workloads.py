@@ -16,7 +16,9 @@ folax_gb300.fields (numpy.random.default_rng; the seeds are arguments).
                      with its own Fourier conductivity.
 * neohooke_tets      the 6-tet split of an n^3 hex grid, neo-Hookean (AD),
                      one two-phase field per instance (seed + i), dofs =
-                     uniaxial field plus N(0, 0.002^2) noise per instance.
+                     uniaxial field plus N(0, (0.01 h)^2) noise per instance
+                     (h = 1/n: displacement-gradient noise of about 0.01, so
+                     every tet keeps det F > 0 and the log terms stay finite).
 """
 from __future__ import annotations
 
@@ -82,5 +84,5 @@ def neohooke_tets(n: int = 64, batch: int = 16, seed: int = 2024):
     rng = np.random.default_rng(seed)
     u = np.zeros((batch, mesh.GetNumberOfNodes(), 3), dtype=np.float32)
     u[:, :, 2] = 0.05 * mesh.nodes_coordinates[None, :, 2]
-    u += (0.002 * rng.standard_normal(u.shape)).astype(np.float32)
+    u += ((0.01 / n) * rng.standard_normal(u.shape)).astype(np.float32)
     return mesh, settings, E, u.reshape(batch, -1)

@@ -129,6 +129,58 @@ def test_hex8_every_variant_matches_oracle(cuda, variant, layout, mesh_kind):
         assert rel_fro(x.cpu().numpy(), z) < TOL
 
 
+def _renumbered(m, seed, isolated=2):
+    """The same mesh with its nodes and elements in a random order and
+    `isolated` extra nodes that no element uses (their gradients must be 0)."""
+    rng = np.random.default_rng(seed)
+    X = m.nodes_coordinates
+    N = len(X)
+    perm = rng.permutation(N)          # new id -> old id
+    inv = np.empty(N, dtype=np.int64)
+    inv[perm] = np.arange(N)
+    conn = m.elements_nodes["hexahedron"]
+    conn = inv[conn][rng.permutation(len(conn))]
+    m.nodes_coordinates = np.concatenate([X[perm], 0.5 + 0.01 * rng.standard_normal((isolated, 3))])
+    m.elements_nodes = {"hexahedron": conn}
+    m.node_sets = {k: np.sort(inv[np.asarray(v)]) for k, v in m.node_sets.items()}
+    m.node_ids = np.arange(len(m.nodes_coordinates))
+    return m
+
+
+@pytest.mark.parametrize("variant", [18, 19])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+@pytest.mark.parametrize("exponent,bf", [(1.0, None), (1.5, [0.2, 0.0, -0.1])])
+@pytest.mark.parametrize("order", ["structured", "renumbered"])
+def test_hex8_tile_kernel_many_tiles(cuda, variant, layout, exponent, bf, order):
+    """The tile-local kernel over many tiles (12^3 jittered hex mesh: about
+    14 tiles of up to 128 elements, most nodes shared by several tiles), in
+    the mesh's own order and with nodes and elements renumbered at random
+    plus two nodes no element uses; the loss exponent 1.5 takes the deferred
+    scaling path."""
+    m = make_mesh("hex8", 12, seed=41, jitter=0.1)
+    if order == "renumbered":
+        m = _renumbered(m, seed=42)
+    s = _settings("hex8", "elastic", layout, exponent, bf)
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(43)
+    ctrl = 0.5 + rng.random((3, gl.GetNumberOfControls()))
+    u = 0.004 * rng.standard_normal((3, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+    if order == "renumbered":
+        du = a[3].cpu().numpy()
+        assert np.all(du[:, -6:] == 0.0)
+        if layout == "nodal":
+            assert np.all(a[4].cpu().numpy()[:, -2:] == 0.0)
+    b = gl.ComputeBatchLossAndGrad(ctrl, u)
+    for x, y in zip(a[2:], b[2:]):
+        assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+
+
 @pytest.mark.parametrize("tma,twin", [(13, 11), (15, 6), (16, 11), (17, 11)])
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 def test_tma_variant_equals_its_per_thread_twin(cuda, tma, twin, layout):
