@@ -93,6 +93,7 @@ PROTOTYPES = {
     "folgb_bicgstab": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
     "folgb_krylov": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz,
                                vp]),
+    "folgb_krylov_async": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, vp, vp, vp, vp, sz, vp]),
     "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
     "folgb_newton_workspace_bytes": (sz, [vp, C.POINTER(NewtonSettings)]),
     "folgb_newton": (C.c_int, [vp, vp, vp, C.POINTER(NewtonSettings), C.POINTER(NewtonInfo), vp, vp, vp, sz, vp]),

@@ -102,6 +102,8 @@ struct folgb_plan {
   int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
   int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
   int* d_in_node = nullptr;             // [NI] interior nodes (rescaled when the loss exponent is not 1)
+  // instantiated Krylov solve graphs of folgb_krylov_async (krylov.cu)
+  void* krylov_graphs = nullptr;
   // CSR tables
   bool has_csr = false;
   int64_t P = 0, nnz = 0, rows = 0;
@@ -158,6 +160,8 @@ constexpr int kTileElems = 128;  // elements per tile at most (one thread each)
 constexpr int kTileNodes = 256;  // distinct nodes per tile at most (8-bit local ids)
 int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz);
 void free_tile_tables(folgb_plan* p);
+// Destroys the plan's cached Krylov solve graphs (krylov.cu).
+void free_krylov_graphs(folgb_plan* p);
 
 // Element-result records: one per (instance, element, node), [b][a][e],
 // padded to 1, 2 or 4 floats so the gather reads them with one vector load.

@@ -21,6 +21,7 @@
 // "replace" are set, so the host enqueues a chunk of iterations and reads
 // the flags once per chunk.
 #include <cmath>
+#include <mutex>
 #include <type_traits>
 
 #include <cooperative_groups.h>
@@ -39,6 +40,12 @@ struct KScalars {
 };
 // done: 1 converged (true residual), 2 maxiter, 3 non-finite, 4 repeated breakdown or divergence
 
+// Outcome of a solve as the stream-ordered entry point reports it.
+struct KReport {
+  int32_t iterations, status;
+  double rel_residual;
+};
+
 // Krylov vectors in VT (float, or double for ill-conditioned / indefinite
 // systems such as the Neo-Hookean tangent); the iterate is always fp64.
 template <class VT>
@@ -49,6 +56,7 @@ struct KWork {
   double* part;              // [2][65536]
   unsigned* counters;        // [8]
   KScalars* sc;
+  KReport* report;           // outcome of the synchronous entry points
 };
 
 constexpr int kVecBlocks = 1024;
@@ -81,6 +89,7 @@ static size_t layout_krylov(const folgb_plan* p, void* base, size_t cap, KWork<V
   t.part = bp.take<double>(2 * 65536);
   t.counters = bp.take<unsigned>(8);
   t.sc = bp.take<KScalars>(1);
+  t.report = bp.take<KReport>(1);
   if (w) *w = t;
   return align_up(bp.off);
 }
@@ -181,8 +190,10 @@ __device__ __forceinline__ bool rows_multi(int64_t N, const int* __restrict__ ad
       const bool on = w < len[u];
       m[u] = on ? __ldg(adj + a0[u] + j) : 0;
       const float* vr = vals + (int64_t)NDOF * NDOF * a0[u] + w;
+      // the values are read once per product: stream them evict-first so
+      // they do not push the vectors and the adjacency out of L2
 #pragma unroll
-      for (int i = 0; i < NDOF; ++i) v[u][i] = on ? __ldg(vr + (int64_t)i * len[u]) : 0.f;
+      for (int i = 0; i < NDOF; ++i) v[u][i] = on ? __ldcs(vr + (int64_t)i * len[u]) : 0.f;
     }
     T xv[U];
 #pragma unroll
@@ -1034,9 +1045,12 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
 }
 
 // capture_sc != NULL: s is being captured into a graph (the device-resident
-// Newton solve); the solve is enqueued as init + one WHILE node over
-// [K iterations, true residual, loop control] + the fp32 copy of x, with no
+// Newton solve, the cached graphs of krylov_async); the solve is enqueued as
+// init + one WHILE node over [K iterations, true residual, loop control] (or
+// one cluster launch for small fp32 systems) + the fp32 copy of x, with no
 // host synchronisation, and *capture_sc receives the solver's device scalars.
+// capture_sc == NULL: the host-driven loop (one flag read per check_every
+// iterations), used while kernel tracing is on.
 template <class VT>
 static int krylov_solve(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
                         float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
@@ -1108,11 +1122,6 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
       };
       const int K = (check_every + 1) & ~1;
       const int max_rounds = 4 * (maxiter / K + 8);
-      // Device-resident solve: the whole iteration loop is one CUDA graph (a
-      // WHILE node over [K iterations, true residual, loop control]), launched
-      // once; the host reads the scalars at the end only.  Not while tracing
-      // (the events would be captured) or while the caller's stream is being
-      // captured itself; any graph API failure falls back to the host loop.
       auto cluster_args = [&]() {
         ClusterArgs<VT> ca;
         ca.N = p->N;
@@ -1186,63 +1195,11 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
         *capture_sc = w.sc;
         return (int)FOLGB_OK;
       }
-      cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-      bool resident = !trace_active() && cudaStreamIsCapturing(s, &cap) == cudaSuccess &&
-                      cap == cudaStreamCaptureStatusNone;
-      // small systems: the whole solve in one cluster launch (fp32 vectors:
-      // with fp64 vectors the per-nonzero fp64 arithmetic of a few SMs is
-      // slower than the all-SM multi-kernel path)
-      if (resident && n <= kClusterMaxDofs && sizeof(VT) == sizeof(float)) {
-        ClusterArgs<VT> ca = cluster_args();
-        if (launch_cluster_solver<NDOF, G, VT>(solver, ca, s)) {
-          FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
-          FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
-          return (int)FOLGB_OK;
-        }
-      }
-      if (resident) {
-        cudaStream_t cs = nullptr;
-        cudaGraph_t g = nullptr;
-        cudaGraphExec_t exec = nullptr;
-        bool ok = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) == cudaSuccess &&
-                  cudaGraphCreate(&g, 0) == cudaSuccess;
-        cudaGraphConditionalHandle loop{};
-        cudaGraph_t body = nullptr;
-        if (ok) ok = cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault) == cudaSuccess;
-        if (ok) {
-          cudaGraphNodeParams np{};
-          np.type = cudaGraphNodeTypeConditional;
-          np.conditional.handle = loop;
-          np.conditional.type = cudaGraphCondTypeWhile;
-          np.conditional.size = 1;
-          cudaGraphNode_t node;
-          ok = cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) == cudaSuccess;
-          if (ok) body = np.conditional.phGraph_out[0];
-        }
-        if (ok) ok = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0,
-                                                   cudaStreamCaptureModeThreadLocal) == cudaSuccess;
-        if (ok) {
-          chunk(K, cs);
-          true_residual(cs);
-          k_krylov_continue<<<1, 32, 0, cs>>>(w.sc, loop, maxiter, max_rounds);
-          cudaGraph_t captured = nullptr;
-          const bool launched_ok = cudaGetLastError() == cudaSuccess;
-          ok = cudaStreamEndCapture(cs, &captured) == cudaSuccess && launched_ok;
-        }
-        if (ok) ok = cudaGraphInstantiate(&exec, g, 0) == cudaSuccess;
-        if (ok) {
-          FOLGB_CUDA_TRY(cudaGraphLaunch(exec, s));
-          FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
-          FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
-        }
-        if (exec) cudaGraphExecDestroy(exec);
-        if (g) cudaGraphDestroy(g);
-        if (cs) cudaStreamDestroy(cs);
-        cudaGetLastError();  // a failed graph set-up is not the caller's error
-        resident = ok;
-      }
+      // host-driven loop (the synchronous entry points while kernel tracing
+      // is on: every launch gets its events); otherwise the solve is a cached
+      // graph (krylov_async)
       int guard = 0;
-      while (!resident) {
+      while (true) {
         chunk(check_every, s);
         FOLGB_LAUNCH_CHECK();
         FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.sc, sizeof(KScalars), cudaMemcpyDeviceToHost, s));
@@ -1278,6 +1235,144 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
   return FOLGB_OK;
 }
 
+__global__ void k_krylov_report(const KScalars* sc, int32_t* iterations, double* rel_residual, int32_t* status) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (iterations) *iterations = sc->iters;
+  if (rel_residual) *rel_residual = sc->bnorm2 > 0.0 ? sqrt(sc->rnorm2 / sc->bnorm2) : 0.0;
+  if (status) *status = sc->done == 3 ? FOLGB_ERR_NAN : (sc->done == 1 ? FOLGB_OK : FOLGB_ERR_NOT_CONVERGED);
+}
+
+// Instantiated solve graphs of one plan, keyed by everything the graph bakes
+// in (buffers, method, precision, tolerance, iteration limits, device); the
+// oldest entry is dropped past kKrylovGraphs.
+struct KrylovGraphKey {
+  const void* ptrs[9];
+  int solver, vbits, maxiter, check_every, device;
+  double rtol;
+  bool operator==(const KrylovGraphKey& o) const {
+    for (int i = 0; i < 9; ++i)
+      if (ptrs[i] != o.ptrs[i]) return false;
+    return solver == o.solver && vbits == o.vbits && maxiter == o.maxiter && check_every == o.check_every &&
+           device == o.device && rtol == o.rtol;
+  }
+};
+struct KrylovGraphs {
+  std::mutex mu;
+  std::vector<std::pair<KrylovGraphKey, cudaGraphExec_t>> entries;
+};
+constexpr size_t kKrylovGraphs = 8;
+
+void free_krylov_graphs(folgb_plan* p) {
+  auto* c = static_cast<KrylovGraphs*>(p->krylov_graphs);
+  if (!c) return;
+  for (auto& e : c->entries) cudaGraphExecDestroy(e.second);
+  delete c;
+  p->krylov_graphs = nullptr;
+}
+
+static std::mutex g_krylov_cache_create;
+
+// Enqueues the whole solve on s with no host synchronisation: init, the WHILE
+// loop, the fp32 copy of x and the report into the caller's device buffers.
+// A stream under capture gets the nodes added to its graph; otherwise the
+// solve runs as a cached instantiated graph (built on the first call with
+// these arguments: capture on a private stream + instantiate).
+template <class VT>
+static int krylov_async(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
+                        float* x, double rtol, int maxiter, int check_every, int32_t* d_iterations,
+                        double* d_rel_residual, int32_t* d_status, void* workspace, size_t workspace_bytes,
+                        cudaStream_t s) {
+  if (!p || !vals || !dinv || !rhs || !x || maxiter <= 0 || !(rtol >= 0.0)) return FOLGB_ERR_INVALID_ARGUMENT;
+  if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
+  if (!workspace || workspace_bytes < layout_krylov<VT>(p, nullptr, 0, nullptr)) return FOLGB_ERR_WORKSPACE;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  FOLGB_CUDA_TRY(cudaStreamIsCapturing(s, &cap));
+  if (cap == cudaStreamCaptureStatusActive) {
+    KScalars* sc = nullptr;
+    int rc = krylov_solve<VT>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, nullptr, nullptr, workspace,
+                              workspace_bytes, s, &sc);
+    if (rc) return rc;
+    k_krylov_report<<<1, 32, 0, s>>>(sc, d_iterations, d_rel_residual, d_status);
+    FOLGB_LAUNCH_CHECK();
+    return FOLGB_OK;
+  }
+  KrylovGraphKey key{};
+  const void* ptrs[9] = {vals, dinv, rhs, x, workspace, d_iterations, d_rel_residual, d_status,
+                         reinterpret_cast<const void*>(workspace_bytes)};
+  for (int i = 0; i < 9; ++i) key.ptrs[i] = ptrs[i];
+  key.solver = solver;
+  key.vbits = (int)(8 * sizeof(VT));
+  key.maxiter = maxiter;
+  key.check_every = check_every;
+  key.rtol = rtol;
+  FOLGB_CUDA_TRY(cudaGetDevice(&key.device));
+  folgb_plan* mp = const_cast<folgb_plan*>(p);  // the cache is the plan's only mutable state
+  {
+    std::lock_guard<std::mutex> g(g_krylov_cache_create);
+    if (!mp->krylov_graphs) mp->krylov_graphs = new KrylovGraphs();
+  }
+  auto* cache = static_cast<KrylovGraphs*>(mp->krylov_graphs);
+  std::lock_guard<std::mutex> lock(cache->mu);
+  cudaGraphExec_t exec = nullptr;
+  for (auto& e : cache->entries)
+    if (e.first == key) exec = e.second;
+  if (!exec) {
+    cudaStream_t cs = nullptr;
+    FOLGB_CUDA_TRY(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    int rc = FOLGB_OK;
+    cudaGraph_t graph = nullptr;
+    if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      rc = FOLGB_ERR_CUDA;
+    } else {
+      KScalars* sc = nullptr;
+      rc = krylov_solve<VT>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, nullptr, nullptr, workspace,
+                            workspace_bytes, cs, &sc);
+      if (rc == FOLGB_OK) {
+        k_krylov_report<<<1, 32, 0, cs>>>(sc, d_iterations, d_rel_residual, d_status);
+        if (cudaGetLastError() != cudaSuccess) rc = FOLGB_ERR_CUDA;
+      }
+      if (cudaStreamEndCapture(cs, &graph) != cudaSuccess && rc == FOLGB_OK) rc = FOLGB_ERR_CUDA;
+    }
+    if (rc == FOLGB_OK && cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) rc = FOLGB_ERR_CUDA;
+    if (graph) cudaGraphDestroy(graph);
+    cudaStreamDestroy(cs);
+    if (rc) {
+      cudaGetLastError();
+      return rc;
+    }
+    if (cache->entries.size() >= kKrylovGraphs) {
+      cudaGraphExecDestroy(cache->entries.front().second);
+      cache->entries.erase(cache->entries.begin());
+    }
+    cache->entries.emplace_back(key, exec);
+  }
+  FOLGB_CUDA_TRY(cudaGraphLaunch(exec, s));
+  return FOLGB_OK;
+}
+
+// The synchronous entry points: the stream-ordered solve, then one read of
+// its report (or, while kernel tracing is on, the host-driven loop).
+template <class VT>
+static int krylov_sync(const folgb_plan* p, int solver, const float* vals, const float* dinv, const float* rhs,
+                       float* x, double rtol, int maxiter, int check_every, int32_t* iterations,
+                       double* rel_residual, void* workspace, size_t workspace_bytes, cudaStream_t s) {
+  if (trace_active())
+    return krylov_solve<VT>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                            workspace, workspace_bytes, s);
+  KWork<VT> w;
+  if (!p || !workspace || workspace_bytes < layout_krylov<VT>(p, workspace, workspace_bytes, &w))
+    return p ? FOLGB_ERR_WORKSPACE : FOLGB_ERR_INVALID_ARGUMENT;
+  int rc = krylov_async<VT>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, &w.report->iterations,
+                            &w.report->rel_residual, &w.report->status, workspace, workspace_bytes, s);
+  if (rc) return rc;
+  KReport host{};
+  FOLGB_CUDA_TRY(cudaMemcpyAsync(&host, w.report, sizeof(KReport), cudaMemcpyDeviceToHost, s));
+  FOLGB_CUDA_TRY(cudaStreamSynchronize(s));
+  if (iterations) *iterations = host.iterations;
+  if (rel_residual) *rel_residual = host.rel_residual;
+  return host.status;
+}
+
 }  // namespace folgb
 
 using namespace folgb;
@@ -1300,15 +1395,15 @@ extern "C" int folgb_spmv(const folgb_plan* p, const float* vals, const float* x
 extern "C" int folgb_pcg(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
                          double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations, double* rel_residual,
                          void* workspace, size_t workspace_bytes, void* stream) {
-  return krylov_solve<float>(p, SOLVER_CG, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
-                      workspace, workspace_bytes, (cudaStream_t)stream);
+  return krylov_sync<float>(p, SOLVER_CG, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                            workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int folgb_bicgstab(const folgb_plan* p, const float* vals, const float* dinv, const float* rhs, float* x,
                               double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
                               double* rel_residual, void* workspace, size_t workspace_bytes, void* stream) {
-  return krylov_solve<float>(p, SOLVER_BICGSTAB, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations,
-                             rel_residual, workspace, workspace_bytes, (cudaStream_t)stream);
+  return krylov_sync<float>(p, SOLVER_BICGSTAB, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations,
+                            rel_residual, workspace, workspace_bytes, (cudaStream_t)stream);
 }
 
 extern "C" int folgb_krylov(const folgb_plan* p, int32_t method, int32_t vector_bits, const float* vals,
@@ -1318,11 +1413,27 @@ extern "C" int folgb_krylov(const folgb_plan* p, int32_t method, int32_t vector_
   if (method != FOLGB_KRYLOV_CG && method != FOLGB_KRYLOV_BICGSTAB) return FOLGB_ERR_INVALID_ARGUMENT;
   const int solver = method == FOLGB_KRYLOV_CG ? SOLVER_CG : SOLVER_BICGSTAB;
   if (vector_bits == 32)
-    return krylov_solve<float>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
-                               workspace, workspace_bytes, (cudaStream_t)stream);
+    return krylov_sync<float>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                              workspace, workspace_bytes, (cudaStream_t)stream);
   if (vector_bits == 64)
-    return krylov_solve<double>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
-                                workspace, workspace_bytes, (cudaStream_t)stream);
+    return krylov_sync<double>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
+                               workspace, workspace_bytes, (cudaStream_t)stream);
+  return FOLGB_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int folgb_krylov_async(const folgb_plan* p, int32_t method, int32_t vector_bits, const float* vals,
+                                  const float* dinv, const float* rhs, float* x, double rtol, int32_t maxiter,
+                                  int32_t check_every, int32_t* d_iterations, double* d_rel_residual,
+                                  int32_t* d_status, void* workspace, size_t workspace_bytes, void* stream) {
+  if (method != FOLGB_KRYLOV_CG && method != FOLGB_KRYLOV_BICGSTAB) return FOLGB_ERR_INVALID_ARGUMENT;
+  const int solver = method == FOLGB_KRYLOV_CG ? SOLVER_CG : SOLVER_BICGSTAB;
+  if (check_every <= 0) check_every = 32;
+  if (vector_bits == 32)
+    return krylov_async<float>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, d_iterations,
+                               d_rel_residual, d_status, workspace, workspace_bytes, (cudaStream_t)stream);
+  if (vector_bits == 64)
+    return krylov_async<double>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, d_iterations,
+                                d_rel_residual, d_status, workspace, workspace_bytes, (cudaStream_t)stream);
   return FOLGB_ERR_INVALID_ARGUMENT;
 }
 

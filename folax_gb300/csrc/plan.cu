@@ -393,6 +393,7 @@ extern "C" int folgb_plan_destroy(folgb_plan* p) {
   for (void* q : ptrs)
     if (q) cudaFree(q);
   free_tile_tables(p);
+  free_krylov_graphs(p);
   delete p;
   return FOLGB_OK;
 }

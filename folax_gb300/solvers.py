@@ -91,9 +91,18 @@ class FiniteElementSolver(Solver):
     def _krylov(self, method, tangent_matrix, residual_vector):
         torch = _torch()
         plan = tangent_matrix.plan
-        b = -_dev(residual_vector)
-        x = torch.empty_like(b)
         bits = self._vector_bits()
+        # fixed right-hand-side and solution buffers per plan: the library
+        # caches the instantiated solve graph per set of buffers, so repeated
+        # solves on one plan launch the cached graph
+        bufs = getattr(self, "_krylov_bufs", None)
+        if bufs is None or bufs[0] is not plan:
+            n = plan.total_dofs
+            bufs = (plan, torch.empty(n, dtype=torch.float32, device="cuda"),
+                    torch.empty(n, dtype=torch.float32, device="cuda"))
+            self._krylov_bufs = bufs
+        _, b, x = bufs
+        torch.neg(_dev(residual_vector).reshape(-1), out=b)
         ws = plan.workspace(capi.OP_KRYLOV64 if bits == 64 else capi.OP_PCG)
         iters, rel = C.c_int32(), C.c_double()
         s = self.linear_solver_settings
@@ -106,7 +115,7 @@ class FiniteElementSolver(Solver):
                                  "status": rc, "vector_bits": bits}
         if rc not in (capi.OK, capi.ERR_NOT_CONVERGED):
             capi.check(name, rc)
-        return x
+        return x.clone()
 
     def PCGLinearSolver(self, tangent_matrix, residual_vector, dofs_vector=None):
         """Solve tangent_matrix dx = -residual with Jacobi-PCG (x0 = 0); returns dx."""

@@ -228,9 +228,11 @@ int folgb_assemble(const folgb_plan* plan, const float* control, const float* do
  * definite systems.  Matrix and Krylov vectors FP32, inner products, norms and
  * the iterate FP64; reliable updates recompute the true residual b - A x in
  * FP64, and convergence (||b - A x|| <= rtol ||rhs||) is judged on it.
- * The call returns after the solve: it reads the device flags every
- * check_every iterations.  Returns FOLGB_ERR_NOT_CONVERGED at maxiter (x holds
- * the last iterate).  iterations / rel_residual may be NULL. */
+ * The call returns after the solve: it runs folgb_krylov_async and reads its
+ * report (while kernel tracing is on, a host-driven loop that reads the
+ * device flags every check_every iterations instead).  Returns
+ * FOLGB_ERR_NOT_CONVERGED at maxiter (x holds the last iterate).
+ * iterations / rel_residual may be NULL. */
 int folgb_pcg(const folgb_plan* plan, const float* csr_values, const float* inv_diag,
               const float* rhs, float* x, double rtol, int32_t maxiter, int32_t check_every,
               int32_t* iterations, double* rel_residual,
@@ -257,6 +259,29 @@ int folgb_krylov(const folgb_plan* plan, int32_t method, int32_t vector_bits,
                  const float* csr_values, const float* inv_diag, const float* rhs, float* x,
                  double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
                  double* rel_residual, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Stream-ordered folgb_krylov, for callers that must not block (an XLA FFI
+ * LinearSolve handler on XLA's stream; fe_solver.py:60-78 is the reference
+ * call, kr_small_displacement_element.cc:315-337 the handler precedent, whose
+ * handlers enqueue their work on the given stream and return an error code).
+ * Enqueues the whole solve on `stream` and returns: no host synchronisation,
+ * no allocation.  The outcome goes to caller DEVICE buffers (any may be
+ * NULL): *d_iterations, *d_rel_residual (true residual of the fp64 iterate)
+ * and *d_status (FOLGB_OK, FOLGB_ERR_NOT_CONVERGED or FOLGB_ERR_NAN).  The
+ * return value reports argument and launch errors only.
+ * The solve runs as an instantiated CUDA graph (init, a WHILE node over
+ * chunks of check_every iterations with the true-residual check, the fp32
+ * copy of x, the report), built on the first call with a given set of
+ * buffers, method, precision, rtol, maxiter and check_every and cached in the
+ * plan (the 8 most recent sets); later calls with the same arguments launch
+ * the cached graph.  On a stream that is being captured the same nodes are
+ * added to the caller's graph instead.  Workspace as folgb_krylov; calls that
+ * share a workspace must be ordered on one stream. */
+int folgb_krylov_async(const folgb_plan* plan, int32_t method, int32_t vector_bits,
+                       const float* csr_values, const float* inv_diag, const float* rhs, float* x,
+                       double rtol, int32_t maxiter, int32_t check_every, int32_t* d_iterations,
+                       double* d_rel_residual, int32_t* d_status, void* workspace,
+                       size_t workspace_bytes, void* stream);
 
 /* ---- device-resident Newton-Raphson with load stepping --------------------
  * FiniteElementNonLinearResidualBasedSolver.Solve

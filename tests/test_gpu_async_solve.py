@@ -1,0 +1,123 @@
+"""Stream-ordered Krylov solves (folgb_krylov_async) through the C ABI.
+
+Two solves queued back to back on one stream with no host wait between them
+give bit for bit the results of the synchronous entry point; the outcome
+(iterations, true residual, status) lands in device buffers; a repeated call
+with the same buffers launches the cached graph; and inside a stream capture
+the solve becomes part of the caller's CUDA graph."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from gpu_cases import gpu_loss, make_mesh, bc_dict
+from folax_gb300 import fields
+
+pytestmark = pytest.mark.gpu
+
+
+def _system(n=10, seed=51):
+    m = make_mesh("hex8", n, seed=seed, jitter=0.05)
+    s = {"dirichlet_bc_dict": bc_dict("hex8", "elastic"),
+         "material_dict": {"young_modulus": 1.0, "poisson_ratio": 0.3}, "control_layout": "element"}
+    loss = gpu_loss("hex8", "elastic", m, s)
+    import torch
+    E = torch.tensor(fields.two_phase_voxels(n, seed), dtype=torch.float32, device="cuda")
+    u0 = loss.ApplyDirichletBCOnDofVector(torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda"))
+    jac, r = loss.ComputeJacobianMatrixAndResidualVector(E, u0)
+    return loss, jac, r
+
+
+def _sync(lib, capi, jac, method, bits, rhs, tol=1e-8):
+    import torch
+    plan = jac.plan
+    ws = plan.workspace(capi.OP_KRYLOV64 if bits == 64 else capi.OP_PCG)
+    x = torch.empty_like(rhs)
+    it, rel = C.c_int32(), C.c_double()
+    rc = lib.folgb_krylov(plan.handle, method, bits, capi.ptr(jac.data), capi.ptr(jac.inv_diag), capi.ptr(rhs),
+                          capi.ptr(x), tol, 5000, 32, C.byref(it), C.byref(rel), capi.ptr(ws), ws.numel(),
+                          capi.stream_handle())
+    return rc, x.cpu().numpy(), it.value, rel.value
+
+
+@pytest.mark.parametrize("method,bits", [(0, 32), (1, 32), (0, 64), (1, 64)])
+def test_async_back_to_back_equals_sync(cuda, method, bits):
+    torch = cuda
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    loss, jac, r = _system()
+    plan = jac.plan
+    rhs = [(-r).contiguous(), (-0.5 * r + 0.01).contiguous()]
+    ref = [_sync(lib, capi, jac, method, bits, b) for b in rhs]
+    nbytes = lib.folgb_workspace_bytes(plan.handle, capi.OP_KRYLOV64 if bits == 64 else capi.OP_PCG, 1)
+    ws = [torch.empty(nbytes, dtype=torch.uint8, device="cuda") for _ in rhs]
+    xs = [torch.full_like(b, float("nan")) for b in rhs]
+    iters = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    rels = torch.full((2,), -1.0, dtype=torch.float64, device="cuda")
+    status = torch.full((2,), -1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    stream = capi.stream_handle()
+    for rep in range(2):  # the second round launches the cached graphs
+        for k, b in enumerate(rhs):
+            rc = lib.folgb_krylov_async(plan.handle, method, bits, capi.ptr(jac.data), capi.ptr(jac.inv_diag),
+                                        capi.ptr(b), capi.ptr(xs[k]), 1e-8, 5000, 32, iters[k:].data_ptr(),
+                                        rels[k:].data_ptr(), status[k:].data_ptr(), capi.ptr(ws[k]),
+                                        ws[k].numel(), stream)
+            assert rc == capi.OK
+        torch.cuda.synchronize()
+        for k in range(2):
+            rc_ref, x_ref, it_ref, rel_ref = ref[k]
+            assert int(status[k]) == rc_ref == capi.OK
+            assert int(iters[k]) == it_ref and float(rels[k]) == rel_ref and rel_ref <= 1e-8
+            assert np.array_equal(xs[k].cpu().numpy(), x_ref)
+        xs[0].fill_(float("nan"))
+        xs[1].fill_(float("nan"))
+
+
+def test_async_solve_inside_a_captured_graph(cuda):
+    torch = cuda
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    loss, jac, r = _system(n=8, seed=52)
+    plan = jac.plan
+    b = (-r).contiguous()
+    rc_ref, x_ref, it_ref, rel_ref = _sync(lib, capi, jac, 0, 32, b)
+    nbytes = lib.folgb_workspace_bytes(plan.handle, capi.OP_PCG, 1)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    x = torch.empty_like(b)
+    iters = torch.zeros(1, dtype=torch.int32, device="cuda")
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    g = torch.cuda.CUDAGraph()
+    s = torch.cuda.Stream()
+    torch.cuda.synchronize()
+    with torch.cuda.stream(s):
+        with torch.cuda.graph(g, stream=s):
+            rc = lib.folgb_krylov_async(plan.handle, 0, 32, capi.ptr(jac.data), capi.ptr(jac.inv_diag), capi.ptr(b),
+                                        capi.ptr(x), 1e-8, 5000, 32, iters.data_ptr(), None, status.data_ptr(),
+                                        capi.ptr(ws), ws.numel(), capi.stream_handle(s))
+    assert rc == capi.OK
+    for _ in range(2):
+        x.fill_(float("nan"))
+        g.replay()
+        torch.cuda.synchronize()
+        assert int(status[0]) == capi.OK and int(iters[0]) == it_ref
+        assert np.array_equal(x.cpu().numpy(), x_ref)
+
+
+def test_async_reports_not_converged_on_device(cuda):
+    torch = cuda
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    loss, jac, r = _system(n=8, seed=53)
+    plan = jac.plan
+    b = (-r).contiguous()
+    nbytes = lib.folgb_workspace_bytes(plan.handle, capi.OP_PCG, 1)
+    ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
+    x = torch.empty_like(b)
+    out = torch.zeros(4, dtype=torch.int32, device="cuda")
+    rc = lib.folgb_krylov_async(plan.handle, 0, 32, capi.ptr(jac.data), capi.ptr(jac.inv_diag), capi.ptr(b),
+                                capi.ptr(x), 1e-12, 3, 32, out[0:].data_ptr(), None, out[1:].data_ptr(),
+                                capi.ptr(ws), ws.numel(), capi.stream_handle())
+    assert rc == capi.OK
+    torch.cuda.synchronize()
+    assert int(out[1]) == capi.ERR_NOT_CONVERGED and 1 <= int(out[0]) <= 3
