@@ -62,12 +62,14 @@ class Physics(C.Structure):
 class NewtonSettings(C.Structure):
     _fields_ = [("load_steps", C.c_int32), ("max_iterations", C.c_int32), ("abs_tol", C.c_double),
                 ("rel_tol", C.c_double), ("krylov_method", C.c_int32), ("vector_bits", C.c_int32),
-                ("krylov_rtol", C.c_double), ("krylov_maxiter", C.c_int32), ("check_every", C.c_int32)]
+                ("krylov_rtol", C.c_double), ("krylov_maxiter", C.c_int32), ("check_every", C.c_int32),
+                ("line_search", C.c_int32), ("line_search_max_halvings", C.c_int32)]
 
 
 class NewtonInfo(C.Structure):
     _fields_ = [("newton_iterations", C.c_int32), ("krylov_iterations", C.c_int64), ("last_res_norm", C.c_double),
-                ("last_delta_norm", C.c_double), ("krylov_failures", C.c_int32), ("status", C.c_int32)]
+                ("last_delta_norm", C.c_double), ("krylov_failures", C.c_int32), ("status", C.c_int32),
+                ("line_search_halvings", C.c_int32)]
 
 
 vp = C.c_void_p

@@ -782,7 +782,7 @@ static size_t layout_loss(const folgb_plan* p, int B, bool plain, void* base, si
   const size_t recs = (size_t)B * p->E * p->nen * rec, parts = (size_t)B * p->tile_boundary_slots * 4;
   float* g = bp.take<float>(recs > parts ? recs : parts);
   float* partials = bp.take<float>((size_t)B * loss_partial_slots(p));
-  unsigned* counters = bp.take<unsigned>((size_t)B);
+  unsigned* counters = bp.take<unsigned>((size_t)2 * B);  // [B] last-block counters, [B] tile queues
   float* scale = bp.take<float>((size_t)B);
   float* Ke = plain ? bp.take<float>((size_t)B * p->E * ND * ND) : nullptr;
   float* Fe = (plain && p->mat.has_bf) ? bp.take<float>((size_t)B * p->E * ND) : nullptr;
@@ -967,7 +967,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   size_t need = layout_loss(p, B, false, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * B, s));
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * 2 * B, s));
   const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
   VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
                             elem_ctrl ? dloss_dcontrol : nullptr, device_status);
@@ -1020,7 +1020,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   size_t need = layout_loss(p, B, true, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * B, s));
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * 2 * B, s));
   const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
   MatArgs M;
   M.E = p->E;

@@ -93,11 +93,12 @@ struct folgb_plan {
   int* d_tile_eptr = nullptr;           // [T+1] element range of each tile (tile order)
   int* d_tile_nptr = nullptr;           // [T+1] local node range of each tile
   int* d_tile_bptr = nullptr;           // [T+1] boundary slot range of each tile (its first local nodes)
-  int* d_t_elem = nullptr;              // [E] element ids in tile order
+  int* d_t_elem = nullptr;              // [E] element ids in tile order, bit 31: touches a Dirichlet dof
   unsigned char* d_t_lconn = nullptr;   // [E][nen] local node ids, reference node order
   unsigned short* d_tc_pos = nullptr;   // [E*nen] record position a*kTileElems + e_local, grouped by local node
   int* d_tn_gid = nullptr;              // [K] global node id of each local node
-  unsigned short* d_tn_cend = nullptr;  // [K] end of the local node's records in tc_pos (tile-relative)
+  unsigned* d_tn_info = nullptr;        // [K] bits 0-15: end of the local node's records in tc_pos
+                                        // (tile-relative); bits 16-18: its Dirichlet mask
   int* d_bn_node = nullptr;             // [NB] boundary nodes
   int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
   int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
@@ -158,7 +159,8 @@ void noalloc_prepare_current_device();
 // Element tiles of the tile-local fused loss (tiles.cu).
 constexpr int kTileElems = 128;  // elements per tile at most (one thread each)
 constexpr int kTileNodes = 256;  // distinct nodes per tile at most (8-bit local ids)
-int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz);
+int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz,
+                      const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc);
 void free_tile_tables(folgb_plan* p);
 // Destroys the plan's cached Krylov solve graphs (krylov.cu).
 void free_krylov_graphs(folgb_plan* p);

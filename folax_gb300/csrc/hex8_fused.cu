@@ -714,24 +714,122 @@ struct TileArgs {
   const int* tile_eptr;
   const int* tile_nptr;
   const int* tile_bptr;
-  const int* t_elem;
+  const int* t_elem;  // bit 31: the element touches a Dirichlet dof
   const uint2* t_lconn;
   const unsigned short* tc_pos;
   const int* tn_gid;
-  const unsigned short* tn_cend;
+  const unsigned* tn_info;  // bits 0-15: record list end; bits 16-18: Dirichlet mask
   const int* bn_node;
   const int* bn_ptr;
   const int* bn_slot;
   const int* in_node;
   int64_t nb_nodes, ni_nodes;
+  unsigned* queue;  // [B] next tile of each instance (persistent kernel), zeroed before the launch
 };
 
+// One element of a tile from shared-memory node data: X, U (and nodal
+// controls in U.w) of local nodes loc[]; Dirichlet values substituted when
+// the element touches a Dirichlet dof (masks in info, node ids in gid).
+// Stores the 8 residual records, corner-major, in rec; returns the energy.
+template <int CL, bool BF>
+__device__ __forceinline__ float tile_element(const VecArgs& A, const float* ctrl, int e_tagged, uint2 lc,
+                                              const float4* sX, const float4* sU, const unsigned* info,
+                                              const int* gid, float4* rec, int t, int b, int& bad) {
+  constexpr int kLEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> reference node
+  const int e = e_tagged & 0x7fffffff;
+  const int loc[8] = {(int)(lc.x & 0xff), (int)((lc.x >> 8) & 0xff), (int)((lc.x >> 16) & 0xff), (int)(lc.x >> 24),
+                      (int)(lc.y & 0xff), (int)((lc.y >> 8) & 0xff), (int)((lc.y >> 16) & 0xff), (int)(lc.y >> 24)};
+  float X[3][8], U[3][8];
+  float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+#pragma unroll
+  for (int L = 0; L < 8; ++L) {
+    const int k = loc[kLEX[L]];
+    const float4 x = sX[k], u = sU[k];
+    X[0][L] = x.x;
+    X[1][L] = x.y;
+    X[2][L] = x.z;
+    U[0][L] = u.x;
+    U[1][L] = u.y;
+    U[2][L] = u.z;
+    if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = u.w;
+  }
+  if (A.apply_dirichlet && e_tagged < 0) {
+#pragma unroll
+    for (int L = 0; L < 8; ++L) {
+      const int k = loc[kLEX[L]];
+      const unsigned m = info[k] >> 16;
+      if (m) {
+        const int64_t d = 3 * (int64_t)gid[k];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if ((m >> c) & 1u) U[c][L] = __ldg(A.dval + d + c);
+      }
+    }
+  }
+  if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
+  else egp[0] = __ldg(ctrl + e);
+  float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
+  float g[8][3];
+  float sedsum = 0.f, energy = 0.f;
+  hex8_elastic_core<CL, BF, 2>(A.mat, X, U, egp, energy, sedsum, wsed, g, bad);
+  if (!isfinite(energy)) bad |= 2;
+  if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(wsed);
+#pragma unroll
+  for (int L = 0; L < 8; ++L) {
+    float w = 0.f;
+    if constexpr (CL == FOLGB_CONTROL_NODAL) w = wsed[L];
+    rec[kLEX[L] * kTileElems + t] = make_float4(g[L][0], g[L][1], g[L][2], w);
+  }
+  if (CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
+    A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
+  return energy;
+}
+
+// Node pass of a tile: local node k sums its records (list end in info,
+// positions in pos) in order; an interior node writes its gradient, a
+// boundary node (k < nb) its partial record.
+template <int CL>
+__device__ __forceinline__ void tile_nodes(const VecArgs& A, const float4* rec, const unsigned short* pos,
+                                           const unsigned* info, const int* gid, int nl, int nb, float4* bpart,
+                                           int b) {
+  const float sc = (A.exponent == 1.f) ? A.inv_batch : 1.f;
+  for (int k = threadIdx.x; k < nl; k += kTileElems) {
+    const unsigned inf = info[k];
+    const int c0 = k == 0 ? 0 : (int)(info[k - 1] & 0xffffu), c1 = (int)(inf & 0xffffu);
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int j = c0; j < c1; ++j) {
+      const float4 r = rec[pos[j]];
+      acc.x += r.x;
+      acc.y += r.y;
+      acc.z += r.z;
+      acc.w += r.w;
+    }
+    if (k < nb) {
+      bpart[k] = acc;
+    } else {
+      const int n = gid[k];
+      const unsigned m = inf >> 16;
+      if (A.out) {
+        float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
+        o[0] = (m & 1u) ? 0.f : sc * acc.x;
+        o[1] = (m & 2u) ? 0.f : sc * acc.y;
+        o[2] = (m & 4u) ? 0.f : sc * acc.z;
+      }
+      if (CL == FOLGB_CONTROL_NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = sc * acc.w;
+    }
+  }
+}
+
+// Simple tile kernel: one block per (tile, instance), the tile's nodes loaded
+// with plain loads, then elements, then nodes.
 template <int CL, bool BF, int MINB>
 __global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const VecArgs A, const TileArgs T) {
   __shared__ float4 sX[kTileNodes];
   __shared__ float4 sU[kTileNodes];  // displacements, nodal control in w
-  __shared__ unsigned char sM[kTileNodes];
+  __shared__ unsigned sInfo[kTileNodes];
+  __shared__ int sGid[kTileNodes];
   __shared__ float4 sR[8 * kTileElems];
+  __shared__ unsigned short sPos[8 * kTileElems];
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   pdl_launch_dependents();
@@ -744,88 +842,206 @@ __global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const Ve
   for (int k = threadIdx.x; k < nl; k += kTileElems) {
     const int n = __ldg(T.tn_gid + n0 + k);
     const float4 x = __ldg(A.xyz4 + n);
-    const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
-    float u[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-      const int64_t d = 3 * (int64_t)n + c;
-      u[c] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
-    }
+    const int64_t d = 3 * (int64_t)n;
     sX[k] = x;
-    sU[k] = make_float4(u[0], u[1], u[2], CL == FOLGB_CONTROL_NODAL ? __ldg(ctrl + n) : 0.f);
-    sM[k] = (unsigned char)m;
+    sU[k] = make_float4(__ldg(dofs + d), __ldg(dofs + d + 1), __ldg(dofs + d + 2),
+                        CL == FOLGB_CONTROL_NODAL ? __ldg(ctrl + n) : 0.f);
+    sInfo[k] = __ldg(T.tn_info + n0 + k);
+    sGid[k] = n;
   }
+  for (int j = threadIdx.x; j < 8 * ne; j += kTileElems) sPos[j] = __ldg(T.tc_pos + (int64_t)e0 * 8 + j);
   __syncthreads();
   float energy = 0.f;
   int bad = 0;
   const int t = threadIdx.x;
-  if (t < ne) {
-    constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
-    const int e = __ldg(T.t_elem + e0 + t);
-    const uint2 lc = __ldg(T.t_lconn + e0 + t);
-    const int loc[8] = {(int)(lc.x & 0xff), (int)((lc.x >> 8) & 0xff), (int)((lc.x >> 16) & 0xff), (int)(lc.x >> 24),
-                        (int)(lc.y & 0xff), (int)((lc.y >> 8) & 0xff), (int)((lc.y >> 16) & 0xff), (int)(lc.y >> 24)};
-    float X[3][8], U[3][8];
-    float egp[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
-#pragma unroll
-    for (int L = 0; L < 8; ++L) {
-      const int k = loc[LEX[L]];
-      const float4 x = sX[k], u = sU[k];
-      X[0][L] = x.x;
-      X[1][L] = x.y;
-      X[2][L] = x.z;
-      U[0][L] = u.x;
-      U[1][L] = u.y;
-      U[2][L] = u.z;
-      if constexpr (CL == FOLGB_CONTROL_NODAL) egp[L] = u.w;
-    }
-    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(egp);
-    else egp[0] = __ldg(ctrl + e);
-    float wsed[CL == FOLGB_CONTROL_NODAL ? 8 : 1];
-    float g[8][3];
-    float sedsum = 0.f;
-    hex8_elastic_core<CL, BF, 2>(A.mat, X, U, egp, energy, sedsum, wsed, g, bad);
-    if (!isfinite(energy)) bad |= 2;
-    if constexpr (CL == FOLGB_CONTROL_NODAL) interp8(wsed);
-#pragma unroll
-    for (int L = 0; L < 8; ++L) {
-      float w = 0.f;
-      if constexpr (CL == FOLGB_CONTROL_NODAL) w = wsed[L];
-      sR[LEX[L] * kTileElems + t] = make_float4(g[L][0], g[L][1], g[L][2], w);
-    }
-    if (CL != FOLGB_CONTROL_NODAL && A.dctrl_elem)
-      A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sedsum * A.inv_batch : sedsum;
-  }
+  if (t < ne)
+    energy = tile_element<CL, BF>(A, ctrl, __ldg(T.t_elem + e0 + t), __ldg(T.t_lconn + e0 + t), sX, sU, sInfo, sGid,
+                                  sR, t, b, bad);
   __syncthreads();
   const int bbase = __ldg(T.tile_bptr + tile), nb = __ldg(T.tile_bptr + tile + 1) - bbase;
-  const float sc = (A.exponent == 1.f) ? A.inv_batch : 1.f;
-  const unsigned short* cp = T.tc_pos + (int64_t)e0 * 8;
-  float4* bpart = reinterpret_cast<float4*>(A.g) + (int64_t)b * T.S;
-  for (int k = threadIdx.x; k < nl; k += kTileElems) {
-    const int c0 = k == 0 ? 0 : (int)__ldg(T.tn_cend + n0 + k - 1), c1 = __ldg(T.tn_cend + n0 + k);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int j = c0; j < c1; ++j) {
-      const float4 r = sR[__ldg(cp + j)];
-      acc.x += r.x;
-      acc.y += r.y;
-      acc.z += r.z;
-      acc.w += r.w;
-    }
-    if (k < nb) {
-      bpart[bbase + k] = acc;
-    } else {
-      const int n = __ldg(T.tn_gid + n0 + k);
-      const unsigned m = sM[k];
-      if (A.out) {
-        float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
-        o[0] = (m & 1u) ? 0.f : sc * acc.x;
-        o[1] = (m & 2u) ? 0.f : sc * acc.y;
-        o[2] = (m & 4u) ? 0.f : sc * acc.z;
-      }
-      if (CL == FOLGB_CONTROL_NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = sc * acc.w;
-    }
-  }
+  tile_nodes<CL>(A, sR, sPos, sInfo, sGid, nl, nb, reinterpret_cast<float4*>(A.g) + (int64_t)b * T.S + bbase, b);
   finish_loss_warp(energy, bad, A, b, wsum, &wcount, tile, T.ntiles);
+}
+
+// ---- persistent, pipelined tile kernel -----------------------------------
+// A fixed grid of blocks per instance takes tiles from a per-instance queue
+// (an atomic counter, so SMs that finish early take more tiles).  Each
+// tile's inputs move into shared memory with asynchronous copies (cp.async)
+// while the block computes the tile before it:
+//   iteration k:  [wait for tile k's inputs]  issue the copies of tile k+1's
+//   node data (ids already in shared memory) and of tile k+2's node ids,
+//   elements (tile k), node pass (tile k).
+// The tile's energy goes to its own partial slot (partials[tile]); the last
+// block of the instance sums the slots in tile order.
+__device__ __forceinline__ void cp_async4(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void* dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* dst, const void* src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+struct TileMeta {
+  int tile, e0, ne, n0, nl, bbase, nb, pad;
+};
+
+struct TileStage {
+  float4 X[kTileNodes];
+  float4 U[kTileNodes];
+  unsigned info[kTileNodes];
+  uint2 lconn[kTileElems];
+  int elem[kTileElems];
+  unsigned short pos[8 * kTileElems];
+};
+
+struct TileSmem {
+  TileStage st[2];
+  int gid[3][kTileNodes];
+  float4 rec[8 * kTileElems];
+  TileMeta meta[4];
+  float wsum[2][kTileElems / 32];
+  int last;
+};
+
+__device__ __forceinline__ TileMeta tile_meta(const TileArgs& T, int tile) {
+  TileMeta m{};
+  m.tile = tile;
+  if (tile < T.ntiles) {
+    m.e0 = __ldg(T.tile_eptr + tile);
+    m.ne = __ldg(T.tile_eptr + tile + 1) - m.e0;
+    m.n0 = __ldg(T.tile_nptr + tile);
+    m.nl = __ldg(T.tile_nptr + tile + 1) - m.n0;
+    m.bbase = __ldg(T.tile_bptr + tile);
+    m.nb = __ldg(T.tile_bptr + tile + 1) - m.bbase;
+  }
+  return m;
+}
+
+// copies of a tile's node ids (ring slot g)
+__device__ __forceinline__ void issue_ids(TileSmem& S, const TileArgs& T, const TileMeta& m, int g) {
+  if (m.tile >= T.ntiles) return;
+  for (int k = threadIdx.x; k < m.nl; k += kTileElems) cp_async4(&S.gid[g][k], T.tn_gid + m.n0 + k);
+}
+
+// copies of a tile's inputs (node ids already in ring slot g) into stage st
+template <int CL>
+__device__ __forceinline__ void issue_inputs(TileSmem& S, const VecArgs& A, const TileArgs& T, const TileMeta& m,
+                                             int st, int g, const float* dofs, const float* ctrl) {
+  if (m.tile >= T.ntiles) return;
+  TileStage& Z = S.st[st];
+  for (int k = threadIdx.x; k < m.nl; k += kTileElems) {
+    const int n = S.gid[g][k];
+    cp_async16(&Z.X[k], A.xyz4 + n);
+    const float* du = dofs + 3 * (int64_t)n;
+    cp_async4(&Z.U[k].x, du);
+    cp_async4(&Z.U[k].y, du + 1);
+    cp_async4(&Z.U[k].z, du + 2);
+    if (CL == FOLGB_CONTROL_NODAL) cp_async4(&Z.U[k].w, ctrl + n);
+    cp_async4(&Z.info[k], T.tn_info + m.n0 + k);
+  }
+  for (int j = threadIdx.x; j < m.ne; j += kTileElems) {
+    cp_async8(&Z.lconn[j], T.t_lconn + m.e0 + j);
+    cp_async4(&Z.elem[j], T.t_elem + m.e0 + j);
+    cp_async16(&Z.pos[8 * j], T.tc_pos + (int64_t)(m.e0 + j) * 8);
+  }
+}
+
+template <int CL, bool BF>
+__global__ void __launch_bounds__(kTileElems, 4) k_hex8_elastic_tile_pipe(const VecArgs A, const TileArgs T) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  TileSmem& S = *reinterpret_cast<TileSmem*>(smem_raw);
+  pdl_launch_dependents();
+  const int b = blockIdx.y;
+  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+  float4* bpart = reinterpret_cast<float4*>(A.g) + (int64_t)b * T.S;
+  float* partials = A.partials + (int64_t)b * T.ntiles;
+  // tiles k = 0, 1 of this block: blockIdx.x and gridDim.x + blockIdx.x; from
+  // k = 2 on from the queue (offset by the 2 * gridDim.x tiles taken so)
+  auto next_tile = [&]() { return 2 * (int)gridDim.x + (int)atomicAdd(T.queue + b, 1u); };
+  if (threadIdx.x == 0) {
+    S.meta[0] = tile_meta(T, blockIdx.x);
+    S.meta[1] = tile_meta(T, gridDim.x + blockIdx.x);
+    S.meta[2] = tile_meta(T, S.meta[1].tile < T.ntiles ? next_tile() : T.ntiles);
+  }
+  __syncthreads();
+  issue_ids(S, T, S.meta[0], 0);
+  cp_async_commit();
+  cp_async_wait<0>();
+  __syncthreads();
+  issue_inputs<CL>(S, A, T, S.meta[0], 0, 0, dofs, ctrl);
+  issue_ids(S, T, S.meta[1], 1);
+  cp_async_commit();
+  float energy_all = 0.f;  // unused beyond the flags: energies go per tile
+  int bad = 0;
+  for (int k = 0;; ++k) {
+    const TileMeta cur = S.meta[k & 3];
+    if (cur.tile >= T.ntiles) break;
+    cp_async_wait<0>();  // tile k's inputs and tile k+1's ids
+    __syncthreads();
+    const TileMeta nx = S.meta[(k + 1) & 3], nn = S.meta[(k + 2) & 3];
+    // next tile's inputs, the tile after it's ids; the tile after that from the queue
+    issue_inputs<CL>(S, A, T, nx, (k + 1) & 1, (k + 1) % 3, dofs, ctrl);
+    issue_ids(S, T, nn, (k + 2) % 3);
+    cp_async_commit();
+    if (threadIdx.x == 0) S.meta[(k + 3) & 3] = tile_meta(T, nn.tile < T.ntiles ? next_tile() : T.ntiles);
+    const TileStage& Z = S.st[k & 1];
+    const int t = threadIdx.x;
+    float energy = 0.f;
+    if (t < cur.ne)
+      energy = tile_element<CL, BF>(A, ctrl, Z.elem[t], Z.lconn[t], Z.X, Z.U, Z.info, S.gid[k % 3], S.rec, t, b,
+                                    bad);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) energy += __shfl_xor_sync(0xffffffffu, energy, o);
+    if ((t & 31) == 0) S.wsum[k & 1][t >> 5] = energy;
+    __syncthreads();
+    if (t == 0) {
+      float e = 0.f;
+#pragma unroll
+      for (int w = 0; w < kTileElems / 32; ++w) e += S.wsum[k & 1][w];
+      partials[cur.tile] = e;
+    }
+    tile_nodes<CL>(A, S.rec, Z.pos, Z.info, S.gid[k % 3], cur.nl, cur.nb, bpart + cur.bbase, b);
+  }
+  cp_async_wait<0>();
+  (void)energy_all;
+  report_bad_warp(bad, A.status);
+  // the last block of the instance sums the tile energies in tile order
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    S.last = atomicAdd(A.counters + b, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!S.last) return;
+  __threadfence();
+  float s = 0.f;
+  const volatile float* pv = partials;
+  for (int i = threadIdx.x; i < T.ntiles; i += kTileElems) s += pv[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) S.wsum[0][threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float L = 0.f;
+#pragma unroll
+    for (int w = 0; w < kTileElems / 32; ++w) L += S.wsum[0][w];
+    const float p = A.exponent;
+    const float Lp = (p == 1.f) ? L : powf(L, p);
+    const float sc = (p == 1.f) ? A.inv_batch : p * powf(L, p - 1.f) * A.inv_batch;
+    A.losses[b] = Lp;
+    A.scale[b] = sc;
+    if (!isfinite(Lp) && A.status) atomicOr(A.status, 1 << FOLGB_ERR_NAN);
+    A.counters[b] = 0u;
+    T.queue[b] = 0u;  // ready for the next launch
+  }
 }
 
 // The nodes on tile boundaries (and nodes of no element): the partial
@@ -887,7 +1103,8 @@ static TileArgs tile_args(const folgb_plan* p) {
   T.t_lconn = reinterpret_cast<const uint2*>(p->d_t_lconn);
   T.tc_pos = p->d_tc_pos;
   T.tn_gid = p->d_tn_gid;
-  T.tn_cend = p->d_tn_cend;
+  T.tn_info = p->d_tn_info;
+  T.queue = nullptr;
   T.bn_node = p->d_bn_node;
   T.bn_ptr = p->d_bn_ptr;
   T.bn_slot = p->d_bn_slot;
@@ -897,16 +1114,27 @@ static TileArgs tile_args(const folgb_plan* p) {
   return T;
 }
 
-template <int CL, int MINB>
-static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, cudaStream_t s) {
-  const TileArgs T = tile_args(p);
-  dim3 grid((unsigned)p->tiles, (unsigned)B);
-  if (bf) k_hex8_elastic_tile<CL, true, MINB><<<grid, kTileElems, 0, s>>>(A, T);
-  else k_hex8_elastic_tile<CL, false, MINB><<<grid, kTileElems, 0, s>>>(A, T);
+template <int CL>
+static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, bool pipe, cudaStream_t s) {
+  TileArgs T = tile_args(p);
+  T.queue = A.counters + B;  // zeroed with the loss counters before the launch
+  if (!pipe) {
+    dim3 grid((unsigned)p->tiles, (unsigned)B);
+    if (bf) k_hex8_elastic_tile<CL, true, 4><<<grid, kTileElems, 0, s>>>(A, T);
+    else k_hex8_elastic_tile<CL, false, 4><<<grid, kTileElems, 0, s>>>(A, T);
+    return;
+  }
+  static std::atomic<int> occ_bf[kOccDevices], occ[kOccDevices];  // per instantiation and device
+  auto k = bf ? k_hex8_elastic_tile_pipe<CL, true> : k_hex8_elastic_tile_pipe<CL, false>;
+  const int per_sm = blocks_per_sm(k, kTileElems, sizeof(TileSmem), bf ? occ_bf : occ);
+  int64_t g = (int64_t)per_sm * num_sms() / B;
+  if (g > p->tiles) g = p->tiles;
+  if (g < 1) g = 1;
+  k<<<dim3((unsigned)g, (unsigned)B), kTileElems, sizeof(TileSmem), s>>>(A, T);
 }
 
-// Variants of the tile-local kernel: index - kHex8TileFirst -> blocks per SM
-// of its register budget (4: 128 registers, 5: 102).
+// Tile-local variants: kHex8TileFirst the persistent pipelined kernel,
+// kHex8TileFirst + 1 the one-block-per-tile kernel.
 constexpr int kHex8TileFirst = 18;
 
 template <int CL, int MODE>
@@ -953,14 +1181,9 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
   if (variant >= kHex8TileFirst && (mode != MODE_LOSS || !tile)) variant = 11;
   trace_begin(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
   if (mode == MODE_LOSS && tile) {
-    const bool minb5 = variant == kHex8TileFirst + 1;
-    if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
-      if (minb5) launch_tile<FOLGB_CONTROL_NODAL, 5>(p, A, (int)grid.y, bf, s);
-      else launch_tile<FOLGB_CONTROL_NODAL, 4>(p, A, (int)grid.y, bf, s);
-    } else {
-      if (minb5) launch_tile<FOLGB_CONTROL_ELEMENT, 5>(p, A, (int)grid.y, bf, s);
-      else launch_tile<FOLGB_CONTROL_ELEMENT, 4>(p, A, (int)grid.y, bf, s);
-    }
+    const bool pipe = variant == kHex8TileFirst;
+    if (p->ctrl_layout == FOLGB_CONTROL_NODAL) launch_tile<FOLGB_CONTROL_NODAL>(p, A, (int)grid.y, bf, pipe, s);
+    else launch_tile<FOLGB_CONTROL_ELEMENT>(p, A, (int)grid.y, bf, pipe, s);
   } else if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
     if (mode == MODE_LOSS) launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_LOSS>(A, grid, bf, variant, s);
     else launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_RESIDUAL>(A, grid, bf, variant, s);

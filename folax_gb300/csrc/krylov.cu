@@ -251,9 +251,11 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
   // runs only when an iteration kernel asked for it (in the device-resident
   // loop it is launched after every chunk)
   if (!sc->replace || sc->done) return;
-  // BiCGSTAB keeps its shadow residual and directions across a residual
-  // replacement; only a breakdown (replace == 2) restarts it from rhat = r.
-  const bool restart = BICG && sc->replace == 2;
+  // Both solvers keep their search directions across a residual replacement
+  // (restarting CG there would discard the conjugacy of the directions built
+  // so far and slow the convergence of the error); only a breakdown
+  // (replace == 2) restarts them: BiCGSTAB from rhat = r, CG from p = z.
+  const bool restart = sc->replace == 2;
   VT rzf = VT(0);
   double rr = 0.0;
   FOLGB_NODE_BLOCKS(NDOF, G) {
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
         const VT zf = (VT)dinv[d] * rf;
         z[d] = zf;
         rzf = vfma(rf, zf, rzf);
-      } else if (restart) {
+      } else if (BICG && restart) {
         rhat[d] = rf;
         rzf = vfma(rf, rf, rzf);
       } else {
@@ -290,12 +292,17 @@ __global__ void __launch_bounds__(256) k_true_residual(int64_t N, const int* __r
     sc->rnorm2 = RR;
     sc->rref2 = RR;
     sc->replace = 0;
-    sc->rho = RZ;  // PCG: r . z;  BiCGSTAB: rhat . r
     if (BICG) {
       if (restart) sc->restart = 1;
+    } else if (restart || !(sc->rho > 0.0) || sc->beta == 0.0) {
+      sc->beta = 0.0;  // breakdown: restart the search direction, p = z
     } else {
-      sc->beta = 0.0;  // restart the search direction: p = z
+      // the next direction p = z + beta p_old with beta = (r . z) / rho_old
+      // of the replaced residual; the update kernel left beta = rz / rho_old
+      // and rho = rz of the recurrence residual, so rho_old = rho / beta
+      sc->beta = RZ * sc->beta / sc->rho;
     }
+    sc->rho = RZ;  // PCG: r . z;  BiCGSTAB: rhat . r
     if (!isfinite(RR)) sc->done = 3;
     else if (RR <= sc->tol2) sc->done = 1;
     else if (RR > kDiverge2 * sc->bnorm2) sc->done = 4;
@@ -388,7 +395,7 @@ __global__ void __launch_bounds__(256, kSpmvMinBlocks<VT>) k_pcg_spmv(int64_t N,
       sc->breakdowns += 1;
       if (!isfinite(PQ)) sc->done = 3;
       else if (sc->breakdowns > kMaxBreakdowns) sc->done = 4;
-      else sc->replace = 1;
+      else sc->replace = 2;
     } else {
       sc->alpha = sc->rho / PQ;
     }
@@ -941,7 +948,7 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_krylov_cluster(const Clu
           ++breakdowns;
           if (!isfinite(PQ)) done = 3;
           else if (breakdowns > kMaxBreakdowns) done = 4;
-          else replace = 1;
+          else replace = 2;
           continue;
         }
         alpha = rho / PQ;
@@ -992,10 +999,12 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_krylov_cluster(const Clu
       dr[1] += ri * ri;
     });
     cluster_sum<2>(dr, sh, slot, parity);
+    // CG keeps its direction across a replacement (beta = (r . z) / rho_old
+    // of the replaced residual, rho_old = rho / beta); a breakdown restarts it
+    if (!BICG) beta = (replace == 2 || !(rho > 0.0) || beta == 0.0) ? 0.0 : dr[0] * beta / rho;
     rho = dr[0];
     rref2 = rnorm2 = dr[1];
     if (fresh) restart = true;
-    if (!BICG) beta = 0.0;
     replace = 0;
     if (!isfinite(dr[1])) done = 3;
     else if (dr[1] <= tol2) done = 1;
@@ -1458,9 +1467,10 @@ extern "C" int folgb_adam_step(float* params, const float* grads, float* m, floa
 // is one CUDA graph: a WHILE node whose body is one Newton iteration
 // [load-scaled Dirichlet values at the start of a load step, residual and
 // CSR tangent assembly, |r| and rhs = -r, the Krylov solve (a nested WHILE
-// node), |du|, the convergence test, u += du], launched once; the host reads
-// the Newton state when the graph has finished.  Convergence as the
-// reference: |r| < abs_tol or |du| < rel_tol or the iteration cap, the
+// node), |du|, the convergence test, (optionally) a backtracking line search
+// on the element energy (a nested WHILE node), u += t du], launched once; the
+// host reads the Newton state when the graph has finished.  Convergence as
+// the reference: |r| < abs_tol or |du| < rel_tol or the iteration cap, the
 // converged iteration's update not applied; a non-finite |r| stops the solve.
 // ---------------------------------------------------------------------------
 namespace folgb {
@@ -1469,6 +1479,9 @@ struct NState {
   double rn2, dn2, abs2, rel2;
   long long krylov_total;
   int step, it, steps, maxit, done, status, newton_total, apply, krylov_fail;
+  // line search: slope r . du (r is -rhs), step length t, halvings
+  double slope, t;
+  int ls_it, ls_max, ls_halvings;
 };
 
 constexpr int kNewtonBlocks = 1024;
@@ -1505,8 +1518,7 @@ __global__ void k_newton_norm(int64_t n, const float* __restrict__ v, float* __r
 }
 
 // hist[k] = (load step, iteration, |r|, |du|) of Newton iteration k
-__global__ void k_newton_control(NState* st, const KScalars* sc, cudaGraphConditionalHandle loop, double* hist,
-                                 int hist_cap) {
+__global__ void k_newton_control(NState* st, const KScalars* sc, double* hist, int hist_cap) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   const int k = st->newton_total;
   if (k < hist_cap) {
@@ -1532,13 +1544,91 @@ __global__ void k_newton_control(NState* st, const KScalars* sc, cudaGraphCondit
   }
   // every body execution is one Newton iteration: at most steps * maxit
   if (st->newton_total >= st->steps * st->maxit) st->done = 1;
-  cudaGraphSetConditional(loop, st->done ? 0u : 1u);
+}
+
+// Last kernel of the Newton body: continue unless the solve has ended (in
+// this iteration's control or its line search).
+__global__ void k_newton_loop(const NState* st, cudaGraphConditionalHandle loop) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) cudaGraphSetConditional(loop, st->done ? 0u : 1u);
 }
 
 __global__ void k_newton_update(int64_t n, float* __restrict__ u, const float* __restrict__ du, const NState* st) {
   if (!st->apply) return;
+  const float t = (float)st->t;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    u[i] += du[i];
+    u[i] = t == 1.f ? u[i] + du[i] : fmaf(t, du[i], u[i]);
+}
+
+// fp64 dot product a . b into *out, fixed order (the line search's slope)
+__global__ void k_newton_dot(int64_t n, const float* __restrict__ a, const float* __restrict__ b, double* part,
+                             unsigned* counter, double* out) {
+  __shared__ double sh[32];
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    acc += (double)a[i] * (double)b[i];
+  const double s = block_sum_d(acc, sh);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (!last_block(counter)) return;
+  const double tot = sum_partials(part, gridDim.x, sh);
+  if (threadIdx.x == 0) {
+    *out = tot;
+    *counter = 0u;
+  }
+}
+
+// Line search (backtracking on the element energy).  Arm: full step, and the
+// loop runs only for an iteration whose update is applied and whose
+// predicted decrease -(r . du) = slope (rhs = -r, so slope = -(rhs . du))
+// is above the energy's fp32 resolution.
+__global__ void k_ls_arm(NState* st, const float* e0, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  st->t = 1.0;
+  st->ls_it = 0;
+  const double pred = st->slope;  // rhs . du = -(r . du): the predicted decrease
+  // a tiny predicted decrease (below the energy's fp32 resolution) takes the
+  // whole step; a direction that is not a descent one is searched as well
+  const bool tiny = pred >= 0.0 && pred <= 1e-6 * fabs((double)*e0);
+  const bool run = st->apply && !st->done && !tiny;
+  cudaGraphSetConditional(h, run ? 1u : 0u);
+}
+
+// A Newton step that is not a descent direction (indefinite tangent: slope
+// = rhs . du <= 0) or that the Krylov solve left non-finite is replaced by the
+// Jacobi-preconditioned steepest descent step du = D^-1 rhs = -D^-1 r.
+__global__ void k_ls_direction(int64_t n, const float* __restrict__ rhs, const float* __restrict__ dinv,
+                               float* __restrict__ du, const NState* st) {
+  const double sl = st->slope;
+  if (isfinite(sl) && sl > 0.0) return;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    du[i] = dinv[i] * rhs[i];
+}
+
+__global__ void k_ls_trial(int64_t n, const float* __restrict__ u, const float* __restrict__ du, float* __restrict__ ut,
+                           const NState* st) {
+  const float t = (float)st->t;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    ut[i] = fmaf(t, du[i], u[i]);
+}
+
+__global__ void k_ls_control(NState* st, const float* e0, const float* et, cudaGraphConditionalHandle h) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const double E0 = *e0, Et = *et;
+  const bool ok = isfinite(Et) && Et <= E0 - 1e-4 * st->t * fmax(st->slope, 0.0) + 2e-6 * fabs(E0);
+  if (ok) {
+    cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  if (st->ls_it >= st->ls_max) {  // no acceptable step: stop the solve
+    st->apply = 0;
+    st->done = 1;
+    st->status = FOLGB_ERR_NOT_CONVERGED;
+    cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  st->t *= 0.5;
+  st->ls_it += 1;
+  st->ls_halvings += 1;
+  cudaGraphSetConditional(h, 1u);
 }
 
 struct NewtonWS {
@@ -1546,15 +1636,19 @@ struct NewtonWS {
   size_t asm_bytes;
   void* kry_ws;
   size_t kry_bytes;
+  void* loss_ws;  // line search: energy evaluations
+  size_t loss_bytes;
   float *r, *rhs, *du, *vals, *dinv;
+  float *ut, *energy;  // line search: trial dofs, energies E(u) and E(u + t du)
+  int* ls_status;
   NState* st;
   double* part;
   unsigned* counter;
   double* hist;
 };
 
-static size_t layout_newton(const folgb_plan* p, int vector_bits, int hist_cap, void* base, size_t cap,
-                            NewtonWS* w) {
+static size_t layout_newton(const folgb_plan* p, int vector_bits, int hist_cap, int line_search, void* base,
+                            size_t cap, NewtonWS* w) {
   Bump bp(base, cap);
   const size_t n = (size_t)p->ndof * p->N;
   NewtonWS t;
@@ -1569,8 +1663,13 @@ static size_t layout_newton(const folgb_plan* p, int vector_bits, int hist_cap, 
   t.dinv = bp.take<float>(n);
   t.st = bp.take<NState>(1);
   t.part = bp.take<double>(kNewtonBlocks);
-  t.counter = bp.take<unsigned>(2);
+  t.counter = bp.take<unsigned>(4);
   t.hist = bp.take<double>((size_t)4 * hist_cap);
+  t.loss_bytes = line_search ? folgb_workspace_bytes(p, FOLGB_OP_LOSS_ADJOINT, 1) : 0;
+  t.loss_ws = line_search ? bp.take<char>(t.loss_bytes) : nullptr;
+  t.ut = line_search ? bp.take<float>(n) : nullptr;
+  t.energy = bp.take<float>(2);
+  t.ls_status = bp.take<int>(1);
   if (w) *w = t;
   return align_up(bp.off);
 }
@@ -1579,7 +1678,7 @@ static size_t layout_newton(const folgb_plan* p, int vector_bits, int hist_cap, 
 
 extern "C" size_t folgb_newton_workspace_bytes(const folgb_plan* p, const folgb_newton_settings* s) {
   if (!p || !s || !p->has_csr || s->load_steps <= 0 || s->max_iterations <= 0) return 0;
-  return layout_newton(p, s->vector_bits, s->load_steps * s->max_iterations, nullptr, 0, nullptr);
+  return layout_newton(p, s->vector_bits, s->load_steps * s->max_iterations, s->line_search, nullptr, 0, nullptr);
 }
 
 extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* dofs, const folgb_newton_settings* s,
@@ -1589,7 +1688,9 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
   if (!p->has_csr) return FOLGB_ERR_NO_PATTERN;
   if (s->load_steps <= 0 || s->max_iterations <= 0 || s->krylov_maxiter <= 0 || !(s->krylov_rtol >= 0.0) ||
       !(s->abs_tol >= 0.0) || !(s->rel_tol >= 0.0) || (s->vector_bits != 32 && s->vector_bits != 64) ||
-      (s->krylov_method != FOLGB_KRYLOV_CG && s->krylov_method != FOLGB_KRYLOV_BICGSTAB))
+      (s->krylov_method != FOLGB_KRYLOV_CG && s->krylov_method != FOLGB_KRYLOV_BICGSTAB) ||
+      (s->line_search != 0 && s->line_search != 1) ||
+      (s->line_search && (s->line_search_max_halvings < 0 || p->phys.loss_exponent != 1.0)))
     return FOLGB_ERR_INVALID_ARGUMENT;
   cudaStream_t st = (cudaStream_t)stream;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
@@ -1598,7 +1699,7 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
   if (cap != cudaStreamCaptureStatusNone || trace_active()) return FOLGB_ERR_INVALID_ARGUMENT;
   const int hist_cap = s->load_steps * s->max_iterations;
   NewtonWS w;
-  const size_t need = layout_newton(p, s->vector_bits, hist_cap, workspace, workspace_bytes, &w);
+  const size_t need = layout_newton(p, s->vector_bits, hist_cap, s->line_search, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   const int64_t n = (int64_t)p->ndof * p->N;
   const int solver = s->krylov_method == FOLGB_KRYLOV_CG ? SOLVER_CG : SOLVER_BICGSTAB;
@@ -1613,6 +1714,8 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
   init.steps = s->load_steps;
   init.maxit = s->max_iterations;
   init.status = FOLGB_OK;
+  init.t = 1.0;
+  init.ls_max = s->line_search_max_halvings;
 
   cudaGraph_t g = nullptr;
   cudaGraphExec_t exec = nullptr;
@@ -1634,10 +1737,16 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
                                       cudaStreamCaptureModeRelaxed) != cudaSuccess)
       rc = FOLGB_ERR_CUDA;
   }
+  // the element energy of dofs-like array v into *e (the plan's loss, no gradients)
+  auto energy = [&](const float* v, float* e) {
+    return folgb_loss_adjoint(p, 1, control, 0, v, n, 0, e, nullptr, nullptr, w.ls_status, w.loss_ws, w.loss_bytes,
+                              cs);
+  };
   if (rc == FOLGB_OK) {
     KScalars* ksc = nullptr;
     k_newton_bc<<<nb, 256, 0, cs>>>(p->N, p->ndof, p->d_dmask, p->d_dval, dofs, w.st);
     rc = folgb_assemble(p, control, dofs, 0, w.r, w.vals, w.dinv, device_status, w.asm_ws, w.asm_bytes, cs);
+    if (rc == FOLGB_OK && s->line_search) rc = energy(dofs, w.energy);
     if (rc == FOLGB_OK) {
       k_newton_norm<<<vb, 256, 0, cs>>>(n, w.r, w.rhs, w.part, w.counter, &w.st->rn2);
       rc = s->vector_bits == 64
@@ -1648,8 +1757,58 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
     }
     if (rc == FOLGB_OK) {
       k_newton_norm<<<vb, 256, 0, cs>>>(n, w.du, nullptr, w.part, w.counter + 1, &w.st->dn2);
-      k_newton_control<<<1, 32, 0, cs>>>(w.st, ksc, loop, w.hist, hist_cap);
+      if (s->line_search) {
+        k_newton_dot<<<vb, 256, 0, cs>>>(n, w.rhs, w.du, w.part, w.counter + 2, &w.st->slope);
+        k_ls_direction<<<vb, 256, 0, cs>>>(n, w.rhs, w.dinv, w.du, w.st);
+        k_newton_dot<<<vb, 256, 0, cs>>>(n, w.rhs, w.du, w.part, w.counter + 2, &w.st->slope);
+      }
+      k_newton_control<<<1, 32, 0, cs>>>(w.st, ksc, w.hist, hist_cap);
+      if (cudaGetLastError() != cudaSuccess) rc = FOLGB_ERR_CUDA;
+    }
+    if (rc == FOLGB_OK && s->line_search) {
+      // nested WHILE node: trial step, its energy, accept or halve
+      cudaStreamCaptureStatus bcst = cudaStreamCaptureStatusNone;
+      cudaGraph_t body = nullptr;
+      const cudaGraphNode_t* deps = nullptr;
+      size_t ndeps = 0;
+      cudaGraphConditionalHandle ls{};
+      cudaStream_t ls_stream = nullptr;
+      if (cudaStreamGetCaptureInfo(cs, &bcst, nullptr, &body, &deps, nullptr, &ndeps) != cudaSuccess ||
+          cudaGraphConditionalHandleCreate(&ls, body, 0u, 0u) != cudaSuccess) {
+        rc = FOLGB_ERR_CUDA;
+      } else {
+        k_ls_arm<<<1, 32, 0, cs>>>(w.st, w.energy, ls);
+        cudaGraphNodeParams lp{};
+        lp.type = cudaGraphNodeTypeConditional;
+        lp.conditional.handle = ls;
+        lp.conditional.type = cudaGraphCondTypeWhile;
+        lp.conditional.size = 1;
+        cudaGraphNode_t lnode;
+        if (cudaGetLastError() != cudaSuccess ||
+            cudaStreamGetCaptureInfo(cs, &bcst, nullptr, &body, &deps, nullptr, &ndeps) != cudaSuccess ||
+            cudaGraphAddNode(&lnode, body, deps, nullptr, ndeps, &lp) != cudaSuccess ||
+            cudaStreamUpdateCaptureDependencies(cs, &lnode, nullptr, 1, cudaStreamSetCaptureDependencies) !=
+                cudaSuccess ||
+            cudaStreamCreateWithFlags(&ls_stream, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamBeginCaptureToGraph(ls_stream, lp.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+          rc = FOLGB_ERR_CUDA;
+        } else {
+          k_ls_trial<<<vb, 256, 0, ls_stream>>>(n, dofs, w.du, w.ut, w.st);
+          int erc = folgb_loss_adjoint(p, 1, control, 0, w.ut, n, 0, w.energy + 1, nullptr, nullptr, w.ls_status,
+                                       w.loss_ws, w.loss_bytes, ls_stream);
+          k_ls_control<<<1, 32, 0, ls_stream>>>(w.st, w.energy, w.energy + 1, ls);
+          const bool launched = cudaGetLastError() == cudaSuccess;
+          cudaGraph_t ls_out = nullptr;
+          if (cudaStreamEndCapture(ls_stream, &ls_out) != cudaSuccess || !launched || erc != FOLGB_OK)
+            rc = erc != FOLGB_OK ? erc : FOLGB_ERR_CUDA;
+        }
+        if (ls_stream) cudaStreamDestroy(ls_stream);
+      }
+    }
+    if (rc == FOLGB_OK) {
       k_newton_update<<<vb, 256, 0, cs>>>(n, dofs, w.du, w.st);
+      k_newton_loop<<<1, 32, 0, cs>>>(w.st, loop);
       if (cudaGetLastError() != cudaSuccess) rc = FOLGB_ERR_CUDA;
     }
     cudaGraph_t body_out = nullptr;
@@ -1658,7 +1817,7 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
   if (rc == FOLGB_OK && cudaGraphInstantiate(&exec, g, 0) != cudaSuccess) rc = FOLGB_ERR_CUDA;
   NState fin{};
   if (rc == FOLGB_OK) {
-    if (cudaMemsetAsync(w.counter, 0, 2 * sizeof(unsigned), st) != cudaSuccess ||
+    if (cudaMemsetAsync(w.counter, 0, 4 * sizeof(unsigned), st) != cudaSuccess ||
         cudaMemcpyAsync(w.st, &init, sizeof(NState), cudaMemcpyHostToDevice, st) != cudaSuccess ||
         cudaGraphLaunch(exec, st) != cudaSuccess ||
         cudaMemcpyAsync(&fin, w.st, sizeof(NState), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
@@ -1681,6 +1840,7 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
     info->last_delta_norm = fin.newton_total > 0 ? std::sqrt(fin.dn2) : 0.0;
     info->krylov_failures = fin.krylov_fail;
     info->status = fin.status;
+    info->line_search_halvings = fin.ls_halvings;
   }
   return fin.status;
 }

@@ -375,7 +375,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
   }
   // tile tables of the tile-local fused kernel (hex8 elasticity, 2x2x2 Gauss)
   if (p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && phys->num_gp == 2 &&
-      (rc = build_tile_tables(p, c32, xyz))) {
+      (rc = build_tile_tables(p, c32, xyz, dmask, elem_bc))) {
     folgb_plan_destroy(p);
     return rc;
   }

@@ -23,7 +23,7 @@
 //      ascending node id;
 //   4. per local node, the list of records (a * kTileElems + element-in-tile)
 //      of the tile's elements that touch it, in ascending element then corner
-//      order;
+//      order, and the node's Dirichlet mask;
 //   5. per boundary node, its partial slots in ascending tile order.
 #include <algorithm>
 #include <cstring>
@@ -55,7 +55,8 @@ int upload_vec(T** dst, const std::vector<T>& v) {
 
 }  // namespace
 
-int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz) {
+int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz,
+                      const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc) {
   const int nen = p->nen;
   const int64_t E = p->E, N = p->N;
   if (nen != 8 || E > (int64_t)INT32_MAX / nen) return FOLGB_OK;  // hex8 only; no tables otherwise
@@ -132,7 +133,8 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
       }
   // 3.-4. local nodes, local connectivity, record lists
   std::vector<int> tile_nptr{0}, tile_bptr{0}, tn_gid;
-  std::vector<unsigned short> tn_cend, tc_pos((size_t)E * nen);
+  std::vector<unsigned> tn_info;
+  std::vector<unsigned short> tc_pos((size_t)E * nen);
   std::vector<unsigned char> t_lconn((size_t)E * nen);
   std::vector<int> local(N, -1), nodes, counts;
   std::fill(stamp.begin(), stamp.end(), -1);
@@ -175,7 +177,7 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
       }
     for (int k = 0; k < nl; ++k) {
       tn_gid.push_back(nodes[k]);
-      tn_cend.push_back((unsigned short)counts[k + 1]);
+      tn_info.push_back((unsigned)counts[k + 1] | ((unsigned)dmask[nodes[k]] << 16));
     }
     tile_nptr.push_back(tile_nptr.back() + nl);
     tile_bptr.push_back(tile_bptr.back() + nb);
@@ -197,12 +199,14 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
     const int n0 = tile_nptr[t], nb = tile_bptr[t + 1] - tile_bptr[t];
     for (int k = 0; k < nb; ++k) bn_slot[node_pos[tn_gid[n0 + k]]++] = tile_bptr[t] + k;
   }
-  std::vector<int> t_elem(order.begin(), order.end());
+  // element ids in tile order; bit 31: the element touches a Dirichlet dof
+  std::vector<int> t_elem(E);
+  for (int64_t i = 0; i < E; ++i) t_elem[i] = order[i] | (elem_bc[order[i]] ? (int)0x80000000u : 0);
   int rc;
   if ((rc = upload_vec(&p->d_tile_eptr, tile_eptr)) || (rc = upload_vec(&p->d_tile_nptr, tile_nptr)) ||
       (rc = upload_vec(&p->d_tile_bptr, tile_bptr)) || (rc = upload_vec(&p->d_t_elem, t_elem)) ||
       (rc = upload_vec(&p->d_t_lconn, t_lconn)) || (rc = upload_vec(&p->d_tc_pos, tc_pos)) ||
-      (rc = upload_vec(&p->d_tn_gid, tn_gid)) || (rc = upload_vec(&p->d_tn_cend, tn_cend)) ||
+      (rc = upload_vec(&p->d_tn_gid, tn_gid)) || (rc = upload_vec(&p->d_tn_info, tn_info)) ||
       (rc = upload_vec(&p->d_bn_node, bn_node)) || (rc = upload_vec(&p->d_bn_ptr, bn_ptr)) ||
       (rc = upload_vec(&p->d_bn_slot, bn_slot)) || (rc = upload_vec(&p->d_in_node, in_node))) {
     free_tile_tables(p);
@@ -218,12 +222,13 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
 
 void free_tile_tables(folgb_plan* p) {
   void* ptrs[] = {p->d_tile_eptr, p->d_tile_nptr, p->d_tile_bptr, p->d_t_elem, p->d_t_lconn, p->d_tc_pos,
-                  p->d_tn_gid,    p->d_tn_cend,   p->d_bn_node,   p->d_bn_ptr, p->d_bn_slot, p->d_in_node};
+                  p->d_tn_gid,    p->d_tn_info,   p->d_bn_node,   p->d_bn_ptr, p->d_bn_slot, p->d_in_node};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_tile_eptr = p->d_tile_nptr = p->d_tile_bptr = p->d_t_elem = nullptr;
   p->d_t_lconn = nullptr;
-  p->d_tc_pos = p->d_tn_cend = nullptr;
+  p->d_tc_pos = nullptr;
+  p->d_tn_info = nullptr;
   p->d_tn_gid = p->d_bn_node = p->d_bn_ptr = p->d_bn_slot = p->d_in_node = nullptr;
   p->tiles = 0;
 }

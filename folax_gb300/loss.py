@@ -47,8 +47,9 @@ HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, du
                       "persistent, TMA-staged rows, 96 regs, point sums",
                       "persistent, TMA-staged rows, next tile's nodes prefetched to L1, paired points (f32x2)",
                       "persistent, TMA-staged rows, next tile's nodes prefetched to L2, paired points (f32x2)",
-                      "tile-local: nodes staged and residuals summed in shared memory, paired points (f32x2)",
-                      "tile-local, 96 regs, paired points (f32x2)"]
+                      "tile-local, persistent: tile inputs copied ahead by cp.async, residuals summed in shared "
+                      "memory, paired points (f32x2)",
+                      "tile-local, one block per tile, paired points (f32x2)"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 

@@ -161,12 +161,17 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
     "device_resident" (default True): the whole solve, load steps, Newton
     iterations and Krylov iterations, runs as one CUDA graph (folgb_newton)
     with no host synchronisation until it ends; False: a host loop with one
-    host read per Newton iteration."""
+    host read per Newton iteration.
+    "line_search" (default False, the reference's full steps): True takes
+    t dx with the backtracking rule of folgb_newton on the element energy
+    (for losses whose residual is the energy gradient, e.g. neo-Hooke with
+    voigt_shear_mode "consistent"); "line_search_max_halvings" (default 30)."""
 
     def __init__(self, fe_solver_name, fe_loss_function, fe_solver_settings: dict = {}, history_plot_settings: dict = {}):
         super().__init__(fe_solver_name, fe_loss_function, fe_solver_settings)
         self.nonlinear_solver_settings = {"rel_tol": 1e-8, "abs_tol": 1e-8, "maxiter": 20, "load_incr": 5,
-                                          "device_resident": True}
+                                          "device_resident": True, "line_search": False,
+                                          "line_search_max_halvings": 30}
         self.history = []
         self.last_newton_info = None
 
@@ -189,6 +194,8 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
         st.vector_bits = self._vector_bits()
         st.krylov_rtol, st.krylov_maxiter = float(ls["tol"]), int(ls["maxiter"])
         st.check_every = int(ls.get("check_every", 32))
+        st.line_search = 1 if s.get("line_search", False) else 0
+        st.line_search_max_halvings = int(s.get("line_search_max_halvings", 30))
         nbytes = plan.lib.folgb_newton_workspace_bytes(plan.handle, C.byref(st))
         ws = torch.empty(nbytes, dtype=torch.uint8, device="cuda")
         u = _dev(current_dofs).clone().reshape(-1)
@@ -201,13 +208,37 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
         self.last_newton_info = {"newton_iterations": info.newton_iterations,
                                  "krylov_iterations": info.krylov_iterations,
                                  "res_norm": info.last_res_norm, "delta_norm": info.last_delta_norm,
-                                 "krylov_failures": info.krylov_failures, "status": info.status}
+                                 "krylov_failures": info.krylov_failures, "status": info.status,
+                                 "line_search_halvings": info.line_search_halvings}
         self.history = [{"load_step": int(h[0]), "iteration": int(h[1]), "res_norm": float(h[2]),
                          "delta_dofs_norm": float(h[3])} for h in hist[:info.newton_iterations]]
         if rc == capi.ERR_NAN:
             raise ValueError("Residual norm contains NaN values.")
+        if rc == capi.ERR_NOT_CONVERGED:
+            raise ValueError("Newton line search found no step that decreases the energy.")
         capi.check("folgb_newton", rc)
         return u
+
+    def _line_search(self, control, u, du, r):
+        """Host-loop twin of folgb_newton's backtracking rule: returns t."""
+        torch = _torch()
+        loss = self.fe_loss_function
+        s = self.nonlinear_solver_settings
+        e0 = float(loss.ComputeTotalEnergy(control, u))
+        slope = -torch.dot(r.double(), du.double()).item()  # predicted decrease
+        if not np.isfinite(slope) or slope <= 0.0:
+            # not a descent direction: the Jacobi-preconditioned steepest descent step
+            du.copy_(-r / self._last_diag)
+            slope = -torch.dot(r.double(), du.double()).item()
+        if 0.0 <= slope <= 1e-6 * abs(e0):
+            return 1.0
+        t = 1.0
+        for _ in range(int(s["line_search_max_halvings"]) + 1):
+            et = float(loss.ComputeTotalEnergy(control, u + t * du))
+            if np.isfinite(et) and et <= e0 - 1e-4 * t * max(slope, 0.0) + 2e-6 * abs(e0):
+                return t
+            t *= 0.5
+        raise ValueError("Newton line search found no step that decreases the energy.")
 
     def Solve(self, current_control_vars, current_dofs):
         torch = _torch()
@@ -231,5 +262,7 @@ class FiniteElementNonLinearResidualBasedSolver(FiniteElementLinearResidualBased
                                      "delta_dofs_norm": delta_norm, "linear": self.last_linear_info})
                 if res_norm < s["abs_tol"] or delta_norm < s["rel_tol"] or it == s["maxiter"]:
                     break
-                u = u + du
+                self._last_diag = 1.0 / jac.inv_diag
+                t = self._line_search(current_control_vars, u, du, r) if s.get("line_search", False) else 1.0
+                u = u + du if t == 1.0 else u + t * du
         return u

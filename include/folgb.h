@@ -304,13 +304,28 @@ typedef struct folgb_newton_settings {
   int32_t vector_bits;      /* 32 or 64 (folgb_krylov)                */
   double krylov_rtol;       /* linear_solver_settings "tol"           */
   int32_t krylov_maxiter, check_every;
+  /* Globalisation (no counterpart in the reference, whose Newton takes full
+   * steps): 0 full steps; 1 backtracking line search on the element energy
+   * (the plan's loss with exponent 1): the step t du, t = 1, 1/2, 1/4, ...
+   * is taken once E(u + t du) <= E(u) + 1e-4 t (r . du) + 2e-6 |E(u)| and is
+   * finite (no inverted element), at most line_search_max_halvings halvings
+   * (then the solve stops with FOLGB_ERR_NOT_CONVERGED); a step whose
+   * predicted decrease -(r . du) is below 1e-6 |E(u)| (the energy's fp32
+   * resolution) is taken whole; a Newton step that is not a descent
+   * direction (r . du >= 0: an indefinite tangent) or that the Krylov solve
+   * left non-finite is replaced by the Jacobi-preconditioned steepest descent
+   * step -D^-1 r.  Valid where the residual is the energy gradient:
+   * neo-Hooke with FOLGB_SHEAR_CONSISTENT, no body force. */
+  int32_t line_search, line_search_max_halvings;
 } folgb_newton_settings;
 typedef struct folgb_newton_info {
   int32_t newton_iterations;   /* over all load steps                 */
   int64_t krylov_iterations;   /* sum over the Newton iterations      */
   double last_res_norm, last_delta_norm;
   int32_t krylov_failures;     /* linear solves that ended non-finite / broke down */
-  int32_t status;              /* FOLGB_OK or FOLGB_ERR_NAN           */
+  int32_t status;              /* FOLGB_OK, FOLGB_ERR_NAN, or FOLGB_ERR_NOT_CONVERGED
+                                  (a line search that found no acceptable step) */
+  int32_t line_search_halvings; /* over all Newton iterations           */
 } folgb_newton_info;
 size_t folgb_newton_workspace_bytes(const folgb_plan* plan, const folgb_newton_settings* settings);
 /* dofs [total_dofs] (device): the initial guess in, the solution out.

@@ -947,11 +947,17 @@ def linear_solve(loss: FELossOracle, ctrl, u0):
     return u + direct_solve(A, -R)
 
 
-def newton_solve(loss: FELossOracle, ctrl, u0, load_incr=5, maxiter=20, abs_tol=1e-8, rel_tol=1e-8):
+def newton_solve(loss: FELossOracle, ctrl, u0, load_incr=5, maxiter=20, abs_tol=1e-8, rel_tol=1e-8,
+                 line_search=False, max_halvings=30):
     """FiniteElementNonLinearResidualBasedSolver.Solve
     (fe_nonlinear_residual_based_solver.py:76-170): load stepping, Newton,
     convergence on |r| < abs_tol or |du| < rel_tol or maxiter; the converged
-    step's update is not applied (:162-166)."""
+    step's update is not applied (:162-166).  line_search=True (not in the
+    reference, which takes full steps): backtracking on the total energy,
+    t = 1, 1/2, ... until E(u + t du) <= E(u) - 1e-4 t max(-(r . du), 0) and
+    finite, with du replaced by the Jacobi-preconditioned steepest descent
+    step -D^-1 r when the Newton step is not a descent direction (FP64; for
+    losses whose residual is the energy gradient)."""
     u = np.array(u0, dtype=np.float64, copy=True)
     history = []
     for step in range(1, load_incr + 1):
@@ -966,7 +972,24 @@ def newton_solve(loss: FELossOracle, ctrl, u0, load_incr=5, maxiter=20, abs_tol=
             history.append((step, it, rn, dn))
             if rn < abs_tol or dn < rel_tol or it == maxiter:
                 break
-            u = u + du
+            t = 1.0
+            if line_search:
+                with np.errstate(all="ignore"):
+                    e0 = loss.total_energy(ctrl, u)
+                    slope = -float(R @ du)
+                    if not np.isfinite(dn) or slope <= 0.0:
+                        # not a descent direction (indefinite tangent): the
+                        # Jacobi-preconditioned steepest descent step instead
+                        du = -R / A.diagonal()
+                        slope = -float(R @ du)
+                    for _ in range(max_halvings + 1):
+                        et = loss.total_energy(ctrl, u + t * du)
+                        if np.isfinite(et) and et <= e0 - 1e-4 * t * max(slope, 0.0):
+                            break
+                        t *= 0.5
+                    else:
+                        raise ValueError("line search found no decrease")
+            u = u + t * du
     return u, history
 
 
