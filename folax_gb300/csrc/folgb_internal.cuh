@@ -95,10 +95,10 @@ struct folgb_plan {
   int* d_tile_bptr = nullptr;           // [T+1] boundary slot range of each tile (its first local nodes)
   int* d_t_elem = nullptr;              // [E] element ids in tile order, bit 31: touches a Dirichlet dof
   unsigned char* d_t_lconn = nullptr;   // [E][nen] local node ids, reference node order
-  unsigned short* d_tc_pos = nullptr;   // [E*nen] record position a*kTileElems + e_local, grouped by local node
+  unsigned short* d_tn_pos = nullptr;   // [K][kTileRecs] record positions a*kTileElems + e_local of each
+                                        // local entry, padded with kTileZeroRec
   int* d_tn_gid = nullptr;              // [K] global node id of each local node
-  unsigned* d_tn_info = nullptr;        // [K] bits 0-15: end of the local node's records in tc_pos
-                                        // (tile-relative); bits 16-18: its Dirichlet mask
+  unsigned* d_tn_info = nullptr;        // [K] bits 16-18: the node's Dirichlet mask
   int* d_bn_node = nullptr;             // [NB] boundary nodes
   int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
   int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
@@ -158,7 +158,9 @@ void noalloc_prepare_current_device();
 
 // Element tiles of the tile-local fused loss (tiles.cu).
 constexpr int kTileElems = 128;  // elements per tile at most (one thread each)
-constexpr int kTileNodes = 256;  // distinct nodes per tile at most (8-bit local ids)
+constexpr int kTileNodes = 256;  // local node entries per tile at most (8-bit local ids)
+constexpr int kTileRecs = 8;     // records per local node entry (one 16-byte row of positions)
+constexpr int kTileZeroRec = 8 * kTileElems;  // position of the zero record padding the rows
 int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz,
                       const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc);
 void free_tile_tables(folgb_plan* p);

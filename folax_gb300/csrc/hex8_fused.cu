@@ -716,9 +716,9 @@ struct TileArgs {
   const int* tile_bptr;
   const int* t_elem;  // bit 31: the element touches a Dirichlet dof
   const uint2* t_lconn;
-  const unsigned short* tc_pos;
+  const uint4* tn_pos;  // [K] kTileRecs record positions (uint16) of each local entry
   const int* tn_gid;
-  const unsigned* tn_info;  // bits 0-15: record list end; bits 16-18: Dirichlet mask
+  const unsigned* tn_info;  // bits 16-18: Dirichlet mask
   const int* bn_node;
   const int* bn_ptr;
   const int* bn_slot;
@@ -785,30 +785,34 @@ __device__ __forceinline__ float tile_element(const VecArgs& A, const float* ctr
   return energy;
 }
 
-// Node pass of a tile: local node k sums its records (list end in info,
-// positions in pos) in order; an interior node writes its gradient, a
-// boundary node (k < nb) its partial record.
+// Node pass of a tile: local entry k sums its kTileRecs records (row k of
+// pos; padding points at the zero record) in order, all loads issued before
+// the adds; an interior node writes its gradient, an entry with partials
+// (k < nb) its partial record.
 template <int CL>
-__device__ __forceinline__ void tile_nodes(const VecArgs& A, const float4* rec, const unsigned short* pos,
+__device__ __forceinline__ void tile_nodes(const VecArgs& A, const float4* rec, const uint4* pos,
                                            const unsigned* info, const int* gid, int nl, int nb, float4* bpart,
                                            int b) {
   const float sc = (A.exponent == 1.f) ? A.inv_batch : 1.f;
   for (int k = threadIdx.x; k < nl; k += kTileElems) {
-    const unsigned inf = info[k];
-    const int c0 = k == 0 ? 0 : (int)(info[k - 1] & 0xffffu), c1 = (int)(inf & 0xffffu);
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int j = c0; j < c1; ++j) {
-      const float4 r = rec[pos[j]];
-      acc.x += r.x;
-      acc.y += r.y;
-      acc.z += r.z;
-      acc.w += r.w;
+    const uint4 pr = pos[k];
+    const unsigned w[4] = {pr.x, pr.y, pr.z, pr.w};
+    float4 r[kTileRecs];
+#pragma unroll
+    for (int j = 0; j < kTileRecs; ++j) r[j] = rec[(w[j >> 1] >> (16 * (j & 1))) & 0xffffu];
+    float4 acc = r[0];
+#pragma unroll
+    for (int j = 1; j < kTileRecs; ++j) {
+      acc.x += r[j].x;
+      acc.y += r[j].y;
+      acc.z += r[j].z;
+      acc.w += r[j].w;
     }
     if (k < nb) {
       bpart[k] = acc;
     } else {
       const int n = gid[k];
-      const unsigned m = inf >> 16;
+      const unsigned m = info[k] >> 16;
       if (A.out) {
         float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
         o[0] = (m & 1u) ? 0.f : sc * acc.x;
@@ -828,8 +832,8 @@ __global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const Ve
   __shared__ float4 sU[kTileNodes];  // displacements, nodal control in w
   __shared__ unsigned sInfo[kTileNodes];
   __shared__ int sGid[kTileNodes];
-  __shared__ float4 sR[8 * kTileElems];
-  __shared__ unsigned short sPos[8 * kTileElems];
+  __shared__ float4 sR[8 * kTileElems + 1];  // + the zero record
+  __shared__ uint4 sPos[kTileNodes];
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   pdl_launch_dependents();
@@ -838,7 +842,10 @@ __global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const Ve
   const int n0 = __ldg(T.tile_nptr + tile), nl = __ldg(T.tile_nptr + tile + 1) - n0;
   const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
   const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
-  if (threadIdx.x == 0) wcount = 0u;
+  if (threadIdx.x == 0) {
+    wcount = 0u;
+    sR[kTileZeroRec] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
   for (int k = threadIdx.x; k < nl; k += kTileElems) {
     const int n = __ldg(T.tn_gid + n0 + k);
     const float4 x = __ldg(A.xyz4 + n);
@@ -848,8 +855,8 @@ __global__ void __launch_bounds__(kTileElems, MINB) k_hex8_elastic_tile(const Ve
                         CL == FOLGB_CONTROL_NODAL ? __ldg(ctrl + n) : 0.f);
     sInfo[k] = __ldg(T.tn_info + n0 + k);
     sGid[k] = n;
+    sPos[k] = __ldg(T.tn_pos + n0 + k);
   }
-  for (int j = threadIdx.x; j < 8 * ne; j += kTileElems) sPos[j] = __ldg(T.tc_pos + (int64_t)e0 * 8 + j);
   __syncthreads();
   float energy = 0.f;
   int bad = 0;
@@ -895,16 +902,16 @@ struct TileMeta {
 struct TileStage {
   float4 X[kTileNodes];
   float4 U[kTileNodes];
+  uint4 pos[kTileNodes];
   unsigned info[kTileNodes];
   uint2 lconn[kTileElems];
   int elem[kTileElems];
-  unsigned short pos[8 * kTileElems];
 };
 
 struct TileSmem {
   TileStage st[2];
   int gid[3][kTileNodes];
-  float4 rec[8 * kTileElems];
+  float4 rec[8 * kTileElems + 1];  // + the zero record
   TileMeta meta[4];
   float wsum[2][kTileElems / 32];
   int last;
@@ -945,11 +952,11 @@ __device__ __forceinline__ void issue_inputs(TileSmem& S, const VecArgs& A, cons
     cp_async4(&Z.U[k].z, du + 2);
     if (CL == FOLGB_CONTROL_NODAL) cp_async4(&Z.U[k].w, ctrl + n);
     cp_async4(&Z.info[k], T.tn_info + m.n0 + k);
+    cp_async16(&Z.pos[k], T.tn_pos + m.n0 + k);
   }
   for (int j = threadIdx.x; j < m.ne; j += kTileElems) {
     cp_async8(&Z.lconn[j], T.t_lconn + m.e0 + j);
     cp_async4(&Z.elem[j], T.t_elem + m.e0 + j);
-    cp_async16(&Z.pos[8 * j], T.tc_pos + (int64_t)(m.e0 + j) * 8);
   }
 }
 
@@ -967,6 +974,7 @@ __global__ void __launch_bounds__(kTileElems, 4) k_hex8_elastic_tile_pipe(const 
   // k = 2 on from the queue (offset by the 2 * gridDim.x tiles taken so)
   auto next_tile = [&]() { return 2 * (int)gridDim.x + (int)atomicAdd(T.queue + b, 1u); };
   if (threadIdx.x == 0) {
+    S.rec[kTileZeroRec] = make_float4(0.f, 0.f, 0.f, 0.f);
     S.meta[0] = tile_meta(T, blockIdx.x);
     S.meta[1] = tile_meta(T, gridDim.x + blockIdx.x);
     S.meta[2] = tile_meta(T, S.meta[1].tile < T.ntiles ? next_tile() : T.ntiles);
@@ -1101,7 +1109,7 @@ static TileArgs tile_args(const folgb_plan* p) {
   T.tile_bptr = p->d_tile_bptr;
   T.t_elem = p->d_t_elem;
   T.t_lconn = reinterpret_cast<const uint2*>(p->d_t_lconn);
-  T.tc_pos = p->d_tc_pos;
+  T.tn_pos = reinterpret_cast<const uint4*>(p->d_tn_pos);
   T.tn_gid = p->d_tn_gid;
   T.tn_info = p->d_tn_info;
   T.queue = nullptr;
@@ -1126,6 +1134,14 @@ static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, b
   }
   static std::atomic<int> occ_bf[kOccDevices], occ[kOccDevices];  // per instantiation and device
   auto k = bf ? k_hex8_elastic_tile_pipe<CL, true> : k_hex8_elastic_tile_pipe<CL, false>;
+  static std::atomic<int> attr_set[kOccDevices][2];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= kOccDevices) dev = 0;
+  if (!attr_set[dev][bf ? 1 : 0].load()) {  // more than the default 48 KB of dynamic shared memory
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem));
+    attr_set[dev][bf ? 1 : 0].store(1);
+  }
   const int per_sm = blocks_per_sm(k, kTileElems, sizeof(TileSmem), bf ? occ_bf : occ);
   int64_t g = (int64_t)per_sm * num_sms() / B;
   if (g > p->tiles) g = p->tiles;

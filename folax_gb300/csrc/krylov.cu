@@ -37,6 +37,10 @@ struct KScalars {
   double alpha, beta, omega;
   int iters, done, replace, maxiter, restart, breakdowns;
   int rounds;  // device-resident solve: executions of the loop body
+  // which of the two direction buffers (p, and v for BiCGSTAB) holds the
+  // current direction: flipped by the update kernel of every iteration that
+  // ran, so iterations skipped after a replacement leave it in place
+  int pcur;
 };
 // done: 1 converged (true residual), 2 maxiter, 3 non-finite, 4 repeated breakdown or divergence
 
@@ -357,6 +361,7 @@ __global__ void k_pcg_init(int64_t n, const float* __restrict__ b, const float* 
     sc->restart = 0;
     sc->breakdowns = 0;
     sc->rounds = 0;
+    sc->pcur = 0;
     sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
     counters[0] = 0u;
   }
@@ -366,11 +371,12 @@ template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(256, kSpmvMinBlocks<VT>) k_pcg_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                   const int* __restrict__ adj, int maxdeg,
                                                   const float* __restrict__ vals, const VT* __restrict__ z,
-                                                  const VT* __restrict__ pold, VT* __restrict__ pnew,
-                                                  VT* __restrict__ q, double* part, unsigned* counters,
-                                                  KScalars* sc) {
+                                                  VT* pbuf0, VT* pbuf1, VT* __restrict__ q, double* part,
+                                                  unsigned* counters, KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
+  const VT* __restrict__ pold = sc->pcur ? pbuf1 : pbuf0;
+  VT* __restrict__ pnew = sc->pcur ? pbuf0 : pbuf1;
   const VT beta = (VT)sc->beta;
   VT dot = VT(0);  // this lane's rows only (a handful); fp64 from the block sum on
   FOLGB_NODE_BLOCKS(NDOF, G) {
@@ -406,10 +412,11 @@ __global__ void __launch_bounds__(256, kSpmvMinBlocks<VT>) k_pcg_spmv(int64_t N,
 template <class VT>
 __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __restrict__ dinv,
                                                     double* __restrict__ x, VT* __restrict__ r, VT* __restrict__ z,
-                                                    const VT* __restrict__ p, const VT* __restrict__ q, double* part,
-                                                    unsigned* counters, KScalars* sc) {
+                                                    const VT* pbuf0, const VT* pbuf1, const VT* __restrict__ q,
+                                                    double* part, unsigned* counters, KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
+  const VT* __restrict__ p = sc->pcur ? pbuf0 : pbuf1;  // the direction the SpMV just wrote
   const double alpha = sc->alpha;
   const VT af = (VT)alpha;
   VT rz = VT(0), rr = VT(0);  // per-thread partials over a few entries
@@ -465,6 +472,7 @@ __global__ void __launch_bounds__(256) k_pcg_update(int64_t n, const float* __re
     sc->rnorm2 = RR;
     sc->iters += 1;
     sc->breakdowns = 0;
+    sc->pcur ^= 1;
     if (!isfinite(RR)) sc->done = 3;
     else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2) sc->replace = 1;
     if (!sc->done && sc->iters >= sc->maxiter) sc->replace = 1;
@@ -507,6 +515,7 @@ __global__ void k_bicg_init(int64_t n, const float* __restrict__ b, double* __re
     sc->restart = 1;
     sc->breakdowns = 0;
     sc->rounds = 0;
+    sc->pcur = 0;
     sc->done = (BB == 0.0 || !isfinite(BB)) ? (BB == 0.0 ? 1 : 3) : 0;
     counters[0] = 0u;
   }
@@ -519,12 +528,16 @@ __global__ void __launch_bounds__(256) k_bicg_p_spmv(int64_t N, const int* __res
                                                      const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
                                                      const VT* __restrict__ r, const VT* __restrict__ rhat,
-                                                     const VT* __restrict__ pold, const VT* __restrict__ vold,
-                                                     VT* __restrict__ pnew, VT* __restrict__ y,
-                                                     VT* __restrict__ vnew, double* part, unsigned* counters,
+                                                     VT* pbuf0, VT* pbuf1, VT* vbuf0, VT* vbuf1,
+                                                     VT* __restrict__ y, double* part, unsigned* counters,
                                                      KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
+  const int c = sc->pcur;
+  const VT* __restrict__ pold = c ? pbuf1 : pbuf0;
+  const VT* __restrict__ vold = c ? vbuf1 : vbuf0;
+  VT* __restrict__ pnew = c ? pbuf0 : pbuf1;
+  VT* __restrict__ vnew = c ? vbuf0 : vbuf1;
   const bool rs = sc->restart != 0;
   const VT beta = rs ? VT(0) : (VT)sc->beta;
   const VT omega = rs ? VT(0) : (VT)sc->omega;
@@ -567,11 +580,12 @@ template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __restrict__ adj_ptr,
                                                      const int* __restrict__ adj, int maxdeg,
                                                      const float* __restrict__ vals, const float* __restrict__ dinv,
-                                                     const VT* __restrict__ r, const VT* __restrict__ vnew,
+                                                     const VT* __restrict__ r, const VT* vbuf0, const VT* vbuf1,
                                                      VT* __restrict__ z, VT* __restrict__ t, double* part,
                                                      unsigned* counters, KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
+  const VT* __restrict__ vnew = sc->pcur ? vbuf0 : vbuf1;
   const VT af = (VT)sc->alpha;
   auto sval = [&](int64_t d) -> VT { return vfma(-af, __ldg(vnew + d), __ldg(r + d)); };
   VT ts = VT(0), tt = VT(0);
@@ -604,12 +618,13 @@ __global__ void __launch_bounds__(256) k_bicg_s_spmv(int64_t N, const int* __res
 
 template <class VT>
 __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restrict__ x, VT* __restrict__ r,
-                                                     const VT* __restrict__ rhat, const VT* __restrict__ vnew,
+                                                     const VT* __restrict__ rhat, const VT* vbuf0, const VT* vbuf1,
                                                      const VT* __restrict__ y, const VT* __restrict__ z,
                                                      const VT* __restrict__ t, double* part, unsigned* counters,
                                                      KScalars* sc) {
   __shared__ double sh[32];
   if (sc->done || sc->replace) return;
+  const VT* __restrict__ vnew = sc->pcur ? vbuf0 : vbuf1;
   const double alpha = sc->alpha, omega = sc->omega;
   const VT af = (VT)alpha, of = (VT)omega;
   VT rhr = VT(0), rr = VT(0);  // per-thread partials over a few entries
@@ -637,6 +652,7 @@ __global__ void __launch_bounds__(256) k_bicg_update(int64_t n, double* __restri
     sc->rnorm2 = RR;
     sc->iters += 1;
     sc->breakdowns = 0;
+    sc->pcur ^= 1;
     if (!isfinite(RR)) sc->done = 3;
     else if (RH == 0.0 || omega == 0.0) sc->replace = 2;  // breakdown: restart
     else if (RR <= sc->tol2 || RR <= kReplaceDrop2 * sc->rref2 || RR > kDiverge2 * sc->bnorm2) sc->replace = 1;
@@ -1085,37 +1101,35 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
     k_bicg_init<VT><<<vb, 256, 0, s>>>(n, rhs, w.x, w.r, w.rhat, w.part, w.counters, w.sc, rtol, maxiter);
   FOLGB_LAUNCH_CHECK();
   KScalars host{};
-  VT *pa = w.p0, *pb = w.p1, *va = w.v0, *vb_ = w.v1;
   int rc = with_ndof(p->ndof, [&](auto nd) -> int {
     constexpr int NDOF = decltype(nd)::value;
     return with_group<NDOF>(p->maxdeg, [&](auto gw) -> int {
       constexpr int G = decltype(gw)::value;
       const int sb = spmv_blocks<NDOF>(p, G);
-      // one chunk of iterations on stream cs (an even count keeps the p / v
-      // ping-pong buffers aligned from one chunk to the next)
+      // one chunk of iterations on stream cs (the kernels pick the current
+      // direction buffers from the device scalars)
       auto chunk = [&](int count, cudaStream_t cs) {
         for (int k = 0; k < count; ++k) {
           if (solver == SOLVER_CG) {
             trace_begin(KID_PCG_SPMV, cs);
-            k_pcg_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, pa, pb,
-                                                     w.q, w.part, w.counters, w.sc);
+            k_pcg_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, w.z, w.p0,
+                                                     w.p1, w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, cs);
             trace_begin(KID_PCG_UPDATE, cs);
-            k_pcg_update<VT><<<ub, 256, 0, cs>>>(n, dinv, w.x, w.r, w.z, pb, w.q, w.part, w.counters, w.sc);
+            k_pcg_update<VT><<<ub, 256, 0, cs>>>(n, dinv, w.x, w.r, w.z, w.p0, w.p1, w.q, w.part, w.counters, w.sc);
             trace_end(KID_PCG_UPDATE, cs);
-            std::swap(pa, pb);
           } else {
             trace_begin(KID_PCG_SPMV, cs);
             k_bicg_p_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
-                                                        w.rhat, pa, va, pb, w.y, vb_, w.part, w.counters, w.sc);
+                                                        w.rhat, w.p0, w.p1, w.v0, w.v1, w.y, w.part, w.counters,
+                                                        w.sc);
             k_bicg_s_spmv<NDOF, G, VT><<<sb, 256, 0, cs>>>(p->N, p->d_adj_ptr, p->d_adj, p->maxdeg, vals, dinv, w.r,
-                                                        vb_, w.z, w.t, w.part, w.counters, w.sc);
+                                                        w.v0, w.v1, w.z, w.t, w.part, w.counters, w.sc);
             trace_end(KID_PCG_SPMV, cs);
             trace_begin(KID_PCG_UPDATE, cs);
-            k_bicg_update<VT><<<vb, 256, 0, cs>>>(n, w.x, w.r, w.rhat, vb_, w.y, w.z, w.t, w.part, w.counters, w.sc);
+            k_bicg_update<VT><<<vb, 256, 0, cs>>>(n, w.x, w.r, w.rhat, w.v0, w.v1, w.y, w.z, w.t, w.part, w.counters,
+                                                  w.sc);
             trace_end(KID_PCG_UPDATE, cs);
-            std::swap(pa, pb);
-            std::swap(va, vb_);
           }
         }
       };

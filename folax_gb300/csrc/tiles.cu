@@ -18,16 +18,20 @@
 //   2. tiles are cut greedily along that order: an element joins the current
 //      tile unless the tile already has kTileElems elements or the element's
 //      new nodes would take it past kTileNodes distinct nodes;
-//   3. per tile, its distinct nodes get local ids: nodes that also belong to
-//      other tiles (boundary) first, then the tile's own nodes, each group in
-//      ascending node id;
-//   4. per local node, the list of records (a * kTileElems + element-in-tile)
-//      of the tile's elements that touch it, in ascending element then corner
-//      order, and the node's Dirichlet mask;
-//   5. per boundary node, its partial slots in ascending tile order.
+//   3. per tile, its distinct nodes get local entries: nodes that need
+//      partial records (they also belong to other tiles, or have more than
+//      kTileRecs records in this tile) first, then the tile's own nodes, each
+//      group in ascending node id;
+//   4. per entry, up to kTileRecs records (a * kTileElems + element-in-tile)
+//      of the tile's elements that touch the node, in ascending element then
+//      corner order, padded with the index of a zero record; a node with more
+//      records gets further entries (all of them partial), its first entry
+//      is the one the elements load from; and the node's Dirichlet mask;
+//   5. per node with partial records, its slots in ascending tile order.
 #include <algorithm>
 #include <cstring>
 #include <numeric>
+#include <vector>
 
 #include "folgb_internal.cuh"
 
@@ -87,40 +91,55 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return key[a] < key[b]; });
   key.clear();
   key.shrink_to_fit();
-  // 2. greedy tiles
+  // 2. greedy tiles.  A local node has at most kTileRecs records per entry;
+  // a node with more records in one tile gets further entries (see 4.), so
+  // the cut bounds the entries: sum over nodes of ceil(records / kTileRecs).
   std::vector<int> tile_eptr{0};
-  std::vector<int> stamp(N, -1);
-  int cur = 0, cur_nodes = 0, cur_elems = 0;
-  for (int64_t i = 0; i < E; ++i) {
-    const int e = order[i];
-    int fresh = 0;
+  std::vector<int> stamp(N, -1), cnt(N, 0);
+  int cur = 0, cur_entries = 0, cur_elems = 0;
+  auto entries_added = [&](int e, bool fresh_tile) {
+    // entries the element adds: corners in order, counting repeats
+    int add = 0;
+    int seen_n[8], seen_c[8], ns = 0;
     for (int a = 0; a < nen; ++a) {
       const int n = conn[(int64_t)e * nen + a];
-      bool dup = stamp[n] == cur;
-      for (int b = 0; b < a && !dup; ++b) dup = conn[(int64_t)e * nen + b] == n;
-      fresh += dup ? 0 : 1;
+      int j = 0;
+      while (j < ns && seen_n[j] != n) ++j;
+      if (j == ns) {
+        seen_n[ns] = n;
+        seen_c[ns++] = (!fresh_tile && stamp[n] == cur) ? cnt[n] : 0;
+      }
+      if (seen_c[j]++ % kTileRecs == 0) ++add;
     }
-    if (cur_elems == kTileElems || cur_nodes + fresh > kTileNodes) {
+    return add;
+  };
+  for (int64_t i = 0; i < E; ++i) {
+    const int e = order[i];
+    int add = entries_added(e, false);
+    if (cur_elems == kTileElems || cur_entries + add > kTileNodes) {
       tile_eptr.push_back((int)i);
       ++cur;
-      cur_nodes = 0;
+      cur_entries = 0;
       cur_elems = 0;
-      fresh = 0;
-      for (int a = 0; a < nen; ++a) {
-        const int n = conn[(int64_t)e * nen + a];
-        bool dup = false;
-        for (int b = 0; b < a && !dup; ++b) dup = conn[(int64_t)e * nen + b] == n;
-        fresh += dup ? 0 : 1;
-      }
+      add = entries_added(e, true);
     }
-    for (int a = 0; a < nen; ++a) stamp[conn[(int64_t)e * nen + a]] = cur;
-    cur_nodes += fresh;
+    for (int a = 0; a < nen; ++a) {
+      const int n = conn[(int64_t)e * nen + a];
+      if (stamp[n] != cur) {
+        stamp[n] = cur;
+        cnt[n] = 0;
+      }
+      cnt[n]++;
+    }
+    cur_entries += add;
     ++cur_elems;
   }
   tile_eptr.push_back((int)E);
   const int T = (int)tile_eptr.size() - 1;
-  // tiles touching each node
+  // tiles touching each node, and whether a node needs partial records
+  // (in no tile, in several, or with several entries in its tile)
   std::vector<int> ntiles(N, 0);
+  std::vector<unsigned char> partial(N, 0);
   std::fill(stamp.begin(), stamp.end(), -1);
   for (int t = 0; t < T; ++t)
     for (int i = tile_eptr[t]; i < tile_eptr[t + 1]; ++i)
@@ -128,69 +147,83 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
         const int n = conn[(int64_t)order[i] * nen + a];
         if (stamp[n] != t) {
           stamp[n] = t;
+          cnt[n] = 0;
           ntiles[n]++;
         }
+        if (++cnt[n] > kTileRecs) partial[n] = 1;
       }
-  // 3.-4. local nodes, local connectivity, record lists
+  for (int64_t n = 0; n < N; ++n)
+    if (ntiles[n] != 1) partial[n] = 1;
+  // 3.-4. local node entries, local connectivity, record lists
   std::vector<int> tile_nptr{0}, tile_bptr{0}, tn_gid;
   std::vector<unsigned> tn_info;
-  std::vector<unsigned short> tc_pos((size_t)E * nen);
+  std::vector<unsigned short> tn_pos;
   std::vector<unsigned char> t_lconn((size_t)E * nen);
-  std::vector<int> local(N, -1), nodes, counts;
+  std::vector<int> local(N, -1), nodes;
   std::fill(stamp.begin(), stamp.end(), -1);
+  std::vector<int> node_slot_count(N, 0);
   for (int t = 0; t < T; ++t) {
     nodes.clear();
-    for (int i = tile_eptr[t]; i < tile_eptr[t + 1]; ++i)
+    const int e0 = tile_eptr[t], ne = tile_eptr[t + 1] - e0;
+    for (int j = 0; j < ne; ++j)
       for (int a = 0; a < nen; ++a) {
-        const int n = conn[(int64_t)order[i] * nen + a];
+        const int n = conn[(int64_t)order[e0 + j] * nen + a];
         if (stamp[n] != t) {
           stamp[n] = t;
           nodes.push_back(n);
         }
       }
     std::sort(nodes.begin(), nodes.end(), [&](int a, int b) {
-      const bool ba = ntiles[a] > 1, bb = ntiles[b] > 1;
-      return ba != bb ? ba : a < b;
+      return partial[a] != partial[b] ? partial[a] > partial[b] : a < b;
     });
-    const int nl = (int)nodes.size();
-    if (nl > kTileNodes) return FOLGB_ERR_INVALID_ARGUMENT;  // cannot happen: tiles are cut before
-    int nb = 0;
-    for (int k = 0; k < nl; ++k) {
-      local[nodes[k]] = k;
-      nb += ntiles[nodes[k]] > 1 ? 1 : 0;
-    }
-    // records per local node, ascending element-in-tile then corner
-    counts.assign(nl + 1, 0);
-    const int e0 = tile_eptr[t], ne = tile_eptr[t + 1] - e0;
+    const int nn = (int)nodes.size();
+    for (int k = 0; k < nn; ++k) local[nodes[k]] = k;
+    // records of each distinct node, ascending element-in-tile then corner
+    std::vector<std::vector<unsigned short>> nrec(nn);
     for (int j = 0; j < ne; ++j)
       for (int a = 0; a < nen; ++a) {
         const int k = local[conn[(int64_t)order[e0 + j] * nen + a]];
-        t_lconn[(size_t)(e0 + j) * nen + a] = (unsigned char)k;
-        counts[k + 1]++;
+        nrec[k].push_back((unsigned short)(a * kTileElems + j));
       }
-    for (int k = 0; k < nl; ++k) counts[k + 1] += counts[k];
-    std::vector<int> fill(counts.begin(), counts.end() - 1);
-    for (int j = 0; j < ne; ++j)
-      for (int a = 0; a < nen; ++a) {
-        const int k = t_lconn[(size_t)(e0 + j) * nen + a];
-        tc_pos[(size_t)e0 * nen + fill[k]++] = (unsigned short)(a * kTileElems + j);
+    // entries: a node's records in chunks of kTileRecs; the first entry is
+    // the one the elements load from
+    std::vector<int> primary(nn);
+    int nl = 0, nb = 0;
+    for (int k = 0; k < nn; ++k) {
+      const int n = nodes[k];
+      const int chunks = std::max(1, (int)((nrec[k].size() + kTileRecs - 1) / kTileRecs));
+      primary[k] = nl;
+      for (int c = 0; c < chunks; ++c) {
+        tn_gid.push_back(n);
+        tn_info.push_back((unsigned)dmask[n] << 16);
+        for (int r = 0; r < kTileRecs; ++r) {
+          const size_t q = (size_t)c * kTileRecs + r;
+          tn_pos.push_back(q < nrec[k].size() ? nrec[k][q] : (unsigned short)kTileZeroRec);
+        }
+        ++nl;
+        if (partial[n]) {
+          ++nb;
+          node_slot_count[n]++;
+        }
       }
-    for (int k = 0; k < nl; ++k) {
-      tn_gid.push_back(nodes[k]);
-      tn_info.push_back((unsigned)counts[k + 1] | ((unsigned)dmask[nodes[k]] << 16));
     }
+    if (nl > kTileNodes) return FOLGB_ERR_INVALID_ARGUMENT;  // cannot happen: tiles are cut before
+    for (int j = 0; j < ne; ++j)
+      for (int a = 0; a < nen; ++a)
+        t_lconn[(size_t)(e0 + j) * nen + a] =
+            (unsigned char)primary[local[conn[(int64_t)order[e0 + j] * nen + a]]];
     tile_nptr.push_back(tile_nptr.back() + nl);
     tile_bptr.push_back(tile_bptr.back() + nb);
   }
-  // 5. boundary nodes (in no tile or in several), their slots in tile order
+  // 5. nodes with partial records, their slots in tile order (entries in order)
   const int64_t S = tile_bptr.back();
-  std::vector<int> bn_node, bn_ptr{0}, bn_slot(S), in_node, slot_fill(N + 1, 0);
+  std::vector<int> bn_node, bn_ptr{0}, bn_slot(S), in_node;
   for (int64_t n = 0; n < N; ++n) {
-    if (ntiles[n] == 1) {
+    if (!partial[n]) {
       in_node.push_back((int)n);
     } else {
       bn_node.push_back((int)n);
-      bn_ptr.push_back(bn_ptr.back() + ntiles[n]);
+      bn_ptr.push_back(bn_ptr.back() + node_slot_count[n]);
     }
   }
   std::vector<int> node_pos(N, -1);
@@ -205,7 +238,7 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
   int rc;
   if ((rc = upload_vec(&p->d_tile_eptr, tile_eptr)) || (rc = upload_vec(&p->d_tile_nptr, tile_nptr)) ||
       (rc = upload_vec(&p->d_tile_bptr, tile_bptr)) || (rc = upload_vec(&p->d_t_elem, t_elem)) ||
-      (rc = upload_vec(&p->d_t_lconn, t_lconn)) || (rc = upload_vec(&p->d_tc_pos, tc_pos)) ||
+      (rc = upload_vec(&p->d_t_lconn, t_lconn)) || (rc = upload_vec(&p->d_tn_pos, tn_pos)) ||
       (rc = upload_vec(&p->d_tn_gid, tn_gid)) || (rc = upload_vec(&p->d_tn_info, tn_info)) ||
       (rc = upload_vec(&p->d_bn_node, bn_node)) || (rc = upload_vec(&p->d_bn_ptr, bn_ptr)) ||
       (rc = upload_vec(&p->d_bn_slot, bn_slot)) || (rc = upload_vec(&p->d_in_node, in_node))) {
@@ -221,13 +254,13 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
 }
 
 void free_tile_tables(folgb_plan* p) {
-  void* ptrs[] = {p->d_tile_eptr, p->d_tile_nptr, p->d_tile_bptr, p->d_t_elem, p->d_t_lconn, p->d_tc_pos,
+  void* ptrs[] = {p->d_tile_eptr, p->d_tile_nptr, p->d_tile_bptr, p->d_t_elem, p->d_t_lconn, p->d_tn_pos,
                   p->d_tn_gid,    p->d_tn_info,   p->d_bn_node,   p->d_bn_ptr, p->d_bn_slot, p->d_in_node};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_tile_eptr = p->d_tile_nptr = p->d_tile_bptr = p->d_t_elem = nullptr;
   p->d_t_lconn = nullptr;
-  p->d_tc_pos = nullptr;
+  p->d_tn_pos = nullptr;
   p->d_tn_info = nullptr;
   p->d_tn_gid = p->d_bn_node = p->d_bn_ptr = p->d_bn_slot = p->d_in_node = nullptr;
   p->tiles = 0;

@@ -8,6 +8,8 @@
   FP64-assembled system (the whole fp32 pipeline).  That last error is set by
   storing the matrix in fp32: it is compared with the error of an FP64 solve
   whose only approximation is the FP64 matrix rounded to fp32.
+* 50 x 50 quad4 heat conduction (the small plain-method configuration): the
+  fp32 solve against FP64 assembly + direct solve (bound 1e-6).
 * 6-tet split of 64^3 (1,572,864 tets), neo-Hookean, batch 16: losses and
   both gradients of two instances against the C oracle (1e-5).
 * 512 uneven quad4 thermal instances (the benchmark's seed): losses and both
@@ -69,6 +71,39 @@ def test_c1_pcg_64cubed_solution_against_fp64(cuda):
     assert err_same <= 1e-6
     assert err_conv[1e-9] <= 1e-6
     assert err_pipeline <= 2.0 * err_floor + 1e-6
+
+
+def test_c0_thermal_50_solve_against_fp64_pipeline(cuda):
+    """Plain method, small: the 50 x 50 quad4 heat conduction solve through
+    the solver API (fp32 assembly, PCG to rtol 1e-10 with fp64 dots and
+    iterate) against the FP64 pipeline the configuration names (FP64
+    assembly and a direct solve), and the assembled system against the FP64
+    assembly."""
+    torch = cuda
+    from folax_gb300.loss import ThermalLoss2DQuad
+    from folax_gb300.solvers import FiniteElementLinearResidualBasedSolver
+    from oracle import fe_oracle as fo
+    m, settings, k = workloads.square_thermal(50, 5)
+    loss = ThermalLoss2DQuad("c0", dict(settings), m)
+    loss.Initialize()
+    solver = FiniteElementLinearResidualBasedSolver("c0", loss, {"linear_solver_settings": {
+        "solver": "GB300-pcg", "tol": 1e-10, "maxiter": 20000, "vector_precision": "fp32"}})
+    solver.Initialize()
+    T = solver.Solve(torch.tensor(k, dtype=torch.float32, device="cuda"),
+                     torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda")).double().cpu().numpy()
+    assert solver.last_linear_info["status"] == 0
+    ol = fo.FELossOracle("quad4", "thermal", m.nodes_coordinates, m.elements_nodes["quad"],
+                         dirichlet=settings["dirichlet_bc_dict"], node_sets=m.node_sets, num_gp=2,
+                         control_layout="element")
+    T_ref = fo.linear_solve(ol, k, np.zeros(ol.total_dofs))
+    jac, r = loss.ComputeJacobianMatrixAndResidualVector(torch.tensor(k, dtype=torch.float32, device="cuda"),
+                                                         loss.ApplyDirichletBCOnDofVector(torch.zeros(
+                                                             loss.GetTotalNumberOfDOFs(), device="cuda")))
+    A, R = ol.csr(k, ol.full_dof_vector(np.zeros(ol.total_dofs)))
+    err_T, err_A = rel_fro(T, T_ref), rel_fro(jac.data.cpu().numpy(), A.data)
+    print(f"\nC0 50^2: solution vs FP64 assembly + direct solve {err_T:.3e}; CSR values vs FP64 {err_A:.3e}")
+    assert err_A < TOL
+    assert err_T < 1e-6
 
 
 def test_c4_neohooke_64cubed_batch16_against_c_oracle(cuda):

@@ -181,6 +181,45 @@ def test_hex8_tile_kernel_many_tiles(cuda, variant, layout, exponent, bf, order)
         assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
 
 
+def _star_mesh():
+    """Hexahedra around an irregular edge: a pentagon split into 5 quads
+    (centre, edge midpoints, corners), extruded in two layers; the centre
+    node of the middle layer belongs to 10 hexahedra, so a tile holds more
+    than 8 of its records (a second local entry)."""
+    from folax_gb300.mesh import Mesh
+    ang = np.deg2rad(72.0) * np.arange(5)
+    corners = np.stack([np.cos(ang), np.sin(ang)], 1)
+    mids = 0.5 * (corners + np.roll(corners, -1, axis=0))
+    pts2 = np.concatenate([[[0.0, 0.0]], mids, corners])  # 0 centre, 1..5 mids, 6..10 corners
+    quads = [(0, 1 + (i - 1) % 5, 6 + i, 1 + i) for i in range(5)]
+    zs = [0.0, 0.5, 1.0]
+    xyz = np.concatenate([np.column_stack([pts2, np.full(len(pts2), z)]) for z in zs])
+    hexes = [[c + 11 * k for c in quad] + [c + 11 * (k + 1) for c in quad] for k in range(2) for quad in quads]
+    m = Mesh("star", "star.mem")
+    m.nodes_coordinates = xyz
+    m.node_ids = np.arange(len(xyz))
+    m.elements_nodes = {"hexahedron": np.asarray(hexes, dtype=np.int64)}
+    m.node_sets = {"bottom": np.arange(11), "top": np.arange(22, 33)}
+    return m
+
+
+@pytest.mark.parametrize("variant", [18, 19])
+@pytest.mark.parametrize("layout", ["nodal", "element"])
+def test_hex8_tile_kernel_irregular_edge(cuda, variant, layout):
+    m = _star_mesh()
+    s = _settings("hex8", "elastic", layout, 1.0, [0.1, 0.0, 0.2])
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(44)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+
+
 @pytest.mark.parametrize("tma,twin", [(13, 11), (15, 6), (16, 11), (17, 11)])
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 def test_tma_variant_equals_its_per_thread_twin(cuda, tma, twin, layout):
