@@ -36,6 +36,7 @@ CONTROL_NODAL, CONTROL_ELEMENT = 0, 1
 SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
 OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
+KRYLOV_ENGINE_GRID, KRYLOV_ENGINE_KERNELS = 0, 1
 
 
 class FolgbError(RuntimeError):
@@ -95,6 +96,7 @@ PROTOTYPES = {
     "folgb_bicgstab": (C.c_int, [vp, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz, vp]),
     "folgb_krylov": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, C.POINTER(i32), C.POINTER(f64), vp, sz,
                                vp]),
+    "folgb_krylov_set_engine": (C.c_int, [i32]),
     "folgb_krylov_async": (C.c_int, [vp, i32, i32, vp, vp, vp, vp, f64, i32, i32, vp, vp, vp, vp, sz, vp]),
     "folgb_spmv": (C.c_int, [vp, vp, vp, vp, vp]),
     "folgb_newton_workspace_bytes": (sz, [vp, C.POINTER(NewtonSettings)]),

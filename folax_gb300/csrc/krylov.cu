@@ -21,6 +21,7 @@
 // "replace" are set, so the host enqueues a chunk of iterations and reads
 // the flags once per chunk.
 #include <cmath>
+#include <atomic>
 #include <mutex>
 #include <type_traits>
 
@@ -776,6 +777,10 @@ __global__ void k_step_inc(int* step) { *step += 1; }
 
 enum { SOLVER_CG = 0, SOLVER_BICGSTAB = 1 };
 
+// The grid-resident CG is used unless switched off (folgb_krylov_set_engine).
+static std::atomic<int> g_grid_pcg{1};
+static bool grid_pcg_enabled() { return g_grid_pcg.load() != 0; }
+
 // ---------------------------------------------------------------------------
 // Cluster-resident solver for small systems: the whole solve is ONE launch of
 // one thread-block cluster (kClusterCTAs CTAs on as many SMs).  Each CTA owns a
@@ -1069,6 +1074,276 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
   return false;
 }
 
+// ---------------------------------------------------------------------------
+// Grid-resident Jacobi-PCG for large systems: the whole solve is ONE
+// cooperative launch (every block resident), each block owning a contiguous
+// node range; the phases of an iteration are separated by grid barriers on a
+// global counter (bounded waits), and every reduction is each block posting its
+// block sums and every block adding all posts in block order, so all blocks
+// hold bit-identical scalars.  Per iteration two barriers:
+//   B: p_new = z + beta p_old formed on the fly for the SpMV's columns (p is
+//      double-buffered, so no block overwrites what another still reads),
+//      q = A p_new, p . q                                      -> barrier, alpha
+//   C: x += alpha p_new (fp64), r -= alpha q, z = D^-1 r, r . z, r . r
+//                                                              -> barrier, beta
+// Reliable updates as the multi-kernel solver (true residual in fp64, the
+// direction kept unless a breakdown restarts it).  Vectors written during the
+// solve are read through L2 (ld.global.cg), never a stale L1 line.
+// ---------------------------------------------------------------------------
+constexpr int kGridThreads = 512;
+
+template <class VT>
+struct GridArgs {
+  int64_t N;
+  const int* adj_ptr;
+  const int* adj;
+  int maxdeg;
+  const float* vals;
+  const float* dinv;
+  const float* b;
+  VT *r, *z, *p0, *p1, *q;
+  double* x;
+  float* xout;
+  KScalars* sc;
+  double* part;       // [2][4][gridDim.x] block sums
+  unsigned* barrier;  // [2] arrivals, generation (zero at launch)
+  double rtol;
+  int maxiter;
+};
+
+// Bounded grid barrier: the last block to arrive bumps the generation the
+// others poll; a wait that exceeds its poll limit returns false.
+__device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, int* s_flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = bar + 1;
+    const unsigned g = *gen;
+    int ok = 1;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      for (int i = 0; *gen == g; ++i) {
+        if (i >= (1 << 22)) {
+          ok = 0;
+          break;
+        }
+        if (i >= 32) __nanosleep(64);
+      }
+    }
+    __threadfence();
+    *s_flag = ok;
+  }
+  __syncthreads();
+  const bool ok = *s_flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+// sum of K doubles over the grid, the same totals in every thread of every
+// block (block sums added in block order); false if a barrier gave up
+template <int K, class VT>
+__device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const GridArgs<VT>& A, int& parity,
+                                         int* s_flag, double* s_bcast) {
+  const unsigned nb = gridDim.x;
+  double* slot = A.part + (size_t)parity * 4 * nb;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    const double s = block_sum_d(v[k], sh);
+    if (threadIdx.x == 0) __stcg(slot + (size_t)k * nb + blockIdx.x, s);
+  }
+  if (!grid_barrier(A.barrier, nb, s_flag)) return false;
+#pragma unroll
+  for (int k = 0; k < K; ++k) {
+    double t = 0.0;
+    for (unsigned i = threadIdx.x; i < nb; i += blockDim.x) t += __ldcg(slot + (size_t)k * nb + i);
+    t = block_sum_d(t, sh);
+    if (threadIdx.x == 0) s_bcast[k] = t;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < K; ++k) v[k] = s_bcast[k];
+  __syncthreads();
+  parity ^= 1;
+  return true;
+}
+
+template <int NDOF, int G, class T, class VT, class Col, class Epi>
+__device__ __forceinline__ void grid_rows(const GridArgs<VT>& A, int64_t n0, int64_t n1, Col col, Epi epi) {
+  constexpr int U = RowsU<NDOF>::U;
+  const int lane = threadIdx.x % G;
+  const int64_t group = threadIdx.x / G, ngroups = blockDim.x / G;
+  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += ngroups * U) {
+    T sum;
+    int64_t d;
+    if (rows_multi<NDOF, G, T>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
+  }
+}
+
+template <int NDOF, int G, class VT>
+__global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT> A) {
+  __shared__ double sh[32];
+  __shared__ double s_bcast[4];
+  __shared__ int s_flag;
+  int parity = 0;
+  const int rank = blockIdx.x, nr = gridDim.x;
+  const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
+  const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
+  const int64_t tid = threadIdx.x, nth = blockDim.x;
+  // init: x = 0, r = b, z = D^-1 b, p = 0
+  VT rz0 = VT(0), bb0 = VT(0);
+  for (int64_t d = d0 + tid; d < d1; d += nth) {
+    const VT bi = (VT)A.b[d];
+    const VT zi = (VT)A.dinv[d] * bi;
+    A.x[d] = 0.0;
+    A.r[d] = bi;
+    A.z[d] = zi;
+    A.p0[d] = VT(0);
+    rz0 = vfma(bi, zi, rz0);
+    bb0 = vfma(bi, bi, bb0);
+  }
+  double red[2] = {(double)bb0, (double)rz0};
+  int done = 0;
+  if (!grid_sum<2>(red, sh, A, parity, &s_flag, s_bcast)) done = 5;
+  const double bb = red[0];
+  const double tol2 = A.rtol * A.rtol * bb;
+  double rho = red[1], rref2 = bb, rnorm2 = bb;
+  double alpha = 0.0, beta = 0.0;
+  if (!done) done = (bb == 0.0) ? 1 : (!isfinite(bb) ? 3 : 0);
+  int iters = 0, breakdowns = 0, replace = 0, cur = 0;
+  while (!done) {
+    if (!replace) {
+      const VT* pold = cur ? A.p1 : A.p0;
+      VT* pnew = cur ? A.p0 : A.p1;
+      const VT vb = (VT)beta;
+      // B: p_new = z + beta p_old (columns on the fly), q = A p_new, p . q
+      VT pq = VT(0);
+      grid_rows<NDOF, G, VT>(
+          A, n0, n1, [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); },
+          [&](int64_t d, VT sum) {
+            const VT pn = vfma(vb, __ldcg(pold + d), __ldcg(A.z + d));
+            __stcg(pnew + d, pn);
+            __stcg(A.q + d, sum);
+            pq = vfma(pn, sum, pq);
+          });
+      double dq[1] = {(double)pq};
+      if (!grid_sum<1>(dq, sh, A, parity, &s_flag, s_bcast)) {
+        done = 5;
+        break;
+      }
+      const double PQ = dq[0];
+      if (!(PQ > 0.0) || !isfinite(PQ)) {
+        ++breakdowns;
+        if (!isfinite(PQ)) done = 3;
+        else if (breakdowns > kMaxBreakdowns) done = 4;
+        else replace = 2;
+        continue;
+      }
+      alpha = rho / PQ;
+      // C: x += alpha p_new, r -= alpha q, z = D^-1 r, r . z, r . r
+      const VT va = (VT)alpha;
+      VT rz = VT(0), rr = VT(0);
+      for (int64_t d = d0 + tid; d < d1; d += nth) {
+        const VT pn = __ldcg(pnew + d);
+        A.x[d] = fma(alpha, (double)pn, A.x[d]);
+        const VT ri = vfma(-va, __ldcg(A.q + d), __ldcg(A.r + d));
+        __stcg(A.r + d, ri);
+        const VT zi = (VT)A.dinv[d] * ri;
+        __stcg(A.z + d, zi);
+        rz = vfma(ri, zi, rz);
+        rr = vfma(ri, ri, rr);
+      }
+      double dc[2] = {(double)rz, (double)rr};
+      if (!grid_sum<2>(dc, sh, A, parity, &s_flag, s_bcast)) {
+        done = 5;
+        break;
+      }
+      const double RZ = dc[0], RR = dc[1];
+      beta = RZ / rho;
+      rho = RZ;
+      rnorm2 = RR;
+      ++iters;
+      breakdowns = 0;
+      cur ^= 1;
+      if (!isfinite(RR)) done = 3;
+      else if (RR <= tol2 || RR <= kReplaceDrop2 * rref2 || RR > kDiverge2 * bb) replace = 1;
+      if (!done && iters >= A.maxiter) replace = replace ? replace : 1;
+      if (done || !replace) continue;
+    }
+    // reliable update: r = b - A x in fp64 (every block's x is visible: the
+    // last grid sum ordered it); the direction is kept unless a breakdown
+    VT rzf = VT(0);
+    double rr = 0.0;
+    grid_rows<NDOF, G, double>(A, n0, n1, [&](int64_t k) { return __ldcg(A.x + k); }, [&](int64_t d, double sum) {
+      const double ri = (double)A.b[d] - sum;
+      const VT rv = (VT)ri;
+      __stcg(A.r + d, rv);
+      const VT zi = (VT)A.dinv[d] * rv;
+      __stcg(A.z + d, zi);
+      rzf = vfma(rv, zi, rzf);
+      rr = fma(ri, ri, rr);
+    });
+    double dr[2] = {(double)rzf, rr};
+    if (!grid_sum<2>(dr, sh, A, parity, &s_flag, s_bcast)) {
+      done = 5;
+      break;
+    }
+    beta = (replace == 2 || !(rho > 0.0) || beta == 0.0) ? 0.0 : dr[0] * beta / rho;
+    rho = dr[0];
+    rref2 = rnorm2 = dr[1];
+    replace = 0;
+    if (!isfinite(dr[1])) done = 3;
+    else if (dr[1] <= tol2) done = 1;
+    else if (dr[1] > kDiverge2 * bb) done = 4;
+    else if (iters >= A.maxiter) done = 2;
+  }
+  for (int64_t d = d0 + tid; d < d1; d += nth) A.xout[d] = (float)A.x[d];
+  if (rank == 0 && threadIdx.x == 0) {
+    A.sc->iters = iters;
+    A.sc->done = done;
+    A.sc->rnorm2 = rnorm2;
+    A.sc->bnorm2 = bb;
+  }
+}
+
+// one cooperative launch of the grid solver (every block resident); returns
+// false if the launch was refused (the caller then uses the multi-kernel path)
+template <int NDOF, int G, class VT>
+static bool launch_grid_pcg(const GridArgs<VT>& A, cudaStream_t s) {
+  auto kernel = k_pcg_grid<NDOF, G, VT>;
+  static std::atomic<int> occ[64];
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  int per_sm = occ[dev].load();
+  if (per_sm == 0) {
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGridThreads, 0) != cudaSuccess ||
+        per_sm < 1) {
+      cudaGetLastError();
+      return false;
+    }
+    occ[dev].store(per_sm);
+  }
+  const int64_t want = (A.N + 63) / 64;  // at least 64 nodes per block
+  int64_t blocks = (int64_t)per_sm * num_sms();
+  if (blocks > want) blocks = want;
+  if (blocks < 1 || blocks > 8192) return false;  // part holds [2][4][blocks] doubles
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)blocks);
+  cfg.blockDim = dim3(kGridThreads);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  if (cudaLaunchKernelEx(&cfg, kernel, A) == cudaSuccess) return true;
+  cudaGetLastError();
+  return false;
+}
+
 // capture_sc != NULL: s is being captured into a graph (the device-resident
 // Newton solve, the cached graphs of krylov_async); the solve is enqueued as
 // init + one WHILE node over [K iterations, true residual, loop control] (or
@@ -1176,6 +1451,33 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
           *capture_sc = w.sc;
           return (int)FOLGB_OK;
         }
+        // large fp32 CG systems: one cooperative launch of the grid solver
+        if (solver == SOLVER_CG && n > kClusterMaxDofs && sizeof(VT) == sizeof(float) && grid_pcg_enabled()) {
+          GridArgs<VT> ga;
+          ga.N = p->N;
+          ga.adj_ptr = p->d_adj_ptr;
+          ga.adj = p->d_adj;
+          ga.maxdeg = p->maxdeg;
+          ga.vals = vals;
+          ga.dinv = dinv;
+          ga.b = rhs;
+          ga.r = w.r;
+          ga.z = w.z;
+          ga.p0 = w.p0;
+          ga.p1 = w.p1;
+          ga.q = w.q;
+          ga.x = w.x;
+          ga.xout = x;
+          ga.sc = w.sc;
+          ga.part = w.part;
+          ga.barrier = w.counters + 6;
+          ga.rtol = rtol;
+          ga.maxiter = maxiter;
+          if (launch_grid_pcg<NDOF, G, VT>(ga, s)) {
+            *capture_sc = w.sc;
+            return (int)FOLGB_OK;
+          }
+        }
         cudaStreamCaptureStatus cst = cudaStreamCaptureStatusNone;
         cudaGraph_t graph = nullptr;
         const cudaGraphNode_t* deps = nullptr;
@@ -1262,7 +1564,9 @@ __global__ void k_krylov_report(const KScalars* sc, int32_t* iterations, double*
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (iterations) *iterations = sc->iters;
   if (rel_residual) *rel_residual = sc->bnorm2 > 0.0 ? sqrt(sc->rnorm2 / sc->bnorm2) : 0.0;
-  if (status) *status = sc->done == 3 ? FOLGB_ERR_NAN : (sc->done == 1 ? FOLGB_OK : FOLGB_ERR_NOT_CONVERGED);
+  if (status)
+    *status = sc->done == 3 ? FOLGB_ERR_NAN
+                            : (sc->done == 1 ? FOLGB_OK : (sc->done == 5 ? FOLGB_ERR_TIMEOUT : FOLGB_ERR_NOT_CONVERGED));
 }
 
 // Instantiated solve graphs of one plan, keyed by everything the graph bakes
@@ -1442,6 +1746,12 @@ extern "C" int folgb_krylov(const folgb_plan* p, int32_t method, int32_t vector_
     return krylov_sync<double>(p, solver, vals, dinv, rhs, x, rtol, maxiter, check_every, iterations, rel_residual,
                                workspace, workspace_bytes, (cudaStream_t)stream);
   return FOLGB_ERR_INVALID_ARGUMENT;
+}
+
+extern "C" int folgb_krylov_set_engine(int32_t engine) {
+  if (engine != FOLGB_KRYLOV_ENGINE_GRID && engine != FOLGB_KRYLOV_ENGINE_KERNELS) return FOLGB_ERR_INVALID_ARGUMENT;
+  g_grid_pcg.store(engine == FOLGB_KRYLOV_ENGINE_GRID ? 1 : 0);
+  return FOLGB_OK;
 }
 
 extern "C" int folgb_krylov_async(const folgb_plan* p, int32_t method, int32_t vector_bits, const float* vals,

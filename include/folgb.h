@@ -260,6 +260,17 @@ int folgb_krylov(const folgb_plan* plan, int32_t method, int32_t vector_bits,
                  double rtol, int32_t maxiter, int32_t check_every, int32_t* iterations,
                  double* rel_residual, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Engine of large CG solves (no counterpart in the reference):
+ * FOLGB_KRYLOV_ENGINE_GRID (default) runs a fp32-vector CG on more than
+ * 16,384 dofs as one cooperative launch (every block resident, grid
+ * barriers with bounded waits between the phases of an iteration, the
+ * iteration's vector update fused into it); FOLGB_KRYLOV_ENGINE_KERNELS
+ * runs the loop of SpMV and update kernels (what kernel tracing always uses).
+ * Process-wide; both give the same iterates up to the order of fp32
+ * rounding in the reductions. */
+enum { FOLGB_KRYLOV_ENGINE_GRID = 0, FOLGB_KRYLOV_ENGINE_KERNELS = 1 };
+int folgb_krylov_set_engine(int32_t engine);
+
 /* Stream-ordered folgb_krylov, for callers that must not block (an XLA FFI
  * LinearSolve handler on XLA's stream; fe_solver.py:60-78 is the reference
  * call, kr_small_displacement_element.cc:315-337 the handler precedent, whose
@@ -267,7 +278,8 @@ int folgb_krylov(const folgb_plan* plan, int32_t method, int32_t vector_bits,
  * Enqueues the whole solve on `stream` and returns: no host synchronisation,
  * no allocation.  The outcome goes to caller DEVICE buffers (any may be
  * NULL): *d_iterations, *d_rel_residual (true residual of the fp64 iterate)
- * and *d_status (FOLGB_OK, FOLGB_ERR_NOT_CONVERGED or FOLGB_ERR_NAN).  The
+ * and *d_status (FOLGB_OK, FOLGB_ERR_NOT_CONVERGED, FOLGB_ERR_NAN, or
+ * FOLGB_ERR_TIMEOUT when a grid barrier of the grid engine gave up).  The
  * return value reports argument and launch errors only.
  * The solve runs as an instantiated CUDA graph (init, a WHILE node over
  * chunks of check_every iterations with the true-residual check, the fp32

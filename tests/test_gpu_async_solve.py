@@ -121,3 +121,27 @@ def test_async_reports_not_converged_on_device(cuda):
     assert rc == capi.OK
     torch.cuda.synchronize()
     assert int(out[1]) == capi.ERR_NOT_CONVERGED and 1 <= int(out[0]) <= 3
+
+
+@pytest.mark.parametrize("n", [24, 40])
+def test_grid_engine_matches_kernel_engine(cuda, n):
+    """The one-launch grid CG (more than 16,384 dofs) against the loop of
+    SpMV and update kernels: the same solution to the solve tolerance, about
+    the same iteration count, converged on the true residual."""
+    torch = cuda
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    loss, jac, r = _system(n=n, seed=54)
+    b = (-r).contiguous()
+    out = {}
+    try:
+        for engine in (capi.KRYLOV_ENGINE_KERNELS, capi.KRYLOV_ENGINE_GRID):
+            assert lib.folgb_krylov_set_engine(engine) == capi.OK
+            rc, x, it, rel = _sync(lib, capi, jac, 0, 32, b)
+            assert rc == capi.OK and rel <= 1e-8
+            out[engine] = (x, it)
+    finally:
+        lib.folgb_krylov_set_engine(capi.KRYLOV_ENGINE_GRID)
+    (xk, ik), (xg, ig) = out[capi.KRYLOV_ENGINE_KERNELS], out[capi.KRYLOV_ENGINE_GRID]
+    assert np.linalg.norm(xg - xk) <= 1e-6 * np.linalg.norm(xk)
+    assert abs(ig - ik) <= 0.02 * ik + 2

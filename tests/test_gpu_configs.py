@@ -9,7 +9,9 @@
   storing the matrix in fp32: it is compared with the error of an FP64 solve
   whose only approximation is the FP64 matrix rounded to fp32.
 * 50 x 50 quad4 heat conduction (the small plain-method configuration): the
-  fp32 solve against FP64 assembly + direct solve (bound 1e-6).
+  fp32 solve against an FP64 direct solve of the same system (bound 1e-6),
+  and against FP64 assembly + direct solve, compared with the floor of
+  storing the FP64 matrix in fp32.
 * 6-tet split of 64^3 (1,572,864 tets), neo-Hookean, batch 16: losses and
   both gradients of two instances against the C oracle (1e-5).
 * 512 uneven quad4 thermal instances (the benchmark's seed): losses and both
@@ -96,14 +98,25 @@ def test_c0_thermal_50_solve_against_fp64_pipeline(cuda):
                          dirichlet=settings["dirichlet_bc_dict"], node_sets=m.node_sets, num_gp=2,
                          control_layout="element")
     T_ref = fo.linear_solve(ol, k, np.zeros(ol.total_dofs))
-    jac, r = loss.ComputeJacobianMatrixAndResidualVector(torch.tensor(k, dtype=torch.float32, device="cuda"),
-                                                         loss.ApplyDirichletBCOnDofVector(torch.zeros(
-                                                             loss.GetTotalNumberOfDOFs(), device="cuda")))
+    u0 = loss.ApplyDirichletBCOnDofVector(torch.zeros(loss.GetTotalNumberOfDOFs(), device="cuda"))
+    jac, r = loss.ComputeJacobianMatrixAndResidualVector(torch.tensor(k, dtype=torch.float32, device="cuda"), u0)
     A, R = ol.csr(k, ol.full_dof_vector(np.zeros(ol.total_dofs)))
+    # the solver: the GPU solve against an FP64 direct solve of the same fp32 system
+    A32 = jac.to_scipy().astype(np.float64)
+    T_same = u0.double().cpu().numpy() + fo.direct_solve(A32, -r.double().cpu().numpy())
+    # the floor of storing the matrix in fp32: the FP64 matrix rounded to fp32
+    A_rounded = A.copy()
+    A_rounded.data = A_rounded.data.astype(np.float32).astype(np.float64)
+    u_full = ol.full_dof_vector(np.zeros(ol.total_dofs))
+    T_floor = u_full + fo.direct_solve(A_rounded, -R)
     err_T, err_A = rel_fro(T, T_ref), rel_fro(jac.data.cpu().numpy(), A.data)
-    print(f"\nC0 50^2: solution vs FP64 assembly + direct solve {err_T:.3e}; CSR values vs FP64 {err_A:.3e}")
+    err_solver, err_floor = rel_fro(T, T_same), rel_fro(T_floor, T_ref)
+    print(f"\nC0 50^2: solution vs the same fp32 system solved in FP64 {err_solver:.3e}; vs FP64 assembly + "
+          f"direct solve {err_T:.3e}; fp32-rounded FP64 matrix alone {err_floor:.3e}; CSR values vs FP64 "
+          f"{err_A:.3e}")
     assert err_A < TOL
-    assert err_T < 1e-6
+    assert err_solver < 1e-6
+    assert err_T <= 2.0 * err_floor + 1e-6
 
 
 def test_c4_neohooke_64cubed_batch16_against_c_oracle(cuda):
