@@ -1574,13 +1574,13 @@ __global__ void k_krylov_report(const KScalars* sc, int32_t* iterations, double*
 // oldest entry is dropped past kKrylovGraphs.
 struct KrylovGraphKey {
   const void* ptrs[9];
-  int solver, vbits, maxiter, check_every, device;
+  int solver, vbits, maxiter, check_every, device, engine;
   double rtol;
   bool operator==(const KrylovGraphKey& o) const {
     for (int i = 0; i < 9; ++i)
       if (ptrs[i] != o.ptrs[i]) return false;
     return solver == o.solver && vbits == o.vbits && maxiter == o.maxiter && check_every == o.check_every &&
-           device == o.device && rtol == o.rtol;
+           device == o.device && engine == o.engine && rtol == o.rtol;
   }
 };
 struct KrylovGraphs {
@@ -1632,6 +1632,7 @@ static int krylov_async(const folgb_plan* p, int solver, const float* vals, cons
   key.maxiter = maxiter;
   key.check_every = check_every;
   key.rtol = rtol;
+  key.engine = grid_pcg_enabled() ? 1 : 0;
   FOLGB_CUDA_TRY(cudaGetDevice(&key.device));
   folgb_plan* mp = const_cast<folgb_plan*>(p);  // the cache is the plan's only mutable state
   {

@@ -567,7 +567,9 @@ def test_device_resident_krylov_loop_matches_host_loop(cuda, solver_name):
     """The solve loop as one CUDA graph (WHILE node, no host sync until the
     end) runs the same kernels in the same order as the host-driven loop
     (forced here by enabling kernel tracing): bit-identical results.  32^3
-    hex8 (107,811 dofs) is above the size the single-cluster solver takes."""
+    hex8 (107,811 dofs) is above the size the single-cluster solver takes;
+    the kernel-loop engine is selected, since the grid engine (one launch)
+    sums its reductions in another order."""
     from folax_gb300 import _capi
     from folax_gb300.solvers import FiniteElementSolver
     torch = cuda
@@ -580,14 +582,16 @@ def test_device_resident_krylov_loop_matches_host_loop(cuda, solver_name):
     solver = FiniteElementSolver("k", gl, {"linear_solver_settings": {"solver": solver_name, "tol": 1e-8,
                                                                        "maxiter": 5000, "check_every": 32}})
     solver.Initialize()
-    x_dev = solver.LinearSolve(jac, R)
-    info_dev = dict(solver.last_linear_info)
     lib = _capi.load()
-    lib.folgb_trace_enable(1)
+    lib.folgb_krylov_set_engine(_capi.KRYLOV_ENGINE_KERNELS)
     try:
+        x_dev = solver.LinearSolve(jac, R)
+        info_dev = dict(solver.last_linear_info)
+        lib.folgb_trace_enable(1)
         x_host = solver.LinearSolve(jac, R)
     finally:
         lib.folgb_trace_enable(0)
+        lib.folgb_krylov_set_engine(_capi.KRYLOV_ENGINE_GRID)
     info_host = dict(solver.last_linear_info)
     assert info_dev["status"] == 0 and info_dev["iterations"] == info_host["iterations"]
     assert torch.equal(x_dev, x_host)
