@@ -770,10 +770,6 @@ static int loss_partial_slots(const folgb_plan* p) {
   return blocks > p->tiles ? blocks : p->tiles;
 }
 
-static size_t loss_counter_count(const folgb_plan* p, int B) {
-  return (size_t)2 * B + (size_t)B * (size_t)p->tile_boundary_nodes;
-}
-
 // record width of the loss path: ndof components (+ the nodal control sensitivity)
 static int loss_rec(const folgb_plan* p) { return loss_record(p); }
 
@@ -786,9 +782,7 @@ static size_t layout_loss(const folgb_plan* p, int B, bool plain, void* base, si
   const size_t recs = (size_t)B * p->E * p->nen * rec, parts = (size_t)B * p->tile_boundary_slots * 4;
   float* g = bp.take<float>(recs > parts ? recs : parts);
   float* partials = bp.take<float>((size_t)B * loss_partial_slots(p));
-  // [B] last-block counters, [B] tile queues, [B][partial nodes] arrivals of
-  // the fused tile kernel: all zeroed by one memset per call
-  unsigned* counters = bp.take<unsigned>(loss_counter_count(p, B));
+  unsigned* counters = bp.take<unsigned>((size_t)2 * B);  // [B] last-block counters, [B] tile queues
   float* scale = bp.take<float>((size_t)B);
   float* Ke = plain ? bp.take<float>((size_t)B * p->E * ND * ND) : nullptr;
   float* Fe = (plain && p->mat.has_bf) ? bp.take<float>((size_t)B * p->E * ND) : nullptr;
@@ -973,7 +967,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   size_t need = layout_loss(p, B, false, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * loss_counter_count(p, B), s));
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * 2 * B, s));
   const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
   VecArgs A = make_vec_args(p, B, control, control_stride, dofs, dofs_stride, apply_dirichlet, w, losses,
                             elem_ctrl ? dloss_dcontrol : nullptr, device_status);
@@ -1003,9 +997,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     });
   }
   if (rc) return rc;
-  if (fast == 3) {
-    // the tile kernel finished every node itself
-  } else if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
+  if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
     rc = launch_tile_boundary(p, A, B, s, trace_active() ? 0 : 1);
   } else if (dloss_ddofs || dloss_dcontrol) {
     rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
@@ -1028,7 +1020,7 @@ extern "C" int folgb_loss_adjoint_plain(const folgb_plan* p, int32_t B, const fl
   size_t need = layout_loss(p, B, true, workspace, workspace_bytes, &w);
   if (!workspace || workspace_bytes < need) return FOLGB_ERR_WORKSPACE;
   cudaStream_t s = (cudaStream_t)stream;
-  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * loss_counter_count(p, B), s));
+  FOLGB_CUDA_TRY(cudaMemsetAsync(w.counters, 0, sizeof(unsigned) * 2 * B, s));
   const bool elem_ctrl = p->ctrl_layout == FOLGB_CONTROL_ELEMENT;
   MatArgs M;
   M.E = p->E;

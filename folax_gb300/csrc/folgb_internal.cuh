@@ -103,9 +103,6 @@ struct folgb_plan {
   int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
   int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
   int* d_in_node = nullptr;             // [NI] interior nodes (rescaled when the loss exponent is not 1)
-  int* d_tn_bn = nullptr;               // [K] partial-node list index of an entry with partials, else -1
-  int* d_iso_node = nullptr;            // nodes of no element (gradient 0)
-  int64_t tile_isolated_nodes = 0;
   // instantiated Krylov solve graphs of folgb_krylov_async (krylov.cu)
   void* krylov_graphs = nullptr;
   // CSR tables

@@ -725,13 +725,6 @@ struct TileArgs {
   const int* in_node;
   int64_t nb_nodes, ni_nodes;
   unsigned* queue;  // [B] next tile of each instance (persistent kernel), zeroed before the launch
-  // fused partial sums (persistent kernel): per entry with partials the index
-  // of its node in the partial-node list; per (instance, node) an arrival
-  // counter zeroed before the launch; nodes of no element
-  const int* tn_bn;
-  unsigned* arrivals;  // [B][nb_nodes]
-  const int* iso_node;
-  int64_t n_iso;
 };
 
 // One element of a tile from shared-memory node data: X, U (and nodal
@@ -911,7 +904,6 @@ struct TileStage {
   float4 U[kTileNodes];
   uint4 pos[kTileNodes];
   unsigned info[kTileNodes];
-  int bn[kTileNodes];  // partial-node index of the entries with partials
   uint2 lconn[kTileElems];
   int elem[kTileElems];
 };
@@ -961,7 +953,6 @@ __device__ __forceinline__ void issue_inputs(TileSmem& S, const VecArgs& A, cons
     if (CL == FOLGB_CONTROL_NODAL) cp_async4(&Z.U[k].w, ctrl + n);
     cp_async4(&Z.info[k], T.tn_info + m.n0 + k);
     cp_async16(&Z.pos[k], T.tn_pos + m.n0 + k);
-    if (k < m.nb) cp_async4(&Z.bn[k], T.tn_bn + m.n0 + k);
   }
   for (int j = threadIdx.x; j < m.ne; j += kTileElems) {
     cp_async8(&Z.lconn[j], T.t_lconn + m.e0 + j);
@@ -969,47 +960,7 @@ __device__ __forceinline__ void issue_inputs(TileSmem& S, const VecArgs& A, cons
   }
 }
 
-// Fused partial sums: after its node pass a tile announces each partial it
-// wrote (one arrival on the node's counter, after a fence that makes the
-// partial visible); the tile whose arrival completes a node sums all of that
-// node's partials in slot order (the order of the partial-node list, so the
-// result does not depend on which tile finishes) and writes the gradient.
-// Loss exponent 1 only (the scale 1 / batch is known before the loss).
-template <int CL>
-__device__ __forceinline__ void tile_finish_partials(const VecArgs& A, const TileArgs& T, const float4* bpart,
-                                                     const int* bn, const int* gid, int nb, int b) {
-  bool any = false;
-  for (int k = threadIdx.x; k < nb; k += kTileElems) any = true;
-  if (!any) return;
-  __threadfence();  // this thread's partials are visible before its arrivals
-  for (int k = threadIdx.x; k < nb; k += kTileElems) {
-    const int i = bn[k];
-    const int s0 = __ldg(T.bn_ptr + i), s1 = __ldg(T.bn_ptr + i + 1);
-    const unsigned prev = atomicAdd(T.arrivals + (int64_t)b * T.nb_nodes + i, 1u);
-    if (prev != (unsigned)(s1 - s0 - 1)) continue;
-    __threadfence();  // the other tiles' partials, announced before their arrivals
-    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int j = s0; j < s1; ++j) {
-      const float4 r = __ldcg(bpart + __ldg(T.bn_slot + j));
-      acc.x += r.x;
-      acc.y += r.y;
-      acc.z += r.z;
-      acc.w += r.w;
-    }
-    const int n = gid[k];
-    const float sc = A.inv_batch;
-    if (A.out) {
-      const unsigned m = __ldg(A.dmask + n);
-      float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
-      o[0] = (m & 1u) ? 0.f : sc * acc.x;
-      o[1] = (m & 2u) ? 0.f : sc * acc.y;
-      o[2] = (m & 4u) ? 0.f : sc * acc.z;
-    }
-    if (CL == FOLGB_CONTROL_NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = sc * acc.w;
-  }
-}
-
-template <int CL, bool BF, bool FUSED>
+template <int CL, bool BF>
 __global__ void __launch_bounds__(kTileElems, 4) k_hex8_elastic_tile_pipe(const VecArgs A, const TileArgs T) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   TileSmem& S = *reinterpret_cast<TileSmem*>(smem_raw);
@@ -1022,16 +973,6 @@ __global__ void __launch_bounds__(kTileElems, 4) k_hex8_elastic_tile_pipe(const 
   // tiles k = 0, 1 of this block: blockIdx.x and gridDim.x + blockIdx.x; from
   // k = 2 on from the queue (offset by the 2 * gridDim.x tiles taken so)
   auto next_tile = [&]() { return 2 * (int)gridDim.x + (int)atomicAdd(T.queue + b, 1u); };
-  if constexpr (FUSED) {  // nodes of no element: gradient 0
-    for (int64_t i = (int64_t)blockIdx.x * kTileElems + threadIdx.x; i < T.n_iso; i += (int64_t)gridDim.x * kTileElems) {
-      const int n = __ldg(T.iso_node + i);
-      if (A.out) {
-        float* o = A.out + (int64_t)b * A.out_stride + 3 * (int64_t)n;
-        o[0] = o[1] = o[2] = 0.f;
-      }
-      if (CL == FOLGB_CONTROL_NODAL && A.dctrl_nodal) A.dctrl_nodal[(int64_t)b * A.N + n] = 0.f;
-    }
-  }
   if (threadIdx.x == 0) {
     S.rec[kTileZeroRec] = make_float4(0.f, 0.f, 0.f, 0.f);
     S.meta[0] = tile_meta(T, blockIdx.x);
@@ -1076,7 +1017,6 @@ __global__ void __launch_bounds__(kTileElems, 4) k_hex8_elastic_tile_pipe(const 
       partials[cur.tile] = e;
     }
     tile_nodes<CL>(A, S.rec, Z.pos, Z.info, S.gid[k % 3], cur.nl, cur.nb, bpart + cur.bbase, b);
-    if constexpr (FUSED) tile_finish_partials<CL>(A, T, bpart, Z.bn, S.gid[k % 3], cur.nb, b);
   }
   cp_async_wait<0>();
   (void)energy_all;
@@ -1173,10 +1113,6 @@ static TileArgs tile_args(const folgb_plan* p) {
   T.tn_gid = p->d_tn_gid;
   T.tn_info = p->d_tn_info;
   T.queue = nullptr;
-  T.tn_bn = p->d_tn_bn;
-  T.arrivals = nullptr;
-  T.iso_node = p->d_iso_node;
-  T.n_iso = p->tile_isolated_nodes;
   T.bn_node = p->d_bn_node;
   T.bn_ptr = p->d_bn_ptr;
   T.bn_slot = p->d_bn_slot;
@@ -1187,30 +1123,26 @@ static TileArgs tile_args(const folgb_plan* p) {
 }
 
 template <int CL>
-static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, bool pipe, bool fused,
-                        cudaStream_t s) {
+static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, bool pipe, cudaStream_t s) {
   TileArgs T = tile_args(p);
-  T.queue = A.counters + B;         // zeroed with the loss counters before the launch
-  T.arrivals = A.counters + 2 * B;  // likewise
+  T.queue = A.counters + B;  // zeroed with the loss counters before the launch
   if (!pipe) {
     dim3 grid((unsigned)p->tiles, (unsigned)B);
     if (bf) k_hex8_elastic_tile<CL, true, 4><<<grid, kTileElems, 0, s>>>(A, T);
     else k_hex8_elastic_tile<CL, false, 4><<<grid, kTileElems, 0, s>>>(A, T);
     return;
   }
-  static std::atomic<int> occ[4][kOccDevices];  // per instantiation and device
-  const int which = (bf ? 1 : 0) + (fused ? 2 : 0);
-  auto k = bf ? (fused ? k_hex8_elastic_tile_pipe<CL, true, true> : k_hex8_elastic_tile_pipe<CL, true, false>)
-              : (fused ? k_hex8_elastic_tile_pipe<CL, false, true> : k_hex8_elastic_tile_pipe<CL, false, false>);
-  static std::atomic<int> attr_set[kOccDevices][4];
+  static std::atomic<int> occ_bf[kOccDevices], occ[kOccDevices];  // per instantiation and device
+  auto k = bf ? k_hex8_elastic_tile_pipe<CL, true> : k_hex8_elastic_tile_pipe<CL, false>;
+  static std::atomic<int> attr_set[kOccDevices][2];
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= kOccDevices) dev = 0;
-  if (!attr_set[dev][which].load()) {  // more than the default 48 KB of dynamic shared memory
+  if (!attr_set[dev][bf ? 1 : 0].load()) {  // more than the default 48 KB of dynamic shared memory
     cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(TileSmem));
-    attr_set[dev][which].store(1);
+    attr_set[dev][bf ? 1 : 0].store(1);
   }
-  const int per_sm = blocks_per_sm(k, kTileElems, sizeof(TileSmem), occ[which]);
+  const int per_sm = blocks_per_sm(k, kTileElems, sizeof(TileSmem), bf ? occ_bf : occ);
   int64_t g = (int64_t)per_sm * num_sms() / B;
   if (g > p->tiles) g = p->tiles;
   if (g < 1) g = 1;
@@ -1254,8 +1186,7 @@ constexpr int kHex8Variants = 20;
 // block count is recomputed for the variant's block size; the caller's
 // partial-sum buffers are sized for the smallest block (64 threads).
 // Returns 2 when the tile-local kernel ran (the caller then finishes with
-// launch_tile_boundary instead of the node gather), 3 when it also finished
-// the nodes shared by tiles itself (nothing left to launch).  The residual path
+// launch_tile_boundary instead of the node gather).  The residual path
 // (MODE_RESIDUAL, records for the node gather) runs variant 11 in place of a
 // tile-local variant.
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
@@ -1265,13 +1196,10 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
   const bool tile = variant >= kHex8TileFirst && p->tiles > 0;
   if (variant >= kHex8TileFirst && (mode != MODE_LOSS || !tile)) variant = 11;
   trace_begin(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
-  const bool pipe = variant == kHex8TileFirst;
-  const bool fused = pipe && A.exponent == 1.f;
   if (mode == MODE_LOSS && tile) {
-    if (p->ctrl_layout == FOLGB_CONTROL_NODAL)
-      launch_tile<FOLGB_CONTROL_NODAL>(p, A, (int)grid.y, bf, pipe, fused, s);
-    else
-      launch_tile<FOLGB_CONTROL_ELEMENT>(p, A, (int)grid.y, bf, pipe, fused, s);
+    const bool pipe = variant == kHex8TileFirst;
+    if (p->ctrl_layout == FOLGB_CONTROL_NODAL) launch_tile<FOLGB_CONTROL_NODAL>(p, A, (int)grid.y, bf, pipe, s);
+    else launch_tile<FOLGB_CONTROL_ELEMENT>(p, A, (int)grid.y, bf, pipe, s);
   } else if (p->ctrl_layout == FOLGB_CONTROL_NODAL) {
     if (mode == MODE_LOSS) launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_LOSS>(A, grid, bf, variant, s);
     else launch_cl_mode<FOLGB_CONTROL_NODAL, MODE_RESIDUAL>(A, grid, bf, variant, s);
@@ -1280,8 +1208,7 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
     else launch_cl_mode<FOLGB_CONTROL_ELEMENT, MODE_RESIDUAL>(A, grid, bf, variant, s);
   }
   trace_end(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
-  if (mode == MODE_LOSS && tile) return fused ? 3 : 2;
-  return 1;
+  return (mode == MODE_LOSS && tile) ? 2 : 1;
 }
 
 // Second launch of the tile-local path (the nodes shared by tiles), as a

@@ -235,25 +235,13 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
   // element ids in tile order; bit 31: the element touches a Dirichlet dof
   std::vector<int> t_elem(E);
   for (int64_t i = 0; i < E; ++i) t_elem[i] = order[i] | (elem_bc[order[i]] ? (int)0x80000000u : 0);
-  // per local entry with partials, the index of its node in the partial-node
-  // list (the fused kernel counts the arrivals of a node's partials there);
-  // nodes of no element, which no tile finishes
-  std::vector<int> bn_index(N, -1), tn_bn(tn_gid.size(), -1), iso_node;
-  for (size_t i = 0; i < bn_node.size(); ++i) {
-    bn_index[bn_node[i]] = (int)i;
-    if (bn_ptr[i + 1] == bn_ptr[i]) iso_node.push_back(bn_node[i]);
-  }
-  for (int t = 0; t < T; ++t)
-    for (int k = 0; k < tile_bptr[t + 1] - tile_bptr[t]; ++k)
-      tn_bn[tile_nptr[t] + k] = bn_index[tn_gid[tile_nptr[t] + k]];
   int rc;
   if ((rc = upload_vec(&p->d_tile_eptr, tile_eptr)) || (rc = upload_vec(&p->d_tile_nptr, tile_nptr)) ||
       (rc = upload_vec(&p->d_tile_bptr, tile_bptr)) || (rc = upload_vec(&p->d_t_elem, t_elem)) ||
       (rc = upload_vec(&p->d_t_lconn, t_lconn)) || (rc = upload_vec(&p->d_tn_pos, tn_pos)) ||
       (rc = upload_vec(&p->d_tn_gid, tn_gid)) || (rc = upload_vec(&p->d_tn_info, tn_info)) ||
       (rc = upload_vec(&p->d_bn_node, bn_node)) || (rc = upload_vec(&p->d_bn_ptr, bn_ptr)) ||
-      (rc = upload_vec(&p->d_bn_slot, bn_slot)) || (rc = upload_vec(&p->d_in_node, in_node)) ||
-      (rc = upload_vec(&p->d_tn_bn, tn_bn)) || (rc = upload_vec(&p->d_iso_node, iso_node))) {
+      (rc = upload_vec(&p->d_bn_slot, bn_slot)) || (rc = upload_vec(&p->d_in_node, in_node))) {
     free_tile_tables(p);
     return rc;
   }
@@ -262,14 +250,12 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
   p->tile_boundary_slots = S;
   p->tile_boundary_nodes = (int64_t)bn_node.size();
   p->tile_interior_nodes = (int64_t)in_node.size();
-  p->tile_isolated_nodes = (int64_t)iso_node.size();
   return FOLGB_OK;
 }
 
 void free_tile_tables(folgb_plan* p) {
   void* ptrs[] = {p->d_tile_eptr, p->d_tile_nptr, p->d_tile_bptr, p->d_t_elem, p->d_t_lconn, p->d_tn_pos,
-                  p->d_tn_gid,    p->d_tn_info,   p->d_bn_node,   p->d_bn_ptr, p->d_bn_slot, p->d_in_node,
-                  p->d_tn_bn,     p->d_iso_node};
+                  p->d_tn_gid,    p->d_tn_info,   p->d_bn_node,   p->d_bn_ptr, p->d_bn_slot, p->d_in_node};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   p->d_tile_eptr = p->d_tile_nptr = p->d_tile_bptr = p->d_t_elem = nullptr;
@@ -277,7 +263,6 @@ void free_tile_tables(folgb_plan* p) {
   p->d_tn_pos = nullptr;
   p->d_tn_info = nullptr;
   p->d_tn_gid = p->d_bn_node = p->d_bn_ptr = p->d_bn_slot = p->d_in_node = nullptr;
-  p->d_tn_bn = p->d_iso_node = nullptr;
   p->tiles = 0;
 }
 
