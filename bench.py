@@ -570,15 +570,19 @@ def fp32_peak(torch, lib):
 
 
 def extra_fused(args, loss, ctrl, u):
-    """The headline step alone, eager, for profiling runs: 3 warm-up and 5
-    more fused loss + adjoint calls on the 64^3 workload (the plan's kernel
-    variant: --hex8-variant forces one)."""
+    """The headline step alone, eager, for profiling runs: 8 fused loss +
+    adjoint calls on the 64^3 workload (the plan's kernel variant:
+    --hex8-variant forces one), then 3 calls of the plain path (element
+    matrices in HBM + separate backward) on the same inputs."""
     import torch
     for _ in range(8):
         loss.ComputeBatchLossAndGrad(ctrl, u)
     torch.cuda.synchronize()
     loss.CheckDeviceStatus()
-    return {"calls": 8, "variant": args.hex8_variant}
+    for _ in range(3):
+        loss.ComputeBatchLossAndGrad(ctrl, u, plain=True)
+    torch.cuda.synchronize()
+    return {"fused_calls": 8, "plain_calls": 3, "variant": args.hex8_variant}
 
 
 def extra_jittered(args):
