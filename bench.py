@@ -43,6 +43,13 @@ FLUSH_BYTES = 512 * 1024 * 1024
 # grad u (72 FMA), stress (~20), B^T sigma (72 FMA), energy and dE (~25):
 # 4 x 72 x 2 + 75 = 651 flops, x 8 points = 5,208 flops; plus gathers ~0.
 FLOPS_PER_ELEMENT = 5208.0
+# FP32 operations of the uniform-box element (variants 20-24), counted from
+# the kernel source: forward Hadamard transforms 72 FADD, eight 3x3 block
+# products 24 FMUL + 48 FFMA, u.K u 24 FFMA, energy 1 FFMA, scaling 24 FMUL,
+# transposed transforms 72 FADD, control gradient 1 FMUL (FFMA = 2 flops).
+BOX_FLOPS_PER_ELEMENT = 72 + 24 + 96 + 48 + 2 + 24 + 72 + 1
+# kernel variants by family (the autotuner's index)
+BOX_VARIANTS, GRID_VARIANTS = (20, 21, 22), (23, 24)
 # ncu figures of one launch of the fused element kernel on the 64^3 workload,
 # per kernel variant (the autotuner's index): DRAM bytes read + written
 # (dram__bytes_read.sum + dram__bytes_write.sum) and warp instructions
@@ -53,10 +60,13 @@ FLOPS_PER_ELEMENT = 5208.0
 #   16, 17: the same with the next tile's nodes prefetched to L1 / L2
 # (13, 16, 17 with the affine-element path; ncu's printed precision for the
 # DRAM bytes: 17.60 MB read, a few KB written)
+#   21: k_hex8_box, 256 threads, uniform box element (the records, 33.5 MB,
+#       stay in L2 for the gather: 25 KB written to DRAM)
 NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16_144_605},
                     13: {"traffic": 17_600_000 + 4_860, "warp_instructions": 10_652_202},
                     16: {"traffic": 17_600_000 + 9_470, "warp_instructions": 10_954_635},
-                    17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421}}}
+                    17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421},
+                    21: {"traffic": 13_081_088 + 25_344, "warp_instructions": 4_817_046}}}
 
 
 def ncu_figure(n, variant, key):
@@ -879,40 +889,60 @@ def main():
     h2d = u_pin.numel() * 4 + c_pin.numel() * 4
     d2h = out_du.numel() * 4 + out_dc.numel() * 4 + 4
 
-    # roofline of the element kernel.  Bytes: conn 32 B + control 4 B +
-    # dLoss/dE 4 B per element; coordinates 12 B and dofs 12 B per node (each
-    # node read once).  Flops: the FP32 operations the kernel variant executes
-    # per launch (ncu's fadd + fmul + 2 x ffma thread-instruction counts,
-    # packed pairs counted twice), over the FP32 peak measured here.
+    # roofline of the element kernel (for the grid variants: the whole step,
+    # one kernel).  Algorithmic bytes: control 4 B + dLoss/dE 4 B per
+    # element, dofs 12 B + dLoss/du 12 B per node (each node read and written
+    # once); the connectivity 32 B per element where the kernel reads it (not
+    # the structured grid) and the coordinates 12 B per node where it reads
+    # them (the pointwise variants).  The element records of the two-kernel
+    # variants are intermediate traffic, not algorithmic.  Flops: the FP32
+    # operations of the variant's element (ncu-counted where a capture
+    # exists; the box element counted from its source).  bound: the resource
+    # whose measured peak the kernel comes closer to.
     N = (args.n + 1) ** 3
-    alg_bytes = nE * (32 + 4 + 4) + N * (12 + 12)
-    achieved_gbs = alg_bytes / (elem_ms * 1e-3) / 1e9
+    chosen = tune["chosen"]
+    alg_bytes = nE * (4 + 4) + N * (12 + 12)
+    if chosen not in GRID_VARIANTS:
+        alg_bytes += nE * 32
+    if chosen not in BOX_VARIANTS + GRID_VARIANTS:
+        alg_bytes += N * 12
+    kernel_ms = elem_ms  # the grid variants launch no gather
+    achieved_gbs = alg_bytes / (kernel_ms * 1e-3) / 1e9
     peaks = measured_peaks()
     hbm = (peaks or {}).get("hbm_gbs", 6800.0)
     fp32_tflops, fp32_probe_ms = fp32_peak(torch, lib)
-    flops_launch = ncu_figure(args.n, tune["chosen"], "fp32_flops")
+    flops_launch = ncu_figure(args.n, chosen, "fp32_flops")
     flops_src = "ncu-counted FP32 operations of this kernel variant"
-    if flops_launch is None:
+    if flops_launch is None and chosen in BOX_VARIANTS + GRID_VARIANTS:
+        flops_launch = BOX_FLOPS_PER_ELEMENT * nE
+        flops_src = "box element counted from the kernel source (owned elements; the grid kernel's halo elements " \
+                    "and node sums not included)"
+    elif flops_launch is None:
         flops_launch = FLOPS_PER_ELEMENT * nE
-        flops_src = "naive per-element count (no ncu figure for this variant)"
-    fp32_achieved = flops_launch / (elem_ms * 1e-3) / 1e12
-    issue = issue_roofline(args.n, tune["chosen"], elem_ms, clk, peaks) or {}
-    roofline = {"bound": "fp32", "achieved": fp32_achieved, "peak": fp32_tflops, "unit": "TFLOP/s",
-                "frac": fp32_achieved / fp32_tflops,
-                "traffic": ncu_figure(args.n, tune["chosen"], "traffic"),
+        flops_src = "naive per-element count, an upper bound (no ncu figure for this variant)"
+    fp32_achieved = flops_launch / (kernel_ms * 1e-3) / 1e12
+    issue = issue_roofline(args.n, chosen, kernel_ms, clk, peaks) or {}
+    fp32_frac, hbm_frac = fp32_achieved / fp32_tflops, achieved_gbs / hbm
+    fp32_bound = fp32_frac >= hbm_frac
+    roofline = {"bound": "fp32" if fp32_bound else "hbm",
+                "achieved": fp32_achieved if fp32_bound else achieved_gbs,
+                "peak": fp32_tflops if fp32_bound else hbm,
+                "unit": "TFLOP/s" if fp32_bound else "GB/s",
+                "frac": fp32_frac if fp32_bound else hbm_frac,
+                "traffic": ncu_figure(args.n, chosen, "traffic"),
                 "traffic_unit": "bytes per launch (ncu dram read + write)",
+                "fp32_achieved_tflops": fp32_achieved, "fp32_peak_tflops": fp32_tflops, "fp32_frac": fp32_frac,
                 "flops_per_launch": flops_launch, "flops_source": flops_src,
                 "naive_flops_per_element": FLOPS_PER_ELEMENT,
-                "peak_source": "measured in this run: folgb_fp32_peak_probe (FFMA2 chains on every SM), "
-                               f"{fp32_probe_ms:.3f} ms per probe launch",
-                "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm, "hbm_frac": achieved_gbs / hbm,
-                "hbm_peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s",
+                "fp32_peak_source": "measured in this run: folgb_fp32_peak_probe (FFMA2 chains on every SM), "
+                                    f"{fp32_probe_ms:.3f} ms per probe launch",
+                "hbm_achieved_gbs": achieved_gbs, "hbm_peak_gbs": hbm, "hbm_frac": hbm_frac,
+                "hbm_peak_source": "of measured: MEASURED_PEAKS.json hbm_gbs" if peaks else "of fallback 6800 GB/s",
                 "algorithmic_bytes": alg_bytes,
                 "issue_frac": issue.get("frac"), "issue_bound_us": issue.get("issue_bound_us"),
                 "warp_instructions": issue.get("warp_instructions"),
-                "kernel_us": elem_ms * 1e3,
-                "kernel": "hex8 2x2x2 element kernel, variant %d (%s)"
-                          % (tune["chosen"], HEX8_VARIANT_NAMES[tune["chosen"]])}
+                "kernel_us": kernel_ms * 1e3,
+                "kernel": "hex8 2x2x2 element kernel, variant %d (%s)" % (chosen, HEX8_VARIANT_NAMES[chosen])}
 
     extras = run_extras(args, loss, ctrl) if rank == 0 and not args.no_extras else None
     cpu = None
@@ -925,7 +955,8 @@ def main():
         line = {"metric": "M elements/s, FE loss+adjoint vs plain assembly on same GPU, at 1e-5 rel err",
                 "value": value, "unit": "M elements/s", "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": ms, "ms_per_step_eager_api": ms_eager,
-                "timing": "CUDA-graph replay of the fused step (memset + element kernel + gather); "
+                "timing": "CUDA-graph replay of the fused step (memset + element kernel + gather, or memset + "
+                          "the one-launch grid kernel for variants 23-24); "
                           "ms_per_step_eager_api = the same step through the Python API call",
                 "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded two-phase voxels, noisy uniaxial u)",
@@ -942,7 +973,7 @@ def main():
                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
                 "cpu_baseline": cpu,
                 "clocks": clk,
-                "gpu_launches": 2 * args.steps,
+                "gpu_launches": (1 if chosen in GRID_VARIANTS else 2) * args.steps,
                 "extras": extras}
         print(json.dumps(line))
     if world > 1:

@@ -37,6 +37,7 @@ SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
 OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
 KRYLOV_ENGINE_GRID, KRYLOV_ENGINE_KERNELS = 0, 1
+FEATURE_TILES, FEATURE_UNIFORM_BOX, FEATURE_BOX_GRID = 1, 2, 4
 
 
 class FolgbError(RuntimeError):
@@ -81,6 +82,7 @@ PROTOTYPES = {
     "folgb_plan_create": (C.c_int, [C.POINTER(vp), C.POINTER(Physics), vp, i64, vp, i64, vp, vp, i64, i32]),
     "folgb_plan_destroy": (C.c_int, [vp]),
     "folgb_plan_info": (C.c_int, [vp, C.POINTER(i64), C.POINTER(i64), C.POINTER(i64), C.POINTER(i64)]),
+    "folgb_plan_features": (C.c_int, [vp, C.POINTER(C.c_int32)]),
     "folgb_plan_set_dirichlet_values": (C.c_int, [vp, vp, f64]),
     "folgb_plan_set_nodal_field": (C.c_int, [vp, vp]),
     "folgb_workspace_bytes": (sz, [vp, i32, i32]),

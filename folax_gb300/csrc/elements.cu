@@ -766,8 +766,10 @@ static int elem_tiles(int64_t nb, int B) {
 // partial-sum slots: enough for the smallest element-kernel block (64 threads)
 // and for one per tile of the tile-local kernel
 static int loss_partial_slots(const folgb_plan* p) {
-  const int blocks = (int)((p->E + 63) / 64);
-  return blocks > p->tiles ? blocks : p->tiles;
+  int64_t slots = (p->E + 63) / 64;
+  if (p->tiles > slots) slots = p->tiles;
+  if (p->box_grid) slots = std::max<int64_t>(slots, grid_blocks(p, 4));  // the smallest grid tile
+  return (int)slots;
 }
 
 // record width of the loss path: ndof components (+ the nodal control sensitivity)
@@ -997,7 +999,9 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     });
   }
   if (rc) return rc;
-  if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
+  if (fast == 3) {
+    // the structured box grid kernel wrote the gradients itself
+  } else if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
     rc = launch_tile_boundary(p, A, B, s, trace_active() ? 0 : 1);
   } else if (dloss_ddofs || dloss_dcontrol) {
     rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
@@ -1160,6 +1164,7 @@ extern "C" int folgb_assemble(const folgb_plan* p, const float* control, const f
 
 namespace folgb {
 int hex8_variant_count();
+bool hex8_variant_applies(const folgb_plan* p, int v);
 }
 
 // Times every kernel variant of the plan's loss + adjoint path on the given
@@ -1185,8 +1190,13 @@ static int autotune_impl(folgb_plan* p, int32_t batch, const float* control, int
   // an untunable plan is timed as it stands (its variant, forced or not, is kept)
   int best = p->hex8_variant;
   float best_ms = 0.f;
+  bool timed_any = false;
   int rc = FOLGB_OK;
   for (int v = 0; v < nv && rc == FOLGB_OK; ++v) {
+    if (tunable && !hex8_variant_applies(p, v)) {  // not timed: -1
+      if (ms_per_variant && v < max_variants) ms_per_variant[v] = -1.f;
+      continue;
+    }
     if (tunable) p->hex8_variant = v;
     for (int k = 0; k < 2 && rc == FOLGB_OK; ++k)
       rc = folgb_loss_adjoint(p, batch, control, control_stride, dofs, dofs_stride, 1, losses, dloss_ddofs,
@@ -1206,9 +1216,10 @@ static int autotune_impl(folgb_plan* p, int32_t batch, const float* control, int
     }
     ms /= repeats;
     if (ms_per_variant && v < max_variants) ms_per_variant[v] = ms;
-    if (tunable && (v == 0 || ms < best_ms)) {
+    if (tunable && (!timed_any || ms < best_ms)) {
       best = v;
       best_ms = ms;
+      timed_any = true;
     }
   }
   cudaEventDestroy(a);

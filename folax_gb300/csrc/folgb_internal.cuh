@@ -51,6 +51,13 @@ struct MatConst {
   float kap_f;          // split neo-Hooke: kappa = kap_f * e_gp, mu = mu_f * e_gp
 };
 
+// Element matrix of a uniform axis-aligned box mesh in the Walsh-Hadamard basis
+// of the nodal values (uniform_box.cu): the 3 x 3 block of each reflection
+// parity p, coupling the modes (component 0, p^1), (1, p^2), (2, p^4).
+struct BoxK {
+  float k[8][3][3];
+};
+
 // Hyperelastic physics: residual B(F)^T S, tangent B^T C B + geometric stiffness.
 constexpr bool is_hyperelastic(int ph) {
   return ph == FOLGB_NEOHOOKE || ph == FOLGB_SAINT_VENANT || ph == FOLGB_NEOHOOKE_SPLIT;
@@ -103,6 +110,13 @@ struct folgb_plan {
   int* d_bn_ptr = nullptr;              // [NB+1] their partial slots
   int* d_bn_slot = nullptr;             // [S] slots in ascending tile order
   int* d_in_node = nullptr;             // [NI] interior nodes (rescaled when the loss exponent is not 1)
+  // every element the same axis-aligned box (uniform_box.cu): the blocks of
+  // its element matrix for the box kernels, box_valid 0 otherwise
+  int box_valid = 0;
+  folgb::BoxK box_k = {};
+  // and the box mesh numbering of an nx x ny x nz grid (nodes x fastest, then
+  // y, then z; the reference local node order): the one-launch grid kernel
+  int box_grid = 0, box_nx = 0, box_ny = 0, box_nz = 0;
   // instantiated Krylov solve graphs of folgb_krylov_async (krylov.cu)
   void* krylov_graphs = nullptr;
   // CSR tables
@@ -164,6 +178,11 @@ constexpr int kTileZeroRec = 8 * kTileElems;  // position of the zero record pad
 int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz,
                       const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc);
 void free_tile_tables(folgb_plan* p);
+// Uniform axis-aligned box elements (uniform_box.cu): sets box_valid and box_k.
+int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn);
+void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, double (&khat)[24][24]);
+// blocks of the structured box grid kernel with tz node layers per block (hex8_fused.cu)
+int64_t grid_blocks(const folgb_plan* p, int tz);
 // Destroys the plan's cached Krylov solve graphs (krylov.cu).
 void free_krylov_graphs(folgb_plan* p);
 

@@ -537,8 +537,8 @@ __device__ __forceinline__ void prefetch_node(const void* p) {
   else asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
-template <int CL, int MODE, bool BF, int ACC, int PF = 0>
-__device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
+template <int CL, int MODE, bool BF, int ACC, int PF, class Elem>
+__device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A, Elem&& elem) {
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   __shared__ __align__(128) int4 rows[kTmaWarps][kTmaStages][64];  // 32 elements x 8 node ids
@@ -598,7 +598,7 @@ __device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
     if (e < E) {
       const int4 p = rows[warp][st][2 * lane], q = rows[warp][st][2 * lane + 1];
       const int nodes[8] = {p.x, p.y, p.z, p.w, q.x, q.y, q.z, q.w};
-      hex8_elastic_elem<CL, MODE, BF, ACC>(A, b, e, nodes, energy, bad);
+      elem(b, e, nodes, energy, bad);
     }
     __syncwarp();  // every lane has used its rows of this stage
     if (lane == 0 && t + kTmaStages * W < ntiles) {
@@ -628,7 +628,104 @@ __device__ __forceinline__ void hex8_elastic_tma_body(const VecArgs& A) {
 
 template <int CL, int MODE, bool BF, int ACC, int MINB, int PF>
 __global__ void __launch_bounds__(kTmaWarps * 32, MINB) k_hex8_elastic_tma(const VecArgs A) {
-  hex8_elastic_tma_body<CL, MODE, BF, ACC, PF>(A);
+  hex8_elastic_tma_body<CL, MODE, BF, ACC, PF>(
+      A, [&](int b, int64_t e, const int (&nodes)[8], float& energy, int& bad) {
+        hex8_elastic_elem<CL, MODE, BF, ACC>(A, b, e, nodes, energy, bad);
+      });
+}
+
+// ---------------------------------------------------------------------------
+// Uniform box meshes (every element the same axis-aligned box; uniform_box.cu
+// builds the blocks).  In the Walsh-Hadamard basis of the nodal values the
+// element matrix K (energy E_e u.K u, residual E_e K u, the quadratic form of
+// the pointwise evaluation above) is block diagonal: the mode (component c,
+// Hadamard index b) couples only with the modes of the same reflection
+// parity p = b ^ (1 << c).  Per element: the forward transform of the three
+// components, eight 3 x 3 block products (72 FMA, the block entries are
+// kernel parameters, read from the constant bank), the energy u.K u as the
+// dot product of the transformed vectors, and the transposed transform of
+// E_e K^ u^ for the residual records.  Loads, Dirichlet substitution, records
+// and the element control sensitivity are those of hex8_elastic_elem
+// (element controls, no body force).
+template <int MODE>
+__device__ __forceinline__ void box_elem(const VecArgs& A, const BoxK& K, const int b, const int64_t e,
+                                         const int (&nodes)[8], float& energy, int& bad) {
+  constexpr int LEX[8] = {0, 1, 3, 2, 4, 5, 7, 6};  // lex position -> node
+  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+  const bool bc = A.apply_dirichlet && __ldg(A.elem_bc + e);
+  float U[3][8];
+#pragma unroll
+  for (int L = 0; L < 8; ++L) {
+    const int n = nodes[LEX[L]];
+    const unsigned m = bc ? __ldg(A.dmask + n) : 0u;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      const int64_t d = 3 * (int64_t)n + c;
+      U[c][L] = ((m >> c) & 1u) ? __ldg(A.dval + d) : __ldg(dofs + d);
+    }
+  }
+  const float ee = __ldg(A.ctrl + (int64_t)b * A.ctrl_stride + e);
+#pragma unroll
+  for (int c = 0; c < 3; ++c) wht8(U[c]);
+  float V[3][8];
+#pragma unroll
+  for (int p = 0; p < 8; ++p) {
+    const float u0 = U[0][p ^ 1], u1 = U[1][p ^ 2], u2 = U[2][p ^ 4];
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      V[c][p ^ (1 << c)] = fmaf(K.k[p][c][2], u2, fmaf(K.k[p][c][1], u1, K.k[p][c][0] * u0));
+  }
+  float sed = 0.f;  // u.K u = sum_q detJ sed_q
+#pragma unroll
+  for (int c = 0; c < 3; ++c)
+#pragma unroll
+    for (int q = 0; q < 8; ++q) sed = fmaf(U[c][q], V[c][q], sed);
+  energy = fmaf(ee, sed, energy);
+  if (!isfinite(energy)) bad |= 2;
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) V[c][q] *= ee;
+    wht8_t(V[c]);
+  }
+  float4* out = reinterpret_cast<float4*>(A.g);
+#pragma unroll
+  for (int L = 0; L < 8; ++L)
+    out[((int64_t)b * 8 + LEX[L]) * A.E + e] = make_float4(V[0][L], V[1][L], V[2][L], 0.f);
+  if (MODE == MODE_LOSS && A.dctrl_elem)
+    A.dctrl_elem[(int64_t)b * A.E + e] = (A.exponent == 1.f) ? sed * A.inv_batch : sed;
+}
+
+// One box element per thread; BLOCK * MINB threads per SM (64 registers at 1,024).
+template <int MODE, int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB) k_hex8_box(const VecArgs A, const BoxK K) {
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  pdl_launch_dependents();
+  if (MODE == MODE_LOSS) {
+    if (threadIdx.x == 0) wcount = 0u;
+    __syncthreads();
+  }
+  const int b = blockIdx.y;
+  const int64_t e = (int64_t)blockIdx.x * BLOCK + threadIdx.x;
+  float energy = 0.f;
+  int bad = 0;
+  if (e < A.E) {
+    int nodes[8];
+    load_nodes<8>(A.conn, e, nodes);
+    box_elem<MODE>(A, K, b, e, nodes, energy, bad);
+  }
+  if constexpr (MODE == MODE_LOSS) finish_loss_warp(energy, bad, A, b, wsum, &wcount);
+  else report_bad_warp(bad, A.status);
+}
+
+// The persistent TMA-staged loop of k_hex8_elastic_tma with the box element.
+template <int MODE, int MINB>
+__global__ void __launch_bounds__(kTmaWarps * 32, MINB) k_hex8_box_tma(const VecArgs A, const BoxK K) {
+  hex8_elastic_tma_body<FOLGB_CONTROL_ELEMENT, MODE, false, 2, 0>(
+      A, [&](int b, int64_t e, const int (&nodes)[8], float& energy, int& bad) {
+        box_elem<MODE>(A, K, b, e, nodes, energy, bad);
+      });
 }
 
 template <int CL, int MODE, bool BF, int ACC, int BLOCK>
@@ -691,6 +788,171 @@ static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_
     auto k = k_hex8_elastic_tma<CL, MODE, false, ACC, MINB, PF>;
     k<<<dim3(persistent_blocks(k, A.E, occ), grid.y), kTmaWarps * 32, 0, s>>>(A);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Structured uniform box meshes (the box mesh numbering: nodes x fastest, then
+// y, then z; element (i, j, k) = i + nx (j + ny k) with the reference's local
+// node order): the whole fused loss + adjoint in one launch, with no element
+// records in global memory and no gather.
+//
+// A block owns the nodes of a column tile [x0, x0 + kGridTX) x [y0, y0 + kGridTY)
+// (the last tiles also own the mesh's last node plane) and the node layers
+// [z0, z0 + tz), and walks the element layers z0 - 1 ... upwards.  Its
+// (kGridTX + 1) x (kGridTY + 1) threads each take one element column
+// (x0 - 1 + tx, y0 - 1 + ty): the elements of the halo row, column and layer
+// below the tile are evaluated by this block too (they belong to the
+// neighbouring tiles), so every owned node is finished here.  Per element
+// layer: each thread evaluates its element (box_elem's algebra), keeps the
+// element's upper-face node values for the next layer, and stores its 8
+// corner residuals in shared memory; after a barrier the same thread, as
+// node (x0 + tx, y0 + ty), adds the lower-corner residuals of the 4 elements
+// around it to the upper-corner sums it kept from the layer below, in a fixed
+// order, and writes the finished node.  Energies and element control
+// gradients are taken from owned elements only.  The loss exponent must be 1
+// (the gradients are scaled as they are written).
+constexpr int kGridTX = 16, kGridTY = 8;
+constexpr int kGridCols = (kGridTX + 1) * (kGridTY + 1);  // element columns per block
+constexpr int kGridBlock = (kGridCols + 31) / 32 * 32;
+
+struct GridDims {
+  int nx, ny, nz;  // elements per direction
+  int tz;          // node layers per block
+  int tiles_x, tiles_y;
+};
+
+__global__ void __launch_bounds__(kGridBlock) k_hex8_box_grid(const VecArgs A, const BoxK K, const GridDims G) {
+  __shared__ float rec[8][3][kGridTY + 1][kGridTX + 1];  // corner residuals of this element layer
+  __shared__ float wsum[32];
+  __shared__ unsigned wcount;
+  pdl_launch_dependents();
+  if (threadIdx.x == 0) wcount = 0u;
+  const int b = blockIdx.y;
+  int t = blockIdx.x;
+  const int bx = t % G.tiles_x;
+  t /= G.tiles_x;
+  const int by = t % G.tiles_y, bz = t / G.tiles_y;
+  const int x0 = bx * kGridTX, y0 = by * kGridTY, z0 = bz * G.tz;
+  const int NX = G.nx + 1, NY = G.ny + 1;  // nodes per row, per column
+  // owned node counts of this tile (the last tiles own the final plane too)
+  const int onx = x0 + kGridTX >= G.nx ? NX - x0 : kGridTX;
+  const int ony = y0 + kGridTY >= G.ny ? NY - y0 : kGridTY;
+  const int zend = z0 + G.tz >= G.nz ? G.nz + 1 : z0 + G.tz;  // node layers [z0, zend)
+  const bool col = threadIdx.x < kGridCols;
+  const int tx = threadIdx.x % (kGridTX + 1), ty = threadIdx.x / (kGridTX + 1);
+  const int ex = x0 - 1 + tx, ey = y0 - 1 + ty;
+  const bool col_valid = col && ex >= 0 && ex < G.nx && ey >= 0 && ey < G.ny;
+  const bool col_owned = col_valid && ex >= x0 && ey >= y0;
+  const bool node_owned = col && tx < onx && ty < ony;
+  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+  float lower[3][4];  // nodal values of the element's lower face (lex 0..3), from the layer below
+  bool have_lower = false;
+  float up[3] = {0.f, 0.f, 0.f};  // node (x0 + tx, y0 + ty, kz): upper-corner sums of element layer kz - 1
+  float energy = 0.f;
+  int bad = 0;
+  auto load_node = [&](int ix, int iy, int iz, float& u0, float& u1, float& u2) {
+    const int64_t n = (int64_t)ix + (int64_t)NX * (iy + (int64_t)NY * iz);
+    const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
+    const float* d = dofs + 3 * n;
+    u0 = (m & 1u) ? __ldg(A.dval + 3 * n) : __ldg(d);
+    u1 = (m & 2u) ? __ldg(A.dval + 3 * n + 1) : __ldg(d + 1);
+    u2 = (m & 4u) ? __ldg(A.dval + 3 * n + 2) : __ldg(d + 2);
+  };
+  for (int kz = z0 - 1; kz < zend; ++kz) {
+    float V[3][8];
+    if (col_valid && kz >= 0 && kz < G.nz) {
+      float U[3][8];
+      // lex L = ax + 2 ay + 4 az at node (ex + ax, ey + ay, kz + az)
+#pragma unroll
+      for (int L = 0; L < 4; ++L) {
+        if (have_lower) {
+          U[0][L] = lower[0][L];
+          U[1][L] = lower[1][L];
+          U[2][L] = lower[2][L];
+        } else {
+          load_node(ex + (L & 1), ey + (L >> 1), kz, U[0][L], U[1][L], U[2][L]);
+        }
+      }
+#pragma unroll
+      for (int L = 4; L < 8; ++L) {
+        load_node(ex + (L & 1), ey + ((L >> 1) & 1), kz + 1, U[0][L], U[1][L], U[2][L]);
+        lower[0][L - 4] = U[0][L];
+        lower[1][L - 4] = U[1][L];
+        lower[2][L - 4] = U[2][L];
+      }
+      have_lower = true;
+      const int64_t e = (int64_t)ex + (int64_t)G.nx * (ey + (int64_t)G.ny * kz);
+      const float ee = __ldg(ctrl + e);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) wht8(U[c]);
+#pragma unroll
+      for (int p = 0; p < 8; ++p) {
+        const float u0 = U[0][p ^ 1], u1 = U[1][p ^ 2], u2 = U[2][p ^ 4];
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          V[c][p ^ (1 << c)] = fmaf(K.k[p][c][2], u2, fmaf(K.k[p][c][1], u1, K.k[p][c][0] * u0));
+      }
+      float sed = 0.f;
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) sed = fmaf(U[c][q], V[c][q], sed);
+      if (col_owned && kz >= z0) {
+        energy = fmaf(ee, sed, energy);
+        if (A.dctrl_elem) A.dctrl_elem[(int64_t)b * A.E + e] = sed * A.inv_batch;
+      }
+      if (!isfinite(sed)) bad |= 2;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+#pragma unroll
+        for (int q = 0; q < 8; ++q) V[c][q] *= ee;
+        wht8_t(V[c]);
+      }
+    } else {
+#pragma unroll
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int q = 0; q < 8; ++q) V[c][q] = 0.f;
+      have_lower = false;
+    }
+    if (col) {
+#pragma unroll
+      for (int L = 0; L < 8; ++L)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) rec[L][c][ty][tx] = V[c][L];
+    }
+    __syncthreads();
+    if (col) {
+      // node (x0 + tx, y0 + ty): element columns tx + ox, ty + oy, corner (1 - ox, 1 - oy)
+      float low[3] = {0.f, 0.f, 0.f}, upn[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+      for (int o = 0; o < 4; ++o) {
+        const int ox = o & 1, oy = o >> 1;
+        if (tx + ox <= kGridTX && ty + oy <= kGridTY) {
+          const int L = (1 - ox) + 2 * (1 - oy);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            low[c] += rec[L][c][ty + oy][tx + ox];
+            upn[c] += rec[L + 4][c][ty + oy][tx + ox];
+          }
+        }
+      }
+      if (node_owned && kz >= z0 && A.out) {
+        const int64_t n = (int64_t)(x0 + tx) + (int64_t)NX * ((y0 + ty) + (int64_t)NY * kz);
+        const unsigned m = __ldg(A.dmask + n);
+        float* o = A.out + (int64_t)b * A.out_stride + 3 * n;
+        o[0] = (m & 1u) ? 0.f : A.inv_batch * (up[0] + low[0]);
+        o[1] = (m & 2u) ? 0.f : A.inv_batch * (up[1] + low[1]);
+        o[2] = (m & 4u) ? 0.f : A.inv_batch * (up[2] + low[2]);
+      }
+      up[0] = upn[0];
+      up[1] = upn[1];
+      up[2] = upn[2];
+    }
+    __syncthreads();  // rec is rewritten by the next layer
+  }
+  finish_loss_warp(energy, bad, A, b, wsum, &wcount);
 }
 
 // ---------------------------------------------------------------------------
@@ -1150,8 +1412,47 @@ static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, b
 }
 
 // Tile-local variants: kHex8TileFirst the persistent pipelined kernel,
-// kHex8TileFirst + 1 the one-block-per-tile kernel.
+// kHex8TileFirst + 1 the one-block-per-tile kernel.  Box variants (uniform
+// box meshes): kHex8BoxFirst the persistent TMA-staged loop, then one element
+// per thread in blocks of 256 and 128.
 constexpr int kHex8TileFirst = 18;
+constexpr int kHex8BoxFirst = 20;
+constexpr int kHex8GridFirst = 23;  // structured box grid, 4 and 8 node layers per block
+
+GridDims grid_dims(const folgb_plan* p, int tz) {
+  GridDims G;
+  G.nx = p->box_nx;
+  G.ny = p->box_ny;
+  G.nz = p->box_nz;
+  G.tz = tz;
+  G.tiles_x = (G.nx + kGridTX - 1) / kGridTX;
+  G.tiles_y = (G.ny + kGridTY - 1) / kGridTY;
+  return G;
+}
+
+// blocks of the structured box grid kernel with tz node layers per block
+int64_t grid_blocks(const folgb_plan* p, int tz) {
+  const GridDims G = grid_dims(p, tz);
+  return (int64_t)G.tiles_x * G.tiles_y * ((G.nz + tz - 1) / tz);
+}
+
+static void launch_box_grid(const folgb_plan* p, const VecArgs& A, dim3 grid, int tz, cudaStream_t s) {
+  const GridDims G = grid_dims(p, tz);
+  k_hex8_box_grid<<<dim3((unsigned)grid_blocks(p, tz), grid.y), kGridBlock, 0, s>>>(A, p->box_k, G);
+}
+
+template <int MODE>
+static void launch_box(const folgb_plan* p, const VecArgs& A, dim3 grid, int variant, cudaStream_t s) {
+  if (variant == kHex8BoxFirst) {
+    static std::atomic<int> occ[kOccDevices];  // per instantiation and device
+    auto k = k_hex8_box_tma<MODE, 6>;
+    k<<<dim3(persistent_blocks(k, A.E, occ), grid.y), kTmaWarps * 32, 0, s>>>(A, p->box_k);
+  } else if (variant == kHex8BoxFirst + 1) {
+    k_hex8_box<MODE, 256, 4><<<dim3((unsigned)((A.E + 255) / 256), grid.y), 256, 0, s>>>(A, p->box_k);
+  } else {
+    k_hex8_box<MODE, 128, 8><<<dim3((unsigned)((A.E + 127) / 128), grid.y), 128, 0, s>>>(A, p->box_k);
+  }
+}
 
 template <int CL, int MODE>
 static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cudaStream_t s) {
@@ -1178,25 +1479,51 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
 }
 
 // Number of sum-factorised variants the autotuner may choose from: 0..17
-// one element per thread with global records, 18..19 tile-local.
-constexpr int kHex8Variants = 20;
+// pointwise with global records, 18..19 tile-local, 20..22 uniform box,
+// 23..24 structured box grid (no records).
+constexpr int kHex8Variants = 25;
+
+// Whether a variant can run on the plan (tile tables; a uniform box mesh; a
+// structured one, loss exponent 1).
+bool hex8_variant_applies(const folgb_plan* p, int v) {
+  if (v >= kHex8GridFirst) return p->box_grid != 0 && p->phys.loss_exponent == 1.0;
+  if (v >= kHex8BoxFirst) return p->box_valid != 0;
+  if (v >= kHex8TileFirst) return p->tiles > 0;
+  return true;
+}
 
 // Launches the sum-factorised kernel when it applies (hex8, linear
 // elasticity, 2x2x2 Gauss); returns 1 if it did, 0 otherwise.  The grid's
 // block count is recomputed for the variant's block size; the caller's
 // partial-sum buffers are sized for the smallest block (64 threads).
 // Returns 2 when the tile-local kernel ran (the caller then finishes with
-// launch_tile_boundary instead of the node gather).  The residual path
-// (MODE_RESIDUAL, records for the node gather) runs variant 11 in place of a
-// tile-local variant.
+// launch_tile_boundary instead of the node gather) and 3 when the structured
+// box grid kernel finished everything.  The residual path (MODE_RESIDUAL,
+// records for the node gather) runs variant 11 in place of a tile-local
+// variant and 21 in place of a grid variant; a grid variant that does not
+// apply runs 21, a box variant on a plan that is not a uniform box mesh 16.
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2) return 0;
   int variant = p->hex8_variant;
   const bool bf = p->mat.has_bf != 0;
-  const bool tile = variant >= kHex8TileFirst && p->tiles > 0;
-  if (variant >= kHex8TileFirst && (mode != MODE_LOSS || !tile)) variant = 11;
+  if (variant >= kHex8GridFirst) {
+    if (mode == MODE_LOSS && p->box_grid && A.exponent == 1.f) {
+      trace_begin(KID_ELEM_LOSS, s);
+      launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 4 : 8, s);
+      trace_end(KID_ELEM_LOSS, s);
+      return 3;
+    }
+    variant = kHex8BoxFirst + 1;
+  }
+  if (variant >= kHex8BoxFirst && !p->box_valid) variant = 16;
+  const bool box = variant >= kHex8BoxFirst;
+  const bool tile = !box && variant >= kHex8TileFirst && p->tiles > 0;
+  if (!box && variant >= kHex8TileFirst && (mode != MODE_LOSS || !tile)) variant = 11;
   trace_begin(mode == MODE_LOSS ? KID_ELEM_LOSS : KID_ELEM_RESIDUAL, s);
-  if (mode == MODE_LOSS && tile) {
+  if (box) {
+    if (mode == MODE_LOSS) launch_box<MODE_LOSS>(p, A, grid, variant, s);
+    else launch_box<MODE_RESIDUAL>(p, A, grid, variant, s);
+  } else if (mode == MODE_LOSS && tile) {
     const bool pipe = variant == kHex8TileFirst;
     if (p->ctrl_layout == FOLGB_CONTROL_NODAL) launch_tile<FOLGB_CONTROL_NODAL>(p, A, (int)grid.y, bf, pipe, s);
     else launch_tile<FOLGB_CONTROL_ELEMENT>(p, A, (int)grid.y, bf, pipe, s);

@@ -379,6 +379,7 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     folgb_plan_destroy(p);
     return rc;
   }
+  build_uniform_box(p, x4, c32);  // box kernels when every element is the same axis-aligned box
   noalloc_prepare_current_device();
   *out = p;
   return FOLGB_OK;
@@ -405,6 +406,13 @@ extern "C" int folgb_plan_info(const folgb_plan* p, int64_t* ndof_per_node, int6
   if (total_dofs) *total_dofs = (int64_t)p->ndof * p->N;
   if (csr_rows) *csr_rows = p->has_csr ? p->rows : 0;
   if (csr_nnz) *csr_nnz = p->has_csr ? p->nnz : 0;
+  return FOLGB_OK;
+}
+
+extern "C" int folgb_plan_features(const folgb_plan* p, int32_t* features) {
+  if (!p || !features) return FOLGB_ERR_INVALID_ARGUMENT;
+  *features = (p->tiles > 0 ? FOLGB_FEATURE_TILES : 0) | (p->box_valid ? FOLGB_FEATURE_UNIFORM_BOX : 0) |
+              (p->box_grid ? FOLGB_FEATURE_BOX_GRID : 0);
   return FOLGB_OK;
 }
 

@@ -35,7 +35,7 @@ from .mesh import Mesh
 
 _ETYPE = {"quad": capi.QUAD4, "hexahedron": capi.HEX8, "tetra": capi.TET4}
 # sum-factorised hex8 kernel variants (threads per block x accumulation scheme)
-HEX8_VARIANTS = 20
+HEX8_VARIANTS = 25
 HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, dual coefficients",
                       "128 thr, dual coefficients", "64 thr, point sums", "64 thr, dual coefficients",
                       "128 thr, 96 regs, point sums", "128 thr, 96 regs, dual coefficients",
@@ -49,7 +49,13 @@ HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, du
                       "persistent, TMA-staged rows, next tile's nodes prefetched to L2, paired points (f32x2)",
                       "tile-local, persistent: tile inputs copied ahead by cp.async, residuals summed in shared "
                       "memory, paired points (f32x2)",
-                      "tile-local, one block per tile, paired points (f32x2)"]
+                      "tile-local, one block per tile, paired points (f32x2)",
+                      "uniform box: 3x3 blocks of the element matrix in the Hadamard basis, persistent, "
+                      "TMA-staged rows",
+                      "uniform box: 3x3 blocks of the element matrix in the Hadamard basis, 256 thr",
+                      "uniform box: 3x3 blocks of the element matrix in the Hadamard basis, 128 thr",
+                      "structured box grid: one launch, no records, 16x8 node columns x 4 layers per block",
+                      "structured box grid: one launch, no records, 16x8 node columns x 8 layers per block"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 
@@ -288,6 +294,17 @@ class FiniteElementLoss:
     def GetDeviceStatus(self) -> int:
         """Status bits raised by the kernels (1 << FOLGB_ERR_*); reading it synchronises."""
         return int(self._status.item())
+
+    def KernelFeatures(self) -> dict:
+        """Kernel paths this mesh allows: "tiles" (tile-local hex8 kernels),
+        "uniform_box" (every element the same axis-aligned box: the box
+        kernels, variants 20-22) and "box_grid" (also numbered as a structured
+        box mesh: the one-launch grid kernels, variants 23-24, loss exponent
+        1).  The autotuner times the variants that apply."""
+        f = C.c_int32()
+        capi.check("folgb_plan_features", self._plan.lib.folgb_plan_features(self._plan.handle, C.byref(f)))
+        return {"tiles": bool(f.value & capi.FEATURE_TILES), "uniform_box": bool(f.value & capi.FEATURE_UNIFORM_BOX),
+                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID)}
 
     def CheckDeviceStatus(self):
         """Raise FolgbError if a kernel flagged a non-positive detJ, a

@@ -114,6 +114,19 @@ int folgb_plan_destroy(folgb_plan* plan);
 int folgb_plan_info(const folgb_plan* plan, int64_t* ndof_per_node, int64_t* total_dofs,
                     int64_t* csr_rows, int64_t* csr_nnz);
 
+/* Kernel paths the plan's mesh allows (bit flags): FOLGB_FEATURE_TILES, tile
+ * tables of the tile-local hex8 kernels; FOLGB_FEATURE_UNIFORM_BOX, every
+ * hexahedron is the same axis-aligned box (exactly, in fp32 coordinates), with
+ * linear elasticity, element controls and no body force, so the box kernels
+ * (hex8 variants 20-22) apply: the element matrix in the Walsh-Hadamard basis
+ * of the nodal values is eight 3 x 3 blocks; FOLGB_FEATURE_BOX_GRID, such a
+ * mesh numbered as the box mesh generator numbers it (nodes x fastest, then y,
+ * then z), so the one-launch grid kernels (variants 23-24, loss exponent 1)
+ * apply.  No counterpart in the reference (a query of this library's
+ * specialisations). */
+enum { FOLGB_FEATURE_TILES = 1, FOLGB_FEATURE_UNIFORM_BOX = 2, FOLGB_FEATURE_BOX_GRID = 4 };
+int folgb_plan_features(const folgb_plan* plan, int32_t* features);
+
 /* Sets the Dirichlet values used by the in-kernel GetFullDofVector, scaled by
  * load_increment (ApplyDirichletBCOnDofVector, fe_loss.py:186-189). values is a
  * HOST array in the order given to folgb_plan_create. */

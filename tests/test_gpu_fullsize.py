@@ -21,7 +21,7 @@ def _compare(gl, cl, ctrl, u):
         assert rel_fro(x.cpu().numpy(), z) < TOL
 
 
-@pytest.mark.parametrize("variant", ["auto", 0, 2, 15, 18, 19])
+@pytest.mark.parametrize("variant", ["auto", 0, 2, 15, 18, 19, 20, 21, 22, 23, 24])
 def test_hex8_64_cubed_two_phase_matches_c_oracle(cuda, variant):
     n = 64
     m = create_3D_box_mesh(n, n, n)

@@ -220,6 +220,143 @@ def test_hex8_tile_kernel_irregular_edge(cuda, variant, layout):
         assert rel_fro(x.cpu().numpy(), z) < TOL
 
 
+def _box_mesh(order="structured"):
+    """8 x 4 x 6 elements, each the box 0.25 x 0.125 x 0.1875 (dyadic edges:
+    every element has exactly the same fp32 Jacobian)."""
+    m = create_3D_box_mesh(8, 4, 6, Lx=2.0, Ly=0.5, Lz=1.125)
+    return _renumbered(m, seed=46) if order == "renumbered" else m
+
+
+@pytest.mark.parametrize("variant", [20, 21, 22, 23, 24])
+@pytest.mark.parametrize("exponent", [1.0, 1.5])
+@pytest.mark.parametrize("order", ["structured", "renumbered"])
+def test_hex8_box_kernels_match_oracle(cuda, variant, exponent, order):
+    """The uniform-box kernels (element matrix as eight 3 x 3 blocks in the
+    Hadamard basis) on a mesh of identical non-cubic boxes, in the mesh's own
+    order and renumbered at random (the detection uses the coordinates, not
+    the numbering; the grid variants need the box numbering and exponent 1,
+    else they run variant 21), batch 3, Dirichlet values on two faces, loss
+    exponents 1 and 1.5: losses and both gradients against the oracle, and
+    bit-identical on a repeat call."""
+    m = _box_mesh(order)
+    s = _settings("hex8", "elastic", "element", exponent)
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    feats = gl.KernelFeatures()
+    assert feats["uniform_box"] and feats["box_grid"] == (order == "structured")
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(47)
+    ctrl = 0.5 + rng.random((3, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((3, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+    assert np.all(a[3].cpu().numpy()[:, ol.dirichlet_indices] == 0)
+    b = gl.ComputeBatchLossAndGrad(ctrl, u)
+    for x, y in zip(a[2:], b[2:]):
+        assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+    if order == "renumbered":
+        assert np.all(a[3].cpu().numpy()[:, -6:] == 0.0)
+
+
+def test_hex8_box_residual_path_matches_oracle(cuda):
+    """The residual-only path (records + node gather, no loss) with a box
+    variant chosen."""
+    m = _box_mesh()
+    s = _settings("hex8", "elastic", "element")
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 21})
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(48)
+    ctrl = 0.5 + rng.random(gl.GetNumberOfControls())
+    uf = ol.full_dof_vector(0.01 * rng.standard_normal(gl.GetTotalNumberOfDOFs()))
+    _, R = gl.ComputeJacobianMatrixAndResidualVector(ctrl, uf, with_matrix=False)
+    _, Ro = ol.csr(ctrl, uf)
+    assert rel_fro(R.cpu().numpy(), Ro) < TOL
+
+
+@pytest.mark.parametrize("kind", ["jittered", "one_node_moved", "sheared", "nodal", "body_force", "uneven"])
+def test_uniform_box_detection_rejects(cuda, kind):
+    """The box kernels apply only to identical axis-aligned boxes with
+    element controls and no body force; any other mesh or setting keeps the
+    pointwise kernels (a box variant then runs variant 16), still exact."""
+    m = _box_mesh()
+    layout, bf = "element", None
+    if kind == "jittered":
+        m = make_mesh("hex8", 4, seed=49, jitter=0.1)
+    elif kind == "one_node_moved":
+        m.nodes_coordinates[20] += np.array([1e-6, 0.0, 0.0])
+    elif kind == "sheared":
+        m.nodes_coordinates[:, 0] += 0.25 * m.nodes_coordinates[:, 2]
+    elif kind == "nodal":
+        layout = "nodal"
+    elif kind == "body_force":
+        bf = [0.1, 0.0, 0.0]
+    elif kind == "uneven":
+        m = create_3D_box_mesh(4, 4, 4)
+        z = m.nodes_coordinates[:, 2]
+        m.nodes_coordinates[:, 2] = z * z
+    s = _settings("hex8", "elastic", layout, 1.0, bf)
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 20})
+    assert not gl.KernelFeatures()["uniform_box"]
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(50)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = 0.01 * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+
+
+@pytest.mark.parametrize("nx,ny,nz", [(37, 19, 11), (16, 8, 4), (17, 9, 5), (1, 1, 7), (40, 2, 3)])
+@pytest.mark.parametrize("variant", [23, 24])
+def test_hex8_box_grid_tiles_match_oracle(cuda, nx, ny, nz, variant):
+    """The one-launch structured grid kernel over many column tiles and layer
+    blocks, with uneven last tiles (37 x 19 x 11), a mesh of exactly one tile
+    (16 x 8 x 4), one element past it in every direction (17 x 9 x 5), a
+    single element column and a thin slab; edge 1/32, batch 2, Dirichlet
+    values on the bottom and top faces: losses and both gradients against the
+    oracle, bit-identical on a repeat call, and the Dirichlet dofs 0."""
+    h = 1.0 / 32
+    m = create_3D_box_mesh(nx, ny, nz, Lx=nx * h, Ly=ny * h, Lz=nz * h)
+    s = _settings("hex8", "elastic", "element")
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    assert gl.KernelFeatures()["box_grid"]
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(52)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = 0.001 * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+    assert np.all(a[3].cpu().numpy()[:, ol.dirichlet_indices] == 0)
+    b = gl.ComputeBatchLossAndGrad(ctrl, u)
+    for x, y in zip(a[2:], b[2:]):
+        assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+
+
+@pytest.mark.parametrize("box", [20, 21, 22, 23, 24])
+def test_box_kernel_agrees_with_pointwise_kernel(cuda, box):
+    """On a 100^3 cube mesh the box kernels and the pointwise kernel (variant
+    11) evaluate the same quadratic form in another order: losses and
+    gradients agree to 1e-6."""
+    m = create_3D_box_mesh(100, 100, 100)
+    s = _settings("hex8", "elastic", "element")
+    a_loss = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": box})
+    b_loss = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 11})
+    rng = np.random.default_rng(51)
+    ctrl = 0.5 + rng.random((2, a_loss.GetNumberOfControls()))
+    u = 0.003 * rng.standard_normal((2, a_loss.GetTotalNumberOfDOFs()))
+    a = a_loss.ComputeBatchLossAndGrad(ctrl, u)
+    b = b_loss.ComputeBatchLossAndGrad(ctrl, u)
+    a_loss.CheckDeviceStatus()
+    for x, y in zip(a[2:], b[2:]):
+        assert rel_fro(x.cpu().numpy(), y.cpu().numpy()) < 1e-6
+
+
 @pytest.mark.parametrize("tma,twin", [(13, 11), (15, 6), (16, 11), (17, 11)])
 @pytest.mark.parametrize("layout", ["nodal", "element"])
 def test_tma_variant_equals_its_per_thread_twin(cuda, tma, twin, layout):
