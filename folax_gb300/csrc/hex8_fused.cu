@@ -802,15 +802,22 @@ static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_
 // (kGridTX + 1) x (kGridTY + 1) threads each take one element column
 // (x0 - 1 + tx, y0 - 1 + ty): the elements of the halo row, column and layer
 // below the tile are evaluated by this block too (they belong to the
-// neighbouring tiles), so every owned node is finished here.  Per element
-// layer: each thread evaluates its element (box_elem's algebra), keeps the
-// element's upper-face node values for the next layer, and stores its 8
-// corner residuals in shared memory; after a barrier the same thread, as
-// node (x0 + tx, y0 + ty), adds the lower-corner residuals of the 4 elements
-// around it to the upper-corner sums it kept from the layer below, in a fixed
-// order, and writes the finished node.  Energies and element control
-// gradients are taken from owned elements only.  The loss exponent must be 1
-// (the gradients are scaled as they are written).
+// neighbouring tiles), so every owned node is finished here.
+//
+// The 8-point Hadamard transform of an element is the 4-point transform of
+// each face (x and y stages) followed by the z stage, so an element column
+// transforms each node layer once: the upper face of one element is the lower
+// face of the next.  The residual runs the same way backwards: the
+// transposed z stage splits the block products into a lower and an upper
+// face part, and the upper part of layer kz - 1 is added to the lower part of
+// layer kz before the one transposed face transform, which gives the element
+// column's four corner contributions to node layer kz.  Per element layer:
+// each thread evaluates its element (the dofs of the layer above were loaded
+// one layer ahead), stores its four corner contributions in shared memory,
+// and after a barrier, as node (x0 + tx, y0 + ty), adds the contributions of
+// the four element columns around it in a fixed order and writes the node.
+// Energies and element control gradients come from owned elements only.  The
+// loss exponent must be 1 (the gradients are scaled as they are written).
 constexpr int kGridTX = 16, kGridTY = 8;
 constexpr int kGridCols = (kGridTX + 1) * (kGridTY + 1);  // element columns per block
 constexpr int kGridBlock = (kGridCols + 31) / 32 * 32;
@@ -821,8 +828,45 @@ struct GridDims {
   int tiles_x, tiles_y;
 };
 
-__global__ void __launch_bounds__(kGridBlock) k_hex8_box_grid(const VecArgs A, const BoxK K, const GridDims G) {
-  __shared__ float rec[8][3][kGridTY + 1][kGridTX + 1];  // corner residuals of this element layer
+// 4-point Hadamard transform of a face (lex a = ax + 2 ay), the x and y stages
+// of wht8; h4t is its transpose (the x and y stages of wht8_t).
+__device__ __forceinline__ void h4(float (&f)[4]) {
+  float a = f[0], b = f[1];
+  f[0] = a + b;
+  f[1] = b - a;
+  a = f[2];
+  b = f[3];
+  f[2] = a + b;
+  f[3] = b - a;
+  a = f[0];
+  b = f[2];
+  f[0] = a + b;
+  f[2] = b - a;
+  a = f[1];
+  b = f[3];
+  f[1] = a + b;
+  f[3] = b - a;
+}
+__device__ __forceinline__ void h4t(float (&d)[4]) {
+  float a = d[0], b = d[1];
+  d[0] = a - b;
+  d[1] = a + b;
+  a = d[2];
+  b = d[3];
+  d[2] = a - b;
+  d[3] = a + b;
+  a = d[0];
+  b = d[2];
+  d[0] = a - b;
+  d[2] = a + b;
+  a = d[1];
+  b = d[3];
+  d[1] = a - b;
+  d[3] = a + b;
+}
+
+__global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A, const BoxK K, const GridDims G) {
+  __shared__ float cnr[4][3][kGridTY + 1][kGridTX + 1];  // corner contributions of each element column
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   pdl_launch_dependents();
@@ -833,10 +877,10 @@ __global__ void __launch_bounds__(kGridBlock) k_hex8_box_grid(const VecArgs A, c
   t /= G.tiles_x;
   const int by = t % G.tiles_y, bz = t / G.tiles_y;
   const int x0 = bx * kGridTX, y0 = by * kGridTY, z0 = bz * G.tz;
-  const int NX = G.nx + 1, NY = G.ny + 1;  // nodes per row, per column
+  const int NX = G.nx + 1, NXY = NX * (G.ny + 1);  // nodes per row, per layer
   // owned node counts of this tile (the last tiles own the final plane too)
   const int onx = x0 + kGridTX >= G.nx ? NX - x0 : kGridTX;
-  const int ony = y0 + kGridTY >= G.ny ? NY - y0 : kGridTY;
+  const int ony = y0 + kGridTY >= G.ny ? G.ny + 1 - y0 : kGridTY;
   const int zend = z0 + G.tz >= G.nz ? G.nz + 1 : z0 + G.tz;  // node layers [z0, zend)
   const bool col = threadIdx.x < kGridCols;
   const int tx = threadIdx.x % (kGridTX + 1), ty = threadIdx.x / (kGridTX + 1);
@@ -846,46 +890,76 @@ __global__ void __launch_bounds__(kGridBlock) k_hex8_box_grid(const VecArgs A, c
   const bool node_owned = col && tx < onx && ty < ony;
   const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
   const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
-  float lower[3][4];  // nodal values of the element's lower face (lex 0..3), from the layer below
-  bool have_lower = false;
-  float up[3] = {0.f, 0.f, 0.f};  // node (x0 + tx, y0 + ty, kz): upper-corner sums of element layer kz - 1
+  const bool dir = A.apply_dirichlet != 0;
+  // the element column's four nodes in a layer: n + {0, 1, NX, NX + 1}
+  const int c0 = ex + NX * ey;
+  // raw dofs of a face (lex a = ax + 2 ay) and its Dirichlet mask bits
+  auto load_face = [&](int kz, float (&u)[3][4], unsigned& mk) {
+    mk = 0u;
+#pragma unroll
+    for (int a = 0; a < 4; ++a) {
+      const int64_t n = (int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz;
+      const unsigned m = dir ? __ldg(A.dmask + n) : 0u;
+      mk |= (m & 7u) << (3 * a);
+      const float* d = dofs + 3 * n;
+      u[0][a] = __ldg(d);
+      u[1][a] = __ldg(d + 1);
+      u[2][a] = __ldg(d + 2);
+    }
+  };
+  // Dirichlet values, then the face transform
+  auto finish_face = [&](int kz, float (&u)[3][4], unsigned mk) {
+    if (mk) {
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int c = 0; c < 3; ++c)
+          if ((mk >> (3 * a + c)) & 1u)
+            u[c][a] = __ldg(A.dval + 3 * ((int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz) + c);
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) h4(u[c]);
+  };
+  float lo_f[3][4];         // face transform of the element's lower face (node layer kz)
+  float nxt[3][4];          // raw dofs of node layer kz + 1, loaded one layer ahead
+  unsigned nxt_m = 0u;
+  float hi_prev[3][4] = {};  // transposed-z upper part of element layer kz - 1
+  bool have_lo = false;
   float energy = 0.f;
   int bad = 0;
-  auto load_node = [&](int ix, int iy, int iz, float& u0, float& u1, float& u2) {
-    const int64_t n = (int64_t)ix + (int64_t)NX * (iy + (int64_t)NY * iz);
-    const unsigned m = A.apply_dirichlet ? __ldg(A.dmask + n) : 0u;
-    const float* d = dofs + 3 * n;
-    u0 = (m & 1u) ? __ldg(A.dval + 3 * n) : __ldg(d);
-    u1 = (m & 2u) ? __ldg(A.dval + 3 * n + 1) : __ldg(d + 1);
-    u2 = (m & 4u) ? __ldg(A.dval + 3 * n + 2) : __ldg(d + 2);
-  };
+  auto layer_valid = [&](int kz) { return col_valid && kz >= 0 && kz < G.nz; };
+  // invariant: at a valid element layer kz, nxt holds node layer kz + 1
+  if (layer_valid(z0 - 1)) load_face(z0, nxt, nxt_m);
   for (int kz = z0 - 1; kz < zend; ++kz) {
-    float V[3][8];
-    if (col_valid && kz >= 0 && kz < G.nz) {
-      float U[3][8];
-      // lex L = ax + 2 ay + 4 az at node (ex + ax, ey + ay, kz + az)
-#pragma unroll
-      for (int L = 0; L < 4; ++L) {
-        if (have_lower) {
-          U[0][L] = lower[0][L];
-          U[1][L] = lower[1][L];
-          U[2][L] = lower[2][L];
-        } else {
-          load_node(ex + (L & 1), ey + (L >> 1), kz, U[0][L], U[1][L], U[2][L]);
-        }
+    float lo[3][4], hi[3][4];
+    if (layer_valid(kz)) {
+      if (!have_lo) {  // first element of the column: its lower face
+        unsigned m;
+        load_face(kz, lo_f, m);
+        finish_face(kz, lo_f, m);
       }
+      float up_f[3][4];
 #pragma unroll
-      for (int L = 4; L < 8; ++L) {
-        load_node(ex + (L & 1), ey + ((L >> 1) & 1), kz + 1, U[0][L], U[1][L], U[2][L]);
-        lower[0][L - 4] = U[0][L];
-        lower[1][L - 4] = U[1][L];
-        lower[2][L - 4] = U[2][L];
-      }
-      have_lower = true;
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) up_f[c][a] = nxt[c][a];
+      const unsigned up_m = nxt_m;
+      if (layer_valid(kz + 1)) load_face(kz + 2, nxt, nxt_m);  // the next element's upper face
+      finish_face(kz + 1, up_f, up_m);
       const int64_t e = (int64_t)ex + (int64_t)G.nx * (ey + (int64_t)G.ny * kz);
       const float ee = __ldg(ctrl + e);
+      // z stage: Hadamard coefficients h[b] (b < 4) and h[b + 4]
+      float U[3][8];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) wht8(U[c]);
+      for (int c = 0; c < 3; ++c)
+#pragma unroll
+        for (int a = 0; a < 4; ++a) {
+          U[c][a] = lo_f[c][a] + up_f[c][a];
+          U[c][a + 4] = up_f[c][a] - lo_f[c][a];
+          lo_f[c][a] = up_f[c][a];  // the next element's lower face
+        }
+      have_lo = true;
+      float V[3][8];
 #pragma unroll
       for (int p = 0; p < 8; ++p) {
         const float u0 = U[0][p ^ 1], u1 = U[1][p ^ 2], u2 = U[2][p ^ 4];
@@ -903,54 +977,59 @@ __global__ void __launch_bounds__(kGridBlock) k_hex8_box_grid(const VecArgs A, c
         if (A.dctrl_elem) A.dctrl_elem[(int64_t)b * A.E + e] = sed * A.inv_batch;
       }
       if (!isfinite(sed)) bad |= 2;
+      // transposed z stage of E_e K^ u^: lower (s = -1) and upper (s = +1) parts
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
+      for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) V[c][q] *= ee;
-        wht8_t(V[c]);
-      }
+        for (int a = 0; a < 4; ++a) {
+          const float va = ee * V[c][a], vb = ee * V[c][a + 4];
+          lo[c][a] = va - vb;
+          hi[c][a] = va + vb;
+        }
     } else {
 #pragma unroll
       for (int c = 0; c < 3; ++c)
 #pragma unroll
-        for (int q = 0; q < 8; ++q) V[c][q] = 0.f;
-      have_lower = false;
+        for (int a = 0; a < 4; ++a) lo[c][a] = hi[c][a] = 0.f;
+      have_lo = false;
+      if (layer_valid(kz + 1)) load_face(kz + 2, nxt, nxt_m);  // the column starts above
     }
+    // node layer kz: upper part of element layer kz - 1 + lower part of layer kz
     if (col) {
 #pragma unroll
-      for (int L = 0; L < 8; ++L)
+      for (int c = 0; c < 3; ++c) {
+        float f[4];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) rec[L][c][ty][tx] = V[c][L];
+        for (int a = 0; a < 4; ++a) {
+          f[a] = hi_prev[c][a] + lo[c][a];
+          hi_prev[c][a] = hi[c][a];
+        }
+        h4t(f);
+#pragma unroll
+        for (int a = 0; a < 4; ++a) cnr[a][c][ty][tx] = f[a];
+      }
     }
     __syncthreads();
-    if (col) {
-      // node (x0 + tx, y0 + ty): element columns tx + ox, ty + oy, corner (1 - ox, 1 - oy)
-      float low[3] = {0.f, 0.f, 0.f}, upn[3] = {0.f, 0.f, 0.f};
+    if (node_owned && kz >= z0 && A.out) {
+      // node (x0 + tx, y0 + ty): element columns (tx + ox, ty + oy), corner (1 - ox, 1 - oy)
+      float s[3] = {0.f, 0.f, 0.f};
 #pragma unroll
       for (int o = 0; o < 4; ++o) {
         const int ox = o & 1, oy = o >> 1;
         if (tx + ox <= kGridTX && ty + oy <= kGridTY) {
-          const int L = (1 - ox) + 2 * (1 - oy);
+          const int a = (1 - ox) + 2 * (1 - oy);
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            low[c] += rec[L][c][ty + oy][tx + ox];
-            upn[c] += rec[L + 4][c][ty + oy][tx + ox];
-          }
+          for (int c = 0; c < 3; ++c) s[c] += cnr[a][c][ty + oy][tx + ox];
         }
       }
-      if (node_owned && kz >= z0 && A.out) {
-        const int64_t n = (int64_t)(x0 + tx) + (int64_t)NX * ((y0 + ty) + (int64_t)NY * kz);
-        const unsigned m = __ldg(A.dmask + n);
-        float* o = A.out + (int64_t)b * A.out_stride + 3 * n;
-        o[0] = (m & 1u) ? 0.f : A.inv_batch * (up[0] + low[0]);
-        o[1] = (m & 2u) ? 0.f : A.inv_batch * (up[1] + low[1]);
-        o[2] = (m & 4u) ? 0.f : A.inv_batch * (up[2] + low[2]);
-      }
-      up[0] = upn[0];
-      up[1] = upn[1];
-      up[2] = upn[2];
+      const int64_t n = (int64_t)(x0 + tx) + (int64_t)NX * (y0 + ty) + (int64_t)NXY * kz;
+      const unsigned m = __ldg(A.dmask + n);
+      float* o = A.out + (int64_t)b * A.out_stride + 3 * n;
+      o[0] = (m & 1u) ? 0.f : A.inv_batch * s[0];
+      o[1] = (m & 2u) ? 0.f : A.inv_batch * s[1];
+      o[2] = (m & 4u) ? 0.f : A.inv_batch * s[2];
     }
-    __syncthreads();  // rec is rewritten by the next layer
+    __syncthreads();  // cnr is rewritten by the next layer
   }
   finish_loss_warp(energy, bad, A, b, wsum, &wcount);
 }
@@ -1417,7 +1496,7 @@ static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, b
 // per thread in blocks of 256 and 128.
 constexpr int kHex8TileFirst = 18;
 constexpr int kHex8BoxFirst = 20;
-constexpr int kHex8GridFirst = 23;  // structured box grid, 4 and 8 node layers per block
+constexpr int kHex8GridFirst = 23;  // structured box grid, 4 and 2 node layers per block
 
 GridDims grid_dims(const folgb_plan* p, int tz) {
   GridDims G;
@@ -1509,7 +1588,7 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
   if (variant >= kHex8GridFirst) {
     if (mode == MODE_LOSS && p->box_grid && A.exponent == 1.f) {
       trace_begin(KID_ELEM_LOSS, s);
-      launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 4 : 8, s);
+      launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 4 : 2, s);
       trace_end(KID_ELEM_LOSS, s);
       return 3;
     }

@@ -1170,12 +1170,49 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const GridA
   return true;
 }
 
+// Asks the memory system to bring [p, p + bytes) into L2 (cp.async.bulk
+// prefetch, a hint that loads nothing into registers): the 16-byte aligned
+// part of the range, so every prefetched byte lies inside it.
+__device__ __forceinline__ void prefetch_l2_range(const void* p, int64_t bytes) {
+  uint64_t a = ((uint64_t)p + 15) & ~(uint64_t)15;
+  const uint64_t e = ((uint64_t)p + (uint64_t)bytes) & ~(uint64_t)15;
+  while (a < e) {
+    const uint64_t chunk = e - a < ((uint64_t)1 << 20) ? e - a : ((uint64_t)1 << 20);
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)chunk) : "memory");
+    a += chunk;
+  }
+}
+
+// Rounds of the block's row loop whose CSR values and adjacency are
+// prefetched into L2 ahead of the loads that use them.
+constexpr int kGridPrefetchRounds = 3;
+
+// The block's rows [n0, n1) in rounds of ngroups * U nodes (group g of the
+// block takes nodes base .. base + U - 1 of each round).  A block's rows are
+// contiguous, and so are their CSR values and adjacency entries: thread 0
+// prefetches the values and adjacency of the round kGridPrefetchRounds ahead
+// of the current one into L2, so the value stream runs ahead of the
+// register-limited loads of the 16 warps per SM.
 template <int NDOF, int G, class T, class VT, class Col, class Epi>
 __device__ __forceinline__ void grid_rows(const GridArgs<VT>& A, int64_t n0, int64_t n1, Col col, Epi epi) {
   constexpr int U = RowsU<NDOF>::U;
   const int lane = threadIdx.x % G;
   const int64_t group = threadIdx.x / G, ngroups = blockDim.x / G;
-  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += ngroups * U) {
+  const int64_t step = ngroups * U;
+  auto prefetch = [&](int64_t a, int64_t b) {  // rows [a, b) of this block
+    if (a >= n1) return;
+    if (b > n1) b = n1;
+    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + b);
+    prefetch_l2_range(A.vals + (int64_t)NDOF * NDOF * ea, (int64_t)NDOF * NDOF * (eb - ea) * (int64_t)sizeof(float));
+    prefetch_l2_range(A.adj + ea, (eb - ea) * (int64_t)sizeof(int));
+  };
+  if (threadIdx.x == 0) prefetch(n0 + step, n0 + kGridPrefetchRounds * step);
+  int64_t ahead = n0 + kGridPrefetchRounds * step;
+  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += step) {
+    if (threadIdx.x == 0) {
+      prefetch(ahead, ahead + step);
+      ahead += step;
+    }
     T sum;
     int64_t d;
     if (rows_multi<NDOF, G, T>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
