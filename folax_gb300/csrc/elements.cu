@@ -768,7 +768,7 @@ static int elem_tiles(int64_t nb, int B) {
 static int loss_partial_slots(const folgb_plan* p) {
   int64_t slots = (p->E + 63) / 64;
   if (p->tiles > slots) slots = p->tiles;
-  if (p->box_grid) slots = std::max<int64_t>(slots, grid_blocks(p, 2));  // the smallest grid tile
+  if (p->box_grid) slots = std::max<int64_t>(slots, grid_blocks_max(p));
   return (int)slots;
 }
 

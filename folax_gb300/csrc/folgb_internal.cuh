@@ -181,8 +181,8 @@ void free_tile_tables(folgb_plan* p);
 // Uniform axis-aligned box elements (uniform_box.cu): sets box_valid and box_k.
 int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn);
 void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, double (&khat)[24][24]);
-// blocks of the structured box grid kernel with tz node layers per block (hex8_fused.cu)
-int64_t grid_blocks(const folgb_plan* p, int tz);
+// most blocks per instance of the structured box grid kernel (hex8_fused.cu)
+int64_t grid_blocks_max(const folgb_plan* p);
 // Destroys the plan's cached Krylov solve graphs (krylov.cu).
 void free_krylov_graphs(folgb_plan* p);
 

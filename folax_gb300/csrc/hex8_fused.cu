@@ -797,8 +797,10 @@ static void launch_variant_tma(const VecArgs& A, dim3 grid, bool bf, cudaStream_
 // records in global memory and no gather.
 //
 // A block owns the nodes of a column tile [x0, x0 + kGridTX) x [y0, y0 + kGridTY)
-// (the last tiles also own the mesh's last node plane) and the node layers
-// [z0, z0 + tz), and walks the element layers z0 - 1 ... upwards.  Its
+// (the last tiles also own the mesh's last node plane) and a chunk of node
+// layers [z0, z1) (the nz + 1 node layers split into nzc nearly equal chunks,
+// nzc chosen so the launch fills the resident blocks of the GPU in one or two
+// waves), and walks the element layers z0 - 1 ... upwards.  Its
 // (kGridTX + 1) x (kGridTY + 1) threads each take one element column
 // (x0 - 1 + tx, y0 - 1 + ty): the elements of the halo row, column and layer
 // below the tile are evaluated by this block too (they belong to the
@@ -824,7 +826,7 @@ constexpr int kGridBlock = (kGridCols + 31) / 32 * 32;
 
 struct GridDims {
   int nx, ny, nz;  // elements per direction
-  int tz;          // node layers per block
+  int nzc;         // chunks of node layers
   int tiles_x, tiles_y;
 };
 
@@ -876,12 +878,13 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
   const int bx = t % G.tiles_x;
   t /= G.tiles_x;
   const int by = t % G.tiles_y, bz = t / G.tiles_y;
-  const int x0 = bx * kGridTX, y0 = by * kGridTY, z0 = bz * G.tz;
+  const int x0 = bx * kGridTX, y0 = by * kGridTY;
+  const int z0 = (int)((int64_t)bz * (G.nz + 1) / G.nzc);
   const int NX = G.nx + 1, NXY = NX * (G.ny + 1);  // nodes per row, per layer
   // owned node counts of this tile (the last tiles own the final plane too)
   const int onx = x0 + kGridTX >= G.nx ? NX - x0 : kGridTX;
   const int ony = y0 + kGridTY >= G.ny ? G.ny + 1 - y0 : kGridTY;
-  const int zend = z0 + G.tz >= G.nz ? G.nz + 1 : z0 + G.tz;  // node layers [z0, zend)
+  const int zend = (int)((int64_t)(bz + 1) * (G.nz + 1) / G.nzc);  // node layers [z0, zend)
   const bool col = threadIdx.x < kGridCols;
   const int tx = threadIdx.x % (kGridTX + 1), ty = threadIdx.x / (kGridTX + 1);
   const int ex = x0 - 1 + tx, ey = y0 - 1 + ty;
@@ -1496,28 +1499,35 @@ static void launch_tile(const folgb_plan* p, const VecArgs& A, int B, bool bf, b
 // per thread in blocks of 256 and 128.
 constexpr int kHex8TileFirst = 18;
 constexpr int kHex8BoxFirst = 20;
-constexpr int kHex8GridFirst = 23;  // structured box grid, 4 and 2 node layers per block
+constexpr int kHex8GridFirst = 23;  // structured box grid, one and two waves of blocks
 
-GridDims grid_dims(const folgb_plan* p, int tz) {
+// The grid kernel's tiling for `waves` waves of resident blocks over B
+// instances: nzc chunks of node layers per column tile (1 <= nzc <= nz + 1).
+static GridDims grid_dims(const folgb_plan* p, int B, int waves) {
   GridDims G;
   G.nx = p->box_nx;
   G.ny = p->box_ny;
   G.nz = p->box_nz;
-  G.tz = tz;
   G.tiles_x = (G.nx + kGridTX - 1) / kGridTX;
   G.tiles_y = (G.ny + kGridTY - 1) / kGridTY;
+  static std::atomic<int> occ[kOccDevices];
+  const int64_t slots = (int64_t)blocks_per_sm(k_hex8_box_grid, kGridBlock, 0, occ) * num_sms() * waves;
+  int64_t nzc = slots / ((int64_t)G.tiles_x * G.tiles_y * B);
+  if (nzc < 1) nzc = 1;
+  if (nzc > G.nz + 1) nzc = G.nz + 1;
+  G.nzc = (int)nzc;
   return G;
 }
 
-// blocks of the structured box grid kernel with tz node layers per block
-int64_t grid_blocks(const folgb_plan* p, int tz) {
-  const GridDims G = grid_dims(p, tz);
-  return (int64_t)G.tiles_x * G.tiles_y * ((G.nz + tz - 1) / tz);
+// most blocks per instance the grid kernel can launch (a chunk per node layer)
+int64_t grid_blocks_max(const folgb_plan* p) {
+  return (int64_t)((p->box_nx + kGridTX - 1) / kGridTX) * ((p->box_ny + kGridTY - 1) / kGridTY) * (p->box_nz + 1);
 }
 
-static void launch_box_grid(const folgb_plan* p, const VecArgs& A, dim3 grid, int tz, cudaStream_t s) {
-  const GridDims G = grid_dims(p, tz);
-  k_hex8_box_grid<<<dim3((unsigned)grid_blocks(p, tz), grid.y), kGridBlock, 0, s>>>(A, p->box_k, G);
+static void launch_box_grid(const folgb_plan* p, const VecArgs& A, dim3 grid, int waves, cudaStream_t s) {
+  const GridDims G = grid_dims(p, (int)grid.y, waves);
+  const unsigned blocks = (unsigned)((int64_t)G.tiles_x * G.tiles_y * G.nzc);
+  k_hex8_box_grid<<<dim3(blocks, grid.y), kGridBlock, 0, s>>>(A, p->box_k, G);
 }
 
 template <int MODE>
@@ -1588,7 +1598,7 @@ int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode,
   if (variant >= kHex8GridFirst) {
     if (mode == MODE_LOSS && p->box_grid && A.exponent == 1.f) {
       trace_begin(KID_ELEM_LOSS, s);
-      launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 4 : 2, s);
+      launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 1 : 2, s);
       trace_end(KID_ELEM_LOSS, s);
       return 3;
     }

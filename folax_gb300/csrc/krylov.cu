@@ -777,9 +777,10 @@ __global__ void k_step_inc(int* step) { *step += 1; }
 
 enum { SOLVER_CG = 0, SOLVER_BICGSTAB = 1 };
 
-// The grid-resident CG is used unless switched off (folgb_krylov_set_engine).
-static std::atomic<int> g_grid_pcg{1};
-static bool grid_pcg_enabled() { return g_grid_pcg.load() != 0; }
+// Engine of large fp32 CG solves (folgb_krylov_set_engine): the grid-resident
+// CG by default.
+static std::atomic<int> g_krylov_engine{FOLGB_KRYLOV_ENGINE_GRID};
+static int krylov_engine() { return g_krylov_engine.load(); }
 
 // ---------------------------------------------------------------------------
 // Cluster-resident solver for small systems: the whole solve is ONE launch of
@@ -1144,9 +1145,9 @@ __device__ __forceinline__ bool grid_barrier(unsigned* bar, unsigned nblocks, in
 
 // sum of K doubles over the grid, the same totals in every thread of every
 // block (block sums added in block order); false if a barrier gave up
-template <int K, class VT>
-__device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const GridArgs<VT>& A, int& parity,
-                                         int* s_flag, double* s_bcast) {
+template <int K, class Args>
+__device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const Args& A, int& parity, int* s_flag,
+                                         double* s_bcast) {
   const unsigned nb = gridDim.x;
   double* slot = A.part + (size_t)parity * 4 * nb;
 #pragma unroll
@@ -1170,49 +1171,12 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const GridA
   return true;
 }
 
-// Asks the memory system to bring [p, p + bytes) into L2 (cp.async.bulk
-// prefetch, a hint that loads nothing into registers): the 16-byte aligned
-// part of the range, so every prefetched byte lies inside it.
-__device__ __forceinline__ void prefetch_l2_range(const void* p, int64_t bytes) {
-  uint64_t a = ((uint64_t)p + 15) & ~(uint64_t)15;
-  const uint64_t e = ((uint64_t)p + (uint64_t)bytes) & ~(uint64_t)15;
-  while (a < e) {
-    const uint64_t chunk = e - a < ((uint64_t)1 << 20) ? e - a : ((uint64_t)1 << 20);
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)chunk) : "memory");
-    a += chunk;
-  }
-}
-
-// Rounds of the block's row loop whose CSR values and adjacency are
-// prefetched into L2 ahead of the loads that use them.
-constexpr int kGridPrefetchRounds = 3;
-
-// The block's rows [n0, n1) in rounds of ngroups * U nodes (group g of the
-// block takes nodes base .. base + U - 1 of each round).  A block's rows are
-// contiguous, and so are their CSR values and adjacency entries: thread 0
-// prefetches the values and adjacency of the round kGridPrefetchRounds ahead
-// of the current one into L2, so the value stream runs ahead of the
-// register-limited loads of the 16 warps per SM.
-template <int NDOF, int G, class T, class VT, class Col, class Epi>
-__device__ __forceinline__ void grid_rows(const GridArgs<VT>& A, int64_t n0, int64_t n1, Col col, Epi epi) {
+template <int NDOF, int G, class T, class Args, class Col, class Epi>
+__device__ __forceinline__ void grid_rows(const Args& A, int64_t n0, int64_t n1, Col col, Epi epi) {
   constexpr int U = RowsU<NDOF>::U;
   const int lane = threadIdx.x % G;
   const int64_t group = threadIdx.x / G, ngroups = blockDim.x / G;
-  const int64_t step = ngroups * U;
-  auto prefetch = [&](int64_t a, int64_t b) {  // rows [a, b) of this block
-    if (a >= n1) return;
-    if (b > n1) b = n1;
-    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + b);
-    prefetch_l2_range(A.vals + (int64_t)NDOF * NDOF * ea, (int64_t)NDOF * NDOF * (eb - ea) * (int64_t)sizeof(float));
-    prefetch_l2_range(A.adj + ea, (eb - ea) * (int64_t)sizeof(int));
-  };
-  if (threadIdx.x == 0) prefetch(n0 + step, n0 + kGridPrefetchRounds * step);
-  int64_t ahead = n0 + kGridPrefetchRounds * step;
-  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += step) {
-    if (threadIdx.x == 0) {
-      prefetch(ahead, ahead + step);
-      ahead += step;
-    }
+  for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += ngroups * U) {
     T sum;
     int64_t d;
     if (rows_multi<NDOF, G, T>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
@@ -1489,7 +1453,8 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
           return (int)FOLGB_OK;
         }
         // large fp32 CG systems: one cooperative launch of the grid solver
-        if (solver == SOLVER_CG && n > kClusterMaxDofs && sizeof(VT) == sizeof(float) && grid_pcg_enabled()) {
+        if (solver == SOLVER_CG && n > kClusterMaxDofs && sizeof(VT) == sizeof(float) &&
+            krylov_engine() == FOLGB_KRYLOV_ENGINE_GRID) {
           GridArgs<VT> ga;
           ga.N = p->N;
           ga.adj_ptr = p->d_adj_ptr;
@@ -1669,7 +1634,7 @@ static int krylov_async(const folgb_plan* p, int solver, const float* vals, cons
   key.maxiter = maxiter;
   key.check_every = check_every;
   key.rtol = rtol;
-  key.engine = grid_pcg_enabled() ? 1 : 0;
+  key.engine = krylov_engine();
   FOLGB_CUDA_TRY(cudaGetDevice(&key.device));
   folgb_plan* mp = const_cast<folgb_plan*>(p);  // the cache is the plan's only mutable state
   {
@@ -1788,7 +1753,7 @@ extern "C" int folgb_krylov(const folgb_plan* p, int32_t method, int32_t vector_
 
 extern "C" int folgb_krylov_set_engine(int32_t engine) {
   if (engine != FOLGB_KRYLOV_ENGINE_GRID && engine != FOLGB_KRYLOV_ENGINE_KERNELS) return FOLGB_ERR_INVALID_ARGUMENT;
-  g_grid_pcg.store(engine == FOLGB_KRYLOV_ENGINE_GRID ? 1 : 0);
+  g_krylov_engine.store(engine);
   return FOLGB_OK;
 }
 

@@ -54,8 +54,8 @@ HEX8_VARIANT_NAMES = ["256 thr, point sums", "128 thr, point sums", "256 thr, du
                       "TMA-staged rows",
                       "uniform box: 3x3 blocks of the element matrix in the Hadamard basis, 256 thr",
                       "uniform box: 3x3 blocks of the element matrix in the Hadamard basis, 128 thr",
-                      "structured box grid: one launch, no records, 16x8 node columns x 4 layers per block",
-                      "structured box grid: one launch, no records, 16x8 node columns x 2 layers per block"]
+                      "structured box grid: one launch, no records, 16x8 node columns, layer chunks for one wave",
+                      "structured box grid: one launch, no records, 16x8 node columns, layer chunks for two waves"]
 _NEN = {"quad": 4, "hexahedron": 8, "tetra": 4}
 
 

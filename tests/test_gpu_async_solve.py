@@ -145,3 +145,10 @@ def test_grid_engine_matches_kernel_engine(cuda, n):
     (xk, ik), (xg, ig) = out[capi.KRYLOV_ENGINE_KERNELS], out[capi.KRYLOV_ENGINE_GRID]
     assert np.linalg.norm(xg - xk) <= 1e-6 * np.linalg.norm(xk)
     assert abs(ig - ik) <= 0.02 * ik + 2
+
+
+def test_engine_selector_refuses_unknown(cuda):
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    assert lib.folgb_krylov_set_engine(7) == capi.ERR_INVALID_ARGUMENT
+    assert lib.folgb_krylov_set_engine(capi.KRYLOV_ENGINE_GRID) == capi.OK
