@@ -183,6 +183,8 @@ int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::v
 void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, double (&khat)[24][24]);
 // most blocks per instance of the structured box grid kernel (hex8_fused.cu)
 int64_t grid_blocks_max(const folgb_plan* p);
+// whether the plan's loss + adjoint currently runs the structured box grid kernel
+bool hex8_grid_path(const folgb_plan* p);
 // Destroys the plan's cached Krylov solve graphs (krylov.cu).
 void free_krylov_graphs(folgb_plan* p);
 

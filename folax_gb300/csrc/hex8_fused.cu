@@ -1572,6 +1572,12 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
 // 23..24 structured box grid (no records).
 constexpr int kHex8Variants = 25;
 
+bool hex8_grid_path(const folgb_plan* p) {
+  return p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && p->phys.num_gp == 2 &&
+         p->phys.kernel_variant != 1 && p->hex8_variant >= kHex8GridFirst && p->box_grid &&
+         p->phys.loss_exponent == 1.0;
+}
+
 // Whether a variant can run on the plan (tile tables; a uniform box mesh; a
 // structured one, loss exponent 1).
 bool hex8_variant_applies(const folgb_plan* p, int v) {

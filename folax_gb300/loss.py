@@ -300,11 +300,14 @@ class FiniteElementLoss:
         "uniform_box" (every element the same axis-aligned box: the box
         kernels, variants 20-22) and "box_grid" (also numbered as a structured
         box mesh: the one-launch grid kernels, variants 23-24, loss exponent
-        1).  The autotuner times the variants that apply."""
+        1), and "reads_nodes_once" (the plan's current kernel is such a grid
+        kernel: pinned host dofs are then read in place).  The autotuner times
+        the variants that apply."""
         f = C.c_int32()
         capi.check("folgb_plan_features", self._plan.lib.folgb_plan_features(self._plan.handle, C.byref(f)))
         return {"tiles": bool(f.value & capi.FEATURE_TILES), "uniform_box": bool(f.value & capi.FEATURE_UNIFORM_BOX),
-                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID)}
+                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID),
+                "reads_nodes_once": bool(f.value & capi.FEATURE_READS_NODES_ONCE)}
 
     def CheckDeviceStatus(self):
         """Raise FolgbError if a kernel flagged a non-positive detJ, a
@@ -366,16 +369,25 @@ class FiniteElementLoss:
         complete once the current stream has finished (mean / min / max stay
         on the GPU).  Pinned host inputs: the dofs are copied to the GPU on the
         current stream; element-layout controls (read once per element) are
-        read by the kernel straight from pinned host memory."""
+        read by the kernel straight from pinned host memory, and so are the
+        dofs when the plan runs the structured box grid kernel (each node read
+        about once, KernelFeatures()["reads_nodes_once"])."""
         torch = _torch()
         direct_ctrl = (isinstance(batch_params, torch.Tensor) and batch_params.device.type == "cpu"
                        and batch_params.is_pinned() and batch_params.dtype == torch.float32
                        and batch_params.is_contiguous() and self._plan.phys.control_layout == capi.CONTROL_ELEMENT
                        and not self.parametric_boundary_learning)
-        U = _dev(batch_dofs)
+        direct_dofs = (isinstance(batch_dofs, torch.Tensor) and batch_dofs.device.type == "cpu"
+                       and batch_dofs.is_pinned() and batch_dofs.dtype == torch.float32
+                       and batch_dofs.is_contiguous() and not self.parametric_boundary_learning
+                       and self.KernelFeatures()["reads_nodes_once"])
+        U = batch_dofs if direct_dofs else _dev(batch_dofs)
         U = U.reshape(-1, self.total_number_of_dofs) if U.dim() != 2 else U
-        if direct_ctrl:
-            P, B = batch_params.reshape(-1, self.GetNumberOfControls()), U.shape[0]
+        if direct_ctrl or direct_dofs:
+            if U.shape[1] != self.total_number_of_dofs:
+                raise ValueError(f"dofs must have {self.total_number_of_dofs} entries per instance")
+            P = batch_params if direct_ctrl else _dev(batch_params)
+            P, B = P.reshape(-1, self.GetNumberOfControls()), U.shape[0]
             if P.shape[0] not in (1, B):
                 raise ValueError("batch_params must have 1 or batch rows")
         else:
@@ -396,7 +408,7 @@ class FiniteElementLoss:
             losses = out_losses if out_losses.is_cuda else torch.empty(B, dtype=torch.float32, device="cuda")
         else:
             losses = torch.empty(B, dtype=torch.float32, device="cuda")
-            du = torch.empty_like(U) if grads else None
+            du = torch.empty(U.shape, dtype=torch.float32, device="cuda") if grads else None
             dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if grads else None
         op = capi.OP_PLAIN if plain else capi.OP_LOSS_ADJOINT
         ws = self._plan.workspace(op, B)
