@@ -61,12 +61,17 @@ BOX_VARIANTS, GRID_VARIANTS = (20, 21, 22), (23, 24)
 # (13, 16, 17 with the affine-element path; ncu's printed precision for the
 # DRAM bytes: 17.60 MB read, a few KB written)
 #   21: k_hex8_box, 256 threads, uniform box element (the records, 33.5 MB,
-#       stay in L2 for the gather: 25 KB written to DRAM)
+#       stay in L2 for the gather: 8 KB written to DRAM)
+# fp32_flops: ncu's FP32 thread-instruction counts of one launch, fadd + fmul +
+# 2 ffma + 2 fadd2 + 2 fmul2 + 4 ffma2 (variant 16: 1,699 flops per element,
+# against the naive 5,208 of FLOPS_PER_ELEMENT; variant 21: 357).
 NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16_144_605},
                     13: {"traffic": 17_600_000 + 4_860, "warp_instructions": 10_652_202},
-                    16: {"traffic": 17_600_000 + 9_470, "warp_instructions": 10_954_635},
+                    16: {"traffic": 17_600_000 + 28_200, "warp_instructions": 10_935_648,
+                         "fp32_flops": 445_300_000},
                     17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421},
-                    21: {"traffic": 13_081_088 + 25_344, "warp_instructions": 4_817_046}}}
+                    21: {"traffic": 13_100_000 + 7_940, "warp_instructions": 4_817_046,
+                         "fp32_flops": 93_490_000}}}
 
 
 def ncu_figure(n, variant, key):

@@ -867,8 +867,55 @@ __device__ __forceinline__ void h4t(float (&d)[4]) {
   d[3] = a + b;
 }
 
+// The x and y displacement components of a face travel as packed fp32 pairs
+// (FADD2 / FFMA2 / FMUL2: each half rounded as the scalar operation), the z
+// component as a scalar.
+struct FacePair {
+  float2 xy[4];
+  float z[4];
+};
+
+__device__ __forceinline__ void h4p(float2 (&f)[4]) {
+  float2 a = f[0], b = f[1];
+  f[0] = add2(a, b);
+  f[1] = sub2(b, a);
+  a = f[2];
+  b = f[3];
+  f[2] = add2(a, b);
+  f[3] = sub2(b, a);
+  a = f[0];
+  b = f[2];
+  f[0] = add2(a, b);
+  f[2] = sub2(b, a);
+  a = f[1];
+  b = f[3];
+  f[1] = add2(a, b);
+  f[3] = sub2(b, a);
+}
+__device__ __forceinline__ void h4tp(float2 (&d)[4]) {
+  float2 a = d[0], b = d[1];
+  d[0] = sub2(a, b);
+  d[1] = add2(a, b);
+  a = d[2];
+  b = d[3];
+  d[2] = sub2(a, b);
+  d[3] = add2(a, b);
+  a = d[0];
+  b = d[2];
+  d[0] = sub2(a, b);
+  d[2] = add2(a, b);
+  a = d[1];
+  b = d[3];
+  d[1] = sub2(a, b);
+  d[3] = add2(a, b);
+}
+
 __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A, const BoxK K, const GridDims G) {
-  __shared__ float cnr[4][3][kGridTY + 1][kGridTX + 1];  // corner contributions of each element column
+  // corner contributions of each element column, double-buffered by layer: a
+  // buffer is rewritten two layers later, after the barrier of the layer
+  // between, so one barrier per layer orders the writes and the reads
+  __shared__ float2 cnr_xy[2][4][kGridTY + 1][kGridTX + 1];
+  __shared__ float cnr_z[2][4][kGridTY + 1][kGridTX + 1];
   __shared__ float wsum[32];
   __shared__ unsigned wcount;
   pdl_launch_dependents();
@@ -897,7 +944,7 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
   // the element column's four nodes in a layer: n + {0, 1, NX, NX + 1}
   const int c0 = ex + NX * ey;
   // raw dofs of a face (lex a = ax + 2 ay) and its Dirichlet mask bits
-  auto load_face = [&](int kz, float (&u)[3][4], unsigned& mk) {
+  auto load_face = [&](int kz, FacePair& u, unsigned& mk) {
     mk = 0u;
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
@@ -905,134 +952,150 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
       const unsigned m = dir ? __ldg(A.dmask + n) : 0u;
       mk |= (m & 7u) << (3 * a);
       const float* d = dofs + 3 * n;
-      u[0][a] = __ldg(d);
-      u[1][a] = __ldg(d + 1);
-      u[2][a] = __ldg(d + 2);
+      u.xy[a] = make_float2(__ldg(d), __ldg(d + 1));
+      u.z[a] = __ldg(d + 2);
     }
   };
   // Dirichlet values, then the face transform
-  auto finish_face = [&](int kz, float (&u)[3][4], unsigned mk) {
+  auto finish_face = [&](int kz, FacePair& u, unsigned mk) {
     if (mk) {
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          if ((mk >> (3 * a + c)) & 1u)
-            u[c][a] = __ldg(A.dval + 3 * ((int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz) + c);
+      for (int a = 0; a < 4; ++a) {
+        const float* v = A.dval + 3 * ((int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz);
+        if ((mk >> (3 * a)) & 1u) u.xy[a].x = __ldg(v);
+        if ((mk >> (3 * a + 1)) & 1u) u.xy[a].y = __ldg(v + 1);
+        if ((mk >> (3 * a + 2)) & 1u) u.z[a] = __ldg(v + 2);
+      }
     }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) h4(u[c]);
+    h4p(u.xy);
+    h4(u.z);
   };
-  float lo_f[3][4];         // face transform of the element's lower face (node layer kz)
-  float nxt[3][4];          // raw dofs of node layer kz + 1, loaded one layer ahead
+  FacePair lo_f;            // face transform of the element's lower face (node layer kz)
+  FacePair nxt;             // raw dofs of node layer kz + 1, loaded one layer ahead
   unsigned nxt_m = 0u;
-  float hi_prev[3][4] = {};  // transposed-z upper part of element layer kz - 1
+  float2 hp_xy[4];          // transposed-z upper part of element layer kz - 1
+  float hp_z[4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    hp_xy[a] = f2(0.f);
+    hp_z[a] = 0.f;
+  }
   bool have_lo = false;
   float energy = 0.f;
   int bad = 0;
   auto layer_valid = [&](int kz) { return col_valid && kz >= 0 && kz < G.nz; };
   // invariant: at a valid element layer kz, nxt holds node layer kz + 1
   if (layer_valid(z0 - 1)) load_face(z0, nxt, nxt_m);
-  for (int kz = z0 - 1; kz < zend; ++kz) {
-    float lo[3][4], hi[3][4];
+  int buf = 0;
+  for (int kz = z0 - 1; kz < zend; ++kz, buf ^= 1) {
+    float2 lo_xy[4], hi_xy[4];
+    float lo_z[4], hi_z[4];
     if (layer_valid(kz)) {
       if (!have_lo) {  // first element of the column: its lower face
         unsigned m;
         load_face(kz, lo_f, m);
         finish_face(kz, lo_f, m);
       }
-      float up_f[3][4];
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) up_f[c][a] = nxt[c][a];
+      FacePair up = nxt;
       const unsigned up_m = nxt_m;
       if (layer_valid(kz + 1)) load_face(kz + 2, nxt, nxt_m);  // the next element's upper face
-      finish_face(kz + 1, up_f, up_m);
+      finish_face(kz + 1, up, up_m);
       const int64_t e = (int64_t)ex + (int64_t)G.nx * (ey + (int64_t)G.ny * kz);
       const float ee = __ldg(ctrl + e);
       // z stage: Hadamard coefficients h[b] (b < 4) and h[b + 4]
-      float U[3][8];
+      float2 Uxy[8];
+      float Uz[8];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          U[c][a] = lo_f[c][a] + up_f[c][a];
-          U[c][a + 4] = up_f[c][a] - lo_f[c][a];
-          lo_f[c][a] = up_f[c][a];  // the next element's lower face
-        }
+      for (int a = 0; a < 4; ++a) {
+        Uxy[a] = add2(lo_f.xy[a], up.xy[a]);
+        Uxy[a + 4] = sub2(up.xy[a], lo_f.xy[a]);
+        Uz[a] = lo_f.z[a] + up.z[a];
+        Uz[a + 4] = up.z[a] - lo_f.z[a];
+      }
+      lo_f = up;  // the next element's lower face
       have_lo = true;
-      float V[3][8];
+      float2 Vxy[8];
+      float Vz[8];
 #pragma unroll
       for (int p = 0; p < 8; ++p) {
-        const float u0 = U[0][p ^ 1], u1 = U[1][p ^ 2], u2 = U[2][p ^ 4];
-#pragma unroll
-        for (int c = 0; c < 3; ++c)
-          V[c][p ^ (1 << c)] = fmaf(K.k[p][c][2], u2, fmaf(K.k[p][c][1], u1, K.k[p][c][0] * u0));
+        const float u0 = Uxy[p ^ 1].x, u1 = Uxy[p ^ 2].y, u2 = Uz[p ^ 4];
+        Vxy[p ^ 1].x = fmaf(K.k[p][0][2], u2, fmaf(K.k[p][0][1], u1, K.k[p][0][0] * u0));
+        Vxy[p ^ 2].y = fmaf(K.k[p][1][2], u2, fmaf(K.k[p][1][1], u1, K.k[p][1][0] * u0));
+        Vz[p ^ 4] = fmaf(K.k[p][2][2], u2, fmaf(K.k[p][2][1], u1, K.k[p][2][0] * u0));
       }
-      float sed = 0.f;
+      float2 sxy = mul2(Uxy[0], Vxy[0]);
+      float sz = Uz[0] * Vz[0];
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int q = 0; q < 8; ++q) sed = fmaf(U[c][q], V[c][q], sed);
+      for (int q = 1; q < 8; ++q) {
+        sxy = fma2(Uxy[q], Vxy[q], sxy);
+        sz = fmaf(Uz[q], Vz[q], sz);
+      }
+      const float sed = (sxy.x + sxy.y) + sz;  // u.K u
       if (col_owned && kz >= z0) {
         energy = fmaf(ee, sed, energy);
         if (A.dctrl_elem) A.dctrl_elem[(int64_t)b * A.E + e] = sed * A.inv_batch;
       }
       if (!isfinite(sed)) bad |= 2;
       // transposed z stage of E_e K^ u^: lower (s = -1) and upper (s = +1) parts
+      const float2 e2 = f2(ee);
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const float va = ee * V[c][a], vb = ee * V[c][a + 4];
-          lo[c][a] = va - vb;
-          hi[c][a] = va + vb;
-        }
+      for (int a = 0; a < 4; ++a) {
+        const float2 va = mul2(e2, Vxy[a]), vb = mul2(e2, Vxy[a + 4]);
+        lo_xy[a] = sub2(va, vb);
+        hi_xy[a] = add2(va, vb);
+        const float za = ee * Vz[a], zb = ee * Vz[a + 4];
+        lo_z[a] = za - zb;
+        hi_z[a] = za + zb;
+      }
     } else {
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-#pragma unroll
-        for (int a = 0; a < 4; ++a) lo[c][a] = hi[c][a] = 0.f;
+      for (int a = 0; a < 4; ++a) {
+        lo_xy[a] = hi_xy[a] = f2(0.f);
+        lo_z[a] = hi_z[a] = 0.f;
+      }
       have_lo = false;
       if (layer_valid(kz + 1)) load_face(kz + 2, nxt, nxt_m);  // the column starts above
     }
     // node layer kz: upper part of element layer kz - 1 + lower part of layer kz
     if (col) {
+      float2 fxy[4];
+      float fz[4];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        float f[4];
+      for (int a = 0; a < 4; ++a) {
+        fxy[a] = add2(hp_xy[a], lo_xy[a]);
+        fz[a] = hp_z[a] + lo_z[a];
+        hp_xy[a] = hi_xy[a];
+        hp_z[a] = hi_z[a];
+      }
+      h4tp(fxy);
+      h4t(fz);
 #pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          f[a] = hi_prev[c][a] + lo[c][a];
-          hi_prev[c][a] = hi[c][a];
-        }
-        h4t(f);
-#pragma unroll
-        for (int a = 0; a < 4; ++a) cnr[a][c][ty][tx] = f[a];
+      for (int a = 0; a < 4; ++a) {
+        cnr_xy[buf][a][ty][tx] = fxy[a];
+        cnr_z[buf][a][ty][tx] = fz[a];
       }
     }
     __syncthreads();
     if (node_owned && kz >= z0 && A.out) {
       // node (x0 + tx, y0 + ty): element columns (tx + ox, ty + oy), corner (1 - ox, 1 - oy)
-      float s[3] = {0.f, 0.f, 0.f};
+      float2 sxy = f2(0.f);
+      float sz = 0.f;
 #pragma unroll
       for (int o = 0; o < 4; ++o) {
         const int ox = o & 1, oy = o >> 1;
         if (tx + ox <= kGridTX && ty + oy <= kGridTY) {
           const int a = (1 - ox) + 2 * (1 - oy);
-#pragma unroll
-          for (int c = 0; c < 3; ++c) s[c] += cnr[a][c][ty + oy][tx + ox];
+          sxy = add2(sxy, cnr_xy[buf][a][ty + oy][tx + ox]);
+          sz += cnr_z[buf][a][ty + oy][tx + ox];
         }
       }
       const int64_t n = (int64_t)(x0 + tx) + (int64_t)NX * (y0 + ty) + (int64_t)NXY * kz;
       const unsigned m = __ldg(A.dmask + n);
       float* o = A.out + (int64_t)b * A.out_stride + 3 * n;
-      o[0] = (m & 1u) ? 0.f : A.inv_batch * s[0];
-      o[1] = (m & 2u) ? 0.f : A.inv_batch * s[1];
-      o[2] = (m & 4u) ? 0.f : A.inv_batch * s[2];
+      o[0] = (m & 1u) ? 0.f : A.inv_batch * sxy.x;
+      o[1] = (m & 2u) ? 0.f : A.inv_batch * sxy.y;
+      o[2] = (m & 4u) ? 0.f : A.inv_batch * sz;
     }
-    __syncthreads();  // cnr is rewritten by the next layer
   }
   finish_loss_warp(energy, bad, A, b, wsum, &wcount);
 }
