@@ -117,6 +117,7 @@ struct folgb_plan {
   // and the box mesh numbering of an nx x ny x nz grid (nodes x fastest, then
   // y, then z; the reference local node order): the one-launch grid kernel
   int box_grid = 0, box_nx = 0, box_ny = 0, box_nz = 0;
+
   // instantiated Krylov solve graphs of folgb_krylov_async (krylov.cu)
   void* krylov_graphs = nullptr;
   // CSR tables
@@ -183,8 +184,7 @@ int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::v
 void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, double (&khat)[24][24]);
 // most blocks per instance of the structured box grid kernel (hex8_fused.cu)
 int64_t grid_blocks_max(const folgb_plan* p);
-// whether the plan's loss + adjoint currently runs the structured box grid kernel
-bool hex8_grid_path(const folgb_plan* p);
+
 // Destroys the plan's cached Krylov solve graphs (krylov.cu).
 void free_krylov_graphs(folgb_plan* p);
 

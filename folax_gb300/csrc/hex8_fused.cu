@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <atomic>
 #include <type_traits>
+#include <vector>
 
 #include "element_body.cuh"
 
@@ -826,8 +827,10 @@ constexpr int kGridBlock = (kGridCols + 31) / 32 * 32;
 
 struct GridDims {
   int nx, ny, nz;  // elements per direction
-  int nzc;         // chunks of node layers
+  int zlo, zhi;    // node layers of this launch [zlo, zhi) (all: 0, nz + 1)
+  int nzc;         // chunks of those layers
   int tiles_x, tiles_y;
+  int blk_off, nblk;  // this launch's first block and the blocks of all launches of the step (loss sum)
 };
 
 // 4-point Hadamard transform of a face (lex a = ax + 2 ay), the x and y stages
@@ -926,12 +929,12 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
   t /= G.tiles_x;
   const int by = t % G.tiles_y, bz = t / G.tiles_y;
   const int x0 = bx * kGridTX, y0 = by * kGridTY;
-  const int z0 = (int)((int64_t)bz * (G.nz + 1) / G.nzc);
+  const int z0 = G.zlo + (int)((int64_t)bz * (G.zhi - G.zlo) / G.nzc);
   const int NX = G.nx + 1, NXY = NX * (G.ny + 1);  // nodes per row, per layer
   // owned node counts of this tile (the last tiles own the final plane too)
   const int onx = x0 + kGridTX >= G.nx ? NX - x0 : kGridTX;
   const int ony = y0 + kGridTY >= G.ny ? G.ny + 1 - y0 : kGridTY;
-  const int zend = (int)((int64_t)(bz + 1) * (G.nz + 1) / G.nzc);  // node layers [z0, zend)
+  const int zend = G.zlo + (int)((int64_t)(bz + 1) * (G.zhi - G.zlo) / G.nzc);  // node layers [z0, zend)
   const bool col = threadIdx.x < kGridCols;
   const int tx = threadIdx.x % (kGridTX + 1), ty = threadIdx.x / (kGridTX + 1);
   const int ex = x0 - 1 + tx, ey = y0 - 1 + ty;
@@ -1097,7 +1100,7 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
       o[2] = (m & 4u) ? 0.f : A.inv_batch * sz;
     }
   }
-  finish_loss_warp(energy, bad, A, b, wsum, &wcount);
+  finish_loss_warp(energy, bad, A, b, wsum, &wcount, G.blk_off + (int)blockIdx.x, G.nblk);
 }
 
 // ---------------------------------------------------------------------------
@@ -1571,6 +1574,8 @@ static GridDims grid_dims(const folgb_plan* p, int B, int waves) {
   G.nx = p->box_nx;
   G.ny = p->box_ny;
   G.nz = p->box_nz;
+  G.zlo = 0;
+  G.zhi = G.nz + 1;
   G.tiles_x = (G.nx + kGridTX - 1) / kGridTX;
   G.tiles_y = (G.ny + kGridTY - 1) / kGridTY;
   static std::atomic<int> occ[kOccDevices];
@@ -1579,6 +1584,8 @@ static GridDims grid_dims(const folgb_plan* p, int B, int waves) {
   if (nzc < 1) nzc = 1;
   if (nzc > G.nz + 1) nzc = G.nz + 1;
   G.nzc = (int)nzc;
+  G.blk_off = 0;
+  G.nblk = G.tiles_x * G.tiles_y * G.nzc;
   return G;
 }
 
@@ -1589,8 +1596,7 @@ int64_t grid_blocks_max(const folgb_plan* p) {
 
 static void launch_box_grid(const folgb_plan* p, const VecArgs& A, dim3 grid, int waves, cudaStream_t s) {
   const GridDims G = grid_dims(p, (int)grid.y, waves);
-  const unsigned blocks = (unsigned)((int64_t)G.tiles_x * G.tiles_y * G.nzc);
-  k_hex8_box_grid<<<dim3(blocks, grid.y), kGridBlock, 0, s>>>(A, p->box_k, G);
+  k_hex8_box_grid<<<dim3((unsigned)G.nblk, grid.y), kGridBlock, 0, s>>>(A, p->box_k, G);
 }
 
 template <int MODE>
@@ -1635,12 +1641,6 @@ static void launch_cl_mode(const VecArgs& A, dim3 grid, bool bf, int variant, cu
 // 23..24 structured box grid (no records).
 constexpr int kHex8Variants = 25;
 
-bool hex8_grid_path(const folgb_plan* p) {
-  return p->etype == FOLGB_HEX8 && p->physics == FOLGB_ELASTIC && p->phys.num_gp == 2 &&
-         p->phys.kernel_variant != 1 && p->hex8_variant >= kHex8GridFirst && p->box_grid &&
-         p->phys.loss_exponent == 1.0;
-}
-
 // Whether a variant can run on the plan (tile tables; a uniform box mesh; a
 // structured one, loss exponent 1).
 bool hex8_variant_applies(const folgb_plan* p, int v) {
@@ -1659,13 +1659,27 @@ bool hex8_variant_applies(const folgb_plan* p, int v) {
 // box grid kernel finished everything.  The residual path (MODE_RESIDUAL,
 // records for the node gather) runs variant 11 in place of a tile-local
 // variant and 21 in place of a grid variant; a grid variant that does not
-// apply runs 21, a box variant on a plan that is not a uniform box mesh 16.
+// apply, or whose gradients go to host memory, runs 21, a box variant on a
+// plan that is not a uniform box mesh 16.
+static bool is_host_pointer(const void* q) {
+  if (!q) return false;
+  cudaPointerAttributes at{};
+  if (cudaPointerGetAttributes(&at, q) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s) {
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2) return 0;
   int variant = p->hex8_variant;
   const bool bf = p->mat.has_bf != 0;
   if (variant >= kHex8GridFirst) {
-    if (mode == MODE_LOSS && p->box_grid && A.exponent == 1.f) {
+    // gradients into host memory (pinned result buffers): the box kernel and
+    // the gather write them over the host link faster than the grid kernel's
+    // scattered node stores
+    if (mode == MODE_LOSS && p->box_grid && A.exponent == 1.f && !is_host_pointer(A.out)) {
       trace_begin(KID_ELEM_LOSS, s);
       launch_box_grid(p, A, grid, variant == kHex8GridFirst ? 1 : 2, s);
       trace_end(KID_ELEM_LOSS, s);

@@ -412,8 +412,7 @@ extern "C" int folgb_plan_info(const folgb_plan* p, int64_t* ndof_per_node, int6
 extern "C" int folgb_plan_features(const folgb_plan* p, int32_t* features) {
   if (!p || !features) return FOLGB_ERR_INVALID_ARGUMENT;
   *features = (p->tiles > 0 ? FOLGB_FEATURE_TILES : 0) | (p->box_valid ? FOLGB_FEATURE_UNIFORM_BOX : 0) |
-              (p->box_grid ? FOLGB_FEATURE_BOX_GRID : 0) |
-              (hex8_grid_path(p) ? FOLGB_FEATURE_READS_NODES_ONCE : 0);
+              (p->box_grid ? FOLGB_FEATURE_BOX_GRID : 0);
   return FOLGB_OK;
 }
 

@@ -266,6 +266,10 @@ class FiniteElementLoss:
         self._csr_plan = None
         self._status = _torch().zeros(1, dtype=_torch().int32, device="cuda")
         self._strict_status = bool(s.get("check_device_status", False))
+        # the last call's validated arguments (ComputeBatchLossAndGrad); the
+        # epoch changes whenever the plan's kernel path may have changed
+        self._memo = None
+        self._epoch = getattr(self, "_epoch", 0) + 1
         self.initialized = True
 
     def _get_csr_plan(self) -> Plan:
@@ -300,14 +304,12 @@ class FiniteElementLoss:
         "uniform_box" (every element the same axis-aligned box: the box
         kernels, variants 20-22) and "box_grid" (also numbered as a structured
         box mesh: the one-launch grid kernels, variants 23-24, loss exponent
-        1), and "reads_nodes_once" (the plan's current kernel is such a grid
-        kernel: pinned host dofs are then read in place).  The autotuner times
-        the variants that apply."""
+        1; a call with host result buffers runs the box kernel and the gather
+        instead).  The autotuner times the variants that apply."""
         f = C.c_int32()
         capi.check("folgb_plan_features", self._plan.lib.folgb_plan_features(self._plan.handle, C.byref(f)))
         return {"tiles": bool(f.value & capi.FEATURE_TILES), "uniform_box": bool(f.value & capi.FEATURE_UNIFORM_BOX),
-                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID),
-                "reads_nodes_once": bool(f.value & capi.FEATURE_READS_NODES_ONCE)}
+                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID)}
 
     def CheckDeviceStatus(self):
         """Raise FolgbError if a kernel flagged a non-positive detJ, a
@@ -369,34 +371,70 @@ class FiniteElementLoss:
         complete once the current stream has finished (mean / min / max stay
         on the GPU).  Pinned host inputs: the dofs are copied to the GPU on the
         current stream; element-layout controls (read once per element) are
-        read by the kernel straight from pinned host memory, and so are the
-        dofs when the plan runs the structured box grid kernel (each node read
-        about once, KernelFeatures()["reads_nodes_once"])."""
+        read by the kernel straight from pinned host memory.  A call with the
+        same tensors as the previous one reuses its validated arguments."""
         torch = _torch()
+        key = self._call_key(torch, batch_params, batch_dofs, grads, plain, out)
+        memo = self._memo
+        if key is not None and memo is not None and memo[0] == key:
+            prep = memo[1]  # the same tensors as the last call, all used in place: no re-validation
+        else:
+            prep, in_place = self._prepare_call(torch, batch_params, batch_dofs, grads, plain, out)
+            self._memo = (key, prep) if (key is not None and in_place) else None
+        return self._run_call(torch, prep)
+
+    def _call_key(self, torch, batch_params, batch_dofs, grads, plain, out):
+        """Identity of a call's tensors (object, data pointer, shape) or None."""
+        if not (isinstance(batch_params, torch.Tensor) and isinstance(batch_dofs, torch.Tensor)):
+            return None
+        k = [self._epoch, grads, plain]
+        for t in (batch_params, batch_dofs) + (tuple(out) if out is not None else ()):
+            if not isinstance(t, torch.Tensor):
+                return None
+            k += [id(t), t.data_ptr(), tuple(t.shape)]
+        return tuple(k)
+
+    def _prepare_call(self, torch, batch_params, batch_dofs, grads, plain, out):
+        """Validated arguments of a loss + adjoint call, and whether every
+        input is used in place (no converted copy, so a later call with the
+        same tensors may reuse them)."""
         direct_ctrl = (isinstance(batch_params, torch.Tensor) and batch_params.device.type == "cpu"
                        and batch_params.is_pinned() and batch_params.dtype == torch.float32
                        and batch_params.is_contiguous() and self._plan.phys.control_layout == capi.CONTROL_ELEMENT
                        and not self.parametric_boundary_learning)
-        direct_dofs = (isinstance(batch_dofs, torch.Tensor) and batch_dofs.device.type == "cpu"
-                       and batch_dofs.is_pinned() and batch_dofs.dtype == torch.float32
-                       and batch_dofs.is_contiguous() and not self.parametric_boundary_learning
-                       and self.KernelFeatures()["reads_nodes_once"])
-        U = batch_dofs if direct_dofs else _dev(batch_dofs)
+        # host tensors are copied to the GPU on every call (into buffers kept
+        # with the prepared call); element controls in pinned memory are read
+        # by the kernel in place
+        copies = []
+
+        def staged(t):
+            if isinstance(t, torch.Tensor) and t.device.type == "cpu":
+                d = torch.empty(t.shape, dtype=torch.float32, device="cuda")
+                copies.append((d, t))
+                d.copy_(t, non_blocking=True)
+                return d
+            return _dev(t)
+
+        U = staged(batch_dofs)
         U = U.reshape(-1, self.total_number_of_dofs) if U.dim() != 2 else U
-        if direct_ctrl or direct_dofs:
+        if direct_ctrl:
             if U.shape[1] != self.total_number_of_dofs:
                 raise ValueError(f"dofs must have {self.total_number_of_dofs} entries per instance")
-            P = batch_params if direct_ctrl else _dev(batch_params)
-            P, B = P.reshape(-1, self.GetNumberOfControls()), U.shape[0]
+            P, B = batch_params.reshape(-1, self.GetNumberOfControls()), U.shape[0]
             if P.shape[0] not in (1, B):
                 raise ValueError("batch_params must have 1 or batch rows")
         else:
-            P, U, B = self._batched(batch_params, U)
+            P, U, B = self._batched(staged(batch_params), U)
+        used = {t.data_ptr() for t in (batch_params, batch_dofs) if isinstance(t, torch.Tensor)}
+        used |= {d.data_ptr() for d, _ in copies}
+        in_place = (isinstance(batch_params, torch.Tensor) and isinstance(batch_dofs, torch.Tensor)
+                    and P.data_ptr() in used and U.data_ptr() in used)
         apply_bc = 1
         if self.parametric_boundary_learning:
             U = self.GetFullDofVector(P, U)
             apply_bc = 0
-        out_losses = None
+            in_place = False
+        out_losses = du = dp = None
         if out is not None:
             out_losses, du, dp = out
             want = [(out_losses, (B,)), (du, (B, U.shape[1])), (dp, (B, P.shape[1]))]
@@ -405,18 +443,32 @@ class FiniteElementLoss:
                         or not (t.is_cuda or t.is_pinned())):
                     raise ValueError(f"out buffers must be float32, contiguous, of {shape} elements, "
                                      "on the GPU or in pinned host memory")
-            losses = out_losses if out_losses.is_cuda else torch.empty(B, dtype=torch.float32, device="cuda")
-        else:
-            losses = torch.empty(B, dtype=torch.float32, device="cuda")
-            du = torch.empty(U.shape, dtype=torch.float32, device="cuda") if grads else None
-            dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if grads else None
         op = capi.OP_PLAIN if plain else capi.OP_LOSS_ADJOINT
         ws = self._plan.workspace(op, B)
         fn = self._plan.lib.folgb_loss_adjoint_plain if plain else self._plan.lib.folgb_loss_adjoint
-        rc = fn(self._plan.handle, B, capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1], capi.ptr(U), U.shape[1],
-                apply_bc, capi.ptr(losses), capi.ptr(du), capi.ptr(dp), capi.ptr(self._status), capi.ptr(ws),
-                ws.numel(), capi.stream_handle())
-        capi.check("folgb_loss_adjoint_plain" if plain else "folgb_loss_adjoint", rc)
+        prep = {"P": P, "U": U, "B": B, "apply_bc": apply_bc, "out_losses": out_losses, "du": du, "dp": dp,
+                "grads": grads, "plain": plain, "ws": ws, "fn": fn, "copies": copies, "fresh": True,
+                "args": (capi.ptr(P), 0 if P.shape[0] == 1 else P.shape[1], capi.ptr(U), U.shape[1], apply_bc)}
+        return prep, in_place
+
+    def _run_call(self, torch, prep):
+        B, out_losses = prep["B"], prep["out_losses"]
+        if not prep["fresh"]:  # the host inputs, copied again for this call
+            for d, t in prep["copies"]:
+                d.copy_(t, non_blocking=True)
+        prep["fresh"] = False
+        if out_losses is not None:
+            du, dp = prep["du"], prep["dp"]
+            losses = out_losses if out_losses.is_cuda else torch.empty(B, dtype=torch.float32, device="cuda")
+        else:
+            losses = torch.empty(B, dtype=torch.float32, device="cuda")
+            U, P = prep["U"], prep["P"]
+            du = torch.empty(U.shape, dtype=torch.float32, device="cuda") if prep["grads"] else None
+            dp = torch.empty((B, P.shape[1]), dtype=torch.float32, device="cuda") if prep["grads"] else None
+        ws = prep["ws"]
+        rc = prep["fn"](self._plan.handle, B, *prep["args"], capi.ptr(losses), capi.ptr(du), capi.ptr(dp),
+                        capi.ptr(self._status), capi.ptr(ws), ws.numel(), capi.stream_handle())
+        capi.check("folgb_loss_adjoint_plain" if prep["plain"] else "folgb_loss_adjoint", rc)
         if self._strict_status:
             self.CheckDeviceStatus()
         if out_losses is not None and out_losses is not losses:
@@ -457,6 +509,8 @@ class FiniteElementLoss:
         tunable = (self.element_type == "hexahedron" and self.physics == capi.ELASTIC and self.num_gp == 2
                    and self.loss_settings.get("kernel_variant", "auto") == "auto")
         n = HEX8_VARIANTS if tunable else 1
+        self._memo = None  # the kernel path (and whether host dofs are read in place) may have changed
+        self._epoch += 1
         return {"chosen": chosen.value, "ms": [times[i] for i in range(n)]}
 
     def ComputeBatchLoss(self, batch_params, batch_dofs):

@@ -122,14 +122,10 @@ int folgb_plan_info(const folgb_plan* plan, int64_t* ndof_per_node, int64_t* tot
  * of the nodal values is eight 3 x 3 blocks; FOLGB_FEATURE_BOX_GRID, such a
  * mesh numbered as the box mesh generator numbers it (nodes x fastest, then y,
  * then z), so the one-launch grid kernels (variants 23-24, loss exponent 1)
- * apply; FOLGB_FEATURE_READS_NODES_ONCE, the plan's current loss + adjoint
- * path is such a grid kernel, which reads each node's dofs about once per
- * instance (plus the halo of its tiles), so a caller with the dofs in pinned
- * host memory can pass that pointer to folgb_loss_adjoint and have the kernel
- * read it in place over the host link instead of copying it first.  No
+ * apply (a call whose dloss_ddofs is host memory runs the box kernel and the
+ * gather instead: they write the gradients over the host link faster).  No
  * counterpart in the reference (a query of this library's specialisations). */
-enum { FOLGB_FEATURE_TILES = 1, FOLGB_FEATURE_UNIFORM_BOX = 2, FOLGB_FEATURE_BOX_GRID = 4,
-       FOLGB_FEATURE_READS_NODES_ONCE = 8 };
+enum { FOLGB_FEATURE_TILES = 1, FOLGB_FEATURE_UNIFORM_BOX = 2, FOLGB_FEATURE_BOX_GRID = 4 };
 int folgb_plan_features(const folgb_plan* plan, int32_t* features);
 
 /* Sets the Dirichlet values used by the in-kernel GetFullDofVector, scaled by

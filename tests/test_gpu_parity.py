@@ -407,32 +407,32 @@ def test_pinned_host_buffers_equal_device_buffers(cuda, layout, B):
 
 
 @pytest.mark.parametrize("B", [1, 3])
-def test_pinned_host_dofs_read_in_place_on_the_grid_path(cuda, B):
-    """With the structured box grid kernel (each node read about once) pinned
-    host dofs are read by the kernel in place over the host link; results are
-    bit-identical to device buffers, and a plan on another kernel path keeps
-    copying them (reads_nodes_once False)."""
+def test_host_result_buffers_on_a_grid_plan(cuda, B):
+    """A plan on the structured box grid kernel given pinned host inputs and
+    result buffers (it then runs the box kernel and the gather, which write
+    the gradients over the host link) agrees with the device-buffer call to
+    fp32 rounding, and the same tensors passed again (the call reuses its
+    validated arguments) give the same results after the inputs change in
+    place."""
     torch = cuda
     h = 1.0 / 16
     m = create_3D_box_mesh(20, 12, 9, Lx=20 * h, Ly=12 * h, Lz=9 * h)
     s = _settings("hex8", "elastic", "element", 1.0)
     gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 23})
-    assert gl.KernelFeatures()["reads_nodes_once"]
-    other = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": 21})
-    assert not other.KernelFeatures()["reads_nodes_once"]
+    assert gl.KernelFeatures()["box_grid"]
     rng = np.random.default_rng(38)
     ctrl = (0.5 + rng.random((B, gl.GetNumberOfControls()))).astype(np.float32)
     u = (0.003 * rng.standard_normal((B, gl.GetTotalNumberOfDOFs()))).astype(np.float32)
-    a = gl.ComputeBatchLossAndGrad(torch.from_numpy(ctrl).cuda(), torch.from_numpy(u).cuda())
-    for pinned_ctrl in (True, False):
-        out = (torch.empty(B).pin_memory(), torch.empty(B, u.shape[1]).pin_memory(),
-               torch.empty(B, ctrl.shape[1]).pin_memory())
-        c = torch.from_numpy(ctrl).pin_memory() if pinned_ctrl else torch.from_numpy(ctrl).cuda()
-        hres = gl.ComputeBatchLossAndGrad(c, torch.from_numpy(u).pin_memory(), out=out)
+    out = (torch.empty(B).pin_memory(), torch.empty(B, u.shape[1]).pin_memory(),
+           torch.empty(B, ctrl.shape[1]).pin_memory())
+    c_pin, u_pin = torch.from_numpy(ctrl).pin_memory(), torch.from_numpy(u).pin_memory()
+    for rep in range(3):
+        a = gl.ComputeBatchLossAndGrad(c_pin.cuda(), u_pin.cuda())
+        hres = gl.ComputeBatchLossAndGrad(c_pin, u_pin, out=out)
         torch.cuda.synchronize()
-        assert np.array_equal(a[0].cpu().numpy(), hres[0].cpu().numpy())
         for x, y in zip(a[2:], hres[2:]):
-            assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
+            assert rel_fro(y.cpu().numpy(), x.cpu().numpy()) < 1e-6
+        u_pin.mul_(1.5)  # in place: the next call must see the new values
     gl.CheckDeviceStatus()
 
 
