@@ -62,6 +62,9 @@ BOX_VARIANTS, GRID_VARIANTS = (20, 21, 22), (23, 24)
 # DRAM bytes: 17.60 MB read, a few KB written)
 #   21: k_hex8_box, 256 threads, uniform box element (the records, 33.5 MB,
 #       stay in L2 for the gather: 8 KB written to DRAM)
+#   23: k_hex8_box_grid, the whole step in one launch (its outputs stay in L2:
+#       no DRAM writes inside the launch; its FP32 count includes the halo
+#       elements and the node sums: 534 per owned element)
 # fp32_flops: ncu's FP32 thread-instruction counts of one launch, fadd + fmul +
 # 2 ffma + 2 fadd2 + 2 fmul2 + 4 ffma2 (variant 16: 1,699 flops per element,
 # against the naive 5,208 of FLOPS_PER_ELEMENT; variant 21: 357).
@@ -71,7 +74,9 @@ NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16
                          "fp32_flops": 445_300_000},
                     17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421},
                     21: {"traffic": 13_100_000 + 7_940, "warp_instructions": 4_817_046,
-                         "fp32_flops": 93_490_000}}}
+                         "fp32_flops": 93_490_000},
+                    23: {"traffic": 4_748_288 + 0, "warp_instructions": 8_079_579,
+                         "fp32_flops": 139_900_000}}}
 
 
 def ncu_figure(n, variant, key):

@@ -141,10 +141,9 @@ __device__ __forceinline__ double sum_partials(const double* part, int n, double
 // instead of U*ndof*log2(G), and lane k ends up holding the row sum of value
 // index k / (G / VP).  The row epilogues (vector updates, dot products) then
 // run on U*ndof lanes in parallel instead of serially on one lane.
-template <int NDOF, int UO = 0>
+template <int NDOF>
 struct RowsU {
-  // nodes per group per round (UO != 0 overrides: fewer nodes, fewer registers)
-  static constexpr int U = UO ? UO : (NDOF == 3 ? 5 : (NDOF == 2 ? 4 : 8));
+  static constexpr int U = NDOF == 3 ? 5 : (NDOF == 2 ? 4 : 8);  // nodes per group per round
   static constexpr int V = U * NDOF;                              // rows per group per round
   static constexpr int VP = V <= 4 ? 4 : (V <= 8 ? 8 : 16);       // V rounded up to a power of two
 };
@@ -168,11 +167,11 @@ __device__ __forceinline__ void halving_reduce(T (&v)[VP], int lane) {
 
 // Returns true on the lane that owns a row of this round; then *sum is the
 // row's product and *dof its index (node-major: ndof*node + component).
-template <int NDOF, int G, class T, int UO = 0, class Col>
+template <int NDOF, int G, class T, class Col>
 __device__ __forceinline__ bool rows_multi(int64_t N, const int* __restrict__ adj_ptr, const int* __restrict__ adj,
                                            const float* __restrict__ vals, int maxdeg, int64_t base, int lane,
                                            Col col, T& sum, int64_t& dof) {
-  constexpr int U = RowsU<NDOF, UO>::U, V = RowsU<NDOF, UO>::V, VP = RowsU<NDOF, UO>::VP;
+  constexpr int U = RowsU<NDOF>::U, V = RowsU<NDOF>::V, VP = RowsU<NDOF>::VP;
   static_assert(VP <= G, "lane group narrower than the rows it reduces");
   int a0[U], len[U];
   T acc[U][NDOF];
@@ -1172,29 +1171,20 @@ __device__ __forceinline__ bool grid_sum(double (&v)[K], double* sh, const Args&
   return true;
 }
 
-// Nodes per lane group in the grid solver's row loop: 2 for 3-dof rows, so
-// the kernel fits two 512-thread blocks per SM (64 registers, no spills) and
-// keeps 32 warps per SM in flight on the dependent adjacency -> vector gathers.
-template <int NDOF>
-constexpr int kGridRowsU = NDOF == 3 ? 2 : 0;
-template <int NDOF, class VT>
-constexpr int kGridMinBlocks = (NDOF == 3 && sizeof(VT) == sizeof(float)) ? 2 : 1;
-
 template <int NDOF, int G, class T, class Args, class Col, class Epi>
 __device__ __forceinline__ void grid_rows(const Args& A, int64_t n0, int64_t n1, Col col, Epi epi) {
-  constexpr int UO = kGridRowsU<NDOF>;
-  constexpr int U = RowsU<NDOF, UO>::U;
+  constexpr int U = RowsU<NDOF>::U;
   const int lane = threadIdx.x % G;
   const int64_t group = threadIdx.x / G, ngroups = blockDim.x / G;
   for (int64_t base = n0 + group * U; __any_sync(0xffffffffu, base < n1); base += ngroups * U) {
     T sum;
     int64_t d;
-    if (rows_multi<NDOF, G, T, UO>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
+    if (rows_multi<NDOF, G, T>(n1, A.adj_ptr, A.adj, A.vals, A.maxdeg, base, lane, col, sum, d)) epi(d, sum);
   }
 }
 
 template <int NDOF, int G, class VT>
-__global__ void __launch_bounds__(kGridThreads, (kGridMinBlocks<NDOF, VT>)) k_pcg_grid(const GridArgs<VT> A) {
+__global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT> A) {
   __shared__ double sh[32];
   __shared__ double s_bcast[4];
   __shared__ int s_flag;
