@@ -117,6 +117,7 @@ struct folgb_plan {
   // and the box mesh numbering of an nx x ny x nz grid (nodes x fastest, then
   // y, then z; the reference local node order): the one-launch grid kernel
   int box_grid = 0, box_nx = 0, box_ny = 0, box_nz = 0;
+  unsigned char* d_box_layer_bc = nullptr;  // [nz + 1] node layer has a Dirichlet dof (grid kernel)
 
   // instantiated Krylov solve graphs of folgb_krylov_async (krylov.cu)
   void* krylov_graphs = nullptr;
@@ -180,7 +181,8 @@ int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double*
                       const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc);
 void free_tile_tables(folgb_plan* p);
 // Uniform axis-aligned box elements (uniform_box.cu): sets box_valid and box_k.
-int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn);
+int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn,
+                      const std::vector<unsigned char>& dmask);
 void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, double (&khat)[24][24]);
 // most blocks per instance of the structured box grid kernel (hex8_fused.cu)
 int64_t grid_blocks_max(const folgb_plan* p);

@@ -831,6 +831,7 @@ struct GridDims {
   int nzc;         // chunks of those layers
   int tiles_x, tiles_y;
   int blk_off, nblk;  // this launch's first block and the blocks of all launches of the step (loss sum)
+  const unsigned char* layer_bc;  // [nz + 1] 1 if the node layer has a Dirichlet dof
 };
 
 // 4-point Hadamard transform of a face (lex a = ax + 2 ay), the x and y stages
@@ -941,22 +942,26 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
   const bool col_valid = col && ex >= 0 && ex < G.nx && ey >= 0 && ey < G.ny;
   const bool col_owned = col_valid && ex >= x0 && ey >= y0;
   const bool node_owned = col && tx < onx && ty < ony;
-  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
-  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
   const bool dir = A.apply_dirichlet != 0;
-  // the element column's four nodes in a layer: n + {0, 1, NX, NX + 1}
+  // the element column's four nodes in a layer: n + {0, 1, NX, NX + 1}; its
+  // dofs, Dirichlet mask and values advance by a layer's stride
+  // 32-bit node, dof and element offsets (a grid plan has fewer than 2^31 dofs)
   const int c0 = ex + NX * ey;
-  // raw dofs of a face (lex a = ax + 2 ay) and its Dirichlet mask bits
+  const float* dofs = A.dofs + (int64_t)b * A.dofs_stride;
+  // raw dofs of a face (lex a = ax + 2 ay) and its Dirichlet mask bits (the
+  // masks are read only on node layers that have a Dirichlet dof)
   auto load_face = [&](int kz, FacePair& u, unsigned& mk) {
+    const int n = c0 + NXY * kz;
     mk = 0u;
+    if (dir && __ldg(G.layer_bc + kz)) {
+      const unsigned char* m = A.dmask + n;
+      mk = (__ldg(m) & 7u) | ((__ldg(m + 1) & 7u) << 3) | ((__ldg(m + NX) & 7u) << 6) | ((__ldg(m + NX + 1) & 7u) << 9);
+    }
 #pragma unroll
     for (int a = 0; a < 4; ++a) {
-      const int64_t n = (int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz;
-      const unsigned m = dir ? __ldg(A.dmask + n) : 0u;
-      mk |= (m & 7u) << (3 * a);
-      const float* d = dofs + 3 * n;
-      u.xy[a] = make_float2(__ldg(d), __ldg(d + 1));
-      u.z[a] = __ldg(d + 2);
+      const float* q = dofs + 3 * (n + (a & 1) + NX * (a >> 1));
+      u.xy[a] = make_float2(__ldg(q), __ldg(q + 1));
+      u.z[a] = __ldg(q + 2);
     }
   };
   // Dirichlet values, then the face transform
@@ -964,7 +969,7 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
     if (mk) {
 #pragma unroll
       for (int a = 0; a < 4; ++a) {
-        const float* v = A.dval + 3 * ((int64_t)c0 + (a & 1) + NX * (a >> 1) + (int64_t)NXY * kz);
+        const float* v = A.dval + 3 * (c0 + NXY * kz + (a & 1) + NX * (a >> 1));
         if ((mk >> (3 * a)) & 1u) u.xy[a].x = __ldg(v);
         if ((mk >> (3 * a + 1)) & 1u) u.xy[a].y = __ldg(v + 1);
         if ((mk >> (3 * a + 2)) & 1u) u.z[a] = __ldg(v + 2);
@@ -973,6 +978,9 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
     h4p(u.xy);
     h4(u.z);
   };
+  const int e0 = ex + G.nx * ey, elay = G.nx * G.ny;  // this column's element in layer 0
+  const float* ctrl = A.ctrl + (int64_t)b * A.ctrl_stride;
+  const int on0 = (x0 + tx) + NX * (y0 + ty);  // this thread's node in layer 0
   FacePair lo_f;            // face transform of the element's lower face (node layer kz)
   FacePair nxt;             // raw dofs of node layer kz + 1, loaded one layer ahead
   unsigned nxt_m = 0u;
@@ -1003,7 +1011,7 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
       const unsigned up_m = nxt_m;
       if (layer_valid(kz + 1)) load_face(kz + 2, nxt, nxt_m);  // the next element's upper face
       finish_face(kz + 1, up, up_m);
-      const int64_t e = (int64_t)ex + (int64_t)G.nx * (ey + (int64_t)G.ny * kz);
+      const int e = e0 + elay * kz;
       const float ee = __ldg(ctrl + e);
       // z stage: Hadamard coefficients h[b] (b < 4) and h[b + 4]
       float2 Uxy[8];
@@ -1092,8 +1100,8 @@ __global__ void __launch_bounds__(kGridBlock, 4) k_hex8_box_grid(const VecArgs A
           sz += cnr_z[buf][a][ty + oy][tx + ox];
         }
       }
-      const int64_t n = (int64_t)(x0 + tx) + (int64_t)NX * (y0 + ty) + (int64_t)NXY * kz;
-      const unsigned m = __ldg(A.dmask + n);
+      const int n = on0 + NXY * kz;
+      const unsigned m = __ldg(G.layer_bc + kz) ? __ldg(A.dmask + n) : 0u;
       float* o = A.out + (int64_t)b * A.out_stride + 3 * n;
       o[0] = (m & 1u) ? 0.f : A.inv_batch * sxy.x;
       o[1] = (m & 2u) ? 0.f : A.inv_batch * sxy.y;
@@ -1586,6 +1594,7 @@ static GridDims grid_dims(const folgb_plan* p, int B, int waves) {
   G.nzc = (int)nzc;
   G.blk_off = 0;
   G.nblk = G.tiles_x * G.tiles_y * G.nzc;
+  G.layer_bc = p->d_box_layer_bc;
   return G;
 }
 

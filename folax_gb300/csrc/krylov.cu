@@ -20,6 +20,7 @@
 // Every iteration kernel returns at once when the device flags "done" or
 // "replace" are set, so the host enqueues a chunk of iterations and reads
 // the flags once per chunk.
+#include <climits>
 #include <cmath>
 #include <atomic>
 #include <mutex>
@@ -1092,6 +1093,9 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
 // solve are read through L2 (ld.global.cg), never a stale L1 line.
 // ---------------------------------------------------------------------------
 constexpr int kGridThreads = 512;
+// dynamic shared memory of a grid CG block for the staged direction (one block
+// per SM; 200 KiB of the 227 KiB a block may have)
+constexpr int kGridStageBytes = 200 * 1024;
 
 template <class VT>
 struct GridArgs {
@@ -1110,6 +1114,7 @@ struct GridArgs {
   unsigned* barrier;  // [2] arrivals, generation (zero at launch)
   double rtol;
   int maxiter;
+  int64_t stage_entries;  // dynamic shared memory for the staged direction, in vector entries
 };
 
 // Bounded grid barrier: the last block to arrive bumps the generation the
@@ -1188,11 +1193,37 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
   __shared__ double sh[32];
   __shared__ double s_bcast[4];
   __shared__ int s_flag;
+  __shared__ int s_wmin, s_wmax;
+  extern __shared__ __align__(16) unsigned char s_dyn[];
+  VT* xs = reinterpret_cast<VT*>(s_dyn);  // the direction over the block's column window
   int parity = 0;
   const int rank = blockIdx.x, nr = gridDim.x;
   const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
   const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
   const int64_t tid = threadIdx.x, nth = blockDim.x;
+  // the column window of the block's rows: the nodes [wmin, wmax] its SpMV
+  // gathers from.  When that window fits the dynamic shared memory, every
+  // SpMV stages the direction p = z + beta p_old over it once (coalesced),
+  // and the products gather from shared memory instead of through L2.
+  if (threadIdx.x == 0) {
+    s_wmin = INT_MAX;
+    s_wmax = -1;
+  }
+  __syncthreads();
+  {
+    int lo = INT_MAX, hi = -1;
+    for (int64_t k = __ldg(A.adj_ptr + n0) + tid; k < __ldg(A.adj_ptr + n1); k += nth) {
+      const int c = __ldg(A.adj + k);
+      lo = min(lo, c);
+      hi = max(hi, c);
+    }
+    atomicMin(&s_wmin, lo);
+    atomicMax(&s_wmax, hi);
+  }
+  __syncthreads();
+  const int64_t wmin = s_wmin, wlen = s_wmax >= s_wmin ? (int64_t)(s_wmax - s_wmin + 1) : 0;
+  const bool staged = wlen > 0 && (int64_t)NDOF * wlen <= A.stage_entries;
+  const int64_t ws0 = NDOF * wmin, wsn = NDOF * wlen;
   // init: x = 0, r = b, z = D^-1 b, p = 0
   VT rz0 = VT(0), bb0 = VT(0);
   for (int64_t d = d0 + tid; d < d1; d += nth) {
@@ -1219,16 +1250,24 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
       const VT* pold = cur ? A.p1 : A.p0;
       VT* pnew = cur ? A.p0 : A.p1;
       const VT vb = (VT)beta;
-      // B: p_new = z + beta p_old (columns on the fly), q = A p_new, p . q
+      // B: p_new = z + beta p_old (staged over the column window, or formed
+      // on the fly per column), q = A p_new, p . q
       VT pq = VT(0);
-      grid_rows<NDOF, G, VT>(
-          A, n0, n1, [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); },
-          [&](int64_t d, VT sum) {
-            const VT pn = vfma(vb, __ldcg(pold + d), __ldcg(A.z + d));
-            __stcg(pnew + d, pn);
-            __stcg(A.q + d, sum);
-            pq = vfma(pn, sum, pq);
-          });
+      auto epi = [&](int64_t d, VT sum, VT pn) {
+        __stcg(pnew + d, pn);
+        __stcg(A.q + d, sum);
+        pq = vfma(pn, sum, pq);
+      };
+      if (staged) {
+        for (int64_t k = tid; k < wsn; k += nth) xs[k] = vfma(vb, __ldcg(pold + ws0 + k), __ldcg(A.z + ws0 + k));
+        __syncthreads();
+        grid_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return xs[k - ws0]; },
+                               [&](int64_t d, VT sum) { epi(d, sum, xs[d - ws0]); });
+      } else {
+        grid_rows<NDOF, G, VT>(
+            A, n0, n1, [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); },
+            [&](int64_t d, VT sum) { epi(d, sum, vfma(vb, __ldcg(pold + d), __ldcg(A.z + d))); });
+      }
       double dq[1] = {(double)pq};
       if (!grid_sum<1>(dq, sh, A, parity, &s_flag, s_bcast)) {
         done = 5;
@@ -1312,20 +1351,32 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
 // one cooperative launch of the grid solver (every block resident); returns
 // false if the launch was refused (the caller then uses the multi-kernel path)
 template <int NDOF, int G, class VT>
-static bool launch_grid_pcg(const GridArgs<VT>& A, cudaStream_t s) {
+static bool launch_grid_pcg(const GridArgs<VT>& A0, cudaStream_t s) {
   auto kernel = k_pcg_grid<NDOF, G, VT>;
-  static std::atomic<int> occ[64];
+  static std::atomic<int> occ[64], stage[64];  // blocks per SM; staging bytes + 1 (0: not set up)
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
+  int bytes = stage[dev].load() - 1;
+  if (bytes < 0) {
+    // the direction's window in dynamic shared memory, if the device allows it
+    bytes = kGridStageBytes;
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      bytes = 0;
+    }
+    stage[dev].store(bytes + 1);
+  }
   int per_sm = occ[dev].load();
   if (per_sm == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGridThreads, 0) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGridThreads, bytes) != cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
       return false;
     }
     occ[dev].store(per_sm);
   }
+  GridArgs<VT> A = A0;
+  A.stage_entries = bytes / (int64_t)sizeof(VT);
   const int64_t want = (A.N + 63) / 64;  // at least 64 nodes per block
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (blocks > want) blocks = want;
@@ -1333,7 +1384,7 @@ static bool launch_grid_pcg(const GridArgs<VT>& A, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)blocks);
   cfg.blockDim = dim3(kGridThreads);
-  cfg.dynamicSmemBytes = 0;
+  cfg.dynamicSmemBytes = (size_t)bytes;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;

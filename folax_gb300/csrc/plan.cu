@@ -379,7 +379,11 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     folgb_plan_destroy(p);
     return rc;
   }
-  build_uniform_box(p, x4, c32);  // box kernels when every element is the same axis-aligned box
+  // box kernels when every element is the same axis-aligned box
+  if ((rc = build_uniform_box(p, x4, c32, dmask))) {
+    folgb_plan_destroy(p);
+    return rc;
+  }
   noalloc_prepare_current_device();
   *out = p;
   return FOLGB_OK;
@@ -390,7 +394,7 @@ extern "C" int folgb_plan_destroy(folgb_plan* p) {
   void* ptrs[] = {p->d_conn, p->d_xyz4, p->d_inc_ptr, p->d_inc_slot, p->d_inc_padded, p->d_dmask, p->d_elem_bc,
                   p->d_k0, p->d_dval, p->d_gp,
                   p->d_adj_ptr, p->d_adj, p->d_rowptr, p->d_colind, p->d_pair_row, p->d_pair_ptr,
-                  p->d_pair_slot};
+                  p->d_pair_slot, p->d_box_layer_bc};
   for (void* q : ptrs)
     if (q) cudaFree(q);
   free_tile_tables(p);

@@ -119,7 +119,8 @@ void box_hadamard_stiffness(const double (&J)[3][3], double lam, double mu, doub
         }
 }
 
-int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn) {
+int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn,
+                      const std::vector<unsigned char>& dmask) {
   p->box_valid = 0;
   if (p->etype != FOLGB_HEX8 || p->physics != FOLGB_ELASTIC || p->phys.num_gp != 2 ||
       p->ctrl_layout != FOLGB_CONTROL_ELEMENT || p->mat.has_bf || p->E <= 0)
@@ -176,13 +177,20 @@ int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::v
   const int64_t nx = NX - 1, ny = NXY / NX - 1;
   if (p->E % (nx * ny)) return FOLGB_OK;
   const int64_t nz = p->E / (nx * ny);
-  if (p->N != NXY * (nz + 1) || nx > (1 << 20) || ny > (1 << 20) || nz > (1 << 20)) return FOLGB_OK;
+  // 32-bit dof offsets in the grid kernel: fewer than 2^31 dofs
+  if (p->N != NXY * (nz + 1) || 3 * p->N >= ((int64_t)1 << 31)) return FOLGB_OK;
   constexpr int dx[8] = {0, 1, 1, 0, 0, 1, 1, 0}, dy[8] = {0, 0, 1, 1, 0, 0, 1, 1}, dz[8] = {0, 0, 0, 0, 1, 1, 1, 1};
   for (int64_t e = 0; e < p->E; ++e) {
     const int64_t i = e % nx, j = (e / nx) % ny, k = e / (nx * ny);
     for (int a = 0; a < 8; ++a)
       if (conn[(size_t)e * 8 + a] != (i + dx[a]) + NX * ((j + dy[a]) + (ny + 1) * (k + dz[a]))) return FOLGB_OK;
   }
+  // node layers with a Dirichlet dof (the grid kernel reads masks only there)
+  std::vector<unsigned char> layer_bc((size_t)nz + 1, 0);
+  for (int64_t n = 0; n < p->N; ++n)
+    if (dmask[(size_t)n]) layer_bc[(size_t)(n / NXY)] = 1;
+  FOLGB_CUDA_TRY(cudaMalloc((void**)&p->d_box_layer_bc, layer_bc.size()));
+  FOLGB_CUDA_TRY(cudaMemcpy(p->d_box_layer_bc, layer_bc.data(), layer_bc.size(), cudaMemcpyHostToDevice));
   p->box_grid = 1;
   p->box_nx = (int)nx;
   p->box_ny = (int)ny;
