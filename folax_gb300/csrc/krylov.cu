@@ -220,6 +220,60 @@ __device__ __forceinline__ bool rows_multi(int64_t N, const int* __restrict__ ad
   return (lane % kSub) == 0 && idx < V && dof < (int64_t)NDOF * N;
 }
 
+// rows_multi with the round's adjacency and values in shared memory: global
+// adjacency index k is at s_adj[k - adj_base], value index k at
+// s_vals[k - val_base].
+template <int NDOF, int G, class T, class Col>
+__device__ __forceinline__ bool rows_multi_s(int64_t N, const int* __restrict__ adj_ptr, const int* s_adj,
+                                             int64_t adj_base, const float* s_vals, int64_t val_base, int maxdeg,
+                                             int64_t base, int lane, Col col, T& sum, int64_t& dof) {
+  constexpr int U = RowsU<NDOF>::U, V = RowsU<NDOF>::V, VP = RowsU<NDOF>::VP;
+  static_assert(VP <= G, "lane group narrower than the rows it reduces");
+  int64_t a0[U];
+  int len[U];
+  T acc[U][NDOF];
+#pragma unroll
+  for (int u = 0; u < U; ++u) {
+    const int64_t n = base + u;
+    const bool act = n < N;
+    a0[u] = act ? __ldg(adj_ptr + n) : 0;
+    len[u] = act ? NDOF * (int)(__ldg(adj_ptr + n + 1) - a0[u]) : 0;
+#pragma unroll
+    for (int i = 0; i < NDOF; ++i) acc[u][i] = T(0);
+  }
+  const int maxlen = NDOF * maxdeg;
+  for (int w0 = 0; w0 < maxlen; w0 += G) {
+    const int w = w0 + lane;
+    const int j = w / NDOF, l = w - NDOF * j;
+    int m[U];
+    float v[U][NDOF];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const bool on = w < len[u];
+      m[u] = on ? s_adj[a0[u] + j - adj_base] : 0;
+      const float* vr = s_vals + (NDOF * NDOF * a0[u] + w - val_base);
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) v[u][i] = on ? vr[i * len[u]] : 0.f;
+    }
+    T xv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) xv[u] = (w < len[u]) ? col((int64_t)NDOF * m[u] + l) : T(0);
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int i = 0; i < NDOF; ++i) acc[u][i] += (T)v[u][i] * xv[u];
+  }
+  T flat[VP];
+#pragma unroll
+  for (int k = 0; k < VP; ++k) flat[k] = k < V ? acc[k / NDOF][k % NDOF] : T(0);
+  halving_reduce<G, VP, G / 2>(flat, lane);
+  constexpr int kSub = G / VP;
+  const int idx = lane / kSub;
+  sum = flat[0];
+  dof = (int64_t)NDOF * base + idx;
+  return (lane % kSub) == 0 && idx < V && dof < (int64_t)NDOF * N;
+}
+
 // Warp-uniform loop over node blocks: every lane runs the same number of
 // rounds so the group shuffles always see the whole warp.
 #define FOLGB_NODE_BLOCKS(NDOF, G)                                                               \
@@ -1093,9 +1147,27 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
 // solve are read through L2 (ld.global.cg), never a stale L1 line.
 // ---------------------------------------------------------------------------
 constexpr int kGridThreads = 512;
-// dynamic shared memory of a grid CG block for the staged direction (one block
-// per SM; 200 KiB of the 227 KiB a block may have)
+// dynamic shared memory of a grid CG block for the SpMV's streamed stages (one
+// block per SM; 200 KiB of the 227 KiB a block may have)
 constexpr int kGridStageBytes = 200 * 1024;
+
+// Rounds of the grid solver's SpMV streamed through shared memory: a round is
+// the R = (kGridThreads / G) * U consecutive rows that the block's lane groups
+// take together, and its CSR values and adjacency entries are contiguous in
+// memory.  A stage holds one round: capacity for R rows of maxdeg blocks plus
+// the up to 3 entries before the 16-byte aligned start.
+template <int NDOF, int G>
+struct TmaRounds {
+  static constexpr int U = RowsU<NDOF>::U;
+  static constexpr int R = (kGridThreads / G) * U;
+  __host__ __device__ static int64_t vals_cap(int maxdeg) {
+    return ((int64_t)NDOF * NDOF * R * maxdeg + 4 + 3) / 4 * 4;
+  }
+  __host__ __device__ static int64_t adj_cap(int maxdeg) { return ((int64_t)R * maxdeg + 4 + 3) / 4 * 4; }
+  __host__ __device__ static bool fits(int maxdeg, int64_t stage_bytes) {
+    return 2 * 4 * (vals_cap(maxdeg) + adj_cap(maxdeg)) <= stage_bytes;
+  }
+};
 
 template <class VT>
 struct GridArgs {
@@ -1114,7 +1186,7 @@ struct GridArgs {
   unsigned* barrier;  // [2] arrivals, generation (zero at launch)
   double rtol;
   int maxiter;
-  int64_t stage_entries;  // dynamic shared memory for the staged direction, in vector entries
+  int64_t stage_bytes;  // dynamic shared memory for the streamed SpMV stages
 };
 
 // Bounded grid barrier: the last block to arrive bumps the generation the
@@ -1188,42 +1260,119 @@ __device__ __forceinline__ void grid_rows(const Args& A, int64_t n0, int64_t n1,
   }
 }
 
+// The block's rows [n0, n1) with the CSR values and adjacency of each round
+// streamed into shared memory by TMA bulk copies, two rounds in flight (thread
+// 0 issues round r + 2 once every thread is done with round r's stage).  A
+// stage gets the 16-byte aligned middle of the round's ranges by one bulk copy
+// each; the up to 3 entries at either end are read by plain loads.  Every
+// wait is bounded: false if a copy never landed (the stages are then left
+// alone and the caller stops the solve).
+template <int NDOF, int G, class T, class VT, class Col, class Epi>
+__device__ __forceinline__ bool grid_rows_streamed(const GridArgs<VT>& A, int64_t n0, int64_t n1,
+                                                   unsigned char* smem, uint64_t* bar, unsigned& phases, Col col,
+                                                   Epi epi) {
+  using TR = TmaRounds<NDOF, G>;
+  constexpr int U = TR::U, R = TR::R, NN = NDOF * NDOF;
+  const int lane = threadIdx.x % G, group = threadIdx.x / G;
+  const int64_t vcap = TR::vals_cap(A.maxdeg), acap = TR::adj_cap(A.maxdeg);
+  float* const sv0 = reinterpret_cast<float*>(smem);
+  float* const sv1 = sv0 + vcap + acap;
+  auto svals = [&](int sl) { return sl ? sv1 : sv0; };
+  auto sadj = [&](int sl) { return reinterpret_cast<int*>((sl ? sv1 : sv0) + vcap); };
+  const int rounds = (int)((n1 - n0 + R - 1) / R);
+  auto range = [&](int r, int64_t& ea, int64_t& eb) {
+    const int64_t a = n0 + (int64_t)r * R, b = a + R < n1 ? a + R : n1;
+    ea = __ldg(A.adj_ptr + a);
+    eb = __ldg(A.adj_ptr + b);
+  };
+  auto issue = [&](int r) {  // thread 0
+    const int sl = r & 1;
+    int64_t ea, eb;
+    range(r, ea, eb);
+    const int64_t v0 = NN * ea, v1 = NN * eb, vlo = (v0 + 3) & ~(int64_t)3, vhi = v1 & ~(int64_t)3;
+    const int64_t alo = (ea + 3) & ~(int64_t)3, ahi = eb & ~(int64_t)3;
+    unsigned bytes = 0;
+    if (vhi > vlo) bytes += (unsigned)(4 * (vhi - vlo));
+    if (ahi > alo) bytes += (unsigned)(4 * (ahi - alo));
+    fence_proxy_async_smem();  // the stage's earlier generic reads and writes come first
+    mbar_arrive_expect_tx(&bar[sl], bytes);
+    if (vhi > vlo)
+      bulk_copy_g2s(svals(sl) + (vlo - (v0 & ~(int64_t)3)), A.vals + vlo, (unsigned)(4 * (vhi - vlo)), &bar[sl]);
+    if (ahi > alo)
+      bulk_copy_g2s(sadj(sl) + (alo - (ea & ~(int64_t)3)), A.adj + alo, (unsigned)(4 * (ahi - alo)), &bar[sl]);
+  };
+  if (threadIdx.x == 0) {
+    if (rounds > 0) issue(0);
+    if (rounds > 1) issue(1);
+  }
+  bool ok = true;
+  for (int r = 0; r < rounds; ++r) {
+    const int sl = r & 1;
+    int64_t ea, eb;
+    range(r, ea, eb);
+    const int64_t v0 = NN * ea, v1 = NN * eb, vlo = (v0 + 3) & ~(int64_t)3, vhi = v1 & ~(int64_t)3;
+    const int64_t alo = (ea + 3) & ~(int64_t)3, ahi = eb & ~(int64_t)3;
+    const int64_t vbase = v0 & ~(int64_t)3, abase = ea & ~(int64_t)3;
+    // the ends outside the bulk copies: [v0, vlo) and [vhi, v1), or all of a
+    // range too short to hold an aligned 16-byte chunk
+    const int t = threadIdx.x;
+    if (t < 8) {
+      const bool mid = vhi > vlo;
+      const int64_t k = t < 4 ? v0 + t : (mid ? vhi : v0 + 4) + (t - 4);
+      const bool in = mid ? (t < 4 ? k < vlo : k < v1) : k < v1;
+      if (in) svals(sl)[k - vbase] = __ldg(A.vals + k);
+    } else if (t < 16) {
+      const int tt = t - 8;
+      const bool mid = ahi > alo;
+      const int64_t k = tt < 4 ? ea + tt : (mid ? ahi : ea + 4) + (tt - 4);
+      const bool in = mid ? (tt < 4 ? k < alo : k < eb) : k < eb;
+      if (in) sadj(sl)[k - abase] = __ldg(A.adj + k);
+    }
+    const bool landed = mbar_wait_bounded(&bar[sl], (phases >> sl) & 1u);
+    phases ^= 1u << sl;  // bit sl: the parity of the stage barrier's next phase
+    ok = __syncthreads_and(ok && landed) != 0;
+    if (!ok) break;
+    const int64_t base = n0 + (int64_t)r * R + (int64_t)group * U;
+    T sum;
+    int64_t d;
+    if (rows_multi_s<NDOF, G, T>(n1, A.adj_ptr, sadj(sl), abase, svals(sl), vbase, A.maxdeg, base, lane, col, sum, d))
+      epi(d, sum);
+    __syncthreads();  // the stage is free
+    if (threadIdx.x == 0 && r + 2 < rounds) issue(r + 2);
+  }
+  if (!ok && threadIdx.x == 0) {
+    // a copy never landed: wait (bounded) for the other stage's copies too
+    // before the shared memory is left
+    mbar_wait_bounded(&bar[0], phases & 1u);
+    mbar_wait_bounded(&bar[1], (phases >> 1) & 1u);
+  }
+  return ok;
+}
+
 template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT> A) {
   __shared__ double sh[32];
   __shared__ double s_bcast[4];
   __shared__ int s_flag;
-  __shared__ int s_wmin, s_wmax;
   extern __shared__ __align__(16) unsigned char s_dyn[];
-  VT* xs = reinterpret_cast<VT*>(s_dyn);  // the direction over the block's column window
+  __shared__ __align__(8) uint64_t s_bar[2];
   int parity = 0;
   const int rank = blockIdx.x, nr = gridDim.x;
   const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
   const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
   const int64_t tid = threadIdx.x, nth = blockDim.x;
-  // the column window of the block's rows: the nodes [wmin, wmax] its SpMV
-  // gathers from.  When that window fits the dynamic shared memory, every
-  // SpMV stages the direction p = z + beta p_old over it once (coalesced),
-  // and the products gather from shared memory instead of through L2.
-  if (threadIdx.x == 0) {
-    s_wmin = INT_MAX;
-    s_wmax = -1;
+  // the SpMV of every iteration streams the block's CSR values and adjacency
+  // through shared memory by TMA bulk copies when two rounds of them fit
+  // (bulk copies need 16-byte aligned arrays: a caller's values may not be)
+  const bool streamed = TmaRounds<NDOF, G>::fits(A.maxdeg, A.stage_bytes) &&
+                        ((reinterpret_cast<uintptr_t>(A.vals) | reinterpret_cast<uintptr_t>(A.adj)) & 15) == 0;
+  if (streamed && threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    fence_mbar_init();
   }
   __syncthreads();
-  {
-    int lo = INT_MAX, hi = -1;
-    for (int64_t k = __ldg(A.adj_ptr + n0) + tid; k < __ldg(A.adj_ptr + n1); k += nth) {
-      const int c = __ldg(A.adj + k);
-      lo = min(lo, c);
-      hi = max(hi, c);
-    }
-    atomicMin(&s_wmin, lo);
-    atomicMax(&s_wmax, hi);
-  }
-  __syncthreads();
-  const int64_t wmin = s_wmin, wlen = s_wmax >= s_wmin ? (int64_t)(s_wmax - s_wmin + 1) : 0;
-  const bool staged = wlen > 0 && (int64_t)NDOF * wlen <= A.stage_entries;
-  const int64_t ws0 = NDOF * wmin, wsn = NDOF * wlen;
+  unsigned phases = 0u;  // bit k: parity of stage barrier k's next phase
   // init: x = 0, r = b, z = D^-1 b, p = 0
   VT rz0 = VT(0), bb0 = VT(0);
   for (int64_t d = d0 + tid; d < d1; d += nth) {
@@ -1250,23 +1399,23 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
       const VT* pold = cur ? A.p1 : A.p0;
       VT* pnew = cur ? A.p0 : A.p1;
       const VT vb = (VT)beta;
-      // B: p_new = z + beta p_old (staged over the column window, or formed
-      // on the fly per column), q = A p_new, p . q
+      // B: p_new = z + beta p_old (columns on the fly), q = A p_new, p . q;
+      // the matrix streamed through shared memory when it fits
       VT pq = VT(0);
-      auto epi = [&](int64_t d, VT sum, VT pn) {
+      auto colf = [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); };
+      auto epi = [&](int64_t d, VT sum) {
+        const VT pn = vfma(vb, __ldcg(pold + d), __ldcg(A.z + d));
         __stcg(pnew + d, pn);
         __stcg(A.q + d, sum);
         pq = vfma(pn, sum, pq);
       };
-      if (staged) {
-        for (int64_t k = tid; k < wsn; k += nth) xs[k] = vfma(vb, __ldcg(pold + ws0 + k), __ldcg(A.z + ws0 + k));
-        __syncthreads();
-        grid_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return xs[k - ws0]; },
-                               [&](int64_t d, VT sum) { epi(d, sum, xs[d - ws0]); });
+      if (streamed) {
+        if (!grid_rows_streamed<NDOF, G, VT>(A, n0, n1, s_dyn, s_bar, phases, colf, epi)) {
+          done = 5;
+          break;
+        }
       } else {
-        grid_rows<NDOF, G, VT>(
-            A, n0, n1, [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); },
-            [&](int64_t d, VT sum) { epi(d, sum, vfma(vb, __ldcg(pold + d), __ldcg(A.z + d))); });
+        grid_rows<NDOF, G, VT>(A, n0, n1, colf, epi);
       }
       double dq[1] = {(double)pq};
       if (!grid_sum<1>(dq, sh, A, parity, &s_flag, s_bcast)) {
@@ -1376,7 +1525,7 @@ static bool launch_grid_pcg(const GridArgs<VT>& A0, cudaStream_t s) {
     occ[dev].store(per_sm);
   }
   GridArgs<VT> A = A0;
-  A.stage_entries = bytes / (int64_t)sizeof(VT);
+  A.stage_bytes = bytes;
   const int64_t want = (A.N + 63) / 64;  // at least 64 nodes per block
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (blocks > want) blocks = want;
