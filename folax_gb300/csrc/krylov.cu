@@ -1151,24 +1151,24 @@ constexpr int kGridThreads = 512;
 // block per SM; 200 KiB of the 227 KiB a block may have)
 constexpr int kGridStageBytes = 200 * 1024;
 
-// Rounds of the grid solver's SpMV streamed through shared memory: a round is
-// the R = (kGridThreads / G) * U consecutive rows that the block's lane groups
-// take together, and its CSR values and adjacency entries are contiguous in
-// memory.  A stage holds one round: capacity for R rows of maxdeg blocks plus
-// the up to 3 entries before the 16-byte aligned start.
+// The grid solver's SpMV streamed through shared memory per warp: a warp (one
+// lane group of G = 32) takes U consecutive rows per round, whose CSR values
+// and adjacency entries are contiguous in memory; each warp keeps two rounds
+// of them in flight in its own stages.  A stage holds U rows of maxdeg blocks
+// plus the up to 3 entries on either side of the 16-byte aligned range.
 template <int NDOF, int G>
-struct TmaRounds {
+struct WarpStages {
   static constexpr int U = RowsU<NDOF>::U;
-  static constexpr int R = (kGridThreads / G) * U;
+  static constexpr int kWarps = kGridThreads / 32;
   __host__ __device__ static int64_t vals_cap(int maxdeg) {
-    return ((int64_t)NDOF * NDOF * R * maxdeg + 4 + 3) / 4 * 4;
+    return ((int64_t)NDOF * NDOF * U * maxdeg + 8 + 3) / 4 * 4;
   }
-  __host__ __device__ static int64_t adj_cap(int maxdeg) { return ((int64_t)R * maxdeg + 4 + 3) / 4 * 4; }
+  __host__ __device__ static int64_t adj_cap(int maxdeg) { return ((int64_t)U * maxdeg + 8 + 3) / 4 * 4; }
+  __host__ __device__ static int64_t stage_floats(int maxdeg) { return vals_cap(maxdeg) + adj_cap(maxdeg); }
   __host__ __device__ static bool fits(int maxdeg, int64_t stage_bytes) {
-    return 2 * 4 * (vals_cap(maxdeg) + adj_cap(maxdeg)) <= stage_bytes;
+    return G == 32 && (int64_t)kWarps * 2 * 4 * stage_floats(maxdeg) <= stage_bytes;
   }
 };
-
 template <class VT>
 struct GridArgs {
   int64_t N;
@@ -1260,91 +1260,78 @@ __device__ __forceinline__ void grid_rows(const Args& A, int64_t n0, int64_t n1,
   }
 }
 
-// The block's rows [n0, n1) with the CSR values and adjacency of each round
-// streamed into shared memory by TMA bulk copies, two rounds in flight (thread
-// 0 issues round r + 2 once every thread is done with round r's stage).  A
-// stage gets the 16-byte aligned middle of the round's ranges by one bulk copy
-// each; the up to 3 entries at either end are read by plain loads.  Every
-// wait is bounded: false if a copy never landed (the stages are then left
-// alone and the caller stops the solve).
+// The block's rows [n0, n1) with each warp's CSR values and adjacency streamed
+// into its own shared-memory stages by TMA bulk copies, two rounds in flight
+// (lane 0 issues round r + 2 once the warp is done with round r).  A stage
+// gets the round's ranges widened to 16-byte boundaries (inside the arrays)
+// by one bulk copy each; only the arrays' last entries past their final
+// 16-byte boundary are read by plain loads.  No block-wide barrier: warps run
+// their rounds independently.  Every wait is bounded; returns false if a copy
+// never landed (after waiting, bounded, for the warp's other copy).
 template <int NDOF, int G, class T, class VT, class Col, class Epi>
 __device__ __forceinline__ bool grid_rows_streamed(const GridArgs<VT>& A, int64_t n0, int64_t n1,
-                                                   unsigned char* smem, uint64_t* bar, unsigned& phases, Col col,
+                                                   unsigned char* smem, uint64_t* bars, unsigned& phase, Col col,
                                                    Epi epi) {
-  using TR = TmaRounds<NDOF, G>;
-  constexpr int U = TR::U, R = TR::R, NN = NDOF * NDOF;
-  const int lane = threadIdx.x % G, group = threadIdx.x / G;
-  const int64_t vcap = TR::vals_cap(A.maxdeg), acap = TR::adj_cap(A.maxdeg);
-  float* const sv0 = reinterpret_cast<float*>(smem);
-  float* const sv1 = sv0 + vcap + acap;
-  auto svals = [&](int sl) { return sl ? sv1 : sv0; };
-  auto sadj = [&](int sl) { return reinterpret_cast<int*>((sl ? sv1 : sv0) + vcap); };
-  const int rounds = (int)((n1 - n0 + R - 1) / R);
-  auto range = [&](int r, int64_t& ea, int64_t& eb) {
-    const int64_t a = n0 + (int64_t)r * R, b = a + R < n1 ? a + R : n1;
-    ea = __ldg(A.adj_ptr + a);
-    eb = __ldg(A.adj_ptr + b);
-  };
-  auto issue = [&](int r) {  // thread 0
+  using WS = WarpStages<NDOF, G>;
+  constexpr int U = WS::U, NN = NDOF * NDOF, kWarps = WS::kWarps;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t vcap = WS::vals_cap(A.maxdeg), sf = WS::stage_floats(A.maxdeg);
+  float* const st0 = reinterpret_cast<float*>(smem) + (int64_t)warp * 2 * sf;
+  float* const st1 = st0 + sf;
+  uint64_t* const bar = bars + 2 * warp;
+  const int64_t vtot = (int64_t)NN * __ldg(A.adj_ptr + A.N), ptot = __ldg(A.adj_ptr + A.N);
+  const int64_t step = (int64_t)kWarps * U;
+  const int64_t first = n0 + (int64_t)warp * U;
+  const int rounds = first < n1 ? (int)((n1 - first + step - 1) / step) : 0;
+  auto issue = [&](int r) {  // lane 0
     const int sl = r & 1;
-    int64_t ea, eb;
-    range(r, ea, eb);
-    const int64_t v0 = NN * ea, v1 = NN * eb, vlo = (v0 + 3) & ~(int64_t)3, vhi = v1 & ~(int64_t)3;
-    const int64_t alo = (ea + 3) & ~(int64_t)3, ahi = eb & ~(int64_t)3;
+    float* sv = sl ? st1 : st0;
+    const int64_t a = first + (int64_t)r * step, b = a + U < n1 ? a + U : n1;
+    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + b);
+    const int64_t vlo = (NN * ea) & ~(int64_t)3, vhi = min((NN * eb + 3) & ~(int64_t)3, vtot & ~(int64_t)3);
+    const int64_t alo = ea & ~(int64_t)3, ahi = min((eb + 3) & ~(int64_t)3, ptot & ~(int64_t)3);
     unsigned bytes = 0;
     if (vhi > vlo) bytes += (unsigned)(4 * (vhi - vlo));
     if (ahi > alo) bytes += (unsigned)(4 * (ahi - alo));
     fence_proxy_async_smem();  // the stage's earlier generic reads and writes come first
     mbar_arrive_expect_tx(&bar[sl], bytes);
-    if (vhi > vlo)
-      bulk_copy_g2s(svals(sl) + (vlo - (v0 & ~(int64_t)3)), A.vals + vlo, (unsigned)(4 * (vhi - vlo)), &bar[sl]);
-    if (ahi > alo)
-      bulk_copy_g2s(sadj(sl) + (alo - (ea & ~(int64_t)3)), A.adj + alo, (unsigned)(4 * (ahi - alo)), &bar[sl]);
+    if (vhi > vlo) bulk_copy_g2s(sv, A.vals + vlo, (unsigned)(4 * (vhi - vlo)), &bar[sl]);
+    if (ahi > alo) bulk_copy_g2s(sv + vcap, A.adj + alo, (unsigned)(4 * (ahi - alo)), &bar[sl]);
   };
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
     if (rounds > 0) issue(0);
     if (rounds > 1) issue(1);
   }
   bool ok = true;
   for (int r = 0; r < rounds; ++r) {
     const int sl = r & 1;
-    int64_t ea, eb;
-    range(r, ea, eb);
-    const int64_t v0 = NN * ea, v1 = NN * eb, vlo = (v0 + 3) & ~(int64_t)3, vhi = v1 & ~(int64_t)3;
-    const int64_t alo = (ea + 3) & ~(int64_t)3, ahi = eb & ~(int64_t)3;
-    const int64_t vbase = v0 & ~(int64_t)3, abase = ea & ~(int64_t)3;
-    // the ends outside the bulk copies: [v0, vlo) and [vhi, v1), or all of a
-    // range too short to hold an aligned 16-byte chunk
-    const int t = threadIdx.x;
-    if (t < 8) {
-      const bool mid = vhi > vlo;
-      const int64_t k = t < 4 ? v0 + t : (mid ? vhi : v0 + 4) + (t - 4);
-      const bool in = mid ? (t < 4 ? k < vlo : k < v1) : k < v1;
-      if (in) svals(sl)[k - vbase] = __ldg(A.vals + k);
-    } else if (t < 16) {
-      const int tt = t - 8;
-      const bool mid = ahi > alo;
-      const int64_t k = tt < 4 ? ea + tt : (mid ? ahi : ea + 4) + (tt - 4);
-      const bool in = mid ? (tt < 4 ? k < alo : k < eb) : k < eb;
-      if (in) sadj(sl)[k - abase] = __ldg(A.adj + k);
+    float* sv = sl ? st1 : st0;
+    int* sa = reinterpret_cast<int*>(sv + vcap);
+    const int64_t a = first + (int64_t)r * step;
+    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + (a + U < n1 ? a + U : n1));
+    const int64_t vbase = (NN * ea) & ~(int64_t)3, abase = ea & ~(int64_t)3;
+    // the arrays' last entries past their final 16-byte boundary (only at the end of the matrix)
+    const int64_t vend = NN * eb, vcut = vtot & ~(int64_t)3, acut = ptot & ~(int64_t)3;
+    if (vend > vcut) {
+      for (int64_t k = (vcut > NN * ea ? vcut : NN * ea) + lane; k < vend; k += 32) sv[k - vbase] = __ldg(A.vals + k);
     }
-    const bool landed = mbar_wait_bounded(&bar[sl], (phases >> sl) & 1u);
-    phases ^= 1u << sl;  // bit sl: the parity of the stage barrier's next phase
-    ok = __syncthreads_and(ok && landed) != 0;
+    if (eb > acut) {
+      for (int64_t k = (acut > ea ? acut : ea) + lane; k < eb; k += 32) sa[k - abase] = __ldg(A.adj + k);
+    }
+    const bool landed = mbar_wait_bounded(&bar[sl], (phase >> sl) & 1u);
+    phase ^= 1u << sl;
+    ok = __all_sync(0xffffffffu, ok && landed);
     if (!ok) break;
-    const int64_t base = n0 + (int64_t)r * R + (int64_t)group * U;
+    __syncwarp();
     T sum;
     int64_t d;
-    if (rows_multi_s<NDOF, G, T>(n1, A.adj_ptr, sadj(sl), abase, svals(sl), vbase, A.maxdeg, base, lane, col, sum, d))
-      epi(d, sum);
-    __syncthreads();  // the stage is free
-    if (threadIdx.x == 0 && r + 2 < rounds) issue(r + 2);
+    if (rows_multi_s<NDOF, G, T>(n1, A.adj_ptr, sa, abase, sv, vbase, A.maxdeg, a, lane, col, sum, d)) epi(d, sum);
+    __syncwarp();  // every lane is done with the stage
+    if (lane == 0 && r + 2 < rounds) issue(r + 2);
   }
-  if (!ok && threadIdx.x == 0) {
-    // a copy never landed: wait (bounded) for the other stage's copies too
-    // before the shared memory is left
-    mbar_wait_bounded(&bar[0], phases & 1u);
-    mbar_wait_bounded(&bar[1], (phases >> 1) & 1u);
+  if (!ok && lane == 0) {
+    mbar_wait_bounded(&bar[0], phase & 1u);
+    mbar_wait_bounded(&bar[1], (phase >> 1) & 1u);
   }
   return ok;
 }
@@ -1355,7 +1342,7 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
   __shared__ double s_bcast[4];
   __shared__ int s_flag;
   extern __shared__ __align__(16) unsigned char s_dyn[];
-  __shared__ __align__(8) uint64_t s_bar[2];
+  __shared__ __align__(8) uint64_t s_bar[2 * (kGridThreads / 32)];  // two stage barriers per warp
   int parity = 0;
   const int rank = blockIdx.x, nr = gridDim.x;
   const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
@@ -1364,15 +1351,12 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
   // the SpMV of every iteration streams the block's CSR values and adjacency
   // through shared memory by TMA bulk copies when two rounds of them fit
   // (bulk copies need 16-byte aligned arrays: a caller's values may not be)
-  const bool streamed = TmaRounds<NDOF, G>::fits(A.maxdeg, A.stage_bytes) &&
+  const bool streamed = WarpStages<NDOF, G>::fits(A.maxdeg, A.stage_bytes) &&
                         ((reinterpret_cast<uintptr_t>(A.vals) | reinterpret_cast<uintptr_t>(A.adj)) & 15) == 0;
-  if (streamed && threadIdx.x == 0) {
-    mbar_init(&s_bar[0], 1);
-    mbar_init(&s_bar[1], 1);
-    fence_mbar_init();
-  }
+  if (streamed && threadIdx.x < 2 * (kGridThreads / 32)) mbar_init(&s_bar[threadIdx.x], 1);
+  if (streamed) fence_mbar_init();
   __syncthreads();
-  unsigned phases = 0u;  // bit k: parity of stage barrier k's next phase
+  unsigned wphase = 0u;  // bit k: parity of this warp's stage barrier k's next phase (kept across SpMVs)
   // init: x = 0, r = b, z = D^-1 b, p = 0
   VT rz0 = VT(0), bb0 = VT(0);
   for (int64_t d = d0 + tid; d < d1; d += nth) {
@@ -1410,7 +1394,8 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
         pq = vfma(pn, sum, pq);
       };
       if (streamed) {
-        if (!grid_rows_streamed<NDOF, G, VT>(A, n0, n1, s_dyn, s_bar, phases, colf, epi)) {
+        const bool ok = grid_rows_streamed<NDOF, G, VT>(A, n0, n1, s_dyn, s_bar, wphase, colf, epi);
+        if (!__syncthreads_and(ok)) {
           done = 5;
           break;
         }
