@@ -20,7 +20,6 @@
 // Every iteration kernel returns at once when the device flags "done" or
 // "replace" are set, so the host enqueues a chunk of iterations and reads
 // the flags once per chunk.
-#include <climits>
 #include <cmath>
 #include <atomic>
 #include <mutex>
@@ -214,60 +213,6 @@ __device__ __forceinline__ bool rows_multi(int64_t N, const int* __restrict__ ad
   for (int k = 0; k < VP; ++k) flat[k] = k < V ? acc[k / NDOF][k % NDOF] : T(0);
   halving_reduce<G, VP, G / 2>(flat, lane);
   constexpr int kSub = G / VP;  // lanes sharing one value index
-  const int idx = lane / kSub;
-  sum = flat[0];
-  dof = (int64_t)NDOF * base + idx;
-  return (lane % kSub) == 0 && idx < V && dof < (int64_t)NDOF * N;
-}
-
-// rows_multi with the round's adjacency and values in shared memory: global
-// adjacency index k is at s_adj[k - adj_base], value index k at
-// s_vals[k - val_base].
-template <int NDOF, int G, class T, class Col>
-__device__ __forceinline__ bool rows_multi_s(int64_t N, const int* __restrict__ adj_ptr, const int* s_adj,
-                                             int64_t adj_base, const float* s_vals, int64_t val_base, int maxdeg,
-                                             int64_t base, int lane, Col col, T& sum, int64_t& dof) {
-  constexpr int U = RowsU<NDOF>::U, V = RowsU<NDOF>::V, VP = RowsU<NDOF>::VP;
-  static_assert(VP <= G, "lane group narrower than the rows it reduces");
-  int64_t a0[U];
-  int len[U];
-  T acc[U][NDOF];
-#pragma unroll
-  for (int u = 0; u < U; ++u) {
-    const int64_t n = base + u;
-    const bool act = n < N;
-    a0[u] = act ? __ldg(adj_ptr + n) : 0;
-    len[u] = act ? NDOF * (int)(__ldg(adj_ptr + n + 1) - a0[u]) : 0;
-#pragma unroll
-    for (int i = 0; i < NDOF; ++i) acc[u][i] = T(0);
-  }
-  const int maxlen = NDOF * maxdeg;
-  for (int w0 = 0; w0 < maxlen; w0 += G) {
-    const int w = w0 + lane;
-    const int j = w / NDOF, l = w - NDOF * j;
-    int m[U];
-    float v[U][NDOF];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const bool on = w < len[u];
-      m[u] = on ? s_adj[a0[u] + j - adj_base] : 0;
-      const float* vr = s_vals + (NDOF * NDOF * a0[u] + w - val_base);
-#pragma unroll
-      for (int i = 0; i < NDOF; ++i) v[u][i] = on ? vr[i * len[u]] : 0.f;
-    }
-    T xv[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) xv[u] = (w < len[u]) ? col((int64_t)NDOF * m[u] + l) : T(0);
-#pragma unroll
-    for (int u = 0; u < U; ++u)
-#pragma unroll
-      for (int i = 0; i < NDOF; ++i) acc[u][i] += (T)v[u][i] * xv[u];
-  }
-  T flat[VP];
-#pragma unroll
-  for (int k = 0; k < VP; ++k) flat[k] = k < V ? acc[k / NDOF][k % NDOF] : T(0);
-  halving_reduce<G, VP, G / 2>(flat, lane);
-  constexpr int kSub = G / VP;
   const int idx = lane / kSub;
   sum = flat[0];
   dof = (int64_t)NDOF * base + idx;
@@ -1147,28 +1092,7 @@ static bool launch_cluster_solver(int solver, const ClusterArgs<VT>& A, cudaStre
 // solve are read through L2 (ld.global.cg), never a stale L1 line.
 // ---------------------------------------------------------------------------
 constexpr int kGridThreads = 512;
-// dynamic shared memory of a grid CG block for the SpMV's streamed stages (one
-// block per SM; 200 KiB of the 227 KiB a block may have)
-constexpr int kGridStageBytes = 200 * 1024;
 
-// The grid solver's SpMV streamed through shared memory per warp: a warp (one
-// lane group of G = 32) takes U consecutive rows per round, whose CSR values
-// and adjacency entries are contiguous in memory; each warp keeps two rounds
-// of them in flight in its own stages.  A stage holds U rows of maxdeg blocks
-// plus the up to 3 entries on either side of the 16-byte aligned range.
-template <int NDOF, int G>
-struct WarpStages {
-  static constexpr int U = RowsU<NDOF>::U;
-  static constexpr int kWarps = kGridThreads / 32;
-  __host__ __device__ static int64_t vals_cap(int maxdeg) {
-    return ((int64_t)NDOF * NDOF * U * maxdeg + 8 + 3) / 4 * 4;
-  }
-  __host__ __device__ static int64_t adj_cap(int maxdeg) { return ((int64_t)U * maxdeg + 8 + 3) / 4 * 4; }
-  __host__ __device__ static int64_t stage_floats(int maxdeg) { return vals_cap(maxdeg) + adj_cap(maxdeg); }
-  __host__ __device__ static bool fits(int maxdeg, int64_t stage_bytes) {
-    return G == 32 && (int64_t)kWarps * 2 * 4 * stage_floats(maxdeg) <= stage_bytes;
-  }
-};
 template <class VT>
 struct GridArgs {
   int64_t N;
@@ -1186,7 +1110,6 @@ struct GridArgs {
   unsigned* barrier;  // [2] arrivals, generation (zero at launch)
   double rtol;
   int maxiter;
-  int64_t stage_bytes;  // dynamic shared memory for the streamed SpMV stages
 };
 
 // Bounded grid barrier: the last block to arrive bumps the generation the
@@ -1260,103 +1183,16 @@ __device__ __forceinline__ void grid_rows(const Args& A, int64_t n0, int64_t n1,
   }
 }
 
-// The block's rows [n0, n1) with each warp's CSR values and adjacency streamed
-// into its own shared-memory stages by TMA bulk copies, two rounds in flight
-// (lane 0 issues round r + 2 once the warp is done with round r).  A stage
-// gets the round's ranges widened to 16-byte boundaries (inside the arrays)
-// by one bulk copy each; only the arrays' last entries past their final
-// 16-byte boundary are read by plain loads.  No block-wide barrier: warps run
-// their rounds independently.  Every wait is bounded; returns false if a copy
-// never landed (after waiting, bounded, for the warp's other copy).
-template <int NDOF, int G, class T, class VT, class Col, class Epi>
-__device__ __forceinline__ bool grid_rows_streamed(const GridArgs<VT>& A, int64_t n0, int64_t n1,
-                                                   unsigned char* smem, uint64_t* bars, unsigned& phase, Col col,
-                                                   Epi epi) {
-  using WS = WarpStages<NDOF, G>;
-  constexpr int U = WS::U, NN = NDOF * NDOF, kWarps = WS::kWarps;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int64_t vcap = WS::vals_cap(A.maxdeg), sf = WS::stage_floats(A.maxdeg);
-  float* const st0 = reinterpret_cast<float*>(smem) + (int64_t)warp * 2 * sf;
-  float* const st1 = st0 + sf;
-  uint64_t* const bar = bars + 2 * warp;
-  const int64_t vtot = (int64_t)NN * __ldg(A.adj_ptr + A.N), ptot = __ldg(A.adj_ptr + A.N);
-  const int64_t step = (int64_t)kWarps * U;
-  const int64_t first = n0 + (int64_t)warp * U;
-  const int rounds = first < n1 ? (int)((n1 - first + step - 1) / step) : 0;
-  auto issue = [&](int r) {  // lane 0
-    const int sl = r & 1;
-    float* sv = sl ? st1 : st0;
-    const int64_t a = first + (int64_t)r * step, b = a + U < n1 ? a + U : n1;
-    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + b);
-    const int64_t vlo = (NN * ea) & ~(int64_t)3, vhi = min((NN * eb + 3) & ~(int64_t)3, vtot & ~(int64_t)3);
-    const int64_t alo = ea & ~(int64_t)3, ahi = min((eb + 3) & ~(int64_t)3, ptot & ~(int64_t)3);
-    unsigned bytes = 0;
-    if (vhi > vlo) bytes += (unsigned)(4 * (vhi - vlo));
-    if (ahi > alo) bytes += (unsigned)(4 * (ahi - alo));
-    fence_proxy_async_smem();  // the stage's earlier generic reads and writes come first
-    mbar_arrive_expect_tx(&bar[sl], bytes);
-    if (vhi > vlo) bulk_copy_g2s(sv, A.vals + vlo, (unsigned)(4 * (vhi - vlo)), &bar[sl]);
-    if (ahi > alo) bulk_copy_g2s(sv + vcap, A.adj + alo, (unsigned)(4 * (ahi - alo)), &bar[sl]);
-  };
-  if (lane == 0) {
-    if (rounds > 0) issue(0);
-    if (rounds > 1) issue(1);
-  }
-  bool ok = true;
-  for (int r = 0; r < rounds; ++r) {
-    const int sl = r & 1;
-    float* sv = sl ? st1 : st0;
-    int* sa = reinterpret_cast<int*>(sv + vcap);
-    const int64_t a = first + (int64_t)r * step;
-    const int64_t ea = __ldg(A.adj_ptr + a), eb = __ldg(A.adj_ptr + (a + U < n1 ? a + U : n1));
-    const int64_t vbase = (NN * ea) & ~(int64_t)3, abase = ea & ~(int64_t)3;
-    // the arrays' last entries past their final 16-byte boundary (only at the end of the matrix)
-    const int64_t vend = NN * eb, vcut = vtot & ~(int64_t)3, acut = ptot & ~(int64_t)3;
-    if (vend > vcut) {
-      for (int64_t k = (vcut > NN * ea ? vcut : NN * ea) + lane; k < vend; k += 32) sv[k - vbase] = __ldg(A.vals + k);
-    }
-    if (eb > acut) {
-      for (int64_t k = (acut > ea ? acut : ea) + lane; k < eb; k += 32) sa[k - abase] = __ldg(A.adj + k);
-    }
-    const bool landed = mbar_wait_bounded(&bar[sl], (phase >> sl) & 1u);
-    phase ^= 1u << sl;
-    ok = __all_sync(0xffffffffu, ok && landed);
-    if (!ok) break;
-    __syncwarp();
-    T sum;
-    int64_t d;
-    if (rows_multi_s<NDOF, G, T>(n1, A.adj_ptr, sa, abase, sv, vbase, A.maxdeg, a, lane, col, sum, d)) epi(d, sum);
-    __syncwarp();  // every lane is done with the stage
-    if (lane == 0 && r + 2 < rounds) issue(r + 2);
-  }
-  if (!ok && lane == 0) {
-    mbar_wait_bounded(&bar[0], phase & 1u);
-    mbar_wait_bounded(&bar[1], (phase >> 1) & 1u);
-  }
-  return ok;
-}
-
 template <int NDOF, int G, class VT>
 __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT> A) {
   __shared__ double sh[32];
   __shared__ double s_bcast[4];
   __shared__ int s_flag;
-  extern __shared__ __align__(16) unsigned char s_dyn[];
-  __shared__ __align__(8) uint64_t s_bar[2 * (kGridThreads / 32)];  // two stage barriers per warp
   int parity = 0;
   const int rank = blockIdx.x, nr = gridDim.x;
   const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
   const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
   const int64_t tid = threadIdx.x, nth = blockDim.x;
-  // the SpMV of every iteration streams the block's CSR values and adjacency
-  // through shared memory by TMA bulk copies when two rounds of them fit
-  // (bulk copies need 16-byte aligned arrays: a caller's values may not be)
-  const bool streamed = WarpStages<NDOF, G>::fits(A.maxdeg, A.stage_bytes) &&
-                        ((reinterpret_cast<uintptr_t>(A.vals) | reinterpret_cast<uintptr_t>(A.adj)) & 15) == 0;
-  if (streamed && threadIdx.x < 2 * (kGridThreads / 32)) mbar_init(&s_bar[threadIdx.x], 1);
-  if (streamed) fence_mbar_init();
-  __syncthreads();
-  unsigned wphase = 0u;  // bit k: parity of this warp's stage barrier k's next phase (kept across SpMVs)
   // init: x = 0, r = b, z = D^-1 b, p = 0
   VT rz0 = VT(0), bb0 = VT(0);
   for (int64_t d = d0 + tid; d < d1; d += nth) {
@@ -1383,25 +1219,16 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
       const VT* pold = cur ? A.p1 : A.p0;
       VT* pnew = cur ? A.p0 : A.p1;
       const VT vb = (VT)beta;
-      // B: p_new = z + beta p_old (columns on the fly), q = A p_new, p . q;
-      // the matrix streamed through shared memory when it fits
+      // B: p_new = z + beta p_old (columns on the fly), q = A p_new, p . q
       VT pq = VT(0);
-      auto colf = [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); };
-      auto epi = [&](int64_t d, VT sum) {
-        const VT pn = vfma(vb, __ldcg(pold + d), __ldcg(A.z + d));
-        __stcg(pnew + d, pn);
-        __stcg(A.q + d, sum);
-        pq = vfma(pn, sum, pq);
-      };
-      if (streamed) {
-        const bool ok = grid_rows_streamed<NDOF, G, VT>(A, n0, n1, s_dyn, s_bar, wphase, colf, epi);
-        if (!__syncthreads_and(ok)) {
-          done = 5;
-          break;
-        }
-      } else {
-        grid_rows<NDOF, G, VT>(A, n0, n1, colf, epi);
-      }
+      grid_rows<NDOF, G, VT>(
+          A, n0, n1, [&](int64_t k) { return vfma(vb, __ldcg(pold + k), __ldcg(A.z + k)); },
+          [&](int64_t d, VT sum) {
+            const VT pn = vfma(vb, __ldcg(pold + d), __ldcg(A.z + d));
+            __stcg(pnew + d, pn);
+            __stcg(A.q + d, sum);
+            pq = vfma(pn, sum, pq);
+          });
       double dq[1] = {(double)pq};
       if (!grid_sum<1>(dq, sh, A, parity, &s_flag, s_bcast)) {
         done = 5;
@@ -1485,32 +1312,20 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
 // one cooperative launch of the grid solver (every block resident); returns
 // false if the launch was refused (the caller then uses the multi-kernel path)
 template <int NDOF, int G, class VT>
-static bool launch_grid_pcg(const GridArgs<VT>& A0, cudaStream_t s) {
+static bool launch_grid_pcg(const GridArgs<VT>& A, cudaStream_t s) {
   auto kernel = k_pcg_grid<NDOF, G, VT>;
-  static std::atomic<int> occ[64], stage[64];  // blocks per SM; staging bytes + 1 (0: not set up)
+  static std::atomic<int> occ[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
-  int bytes = stage[dev].load() - 1;
-  if (bytes < 0) {
-    // the direction's window in dynamic shared memory, if the device allows it
-    bytes = kGridStageBytes;
-    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
-      cudaGetLastError();
-      bytes = 0;
-    }
-    stage[dev].store(bytes + 1);
-  }
   int per_sm = occ[dev].load();
   if (per_sm == 0) {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGridThreads, bytes) != cudaSuccess ||
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kGridThreads, 0) != cudaSuccess ||
         per_sm < 1) {
       cudaGetLastError();
       return false;
     }
     occ[dev].store(per_sm);
   }
-  GridArgs<VT> A = A0;
-  A.stage_bytes = bytes;
   const int64_t want = (A.N + 63) / 64;  // at least 64 nodes per block
   int64_t blocks = (int64_t)per_sm * num_sms();
   if (blocks > want) blocks = want;
@@ -1518,7 +1333,7 @@ static bool launch_grid_pcg(const GridArgs<VT>& A0, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)blocks);
   cfg.blockDim = dim3(kGridThreads);
-  cfg.dynamicSmemBytes = (size_t)bytes;
+  cfg.dynamicSmemBytes = 0;
   cfg.stream = s;
   cudaLaunchAttribute attr[1];
   attr[0].id = cudaLaunchAttributeCooperative;
