@@ -338,6 +338,30 @@ def test_hex8_box_grid_tiles_match_oracle(cuda, nx, ny, nz, variant):
         assert np.array_equal(x.cpu().numpy(), y.cpu().numpy())
 
 
+@pytest.mark.parametrize("variant", [23, 24])
+def test_hex8_box_grid_side_face_constraints(cuda, variant):
+    """Dirichlet values on the x = 0 and y = 0 faces (a constrained node in
+    every node layer, so every layer reads its masks) and on one interior
+    node set; the grid kernel against the oracle."""
+    h = 1.0 / 16
+    m = create_3D_box_mesh(20, 10, 7, Lx=20 * h, Ly=10 * h, Lz=7 * h)
+    m.node_sets["mid"] = np.array([37, 555, 901])
+    s = _settings("hex8", "elastic", "element")
+    s["dirichlet_bc_dict"] = {"Ux": {"left": 0.0, "mid": 0.01}, "Uy": {"front": 0.02}, "Uz": {"left": -0.01}}
+    gl = gpu_loss("hex8", "elastic", m, {**s, "kernel_variant": variant})
+    assert gl.KernelFeatures()["box_grid"]
+    ol = oracle_loss("hex8", "elastic", m, s)
+    rng = np.random.default_rng(62)
+    ctrl = 0.5 + rng.random((2, gl.GetNumberOfControls()))
+    u = 0.002 * rng.standard_normal((2, gl.GetTotalNumberOfDOFs()))
+    a = gl.ComputeBatchLossAndGrad(ctrl, u)
+    gl.CheckDeviceStatus()
+    o = ol.batch_loss_and_grads(ctrl, u)
+    for x, z in zip(a[2:], o[2:]):
+        assert rel_fro(x.cpu().numpy(), z) < TOL
+    assert np.all(a[3].cpu().numpy()[:, ol.dirichlet_indices] == 0)
+
+
 @pytest.mark.parametrize("box", [20, 21, 22, 23, 24])
 def test_box_kernel_agrees_with_pointwise_kernel(cuda, box):
     """On a 100^3 cube mesh the box kernels and the pointwise kernel (variant
