@@ -75,8 +75,8 @@ NCU_FIGURES = {64: {6: {"traffic": 17_498_624 + 108_544, "warp_instructions": 16
                     17: {"traffic": 17_600_000 + 8_960, "warp_instructions": 10_964_421},
                     21: {"traffic": 13_100_000 + 7_940, "warp_instructions": 4_817_046,
                          "fp32_flops": 93_490_000},
-                    23: {"traffic": 4_748_288 + 0, "warp_instructions": 8_079_579,
-                         "fp32_flops": 139_900_000}}}
+                    23: {"traffic": 4_482_560 + 0, "warp_instructions": 7_515_845,
+                         "fp32_flops": 139_940_000}}}
 
 
 def ncu_figure(n, variant, key):
