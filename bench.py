@@ -99,9 +99,11 @@ def parse():
                     help="run only the --extras measurements and print them (profiling runs; no bench line)")
     ap.add_argument("--hex8-variant", type=int, default=None,
                     help="force one hex8 kernel variant (0-17) instead of autotuning (profiling runs)")
-    ap.add_argument("--extras", default="jittered,small,pcg,batched,neohooke,newton,fourier",
+    ap.add_argument("--minimiser-n", type=int, default=16,
+                    help="cells per side of the tet split the loss minimiser is solved on (minimiser extra)")
+    ap.add_argument("--extras", default="jittered,small,pcg,batched,neohooke,minimiser,newton,fourier",
                     help="comma list of the extra measurements to run (jittered, small, pcg, batched, neohooke, "
-                         "newton, fourier; fused: the headline step alone, for profiling)")
+                         "minimiser, newton, fourier; fused: the headline step alone, for profiling)")
     return ap.parse_args()
 
 
@@ -492,14 +494,12 @@ def extra_batched(args, n_inst=512, seed=11):
                                  "eager: the same from the Python API (wall clock)"}
 
 
-def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=16):
+def extra_neohooke(args, n=64, batch=16, seed=2024):
     """C4: tet4 Neo-Hookean (6-tet split of a 64^3 hex grid, 1 Gauss point),
     mu/lambda scaled by the two-phase field, 16 microstructures: fused loss +
-    adjoint throughput; and the Newton oracle of the loss minimiser on a 16^3
-    split (newton_minimiser).  The reference Neo-Hookean model is not
-    stress-free at C = I (S = -mu I): its tangent is indefinite near u = 0 and
-    full Newton steps from u = 0 invert elements beyond ~6^3, so the minimiser
-    is found with the energy line search."""
+    adjoint throughput, by default in one launch (element and node-gather
+    items of k_loss_stream: 1.6 GB of element records beyond L2), and the
+    two-launch path (element kernel + gather) beside it."""
     import torch
     from folax_gb300 import workloads
     from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
@@ -513,11 +513,25 @@ def extra_neohooke(args, n=64, batch=16, seed=2024, newton_n=16):
     torch.cuda.synchronize()
     ms = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
     loss.CheckDeviceStatus()  # no non-finite value or inverted element in the timed work
+    loss.SetFusedGather("off")
+    for _ in range(3):
+        loss.ComputeBatchLossAndGrad(Cb, U)
+    ms_two = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
+    loss.CheckDeviceStatus()
+    loss.SetFusedGather("auto")
     E = len(mesh.elements_nodes["tetra"])
-    out = {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6,
-           "microstructures": "one two-phase field per instance"}
-    out["newton"] = newton_minimiser(newton_n, seed)
-    return out
+    return {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6,
+            "two_launch_ms_per_step": ms_two, "path": "one launch: k_loss_stream (element + node-gather items)",
+            "microstructures": "one two-phase field per instance"}
+
+
+def extra_minimiser(args, n=16, seed=2024):
+    """The Newton oracle of the C4 loss minimiser on the n^3 split
+    (newton_minimiser; n = --minimiser-n, 16 by default).  The reference Neo-Hookean model is not stress-free
+    at C = I (S = -mu I): its tangent is indefinite near u = 0 and full
+    Newton steps from u = 0 invert elements beyond ~6^3, so the minimiser is
+    found with the energy line search."""
+    return newton_minimiser(n, seed)
 
 
 def newton_minimiser(n, seed, abs_tol=1e-7):
@@ -768,6 +782,8 @@ def run_extras(args, loss, ctrl, u=None):
                           ("pcg", "pcg_hex8_64", lambda: extra_pcg(args, loss, ctrl)),
                           ("batched", "batched_quad4_512", lambda: extra_batched(args)),
                           ("neohooke", "neohooke_tet4_batch16", lambda: extra_neohooke(args)),
+                          ("minimiser", f"newton_minimiser_tet4_{args.minimiser_n}",
+                           lambda: extra_minimiser(args, n=args.minimiser_n)),
                           ("newton", "newton_svk_hex8_10", lambda: extra_newton(args)),
                           ("fourier", "fourier_hex8_64_batch4", lambda: extra_fourier(args))):
         if key not in wanted:
