@@ -497,9 +497,7 @@ def extra_batched(args, n_inst=512, seed=11):
 def extra_neohooke(args, n=64, batch=16, seed=2024):
     """C4: tet4 Neo-Hookean (6-tet split of a 64^3 hex grid, 1 Gauss point),
     mu/lambda scaled by the two-phase field, 16 microstructures: fused loss +
-    adjoint throughput, by default in one launch (element and node-gather
-    items of k_loss_stream: 1.6 GB of element records beyond L2), and the
-    two-launch path (element kernel + gather) beside it."""
+    adjoint throughput (element kernel + node gather)."""
     import torch
     from folax_gb300 import workloads
     from folax_gb300.loss import NeoHookeMechanicalLoss3DTetra
@@ -513,15 +511,8 @@ def extra_neohooke(args, n=64, batch=16, seed=2024):
     torch.cuda.synchronize()
     ms = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
     loss.CheckDeviceStatus()  # no non-finite value or inverted element in the timed work
-    loss.SetFusedGather("off")
-    for _ in range(3):
-        loss.ComputeBatchLossAndGrad(Cb, U)
-    ms_two = _events_ms(torch, lambda: loss.ComputeBatchLossAndGrad(Cb, U), 10)
-    loss.CheckDeviceStatus()
-    loss.SetFusedGather("auto")
     E = len(mesh.elements_nodes["tetra"])
     return {"tets": E, "batch": batch, "ms_per_step": ms, "melem_s": batch * E / (ms * 1e-3) / 1e6,
-            "two_launch_ms_per_step": ms_two, "path": "one launch: k_loss_stream (element + node-gather items)",
             "microstructures": "one two-phase field per instance"}
 
 
