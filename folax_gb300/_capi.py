@@ -37,7 +37,7 @@ SHEAR_REFERENCE, SHEAR_CONSISTENT = 0, 1
 OP_LOSS_ADJOINT, OP_ASSEMBLE, OP_PCG, OP_PLAIN, OP_KRYLOV64 = 0, 1, 2, 3, 4
 KRYLOV_CG, KRYLOV_BICGSTAB = 0, 1
 KRYLOV_ENGINE_GRID, KRYLOV_ENGINE_KERNELS = 0, 1
-FEATURE_TILES, FEATURE_UNIFORM_BOX, FEATURE_BOX_GRID = 1, 2, 4
+FEATURE_TILES, FEATURE_UNIFORM_BOX, FEATURE_BOX_GRID, FEATURE_TET_PATCHES = 1, 2, 4, 8
 
 
 class FolgbError(RuntimeError):

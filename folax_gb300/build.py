@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG, "_build")
 LIBDIR = os.path.join(PKG, "lib")
 LIB = os.path.join(LIBDIR, "libfolgb.so")
 SOURCES = ["plan.cu", "elements.cu", "krylov.cu", "batched.cu", "trace.cu", "hex8_fused.cu", "noalloc.cu",
-           "fourier.cu", "response.cu", "tiles.cu", "uniform_box.cu"]
+           "fourier.cu", "response.cu", "tiles.cu", "uniform_box.cu", "tet_patch.cu"]
 HEADERS = ["folgb_internal.cuh", "element_body.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-lineinfo", "-O3", "-std=c++17", "-Xcompiler", "-fPIC",

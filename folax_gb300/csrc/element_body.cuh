@@ -151,11 +151,31 @@ __device__ __forceinline__ void finish_loss(float block_energy, const VecArgs& A
   }
 }
 
-// Per-element body shared by the single-mesh and the batched kernels.  NP > 0:
-// the Gauss rule is the compile-time one of GPc (unrolled point loop).
-template <int ET, int PH, int MODE, int NP = 0>
-__device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable& gp, const int b, const int64_t e,
-                                                 float& energy, int& bad) {
+// One record store of up to 4 floats at float offset off of A.g (records are
+// 1, 2 or 4 floats, padding zeroed); evict-first when the records do not fit
+// in L2, so they do not push the node data out of it.
+__device__ __forceinline__ void store_record(const VecArgs& A, int64_t off, const float (&v)[4]) {
+  float* rec = A.g + off;
+  if (A.rec == 4) {
+    const float4 t = make_float4(v[0], v[1], v[2], v[3]);
+    if (A.stream_rec) __stcs(reinterpret_cast<float4*>(rec), t);
+    else *reinterpret_cast<float4*>(rec) = t;
+  } else if (A.rec == 2) {
+    const float2 t = make_float2(v[0], v[1]);
+    if (A.stream_rec) __stcs(reinterpret_cast<float2*>(rec), t);
+    else *reinterpret_cast<float2*>(rec) = t;
+  } else {
+    if (A.stream_rec) __stcs(rec, v[0]);
+    else rec[0] = v[0];
+  }
+}
+
+// The element body with its per-node results handed to sink(a, v): v holds
+// the ndof vector components of local node a, then the nodal control
+// sensitivity (nodal controls, loss mode), zero padded to 4.
+template <int ET, int PH, int MODE, int NP, class Sink>
+__device__ __forceinline__ void elem_vector_body_to(const VecArgs& A, const GPTable& gp, const int b, const int64_t e,
+                                                    float& energy, int& bad, Sink&& sink) {
   constexpr int NEN = ElemT<ET>::NEN, DIM = ElemT<ET>::DIM, NDOF = NdofT<PH, DIM>::V;
   constexpr int ND = NEN * NDOF;
   {
@@ -428,26 +448,37 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
             H[i][j] = s;
           }
         const float mu = mt.mu_f * egp, lam = mt.lam_f * egp;
-        NHState<DIM> st;
-        nh_state<DIM>(H, mu, lam, st);
-        float M[DIM][DIM];
-        const float off = (MODE == MODE_RESIDUAL && mt.shear_ref) ? 2.f : 1.f;
-#pragma unroll
-        for (int i = 0; i < DIM; ++i)
-#pragma unroll
-          for (int j = 0; j < DIM; ++j) M[i][j] = st.S[i][j] * (i == j ? 1.f : off);
         float P[DIM][DIM];
+        float psi, dpsi_dmu, dpsi_dlam;
+        if constexpr (MODE == MODE_LOSS) {
+          // the loss gradient is the true dpsi/dF
+          nh_first_piola<DIM>(H, mu, lam, P, psi, dpsi_dmu, dpsi_dlam);
+        } else {
+          // the FE residual: F S, the shear entries of S doubled in the
+          // reference convention
+          NHState<DIM> st;
+          nh_state<DIM>(H, mu, lam, st);
+          float M[DIM][DIM];
+          const float off = mt.shear_ref ? 2.f : 1.f;
 #pragma unroll
-        for (int k = 0; k < DIM; ++k)
+          for (int i = 0; i < DIM; ++i)
 #pragma unroll
-          for (int j = 0; j < DIM; ++j) {
-            float s = 0.f;
+            for (int j = 0; j < DIM; ++j) M[i][j] = st.S[i][j] * (i == j ? 1.f : off);
 #pragma unroll
-            for (int p = 0; p < DIM; ++p) s = fmaf(st.F[k][p], M[p][j], s);
-            P[k][j] = s;
-          }
-        energy = fmaf(wd, st.psi, energy);
-        const float dpsi_de = st.dpsi_dmu * mt.mu_f + st.dpsi_dlam * mt.lam_f;
+          for (int k = 0; k < DIM; ++k)
+#pragma unroll
+            for (int j = 0; j < DIM; ++j) {
+              float s = 0.f;
+#pragma unroll
+              for (int p = 0; p < DIM; ++p) s = fmaf(st.F[k][p], M[p][j], s);
+              P[k][j] = s;
+            }
+          psi = st.psi;
+          dpsi_dmu = st.dpsi_dmu;
+          dpsi_dlam = st.dpsi_dlam;
+        }
+        energy = fmaf(wd, psi, energy);
+        const float dpsi_de = dpsi_dmu * mt.mu_f + dpsi_dlam * mt.lam_f;
 #pragma unroll
         for (int a = 0; a < NEN; ++a) {
 #pragma unroll
@@ -475,11 +506,6 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
       for (int q = 0; q < gp.npts; ++q) point(q);
     }
     if (!isfinite(energy)) bad |= 2;
-    // one record per (element, node), local-node-major ([b][a][e]): ndof
-    // vector components, then the nodal control sensitivity when present
-    // One vector store per record (the record widths are 1, 2 or 4 floats,
-    // padding zeroed); evict-first when the records do not fit in L2, so they
-    // do not push the node data out of it.
     const bool nodal_gde = (MODE == MODE_LOSS) && A.ctrl_layout == FOLGB_CONTROL_NODAL;
 #pragma unroll
     for (int a = 0; a < NEN; ++a) {
@@ -487,19 +513,7 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
 #pragma unroll
       for (int c = 0; c < NDOF; ++c) v[c] = g[a * NDOF + c];
       if (nodal_gde) v[NDOF < 4 ? NDOF : 3] = gd[a];
-      float* rec = A.g + (((int64_t)b * NEN + a) * A.E + e) * A.rec;
-      if (A.rec == 4) {
-        const float4 t = make_float4(v[0], v[1], v[2], v[3]);
-        if (A.stream_rec) __stcs(reinterpret_cast<float4*>(rec), t);
-        else *reinterpret_cast<float4*>(rec) = t;
-      } else if (A.rec == 2) {
-        const float2 t = make_float2(v[0], v[1]);
-        if (A.stream_rec) __stcs(reinterpret_cast<float2*>(rec), t);
-        else *reinterpret_cast<float2*>(rec) = t;
-      } else {
-        if (A.stream_rec) __stcs(rec, v[0]);
-        else rec[0] = v[0];
-      }
+      sink(a, v);
     }
     if (MODE == MODE_LOSS) {
       if (!nodal_gde && A.dctrl_elem) {
@@ -511,6 +525,19 @@ __device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable
       }
     }
   }
+}
+
+// Per-element body shared by the single-mesh and the batched kernels: one
+// record per (element, node), local-node-major ([b][a][e]), one vector store
+// each.  NP > 0: the Gauss rule is the compile-time one of GPc (unrolled
+// point loop).
+template <int ET, int PH, int MODE, int NP = 0>
+__device__ __forceinline__ void elem_vector_body(const VecArgs& A, const GPTable& gp, const int b, const int64_t e,
+                                                 float& energy, int& bad) {
+  constexpr int NEN = ElemT<ET>::NEN;
+  elem_vector_body_to<ET, PH, MODE, NP>(A, gp, b, e, energy, bad, [&](int a, const float (&v)[4]) {
+    store_record(A, (((int64_t)b * NEN + a) * A.E + e) * A.rec, v);
+  });
 }
 
 // __syncthreads_or returns whether any thread's predicate is non-zero (not
@@ -588,4 +615,8 @@ namespace folgb {
 // sum-factorised hex8 2x2x2 elasticity (hex8_fused.cu); returns 1 if launched
 int launch_hex8_fast(const folgb_plan* p, const VecArgs& A, dim3 grid, int mode, cudaStream_t s);
 int launch_tile_boundary(const folgb_plan* p, const VecArgs& A, int B, cudaStream_t s, int pdl);
+// tetrahedra in patches of 6 (tet_patch.cu): loss + adjoint records per
+// (instance, patch, patch node); returns 1 if launched, 0 if it does not
+// apply, or the negated error code
+int launch_tet_patch(const folgb_plan* p, const VecArgs& A, int B, cudaStream_t s);
 }  // namespace folgb

@@ -51,8 +51,9 @@ __global__ void __launch_bounds__(256) k_elem_vector(const VecArgs A, const int 
 
 
 struct GatherArgs {
-  int64_t E, N;
-  int nen;
+  int64_t E, N;  // E: the record sources (elements, or tet patches)
+  int nen;       // records per source
+  int64_t E_ctrl;  // elements of the element-layout control gradient
   const int* inc_ptr;
   const int* inc_slot;
   const int* inc_padded;  // [N][pad] slots, -1 padded (pad 4 or 8), or NULL
@@ -168,8 +169,8 @@ __global__ void __launch_bounds__(256) k_node_gather(const GatherArgs A) {
   if (A.rescale_elem && A.dctrl_elem) {
     pdl_wait_primary();
     if (A.scale) scb = A.scale[b];
-    for (int64_t e = (int64_t)blk * blockDim.x + threadIdx.x; e < A.E; e += stride)
-      A.dctrl_elem[(int64_t)b * A.E + e] *= A.elem_inst ? A.scale[__ldg(A.elem_inst + e)] : scb;
+    for (int64_t e = (int64_t)blk * blockDim.x + threadIdx.x; e < A.E_ctrl; e += stride)
+      A.dctrl_elem[(int64_t)b * A.E_ctrl + e] *= A.elem_inst ? A.scale[__ldg(A.elem_inst + e)] : scb;
   }
 }
 
@@ -831,16 +832,18 @@ static int launch_matrix(const MatArgs& A0, int B, int npts, cudaStream_t s) {
 
 int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
-                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl) {
+                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl, int patches) {
   GatherArgs G;
   G.node_inst = node_inst;
   G.elem_inst = elem_inst;
-  G.E = p->E;
+  G.E = patches ? p->n_patches : p->E;
   G.N = p->N;
-  G.nen = p->nen;
-  G.inc_ptr = p->d_inc_ptr;
-  G.inc_slot = p->d_inc_slot;
-  G.inc_padded = p->d_inc_padded;
+  G.nen = patches ? kPatchNodes : p->nen;
+  G.E_ctrl = p->E;
+  G.inc_ptr = patches ? p->d_patch_inc_ptr : p->d_inc_ptr;
+  G.inc_slot = patches ? p->d_patch_inc_slot : p->d_inc_slot;
+  G.inc_padded = patches ? p->d_patch_inc_padded : p->d_inc_padded;
+  const int inc_pad = patches ? p->patch_pad : p->inc_pad;
   G.dmask = p->d_dmask;
   G.g = g;
   G.rec = rec;
@@ -862,8 +865,8 @@ int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_
   auto go = [&](auto nd, auto rc_, auto gde) -> int {
     constexpr int NDOF = decltype(nd)::value, REC = decltype(rc_)::value;
     constexpr bool GDE = decltype(gde)::value;
-    auto kernel = p->inc_pad == 4 ? (ifast ? k_node_gather<NDOF, REC, GDE, 4, true> : k_node_gather<NDOF, REC, GDE, 4>)
-                  : (p->inc_pad == 8 ? (ifast ? k_node_gather<NDOF, REC, GDE, 8, true> : k_node_gather<NDOF, REC, GDE, 8>)
+    auto kernel = inc_pad == 4 ? (ifast ? k_node_gather<NDOF, REC, GDE, 4, true> : k_node_gather<NDOF, REC, GDE, 4>)
+                  : (inc_pad == 8 ? (ifast ? k_node_gather<NDOF, REC, GDE, 8, true> : k_node_gather<NDOF, REC, GDE, 8>)
                                      : (ifast ? k_node_gather<NDOF, REC, GDE, 0, true> : k_node_gather<NDOF, REC, GDE, 0>));
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = grid;
@@ -978,7 +981,10 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   A.dctrl_nodal = elem_ctrl ? nullptr : dloss_dcontrol;
   dim3 grid((unsigned)loss_blocks(p), (unsigned)B);
   const int fast = p->phys.kernel_variant != 1 ? launch_hex8_fast(p, A, grid, MODE_LOSS, s) : 0;
-  if (fast) {
+  // tetrahedra in patches of six: one record per patch node
+  const int patched = fast ? 0 : launch_tet_patch(p, A, B, s);
+  if (patched < 0) return -patched;
+  if (fast || patched) {
     FOLGB_LAUNCH_CHECK();
   } else {
     rc = dispatch(p->etype, p->physics, [&](auto tag) -> int {
@@ -1007,7 +1013,7 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
     rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
                        elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
                        (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr,
-                       trace_active() ? 0 : 1);
+                       trace_active() ? 0 : 1, patched ? 1 : 0);
   }
   return rc;
 }

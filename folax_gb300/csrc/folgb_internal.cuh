@@ -79,6 +79,16 @@ struct folgb_plan {
   int* d_inc_slot = nullptr;
   int inc_pad = 0;          // 4 or 8 when every node has at most that many incidences, else 0
   int* d_inc_padded = nullptr;  // [N][inc_pad] incident slots, -1 padded (vector loads)
+  // tetrahedra in patches of 6 consecutive elements on at most 8 nodes (the
+  // 6-tet split of a hexahedron; tet_patch.cu): per patch the local node
+  // (0..7) of each tet corner, 4 bits each, tet t in bits 16 (t % 2) + 4 a of
+  // word t / 2; and the node -> (corner, patch) incidence of the patch records
+  int64_t n_patches = 0;                // 0: no patch tables
+  uint4* d_patch_local = nullptr;       // [P]
+  int* d_patch_inc_ptr = nullptr;       // [N + 1]
+  int* d_patch_inc_slot = nullptr;      // record indices corner * P + patch, ascending patch
+  int patch_pad = 0;                    // 4 or 8 when every node has at most that many, else 0
+  int* d_patch_inc_padded = nullptr;    // [N][patch_pad], -1 padded
   int hex8_variant = 0;    // sum-factorised hex8 kernel variant (autotuned)
   unsigned char* d_dmask = nullptr;
   unsigned char* d_elem_bc = nullptr;  // [E] 1 if a node of the element has a Dirichlet dof
@@ -180,6 +190,11 @@ constexpr int kTileZeroRec = 8 * kTileElems;  // position of the zero record pad
 int build_tile_tables(folgb_plan* p, const std::vector<int>& conn, const double* xyz,
                       const std::vector<unsigned char>& dmask, const std::vector<unsigned char>& elem_bc);
 void free_tile_tables(folgb_plan* p);
+// Tet patches (tet_patch.cu): sets n_patches and the patch tables when every
+// group of 6 consecutive tetrahedra spans at most 8 nodes.
+constexpr int kPatchTets = 6, kPatchNodes = 8;
+int build_tet_patches(folgb_plan* p, const std::vector<int>& conn);
+void free_tet_patches(folgb_plan* p);
 // Uniform axis-aligned box elements (uniform_box.cu): sets box_valid and box_k.
 int build_uniform_box(folgb_plan* p, const std::vector<float4>& x4, const std::vector<int>& conn,
                       const std::vector<unsigned char>& dmask);
@@ -201,9 +216,11 @@ inline int residual_record(const folgb_plan* p);
 // deterministic node gather of element vectors (elements.cu)
 // pdl = 1: launched as a programmatic dependent of the element kernel just
 // before it on the stream (its incidence loads overlap that kernel's tail).
+// patches = 1: the records are the tet patch kernel's ([B][8][P], the patch
+// incidence tables)
 int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_gde, const float* scale, float* out,
                   int64_t out_stride, float* dctrl, int64_t dctrl_stride, float* dctrl_elem, int rescale_elem,
-                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl = 0);
+                  cudaStream_t s, const int* node_inst, const int* elem_inst, int pdl = 0, int patches = 0);
 
 // Programmatic dependent launch: the primary kernel lets the next kernel on
 // the stream start early; the dependent waits for the primary's completion
@@ -508,6 +525,77 @@ __device__ __forceinline__ void nh_state(const float (&H)[D][D], float mu, float
         st.S[i][j] = mu * ((i == j ? 1.f : 0.f) - st.Ci[i][j]) + lam * lnJ * st.Ci[i][j];
   }
   st.lnJ = lnJ;
+}
+
+// The energy and its gradient P = dpsi/dF = F S of the same model without
+// forming C, C^-1 or S: F C^-1 = F^-T = cof(F) / J, so
+//   3-D: P = mu a F + ((lam lnJ - mu) - mu a I1 / 3) / J cof(F),  a = J^-2/3
+//   2-D: P = mu F + (lam lnJ - mu) / J cof(F)
+// (about 100 fewer operations per point than nh_state + F S).  J - 1, ln J and
+// J^-2/3 I1 - 3 are formed from H as nh_state forms them, so small strains
+// keep their digits.
+template <int D>
+__device__ __forceinline__ void nh_first_piola(const float (&H)[D][D], float mu, float lam, float (&P)[D][D],
+                                               float& psi, float& dpsi_dmu, float& dpsi_dlam) {
+  float F[D][D];
+  float hh = 0.f, trH = 0.f;
+#pragma unroll
+  for (int i = 0; i < D; ++i) {
+    trH += H[i][i];
+#pragma unroll
+    for (int j = 0; j < D; ++j) {
+      F[i][j] = H[i][j] + (i == j ? 1.f : 0.f);
+      hh = fmaf(H[i][j], H[i][j], hh);
+    }
+  }
+  const float trE = fmaf(0.5f, hh, trH);  // tr E, E = (H + H^T + H^T H) / 2
+  float Jm1, cof[D][D];
+  if constexpr (D == 3) {
+    const float m2 = H[0][0] * H[1][1] - H[0][1] * H[1][0] + H[0][0] * H[2][2] - H[0][2] * H[2][0] +
+                     H[1][1] * H[2][2] - H[1][2] * H[2][1];
+    const float dH = H[0][0] * (H[1][1] * H[2][2] - H[1][2] * H[2][1]) -
+                     H[0][1] * (H[1][0] * H[2][2] - H[1][2] * H[2][0]) +
+                     H[0][2] * (H[1][0] * H[2][1] - H[1][1] * H[2][0]);
+    Jm1 = trH + m2 + dH;
+    cof[0][0] = F[1][1] * F[2][2] - F[1][2] * F[2][1];
+    cof[0][1] = F[1][2] * F[2][0] - F[1][0] * F[2][2];
+    cof[0][2] = F[1][0] * F[2][1] - F[1][1] * F[2][0];
+    cof[1][0] = F[0][2] * F[2][1] - F[0][1] * F[2][2];
+    cof[1][1] = F[0][0] * F[2][2] - F[0][2] * F[2][0];
+    cof[1][2] = F[0][1] * F[2][0] - F[0][0] * F[2][1];
+    cof[2][0] = F[0][1] * F[1][2] - F[0][2] * F[1][1];
+    cof[2][1] = F[0][2] * F[1][0] - F[0][0] * F[1][2];
+    cof[2][2] = F[0][0] * F[1][1] - F[0][1] * F[1][0];
+  } else {
+    Jm1 = trH + (H[0][0] * H[1][1] - H[0][1] * H[1][0]);
+    cof[0][0] = F[1][1];
+    cof[0][1] = -F[1][0];
+    cof[1][0] = -F[0][1];
+    cof[1][1] = F[0][0];
+  }
+  const float lnJ = log1pf(Jm1);
+  const float rJ = 1.f / (1.f + Jm1);
+  const float cc = lam * lnJ - mu;
+  float ma, c2;
+  if constexpr (D == 3) {
+    const float I1 = fmaf(2.f, trE, 3.f);
+    const float am1 = expm1f(-2.f / 3.f * lnJ);
+    const float iso = fmaf(am1, I1, 2.f * trE);  // J^-2/3 I1 - 3
+    psi = 0.5f * mu * iso - mu * lnJ + 0.5f * lam * lnJ * lnJ;
+    dpsi_dmu = 0.5f * iso - lnJ;
+    ma = mu * (1.f + am1);
+    c2 = (cc - ma * I1 * (1.f / 3.f)) * rJ;
+  } else {
+    psi = mu * trE - mu * lnJ + 0.5f * lam * lnJ * lnJ;
+    dpsi_dmu = trE - lnJ;
+    ma = mu;
+    c2 = cc * rJ;
+  }
+  dpsi_dlam = 0.5f * lnJ * lnJ;
+#pragma unroll
+  for (int i = 0; i < D; ++i)
+#pragma unroll
+    for (int j = 0; j < D; ++j) P[i][j] = fmaf(ma, F[i][j], c2 * cof[i][j]);
 }
 
 // Directional derivative dS of the true S along a symmetric dC.

@@ -379,6 +379,11 @@ extern "C" int folgb_plan_create(folgb_plan** out, const folgb_physics* phys, co
     folgb_plan_destroy(p);
     return rc;
   }
+  // patches of 6 tetrahedra on 8 nodes (the 6-tet split of a hexahedron)
+  if ((rc = build_tet_patches(p, c32))) {
+    folgb_plan_destroy(p);
+    return rc;
+  }
   // box kernels when every element is the same axis-aligned box
   if ((rc = build_uniform_box(p, x4, c32, dmask))) {
     folgb_plan_destroy(p);
@@ -398,6 +403,7 @@ extern "C" int folgb_plan_destroy(folgb_plan* p) {
   for (void* q : ptrs)
     if (q) cudaFree(q);
   free_tile_tables(p);
+  free_tet_patches(p);
   free_krylov_graphs(p);
   delete p;
   return FOLGB_OK;
@@ -416,7 +422,7 @@ extern "C" int folgb_plan_info(const folgb_plan* p, int64_t* ndof_per_node, int6
 extern "C" int folgb_plan_features(const folgb_plan* p, int32_t* features) {
   if (!p || !features) return FOLGB_ERR_INVALID_ARGUMENT;
   *features = (p->tiles > 0 ? FOLGB_FEATURE_TILES : 0) | (p->box_valid ? FOLGB_FEATURE_UNIFORM_BOX : 0) |
-              (p->box_grid ? FOLGB_FEATURE_BOX_GRID : 0);
+              (p->box_grid ? FOLGB_FEATURE_BOX_GRID : 0) | (p->n_patches > 0 ? FOLGB_FEATURE_TET_PATCHES : 0);
   return FOLGB_OK;
 }
 

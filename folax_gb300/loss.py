@@ -305,11 +305,16 @@ class FiniteElementLoss:
         kernels, variants 20-22) and "box_grid" (also numbered as a structured
         box mesh: the one-launch grid kernels, variants 23-24, loss exponent
         1; a call with host result buffers runs the box kernel and the gather
-        instead).  The autotuner times the variants that apply."""
+        instead) and "tet_patches" (every 6 consecutive tetrahedra on at most
+        8 nodes, as the 6-tet split of hexahedra: the loss + adjoint of
+        3-component mechanics writes one record per group node; the
+        "generic" kernel_variant turns it off).  The autotuner times the
+        hex8 variants that apply."""
         f = C.c_int32()
         capi.check("folgb_plan_features", self._plan.lib.folgb_plan_features(self._plan.handle, C.byref(f)))
         return {"tiles": bool(f.value & capi.FEATURE_TILES), "uniform_box": bool(f.value & capi.FEATURE_UNIFORM_BOX),
-                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID)}
+                "box_grid": bool(f.value & capi.FEATURE_BOX_GRID),
+                "tet_patches": bool(f.value & capi.FEATURE_TET_PATCHES)}
 
     def CheckDeviceStatus(self):
         """Raise FolgbError if a kernel flagged a non-positive detJ, a

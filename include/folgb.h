@@ -123,9 +123,15 @@ int folgb_plan_info(const folgb_plan* plan, int64_t* ndof_per_node, int64_t* tot
  * mesh numbered as the box mesh generator numbers it (nodes x fastest, then y,
  * then z), so the one-launch grid kernels (variants 23-24, loss exponent 1)
  * apply (a call whose dloss_ddofs is host memory runs the box kernel and the
- * gather instead: they write the gradients over the host link faster).  No
- * counterpart in the reference (a query of this library's specialisations). */
-enum { FOLGB_FEATURE_TILES = 1, FOLGB_FEATURE_UNIFORM_BOX = 2, FOLGB_FEATURE_BOX_GRID = 4 };
+ * gather instead: they write the gradients over the host link faster);
+ * FOLGB_FEATURE_TET_PATCHES, a tet mesh whose consecutive groups of 6 elements
+ * each span at most 8 nodes (the 6-tet split of hexahedra), so the loss +
+ * adjoint of 3-component mechanics sums each group's node results before the
+ * gather (one record per group node instead of one per element node; kernel
+ * variant 1, the generic per-element loop, turns it off).  No counterpart in
+ * the reference (a query of this library's specialisations). */
+enum { FOLGB_FEATURE_TILES = 1, FOLGB_FEATURE_UNIFORM_BOX = 2, FOLGB_FEATURE_BOX_GRID = 4,
+       FOLGB_FEATURE_TET_PATCHES = 8 };
 int folgb_plan_features(const folgb_plan* plan, int32_t* features);
 
 /* Sets the Dirichlet values used by the in-kernel GetFullDofVector, scaled by
