@@ -1920,12 +1920,15 @@ __global__ void k_ls_arm(NState* st, const float* e0, cudaGraphConditionalHandle
 }
 
 // A Newton step that is not a descent direction (indefinite tangent: slope
-// = rhs . du <= 0) or that the Krylov solve left non-finite is replaced by the
+// = rhs . du <= 0), that the Krylov solve left non-finite, or whose Krylov
+// solve did not converge (an unconverged iterate on an indefinite system can
+// be a descent direction of useless length) is replaced by the
 // Jacobi-preconditioned steepest descent step du = D^-1 rhs = -D^-1 r.
 __global__ void k_ls_direction(int64_t n, const float* __restrict__ rhs, const float* __restrict__ dinv,
-                               float* __restrict__ du, const NState* st) {
+                               float* __restrict__ du, const NState* st, const KScalars* sc) {
   const double sl = st->slope;
-  if (isfinite(sl) && sl > 0.0) return;
+  const bool failed = sc && (sc->done == 3 || sc->done == 4);
+  if (isfinite(sl) && sl > 0.0 && !failed) return;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
     du[i] = dinv[i] * rhs[i];
 }
@@ -2086,7 +2089,7 @@ extern "C" int folgb_newton(const folgb_plan* p, const float* control, float* do
       k_newton_norm<<<vb, 256, 0, cs>>>(n, w.du, nullptr, w.part, w.counter + 1, &w.st->dn2);
       if (s->line_search) {
         k_newton_dot<<<vb, 256, 0, cs>>>(n, w.rhs, w.du, w.part, w.counter + 2, &w.st->slope);
-        k_ls_direction<<<vb, 256, 0, cs>>>(n, w.rhs, w.dinv, w.du, w.st);
+        k_ls_direction<<<vb, 256, 0, cs>>>(n, w.rhs, w.dinv, w.du, w.st, ksc);
         k_newton_dot<<<vb, 256, 0, cs>>>(n, w.rhs, w.du, w.part, w.counter + 2, &w.st->slope);
       }
       k_newton_control<<<1, 32, 0, cs>>>(w.st, ksc, w.hist, hist_cap);
