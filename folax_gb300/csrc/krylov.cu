@@ -1103,6 +1103,7 @@ struct GridArgs {
   const float* dinv;
   const float* b;
   VT *r, *z, *p0, *p1, *q;
+  VT *rhat, *v, *y, *t;  // BiCGSTAB
   double* x;
   float* xout;
   KScalars* sc;
@@ -1309,11 +1310,169 @@ __global__ void __launch_bounds__(kGridThreads, 1) k_pcg_grid(const GridArgs<VT>
   }
 }
 
+// Grid-resident BiCGSTAB: the whole solve in one cooperative launch, as the
+// grid CG above and with the cluster solver's iteration (right Jacobi
+// preconditioning: y = D^-1 p, z = D^-1 s; fp64 dots and iterate; reliable
+// updates from the fp64 iterate, a breakdown restarting the shadow residual).
+// Each block owns a contiguous node range; the phases are separated by the
+// bounded grid barrier and every reduction is the grid sum in block order, so
+// all blocks hold the same scalars.  Vectors another block wrote are read
+// through L2 (ld.global.cg).
+template <int NDOF, int G, class VT>
+__global__ void __launch_bounds__(kGridThreads, 1) k_bicg_grid(const GridArgs<VT> A) {
+  __shared__ double sh[32];
+  __shared__ double s_bcast[4];
+  __shared__ int s_flag;
+  int parity = 0;
+  const int rank = blockIdx.x, nr = gridDim.x;
+  const int64_t n0 = A.N * rank / nr, n1 = A.N * (rank + 1) / nr;
+  const int64_t d0 = NDOF * n0, d1 = NDOF * n1;
+  const int64_t tid = threadIdx.x, nth = blockDim.x;
+  // init: x = 0, r = rhat = b
+  double red[1] = {0.0};
+  for (int64_t d = d0 + tid; d < d1; d += nth) {
+    const float bi = A.b[d];
+    A.x[d] = 0.0;
+    __stcg(A.r + d, (VT)bi);
+    __stcg(A.rhat + d, (VT)bi);
+    red[0] += (double)bi * (double)bi;
+  }
+  int done = 0;
+  if (!grid_sum<1>(red, sh, A, parity, &s_flag, s_bcast)) done = 5;
+  const double bb = red[0];
+  const double tol2 = A.rtol * A.rtol * bb;
+  double rho = bb, rref2 = bb, rnorm2 = bb;
+  double alpha = 1.0, beta = 0.0, omega = 1.0;
+  if (!done) done = (bb == 0.0) ? 1 : (!isfinite(bb) ? 3 : 0);
+  int iters = 0, breakdowns = 0, replace = 0;
+  bool restart = true;
+  while (!done) {
+    if (!replace) {
+      // A: p = r + beta (p - omega v) (p = r on restart), y = D^-1 p
+      const VT vb = (VT)beta, vo = (VT)omega;
+      for (int64_t d = d0 + tid; d < d1; d += nth) {
+        const VT rd = __ldcg(A.r + d);
+        const VT pn = restart ? rd : vfma(vb, vfma(-vo, __ldcg(A.v + d), __ldcg(A.p0 + d)), rd);
+        __stcg(A.p0 + d, pn);
+        __stcg(A.y + d, (VT)A.dinv[d] * pn);
+      }
+      if (!grid_barrier(A.barrier, nr, &s_flag)) {
+        done = 5;
+        break;
+      }
+      // B: v = A y, rhat . v
+      double dv[1] = {0.0};
+      grid_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return __ldcg(A.y + k); }, [&](int64_t d, VT sum) {
+        __stcg(A.v + d, sum);
+        dv[0] += (double)__ldcg(A.rhat + d) * (double)sum;
+      });
+      if (!grid_sum<1>(dv, sh, A, parity, &s_flag, s_bcast)) {
+        done = 5;
+        break;
+      }
+      const double RV = dv[0];
+      restart = false;
+      if (RV == 0.0 || !isfinite(RV)) {
+        ++breakdowns;
+        if (!isfinite(RV)) done = 3;
+        else if (breakdowns > kMaxBreakdowns) done = 4;
+        else replace = 2;
+        continue;
+      }
+      alpha = rho / RV;
+      // C: s = r - alpha v (kept in q), z = D^-1 s
+      const VT va = (VT)alpha;
+      for (int64_t d = d0 + tid; d < d1; d += nth) {
+        const VT sv = vfma(-va, __ldcg(A.v + d), __ldcg(A.r + d));
+        __stcg(A.q + d, sv);
+        __stcg(A.z + d, (VT)A.dinv[d] * sv);
+      }
+      if (!grid_barrier(A.barrier, nr, &s_flag)) {
+        done = 5;
+        break;
+      }
+      // D: t = A z, t . s, t . t
+      double dt[2] = {0.0, 0.0};
+      grid_rows<NDOF, G, VT>(A, n0, n1, [&](int64_t k) { return __ldcg(A.z + k); }, [&](int64_t d, VT sum) {
+        __stcg(A.t + d, sum);
+        dt[0] += (double)sum * (double)__ldcg(A.q + d);
+        dt[1] += (double)sum * (double)sum;
+      });
+      if (!grid_sum<2>(dt, sh, A, parity, &s_flag, s_bcast)) {
+        done = 5;
+        break;
+      }
+      omega = (dt[1] > 0.0 && isfinite(dt[1])) ? dt[0] / dt[1] : 0.0;
+      // E: x += alpha y + omega z, r = s - omega t, rhat . r, r . r
+      const VT vom = (VT)omega;
+      double de[2] = {0.0, 0.0};
+      for (int64_t d = d0 + tid; d < d1; d += nth) {
+        A.x[d] = fma(omega, (double)__ldcg(A.z + d), fma(alpha, (double)__ldcg(A.y + d), A.x[d]));
+        const VT ri = vfma(-vom, __ldcg(A.t + d), __ldcg(A.q + d));
+        __stcg(A.r + d, ri);
+        de[0] += (double)__ldcg(A.rhat + d) * (double)ri;
+        de[1] += (double)ri * (double)ri;
+      }
+      if (!grid_sum<2>(de, sh, A, parity, &s_flag, s_bcast)) {
+        done = 5;
+        break;
+      }
+      const double RH = de[0], RR = de[1];
+      beta = (omega != 0.0 && rho != 0.0) ? (RH / rho) * (alpha / omega) : 0.0;
+      rho = RH;
+      rnorm2 = RR;
+      ++iters;
+      breakdowns = 0;
+      if (!isfinite(RR)) done = 3;
+      else if (RH == 0.0 || omega == 0.0) replace = 2;
+      else if (RR <= tol2 || RR <= kReplaceDrop2 * rref2 || RR > kDiverge2 * bb) replace = 1;
+      if (!done && iters >= A.maxiter) replace = replace ? replace : 1;
+      if (done || !replace) continue;
+    }
+    // reliable update: r = b - A x in fp64 (every block's x is visible: the
+    // last grid sum ordered it); a breakdown (replace == 2) also restarts the
+    // shadow residual
+    const bool fresh = replace == 2;
+    double dr[2] = {0.0, 0.0};
+    grid_rows<NDOF, G, double>(A, n0, n1, [&](int64_t k) { return __ldcg(A.x + k); }, [&](int64_t d, double sum) {
+      const double ri = (double)A.b[d] - sum;
+      const VT rv = (VT)ri;
+      __stcg(A.r + d, rv);
+      if (fresh) {
+        __stcg(A.rhat + d, rv);
+        dr[0] += (double)rv * (double)rv;
+      } else {
+        dr[0] += (double)__ldcg(A.rhat + d) * (double)rv;
+      }
+      dr[1] += ri * ri;
+    });
+    if (!grid_sum<2>(dr, sh, A, parity, &s_flag, s_bcast)) {
+      done = 5;
+      break;
+    }
+    rho = dr[0];
+    rref2 = rnorm2 = dr[1];
+    if (fresh) restart = true;
+    replace = 0;
+    if (!isfinite(dr[1])) done = 3;
+    else if (dr[1] <= tol2) done = 1;
+    else if (dr[1] > kDiverge2 * bb) done = 4;
+    else if (iters >= A.maxiter) done = 2;
+  }
+  for (int64_t d = d0 + tid; d < d1; d += nth) A.xout[d] = (float)A.x[d];
+  if (rank == 0 && threadIdx.x == 0) {
+    A.sc->iters = iters;
+    A.sc->done = done;
+    A.sc->rnorm2 = rnorm2;
+    A.sc->bnorm2 = bb;
+  }
+}
+
 // one cooperative launch of the grid solver (every block resident); returns
 // false if the launch was refused (the caller then uses the multi-kernel path)
-template <int NDOF, int G, class VT>
+template <int NDOF, int G, class VT, bool BICG = false>
 static bool launch_grid_pcg(const GridArgs<VT>& A, cudaStream_t s) {
-  auto kernel = k_pcg_grid<NDOF, G, VT>;
+  auto kernel = BICG ? k_bicg_grid<NDOF, G, VT> : k_pcg_grid<NDOF, G, VT>;
   static std::atomic<int> occ[64];
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return false;
@@ -1476,6 +1635,44 @@ static int krylov_solve(const folgb_plan* p, int solver, const float* vals, cons
           ga.rtol = rtol;
           ga.maxiter = maxiter;
           if (launch_grid_pcg<NDOF, G, VT>(ga, s)) {
+            *capture_sc = w.sc;
+            return (int)FOLGB_OK;
+          }
+        }
+        // BiCGSTAB with fp64 vectors (the neo-Hookean Newton solves) above
+        // 32,768 dofs: one cooperative launch of the grid solver (24^3 tet
+        // split, 46,875 dofs: 68 us per iteration against 74 in the kernel
+        // loop; 16^3, 14,739 dofs: 53 against 37, the grid barriers dominate
+        // there).  fp32 vectors stay on the kernel loop: their iteration count
+        // swings with the reduction order (24^3 elasticity: 644 iterations in
+        // the grid solver against 417), with fp64 vectors it does not.
+        if (solver == SOLVER_BICGSTAB && sizeof(VT) == sizeof(double) && n > 2 * kClusterMaxDofs &&
+            krylov_engine() == FOLGB_KRYLOV_ENGINE_GRID) {
+          GridArgs<VT> ga;
+          ga.N = p->N;
+          ga.adj_ptr = p->d_adj_ptr;
+          ga.adj = p->d_adj;
+          ga.maxdeg = p->maxdeg;
+          ga.vals = vals;
+          ga.dinv = dinv;
+          ga.b = rhs;
+          ga.r = w.r;
+          ga.z = w.z;
+          ga.p0 = w.p0;
+          ga.p1 = w.p1;
+          ga.q = w.q;
+          ga.rhat = w.rhat;
+          ga.v = w.v0;
+          ga.y = w.y;
+          ga.t = w.t;
+          ga.x = w.x;
+          ga.xout = x;
+          ga.sc = w.sc;
+          ga.part = w.part;
+          ga.barrier = w.counters + 6;
+          ga.rtol = rtol;
+          ga.maxiter = maxiter;
+          if (launch_grid_pcg<NDOF, G, VT, true>(ga, s)) {
             *capture_sc = w.sc;
             return (int)FOLGB_OK;
           }

@@ -152,3 +152,40 @@ def test_engine_selector_refuses_unknown(cuda):
     lib = capi.load()
     assert lib.folgb_krylov_set_engine(7) == capi.ERR_INVALID_ARGUMENT
     assert lib.folgb_krylov_set_engine(capi.KRYLOV_ENGINE_GRID) == capi.OK
+
+
+@pytest.mark.parametrize("n,bits", [(24, 64), (28, 64)])
+def test_grid_bicgstab_matches_kernel_engine(cuda, n, bits):
+    """The one-launch grid BiCGSTAB (taken for fp64 Krylov vectors above
+    32,768 dofs) against the loop of
+    SpMV and update kernels: both converged on the true residual (rtol 1e-8),
+    deterministic, about the same iteration count, and the returned fp32
+    solutions within 1e-6 of b in the FP64 residual computed on the host.
+    The two solutions differ by up to condition number x tolerance (measured
+    1.1e-6 at 24^3): BiCGSTAB's iterates, unlike CG's, drift apart with the
+    reduction order, so they are compared through the residual."""
+    from folax_gb300 import _capi as capi
+    lib = capi.load()
+    loss, jac, r = _system(n=n, seed=55)
+    b = (-r).contiguous()
+    out = {}
+    try:
+        for engine in (capi.KRYLOV_ENGINE_KERNELS, capi.KRYLOV_ENGINE_GRID):
+            assert lib.folgb_krylov_set_engine(engine) == capi.OK
+            rc, x, it, rel = _sync(lib, capi, jac, 1, bits, b)
+            assert rc == capi.OK and rel <= 1e-8
+            out[engine] = (x, it)
+            again = _sync(lib, capi, jac, 1, bits, b)
+            assert again[2] == it and np.array_equal(again[1], x)  # deterministic
+    finally:
+        lib.folgb_krylov_set_engine(capi.KRYLOV_ENGINE_GRID)
+    (xk, ik), (xg, ig) = out[capi.KRYLOV_ENGINE_KERNELS], out[capi.KRYLOV_ENGINE_GRID]
+    A = jac.to_scipy().astype(np.float64)
+    bb = b.double().cpu().numpy()
+    res = [np.linalg.norm(bb - A @ x.astype(np.float64)) / np.linalg.norm(bb) for x in (xk, xg)]
+    diff = np.linalg.norm(xg - xk) / np.linalg.norm(xk)
+    print(f"\nBiCGSTAB {n}^3 fp{bits}: kernels {ik} iterations, grid {ig}; FP64 residuals of the fp32 "
+          f"solutions {res[0]:.2e}, {res[1]:.2e}; solution difference {diff:.2e}")
+    assert max(res) <= 1e-6
+    assert diff <= 1e-4
+    assert abs(ig - ik) <= 0.1 * ik + 5
