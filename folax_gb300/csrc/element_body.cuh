@@ -164,6 +164,16 @@ __device__ __forceinline__ void store_record(const VecArgs& A, int64_t off, cons
     const float2 t = make_float2(v[0], v[1]);
     if (A.stream_rec) __stcs(reinterpret_cast<float2*>(rec), t);
     else *reinterpret_cast<float2*>(rec) = t;
+  } else if (A.rec == 3) {  // unpadded 3-component records (tet patches)
+    if (A.stream_rec) {
+      __stcs(rec, v[0]);
+      __stcs(rec + 1, v[1]);
+      __stcs(rec + 2, v[2]);
+    } else {
+      rec[0] = v[0];
+      rec[1] = v[1];
+      rec[2] = v[2];
+    }
   } else {
     if (A.stream_rec) __stcs(rec, v[0]);
     else rec[0] = v[0];
@@ -619,4 +629,9 @@ int launch_tile_boundary(const folgb_plan* p, const VecArgs& A, int B, cudaStrea
 // (instance, patch, patch node); returns 1 if launched, 0 if it does not
 // apply, or the negated error code
 int launch_tet_patch(const folgb_plan* p, const VecArgs& A, int B, cudaStream_t s);
+// record width of the patch records: 3 unpadded floats with element controls
+// (no nodal control sensitivity to carry), else the loss record
+inline int tet_patch_record(const folgb_plan* p) {
+  return (p->ndof == 3 && p->ctrl_layout == FOLGB_CONTROL_ELEMENT) ? 3 : loss_record(p);
+}
 }  // namespace folgb

@@ -92,6 +92,10 @@ __device__ __forceinline__ void load_rec(const float* __restrict__ p, float (&v)
     const float2 t = __ldg(reinterpret_cast<const float2*>(p));
     v[0] = t.x;
     v[1] = t.y;
+  } else if constexpr (REC == 3) {  // unpadded 3-component records (tet patches)
+    v[0] = __ldg(p);
+    v[1] = __ldg(p + 1);
+    v[2] = __ldg(p + 2);
   } else {
     v[0] = __ldg(p);
   }
@@ -855,7 +859,9 @@ int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_
   G.dctrl_stride = dctrl_stride;
   G.dctrl_elem = dctrl_elem;
   G.rescale_elem = rescale_elem;
-  if (rec != padded_record(p->ndof + (with_gde ? 1 : 0))) return FOLGB_ERR_INVALID_ARGUMENT;
+  // unpadded 12-byte records: the tet patch kernel with element controls
+  const bool rec3 = patches && rec == 3 && p->ndof == 3 && !with_gde;
+  if (rec != padded_record(p->ndof + (with_gde ? 1 : 0)) && !rec3) return FOLGB_ERR_INVALID_ARGUMENT;
   int64_t work = p->N > p->E ? p->N : p->E;
   int blocks = (int)((work + 255) / 256);
   int cap = num_sms() * 8;
@@ -894,7 +900,7 @@ int launch_gather(const folgb_plan* p, int B, const float* g, int rec, int with_
     case 3: rcode = go(I1{}, I2{}, T{}); break;
     case 4: rcode = go(I2{}, I2{}, F{}); break;
     case 5: rcode = go(I2{}, I4{}, T{}); break;
-    case 6: rcode = go(I3{}, I4{}, F{}); break;
+    case 6: rcode = rec3 ? go(I3{}, std::integral_constant<int, 3>{}, F{}) : go(I3{}, I4{}, F{}); break;
     case 7: rcode = go(I3{}, I4{}, T{}); break;
     default: return FOLGB_ERR_INVALID_ARGUMENT;
   }
@@ -1010,10 +1016,10 @@ extern "C" int folgb_loss_adjoint(const folgb_plan* p, int32_t B, const float* c
   } else if (fast == 2 && (dloss_ddofs || dloss_dcontrol)) {
     rc = launch_tile_boundary(p, A, B, s, trace_active() ? 0 : 1);
   } else if (dloss_ddofs || dloss_dcontrol) {
-    rc = launch_gather(p, B, w.g, w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs, (int64_t)p->ndof * p->N,
-                       elem_ctrl ? nullptr : dloss_dcontrol, p->N, elem_ctrl ? dloss_dcontrol : nullptr,
-                       (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s, nullptr, nullptr,
-                       trace_active() ? 0 : 1, patched ? 1 : 0);
+    rc = launch_gather(p, B, w.g, patched ? tet_patch_record(p) : w.rec, elem_ctrl ? 0 : 1, w.scale, dloss_ddofs,
+                       (int64_t)p->ndof * p->N, elem_ctrl ? nullptr : dloss_dcontrol, p->N,
+                       elem_ctrl ? dloss_dcontrol : nullptr, (elem_ctrl && p->phys.loss_exponent != 1.0) ? 1 : 0, s,
+                       nullptr, nullptr, trace_active() ? 0 : 1, patched ? 1 : 0);
   }
   return rc;
 }

@@ -10,9 +10,11 @@
 // kernel gives one thread the 6 tetrahedra of a patch (the same element body
 // for each, its node loads hitting L1 after the first), sums their node
 // results per patch node in a shared-memory column of its own in element
-// order, and writes 8 records per patch; the gather then sums each node's
-// patch records in ascending patch order.  A third of the records, a third of
-// the record traffic; every sum in a fixed order (deterministic, no atomics).
+// order, and writes 8 records per patch (3 unpadded floats with element
+// controls, else the element path's padded record); the gather then sums each
+// node's patch records in ascending patch order.  A third of the records, a
+// quarter of the record bytes; every sum in a fixed order (deterministic, no
+// atomics).
 //
 // Tables (built once per mesh): per patch the local node (0..7, first
 // appearance order) of each of its 24 tet corners, 4 bits each; and the node
@@ -152,7 +154,9 @@ __global__ void __launch_bounds__(kPatchBlock, NP == 1 ? 4 : 2) k_tet_patch(cons
 }
 
 template <int PH>
-int launch_typed(const folgb_plan* p, const VecArgs& A, int B, int64_t nb, int tiles, cudaStream_t s) {
+int launch_typed(const folgb_plan* p, const VecArgs& A0, int B, int64_t nb, int tiles, cudaStream_t s) {
+  VecArgs A = A0;
+  A.rec = tet_patch_record(p);
   with_const_gp<FOLGB_TET4>(p, [&](auto np) {
     constexpr int NP = decltype(np)::value;
     k_tet_patch<PH, NP><<<dim3((unsigned)B, (unsigned)nb), kPatchBlock, 0, s>>>(A, p->d_patch_local, p->n_patches,
